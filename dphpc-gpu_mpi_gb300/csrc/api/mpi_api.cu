@@ -1,0 +1,1253 @@
+// mpi_api.cu — the __device__ MPI surface (include/mpi.h.cuh) on top of the block-rank runtime.
+//
+// One translation unit holds the whole runtime so its internals inline into each MPI call; user
+// programs (and the library's own built-in programs) link against these extern __device__ symbols
+// with relocatable device code, as converted programs link against the reference's libgpu_mpi.a.
+#include <cstdio>
+#include <cstring>
+
+#include "../runtime/rt_core.cuh"
+#include "../runtime/rt_types.cuh"
+#include "../runtime/rt_ops.cuh"
+#include "../runtime/rt_copy.cuh"
+#include "../runtime/rt_coll.cuh"
+#include "../runtime/rt_p2p.cuh"
+#include "../runtime/rt_comm.cuh"
+#include "../runtime/rt_select.cuh"
+
+using namespace gpumpi;
+
+// ------------------------------------------------------------------------------------------------
+// globals of the MPI surface
+// ------------------------------------------------------------------------------------------------
+namespace gpumpi {
+__device__ Runtime* g_rt = nullptr;
+
+#define GPUMPI_PT(sz, dt) {sz, sz, 0, sz, 0, dt, {0, 0, 0, 0}, {0, 0, 0, 0}, 1, 1}
+__device__ TypeDesc g_predef_types[GPUMPI_NUM_PREDEFINED_TYPES] = {
+    GPUMPI_PT(1, 0),   GPUMPI_PT(2, 1),   GPUMPI_PT(4, 2),   GPUMPI_PT(8, 3),   GPUMPI_PT(8, 4),
+    GPUMPI_PT(8, 5),   GPUMPI_PT(1, 6),   GPUMPI_PT(1, 7),   GPUMPI_PT(2, 8),   GPUMPI_PT(4, 9),
+    GPUMPI_PT(8, 10),  GPUMPI_PT(8, 11),  GPUMPI_PT(4, 12),  GPUMPI_PT(8, 13),  GPUMPI_PT(8, 14),
+    GPUMPI_PT(4, 15),  GPUMPI_PT(1, 16),  GPUMPI_PT(1, 17),  GPUMPI_PT(2, 18),  GPUMPI_PT(4, 19),
+    GPUMPI_PT(8, 20),  GPUMPI_PT(1, 21),  GPUMPI_PT(2, 22),  GPUMPI_PT(4, 23),  GPUMPI_PT(8, 24),
+    GPUMPI_PT(8, 25),  GPUMPI_PT(8, 26),  GPUMPI_PT(16, 27), GPUMPI_PT(16, 28), GPUMPI_PT(1, 29),
+    GPUMPI_PT(8, 30),  GPUMPI_PT(8, 31),  GPUMPI_PT(16, 32), GPUMPI_PT(16, 33), GPUMPI_PT(8, 34),
+    GPUMPI_PT(16, 35)};
+#undef GPUMPI_PT
+}
+
+__device__ MPI_Comm MPI_COMM_WORLD = nullptr;
+__device__ MPI_Comm MPI_COMM_NULL = nullptr;
+__device__ MPI_Group MPI_GROUP_WORLD = nullptr;
+__device__ MPI_Group MPI_GROUP_NULL = nullptr;
+__device__ MPI_Group MPI_GROUP_EMPTY = nullptr;
+
+__device__ MPI_Op_impl g_predef_ops[GPUMPI_NUM_PREDEFINED_OPS] = {
+    {GPUMPI_OP_MAX, nullptr, 1},  {GPUMPI_OP_MIN, nullptr, 1},  {GPUMPI_OP_SUM, nullptr, 1},
+    {GPUMPI_OP_PROD, nullptr, 1}, {GPUMPI_OP_LAND, nullptr, 1}, {GPUMPI_OP_BAND, nullptr, 1},
+    {GPUMPI_OP_LOR, nullptr, 1},  {GPUMPI_OP_BOR, nullptr, 1},  {GPUMPI_OP_LXOR, nullptr, 1},
+    {GPUMPI_OP_BXOR, nullptr, 1}, {GPUMPI_OP_MAXLOC, nullptr, 1}, {GPUMPI_OP_MINLOC, nullptr, 1}};
+__device__ MPI_Op MPI_MAX = &g_predef_ops[GPUMPI_OP_MAX];
+__device__ MPI_Op MPI_MIN = &g_predef_ops[GPUMPI_OP_MIN];
+__device__ MPI_Op MPI_SUM = &g_predef_ops[GPUMPI_OP_SUM];
+__device__ MPI_Op MPI_PROD = &g_predef_ops[GPUMPI_OP_PROD];
+__device__ MPI_Op MPI_LAND = &g_predef_ops[GPUMPI_OP_LAND];
+__device__ MPI_Op MPI_BAND = &g_predef_ops[GPUMPI_OP_BAND];
+__device__ MPI_Op MPI_LOR = &g_predef_ops[GPUMPI_OP_LOR];
+__device__ MPI_Op MPI_BOR = &g_predef_ops[GPUMPI_OP_BOR];
+__device__ MPI_Op MPI_LXOR = &g_predef_ops[GPUMPI_OP_LXOR];
+__device__ MPI_Op MPI_BXOR = &g_predef_ops[GPUMPI_OP_BXOR];
+__device__ MPI_Op MPI_MAXLOC = &g_predef_ops[GPUMPI_OP_MAXLOC];
+__device__ MPI_Op MPI_MINLOC = &g_predef_ops[GPUMPI_OP_MINLOC];
+
+// ------------------------------------------------------------------------------------------------
+// block tasks, errors, block roles
+// ------------------------------------------------------------------------------------------------
+namespace gpumpi {
+
+__shared__ Task s_task;
+
+__device__ void record_error(int code, int detail, int line, long long info) {
+    ErrorRecord* e = &g_rt->errors[blockIdx.x];
+    if (e->code == 0) {
+        e->code = code;
+        e->detail = detail;
+        e->line = line;
+        e->rank = (int)blockIdx.x;
+        e->info = info;
+    }
+    if (detail == GPUMPI_ERR_TIMEOUT || code == GPUMPI_ERR_INTERN) atomicExch(g_rt->abort_flag, 1u);
+}
+
+__device__ __noinline__ void execute_task(const Task& t, int tid, int nt) {
+    switch (t.kind) {
+    case TASK_COPY: copy_bytes(t.p1, t.p0, t.n0, tid, nt); break;
+    case TASK_CHUNK: exec_chunk((Job*)t.p0, t.n0, tid, nt); break;
+    case TASK_TYPED_COPY:
+        typed_copy(t.p1, (const TypeDesc*)t.p4, t.p0, (const TypeDesc*)t.p2, t.n0, t.n1, tid, nt);
+        break;
+    case TASK_USER: ((void (*)(void*, int, int))t.p0)(t.p1, tid, nt); break;
+    default: break;
+    }
+}
+
+// Thread 0: run task t on the whole block and return when every thread has finished it.
+__device__ void dispatch(const Task& t) {
+    const int nt = nthreads();
+    if (nt == 1) {
+        execute_task(t, 0, 1);
+        return;
+    }
+    s_task = t;
+    bar_sync(BAR_CMD, nt);
+    execute_task(t, 0, nt);
+    bar_sync(BAR_DONE, nt);
+}
+
+// Threads 1..T-1: sleep on the command barrier, execute, report, until EXIT.
+__device__ void helper_loop() {
+    const int nt = nthreads();
+    const int tid = (int)threadIdx.x;
+    for (;;) {
+        bar_sync(BAR_CMD, nt);
+        Task t = s_task;
+        if (t.kind == TASK_EXIT) return;
+        execute_task(t, tid, nt);
+        bar_sync(BAR_DONE, nt);
+    }
+}
+
+__device__ void release_helpers() {
+    if (nthreads() == 1) return;
+    s_task.kind = TASK_EXIT;
+    bar_sync(BAR_CMD, nthreads());
+}
+
+// Thread 0 of a rank block after the user program returned.
+__device__ void rank_finish(int rc) {
+    release_helpers();
+    g_rt->exit_codes[blockIdx.x] = rc;
+    g_rt->ranks[blockIdx.x].exited = 1;
+    __threadfence();
+    atomicAdd(g_rt->ranks_done, 1u);
+}
+
+// Thread 0 of a copy-engine block.
+__device__ void engine_main() {
+    engine_loop();
+    release_helpers();
+}
+
+__device__ int is_rank_block() { return (int)blockIdx.x < g_rt->nranks; }
+
+}  // namespace gpumpi
+
+// ------------------------------------------------------------------------------------------------
+// helpers shared by the MPI functions
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ const TypeDesc* tdesc(int dt) { return resolve_type(dt); }
+
+// Stages a buffer other ranks cannot address (thread 0's stack) into the device heap.
+struct Stage {
+    void* heap = nullptr;
+    void* user = nullptr;
+    long long bytes = 0;
+};
+__device__ __noinline__ void* stage_in(Stage& s, const void* p, long long bytes, bool copy_in) {
+    if (p == nullptr || p == MPI_IN_PLACE || is_global_ptr(p) || bytes <= 0) return (void*)p;
+    s.heap = malloc(bytes);
+    s.user = (void*)p;
+    s.bytes = bytes;
+    if (!s.heap) return nullptr;
+    if (copy_in) t0_copy(s.heap, nullptr, p, nullptr, bytes);
+    return s.heap;
+}
+__device__ __noinline__ void stage_out(Stage& s, bool copy_out) {
+    if (!s.heap) return;
+    if (copy_out) t0_copy(s.user, nullptr, s.heap, nullptr, s.bytes);
+    free(s.heap);
+    s.heap = nullptr;
+}
+
+struct CollArgs {
+    int kind;
+    long long count;   // folds: elements
+    int dt, op, root, esize;
+    MPI_User_function* ufn;
+    long long est_piece;   // pulls: estimated bytes per piece
+    int variant;
+};
+
+__device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, unsigned e_next) {
+    Job* j = &c->job;
+    unsigned mis = ld_relaxed(&c->misalign[e_next & 1]);
+    c->misalign[(e_next + 1) & 1] = 0;
+    j->kind = a.kind;
+    j->comm = c;
+    j->dt = a.dt;
+    j->op = a.op;
+    j->root = a.root;
+    j->ufn = a.ufn;
+    j->esize = a.esize;
+    j->err = 0;
+    j->aligned16 = (mis & 15) == 0 ? 16 : (mis & 7) == 0 ? 8 : (mis & 3) == 0 ? 4 : 0;
+    j->t_setup = now_ns();
+    const int T = nthreads();
+    const int W = (T + 31) / 32;
+    const int n = c->size;
+    int nchunks = 0;
+    long long bytes = 0;
+    bool may_post = g_rt->nengines > 0;
+    if (a.kind == JOB_ALLREDUCE || a.kind == JOB_REDUCE) {
+        j->count = a.count;
+        bytes = a.count * a.esize * (long long)n;
+        int variant = select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, a.variant);
+        j->variant = variant;
+        may_post = may_post && bytes >= g_rt->engine_min_bytes;
+        long long target = n + (may_post ? g_rt->nengines : 0);
+        int vec = 1;
+        if (fold_has_fast(a.dt, a.op, a.ufn)) {
+            int es = a.esize;
+            int cands[3] = {16 / es, es == 4 ? 2 : 1, 1};
+            for (int k = 0; k < 3; k++) {
+                int v = cands[k];
+                int need = v * es >= 16 ? 16 : v * es;
+                if (v > 1 && j->aligned16 < need) continue;
+                long long nch = (a.count + (long long)T * v - 1) / ((long long)T * v);
+                if (nch >= target || v == 1) { vec = v; break; }
+            }
+        }
+        j->vec = vec;
+        j->tile = 0;
+        j->chunk = (long long)T * vec;
+        nchunks = (int)((a.count + j->chunk - 1) / j->chunk);
+    } else if (a.kind == JOB_BARRIER) {
+        nchunks = 0;
+    } else {
+        long long P = (a.kind == JOB_ALLTOALLV || a.kind == JOB_ALLGATHERV) ? (long long)n * n : (long long)n;
+        j->count = P;
+        j->variant = GPUMPI_VARIANT_DIRECT;
+        bytes = a.est_piece * P;
+        may_post = may_post && bytes >= g_rt->engine_min_bytes;
+        long long target = n + (may_post ? g_rt->nengines : 0);
+        if (a.est_piece >= 65536) {
+            int parts = (int)((a.est_piece + 65535) / 65536);
+            j->vec = parts;
+            j->tile = 1;
+            nchunks = (int)(P * parts);
+        } else {
+            long long tile = P / (target > 0 ? target : 1);
+            if (tile < 1) tile = 1;
+            if (tile > 4 * W) tile = 4 * W;
+            j->vec = 1;
+            j->tile = (int)tile;
+            nchunks = (int)((P + tile - 1) / tile);
+        }
+    }
+    unsigned e = job_open(j, nchunks);
+    if (may_post && nchunks > n) board_post(j, e);
+}
+
+__device__ __noinline__ int coll_run(MPI_Comm_impl* c, const CollSlot& mine, const CollArgs& a, int line) {
+    const int cr = comm_rank_of(c, me());
+    c->slots[cr] = mine;
+    const unsigned e_next = c->job.epoch + 1;
+    unsigned mis = (unsigned)((size_t)mine.sbuf | (size_t)mine.rbuf) & 15u;
+    if (mis) atomicOr(&c->misalign[e_next & 1], mis);
+    RankState* R = &g_rt->ranks[me()];
+    R->coll_calls++;
+    unsigned long long t0 = g_rt->trace_enabled ? now_ns() : 0;
+    int rc = comm_barrier(c, [&]() { coll_setup(c, a, e_next); }, line);
+    if (rc) return rc;
+    if (a.kind == JOB_BARRIER) return 0;
+    rc = job_run_and_wait(&c->job, line);
+    if (rc) return rc;
+    if (g_rt->trace_enabled && cr == 0) trace_record(c, a.kind, c->job.variant, a.dt, a.op,
+                                                    a.kind == JOB_ALLREDUCE || a.kind == JOB_REDUCE
+                                                        ? a.count * a.esize : a.est_piece * c->size,
+                                                    now_ns() - t0);
+    return ld_relaxed(&c->job.err) ? GPUMPI_ERR_TRUNCATE : 0;
+}
+
+__device__ __forceinline__ int op_code_of(MPI_Op op, MPI_User_function** ufn) {
+    *ufn = nullptr;
+    if (!op) return -1;
+    if (op->code == GPUMPI_OP_USER) {
+        *ufn = op->fn;
+        return GPUMPI_OP_USER;
+    }
+    return op->code;
+}
+
+__device__ __noinline__ int fold_collective(int kind, const void* sendbuf, void* recvbuf, int count, MPI_Datatype dt, MPI_Op op,
+                               int root, MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (count < 0) return GPUMPI_ERR_COUNT;
+    if (kind == JOB_REDUCE && (root < 0 || root >= c->size)) return GPUMPI_ERR_ROOT;
+    if (dt < 0 || dt >= GPUMPI_NUM_PREDEFINED_TYPES) return GPUMPI_ERR_TYPE;
+    MPI_User_function* ufn;
+    int opc = op_code_of(op, &ufn);
+    if (opc < 0) return GPUMPI_ERR_OP;
+    if (opc != GPUMPI_OP_USER && !op_allowed(opc, dt)) {
+        record_error(GPUMPI_ERR_OP, dt, __LINE__, opc);
+        return GPUMPI_ERR_OP;
+    }
+    if (count == 0) return 0;
+    const int es = predefined_size(dt);
+    const long long bytes = (long long)count * es;
+    const int cr = comm_rank_of(c, me());
+    const bool has_out = kind == JOB_ALLREDUCE || cr == root;
+    const void* sb = sendbuf == MPI_IN_PLACE ? recvbuf : sendbuf;
+    Stage ss, rs;
+    const void* gsb = stage_in(ss, sb, bytes, true);
+    void* grb = has_out ? stage_in(rs, recvbuf, bytes, sendbuf == MPI_IN_PLACE) : nullptr;
+    if (sendbuf == MPI_IN_PLACE && rs.heap) gsb = rs.heap;
+    if ((sb && !gsb) || (has_out && recvbuf && !grb)) return GPUMPI_ERR_NO_MEM;
+    CollSlot my{};
+    my.sbuf = gsb;
+    my.rbuf = grb;
+    my.scount = count;
+    my.stype = dt;
+    my.op = opc;
+    my.root = root;
+    CollArgs a;
+    a.kind = kind;
+    a.count = count;
+    a.dt = dt;
+    a.op = opc;
+    a.root = root;
+    a.esize = es;
+    a.ufn = ufn;
+    a.est_piece = 0;
+    a.variant = g_rt->variant_override;
+    int rc = coll_run(c, my, a, __LINE__);
+    stage_out(ss, false);
+    stage_out(rs, has_out);
+    return rc;
+}
+
+// pull collectives; `arrays` that live on thread 0's stack are staged so other ranks can read them
+__device__ const int* stage_ints(Stage& s, const int* p, int n) {
+    return (const int*)stage_in(s, p, (long long)n * sizeof(int), true);
+}
+
+__device__ __noinline__ int pull_collective(int kind, MPI_Comm_impl* c, CollSlot& my, long long sbytes, long long rbytes,
+                               long long est_piece, int root) {
+    Stage ss, rs;
+    const void* gsb = stage_in(ss, my.sbuf, sbytes, true);
+    void* grb = stage_in(rs, my.rbuf, rbytes, false);
+    if ((my.sbuf && my.sbuf != MPI_IN_PLACE && sbytes > 0 && !gsb) || (my.rbuf && rbytes > 0 && !grb))
+        return GPUMPI_ERR_NO_MEM;
+    my.sbuf = gsb;
+    my.rbuf = grb;
+    CollArgs a;
+    a.kind = kind;
+    a.count = 0;
+    a.dt = my.stype;
+    a.op = 0;
+    a.root = root;
+    a.esize = 0;
+    a.ufn = nullptr;
+    a.est_piece = est_piece;
+    a.variant = -1;
+    int rc = coll_run(c, my, a, __LINE__);
+    stage_out(ss, false);
+    stage_out(rs, true);
+    return rc;
+}
+
+__device__ long long sample_counts(const int* counts, int n) {
+    if (!counts || n <= 0) return 0;
+    long long s = 0;
+    int k = n < 16 ? n : 16;
+    for (int i = 0; i < k; i++) s += counts[(long long)i * n / k];
+    return s / k;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// environment
+// ------------------------------------------------------------------------------------------------
+__device__ int MPI_Init(int* argc, char*** argv) {
+    (void)argc;
+    (void)argv;
+    g_rt->ranks[me()].initialized = 1;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Init_thread(int* argc, char*** argv, int required, int* provided) {
+    (void)required;
+    if (provided) *provided = MPI_THREAD_SINGLE;
+    return MPI_Init(argc, argv);
+}
+__device__ int MPI_Initialized(int* flag) {
+    *flag = g_rt->ranks[me()].initialized;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Finalize(void) {
+    g_rt->ranks[me()].finalized = 1;
+    return MPI_Barrier(MPI_COMM_WORLD);
+}
+__device__ int MPI_Finalized(int* flag) {
+    *flag = g_rt->ranks[me()].finalized;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Abort(MPI_Comm comm, int errorcode) {
+    (void)comm;
+    record_error(GPUMPI_ERR_OTHER, errorcode, __LINE__, errorcode);
+    atomicExch(g_rt->abort_flag, 1u);
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Get_processor_name(char* name, int* resultlen) {
+    const char n[] = "GB300 block-rank";
+    for (int i = 0; i < (int)sizeof(n); i++) name[i] = n[i];
+    *resultlen = (int)sizeof(n) - 1;
+    return MPI_SUCCESS;
+}
+__device__ double MPI_Wtime(void) { return (double)now_ns() * 1e-9; }
+__device__ double MPI_Wtick(void) { return 1e-9; }
+__device__ int gpumpi_world_rank(void) { return (int)blockIdx.x; }
+__device__ int gpumpi_block_parallel(void (*fn)(void*, int, int), void* arg) {
+    Task t;
+    t.kind = TASK_USER;
+    t.p0 = (const void*)fn;
+    t.p1 = arg;
+    dispatch(t);
+    return MPI_SUCCESS;
+}
+
+// ------------------------------------------------------------------------------------------------
+// point-to-point
+// ------------------------------------------------------------------------------------------------
+__device__ int MPI_Isend(const void* buf, int count, MPI_Datatype datatype, int dest, int tag, MPI_Comm comm,
+                         MPI_Request* request) {
+    return p2p_isend(buf, count, datatype, dest, tag, comm, request, false);
+}
+__device__ int MPI_Issend(const void* buf, int count, MPI_Datatype datatype, int dest, int tag, MPI_Comm comm,
+                          MPI_Request* request) {
+    return p2p_isend(buf, count, datatype, dest, tag, comm, request, true);
+}
+__device__ int MPI_Irecv(void* buf, int count, MPI_Datatype datatype, int source, int tag, MPI_Comm comm,
+                         MPI_Request* request) {
+    return p2p_irecv(buf, count, datatype, source, tag, comm, request);
+}
+__device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int dest, int tag, MPI_Comm comm) {
+    MPI_Request r = nullptr;
+    int rc = p2p_isend(buf, count, datatype, dest, tag, comm, &r, false);
+    int rw = r ? req_wait(&r, MPI_STATUS_IGNORE) : 0;
+    return rc ? rc : rw;
+}
+__device__ int MPI_Ssend(const void* buf, int count, MPI_Datatype datatype, int dest, int tag, MPI_Comm comm) {
+    MPI_Request r = nullptr;
+    int rc = p2p_isend(buf, count, datatype, dest, tag, comm, &r, true);
+    int rw = r ? req_wait(&r, MPI_STATUS_IGNORE) : 0;
+    return rc ? rc : rw;
+}
+__device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source, int tag, MPI_Comm comm,
+                        MPI_Status* status) {
+    MPI_Request r = nullptr;
+    int rc = p2p_irecv(buf, count, datatype, source, tag, comm, &r);
+    int rw = r ? req_wait(&r, status) : 0;
+    return rc ? rc : rw;
+}
+__device__ int MPI_Sendrecv(const void* sendbuf, int sendcount, MPI_Datatype sendtype, int dest, int sendtag,
+                            void* recvbuf, int recvcount, MPI_Datatype recvtype, int source, int recvtag,
+                            MPI_Comm comm, MPI_Status* status) {
+    // the reference returns without doing anything (gpu_libs/gpu_mpi/mpi.cu:255-260); this is MPI's
+    // definition: a send and a receive executed concurrently
+    MPI_Request rq[2] = {nullptr, nullptr};
+    int rc = p2p_irecv(recvbuf, recvcount, recvtype, source, recvtag, comm, &rq[0]);
+    int rs = p2p_isend(sendbuf, sendcount, sendtype, dest, sendtag, comm, &rq[1], false);
+    int w0 = rq[0] ? req_wait(&rq[0], status) : 0;
+    int w1 = rq[1] ? req_wait(&rq[1], MPI_STATUS_IGNORE) : 0;
+    return rc ? rc : rs ? rs : w0 ? w0 : w1;
+}
+__device__ int MPI_Wait(MPI_Request* request, MPI_Status* status) {
+    if (!request) return GPUMPI_ERR_REQUEST;
+    return req_wait(request, status);
+}
+__device__ int MPI_Waitall(int count, MPI_Request reqs[], MPI_Status* statuses) {
+    // statuses may be MPI_STATUSES_IGNORE (the reference indexes it unconditionally, mpi.cu:579-585)
+    int err = 0;
+    Deadline dl = make_deadline();
+    for (;;) {
+        bool all = true;
+        for (int i = 0; i < count; i++) {
+            if (reqs[i] == MPI_REQUEST_NULL) continue;
+            if (req_poll(reqs[i])) {
+                int e = req_wait(&reqs[i], statuses ? &statuses[i] : nullptr);
+                if (e && !err) err = e;
+            } else {
+                all = false;
+            }
+        }
+        if (all) return err;
+        progress();
+        if (int e = wait_tick(dl, __LINE__)) return e;
+    }
+}
+__device__ int MPI_Waitany(int count, MPI_Request reqs[], int* index, MPI_Status* status) {
+    Deadline dl = make_deadline();
+    for (;;) {
+        bool any_active = false;
+        for (int i = 0; i < count; i++) {
+            if (reqs[i] == MPI_REQUEST_NULL) continue;
+            any_active = true;
+            if (req_poll(reqs[i])) {
+                *index = i;
+                return req_wait(&reqs[i], status);
+            }
+        }
+        if (!any_active) {
+            *index = MPI_UNDEFINED;
+            return MPI_SUCCESS;
+        }
+        progress();
+        if (int e = wait_tick(dl, __LINE__)) return e;
+    }
+}
+__device__ int MPI_Waitsome(int incount, MPI_Request reqs[], int* outcount, int indices[], MPI_Status statuses[]) {
+    Deadline dl = make_deadline();
+    for (;;) {
+        int n = 0;
+        bool any_active = false;
+        for (int i = 0; i < incount; i++) {
+            if (reqs[i] == MPI_REQUEST_NULL) continue;
+            any_active = true;
+            if (req_poll(reqs[i])) {
+                req_wait(&reqs[i], statuses ? &statuses[n] : nullptr);
+                indices[n++] = i;
+            }
+        }
+        if (!any_active) {
+            *outcount = MPI_UNDEFINED;
+            return MPI_SUCCESS;
+        }
+        if (n > 0) {
+            *outcount = n;
+            return MPI_SUCCESS;
+        }
+        progress();
+        if (int e = wait_tick(dl, __LINE__)) return e;
+    }
+}
+__device__ int MPI_Test(MPI_Request* request, int* flag, MPI_Status* status) {
+    if (!request) return GPUMPI_ERR_REQUEST;
+    if (*request == MPI_REQUEST_NULL) {
+        *flag = 1;
+        if (status) *status = MPI_Status();
+        return MPI_SUCCESS;
+    }
+    progress();
+    if (req_poll(*request)) {
+        *flag = 1;
+        return req_wait(request, status);
+    }
+    *flag = 0;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Testall(int count, MPI_Request reqs[], int* flag, MPI_Status statuses[]) {
+    progress();
+    for (int i = 0; i < count; i++)
+        if (reqs[i] != MPI_REQUEST_NULL && !req_poll(reqs[i])) {
+            *flag = 0;
+            return MPI_SUCCESS;
+        }
+    *flag = 1;
+    int err = 0;
+    for (int i = 0; i < count; i++)
+        if (reqs[i] != MPI_REQUEST_NULL) {
+            int e = req_wait(&reqs[i], statuses ? &statuses[i] : nullptr);
+            if (e && !err) err = e;
+        }
+    return err;
+}
+__device__ int MPI_Request_free(MPI_Request* request) {
+    if (!request || !*request) return MPI_SUCCESS;
+    MPI_Request_impl* q = *request;
+    if (req_poll(q)) {
+        req_release(q);
+    } else if (q->kind == REQ_RECV) {
+        q->freed = 1;  // recycled when the message arrives
+    } else {
+        // an active rendezvous send: its completion flag is written by the receiver later, so the
+        // request slot is only recycled once that happened (bounded wait)
+        req_wait(request, MPI_STATUS_IGNORE);
+    }
+    *request = MPI_REQUEST_NULL;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Iprobe(int source, int tag, MPI_Comm comm, int* flag, MPI_Status* status) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    progress();
+    RankState* R = &g_rt->ranks[me()];
+    for (int i = 0; i < R->uq_count; i++) {
+        const Envelope& e = uq_at(i)->env;
+        if (e.ctx == c->ctx && (source == MPI_ANY_SOURCE || source == e.src) && (tag == MPI_ANY_TAG || tag == e.tag)) {
+            *flag = 1;
+            if (status) {
+                status->MPI_SOURCE = e.src;
+                status->MPI_TAG = e.tag;
+                status->MPI_ERROR = 0;
+                status->count_bytes = e.bytes;
+            }
+            return MPI_SUCCESS;
+        }
+    }
+    *flag = 0;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Probe(int source, int tag, MPI_Comm comm, MPI_Status* status) {
+    Deadline dl = make_deadline();
+    for (;;) {
+        int flag = 0;
+        int rc = MPI_Iprobe(source, tag, comm, &flag, status);
+        if (rc || flag) return rc;
+        if (int e = wait_tick(dl, __LINE__)) return e;
+    }
+}
+__device__ int MPI_Get_count(const MPI_Status* status, MPI_Datatype datatype, int* count) {
+    const TypeDesc* t = tdesc(datatype);
+    if (!t) return GPUMPI_ERR_TYPE;
+    if (t->size == 0 || status->count_bytes % t->size) {
+        *count = MPI_UNDEFINED;
+        return MPI_SUCCESS;
+    }
+    *count = (int)(status->count_bytes / t->size);
+    return MPI_SUCCESS;
+}
+
+// ------------------------------------------------------------------------------------------------
+// collectives
+// ------------------------------------------------------------------------------------------------
+__device__ int MPI_Barrier(MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    // barrier on any communicator (the reference implements only the world, mpi.cu:324-331)
+    return comm_barrier(c, []() {}, __LINE__);
+}
+
+__device__ int MPI_Allreduce(const void* sendbuf, void* recvbuf, int count, MPI_Datatype datatype, MPI_Op op,
+                             MPI_Comm comm) {
+    return fold_collective(JOB_ALLREDUCE, sendbuf, recvbuf, count, datatype, op, 0, comm);
+}
+
+__device__ int MPI_Reduce(const void* sendbuf, void* recvbuf, int count, MPI_Datatype datatype, MPI_Op op, int root,
+                          MPI_Comm comm) {
+    return fold_collective(JOB_REDUCE, sendbuf, recvbuf, count, datatype, op, root, comm);
+}
+
+__device__ int MPI_Bcast(void* buffer, int count, MPI_Datatype datatype, int root, MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (root < 0 || root >= c->size) return GPUMPI_ERR_ROOT;
+    const TypeDesc* t = tdesc(datatype);
+    if (!t) return GPUMPI_ERR_TYPE;
+    if (count < 0) return GPUMPI_ERR_COUNT;
+    if (count == 0 || c->size == 1) return MPI_SUCCESS;
+    long long bytes = (long long)count * t->size;
+    long long span = t->lb + (long long)count * t->extent;
+    const int cr = comm_rank_of(c, me());
+    Stage st;
+    void* gb = buffer;
+    if (!is_global_ptr(buffer)) {
+        if (t->nlev != 0 || t->lb != 0) return GPUMPI_ERR_BUFFER;
+        gb = stage_in(st, buffer, span, cr == root);
+        if (!gb) return GPUMPI_ERR_NO_MEM;
+    }
+    CollSlot my{};
+    my.sbuf = gb;
+    my.rbuf = gb;
+    my.scount = count;
+    my.rcount = count;
+    my.sdesc = t;
+    my.rdesc = t;
+    my.stype = datatype;
+    my.rtype = datatype;
+    CollArgs a;
+    a.kind = JOB_BCAST;
+    a.count = 0;
+    a.dt = datatype;
+    a.op = 0;
+    a.root = root;
+    a.esize = 0;
+    a.ufn = nullptr;
+    a.est_piece = bytes;
+    a.variant = -1;
+    int rc = coll_run(c, my, a, __LINE__);
+    stage_out(st, cr != root);
+    return rc;
+}
+
+__device__ int MPI_Alltoallv(const void* sendbuf, const int sendcounts[], const int sdispls[], MPI_Datatype sendtype,
+                             void* recvbuf, const int recvcounts[], const int rdispls[], MPI_Datatype recvtype,
+                             MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    const TypeDesc* st = tdesc(sendtype);
+    const TypeDesc* rt = tdesc(recvtype);
+    if (!st || !rt) return GPUMPI_ERR_TYPE;
+    const int n = c->size;
+    if (sendbuf == MPI_IN_PLACE) return GPUMPI_ERR_ARG;
+    // spans of the user buffers (for staging thread-local buffers)
+    long long sspan = 0, rspan = 0;
+    if (!is_global_ptr(sendbuf) || !is_global_ptr(recvbuf)) {
+        for (int i = 0; i < n; i++) {
+            long long se = st->lb + ((long long)sdispls[i] + sendcounts[i]) * st->extent;
+            long long re = rt->lb + ((long long)rdispls[i] + recvcounts[i]) * rt->extent;
+            sspan = se > sspan ? se : sspan;
+            rspan = re > rspan ? re : rspan;
+        }
+    }
+    Stage s1, s2, s3, s4;
+    CollSlot my{};
+    my.sbuf = sendbuf;
+    my.rbuf = recvbuf;
+    my.scounts = stage_ints(s1, sendcounts, n);
+    my.sdispls = stage_ints(s2, sdispls, n);
+    my.rcounts = stage_ints(s3, recvcounts, n);
+    my.rdispls = stage_ints(s4, rdispls, n);
+    my.sdesc = st;
+    my.rdesc = rt;
+    my.stype = sendtype;
+    my.rtype = recvtype;
+    long long est = sample_counts(sendcounts, n) * st->size;
+    int rc = pull_collective(JOB_ALLTOALLV, c, my, sspan, rspan, est, 0);
+    stage_out(s1, false);
+    stage_out(s2, false);
+    stage_out(s3, false);
+    stage_out(s4, false);
+    return rc;
+}
+
+__device__ int MPI_Alltoall(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf, int recvcount,
+                            MPI_Datatype recvtype, MPI_Comm comm) {
+    // the reference builds four count/displacement arrays with malloc and calls Alltoallv
+    // (gpu_libs/gpu_mpi/mpi.cu:333-362); here the uniform layout is described by two scalars
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    const TypeDesc* st = tdesc(sendtype);
+    const TypeDesc* rt = tdesc(recvtype);
+    if (!st || !rt) return GPUMPI_ERR_TYPE;
+    if (sendcount < 0 || recvcount < 0) return GPUMPI_ERR_COUNT;
+    const int n = c->size;
+    Stage tmp;
+    const void* sb = sendbuf;
+    if (sendbuf == MPI_IN_PLACE) {  // in place: the send data is the receive buffer's old contents
+        sendcount = recvcount;
+        sendtype = recvtype;
+        st = rt;
+        long long span = rt->lb + (long long)n * recvcount * rt->extent;
+        tmp.heap = malloc(span > 0 ? span : 1);
+        if (!tmp.heap) return GPUMPI_ERR_NO_MEM;
+        t0_copy(tmp.heap, nullptr, recvbuf, nullptr, span);
+        sb = tmp.heap;
+    }
+    CollSlot my{};
+    my.sbuf = sb;
+    my.rbuf = recvbuf;
+    my.scount = sendcount;
+    my.rcount = recvcount;
+    my.sdesc = st;
+    my.rdesc = rt;
+    my.stype = sendtype;
+    my.rtype = recvtype;
+    long long sspan = st->lb + (long long)n * sendcount * st->extent;
+    long long rspan = rt->lb + (long long)n * recvcount * rt->extent;
+    int rc = pull_collective(JOB_ALLTOALLV, c, my, sspan, rspan, (long long)sendcount * st->size, 0);
+    if (tmp.heap) free(tmp.heap);
+    return rc;
+}
+
+__device__ int MPI_Allgather(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf, int recvcount,
+                             MPI_Datatype recvtype, MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    const TypeDesc* st = tdesc(sendtype);
+    const TypeDesc* rt = tdesc(recvtype);
+    if (!rt || (sendbuf != MPI_IN_PLACE && !st)) return GPUMPI_ERR_TYPE;
+    const int n = c->size;
+    const int cr = comm_rank_of(c, me());
+    CollSlot my{};
+    my.rbuf = recvbuf;
+    my.rcount = recvcount;
+    my.rdesc = rt;
+    my.rtype = recvtype;
+    long long rspan = rt->lb + (long long)n * recvcount * rt->extent;
+    if (sendbuf == MPI_IN_PLACE) {
+        my.sbuf = MPI_IN_PLACE;  // resolved after staging below
+        my.scount = recvcount;
+        my.sdesc = rt;
+        my.stype = recvtype;
+    } else {
+        my.sbuf = sendbuf;
+        my.scount = sendcount;
+        my.sdesc = st;
+        my.stype = sendtype;
+    }
+    long long sspan = my.sbuf == MPI_IN_PLACE ? 0 : st->lb + (long long)sendcount * st->extent;
+    Stage ss, rs;
+    const void* gsb = my.sbuf == MPI_IN_PLACE ? MPI_IN_PLACE : stage_in(ss, my.sbuf, sspan, true);
+    void* grb = stage_in(rs, recvbuf, rspan, sendbuf == MPI_IN_PLACE);
+    if (!grb || !gsb) return GPUMPI_ERR_NO_MEM;
+    if (gsb == MPI_IN_PLACE) gsb = (const char*)grb + (long long)cr * recvcount * rt->extent;
+    my.sbuf = gsb;
+    my.rbuf = grb;
+    CollArgs a;
+    a.kind = JOB_ALLGATHERV;
+    a.count = 0;
+    a.dt = recvtype;
+    a.op = 0;
+    a.root = 0;
+    a.esize = 0;
+    a.ufn = nullptr;
+    a.est_piece = (long long)my.scount * my.sdesc->size;
+    a.variant = -1;
+    int rc = coll_run(c, my, a, __LINE__);
+    stage_out(ss, false);
+    stage_out(rs, true);
+    return rc;
+}
+
+__device__ int MPI_Allgatherv(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf,
+                              const int recvcounts[], const int displs[], MPI_Datatype recvtype, MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    const TypeDesc* st = tdesc(sendtype);
+    const TypeDesc* rt = tdesc(recvtype);
+    if (!rt || (sendbuf != MPI_IN_PLACE && !st)) return GPUMPI_ERR_TYPE;
+    const int n = c->size;
+    const int cr = comm_rank_of(c, me());
+    long long rspan = 0;
+    for (int i = 0; i < n; i++) {
+        long long e = rt->lb + ((long long)displs[i] + recvcounts[i]) * rt->extent;
+        rspan = e > rspan ? e : rspan;
+    }
+    Stage ss, rs, s3, s4;
+    CollSlot my{};
+    my.rcounts = stage_ints(s3, recvcounts, n);
+    my.rdispls = stage_ints(s4, displs, n);
+    my.rdesc = rt;
+    my.rtype = recvtype;
+    void* grb = stage_in(rs, recvbuf, rspan, sendbuf == MPI_IN_PLACE);
+    if (!grb) return GPUMPI_ERR_NO_MEM;
+    if (sendbuf == MPI_IN_PLACE) {
+        my.sbuf = (const char*)grb + (long long)displs[cr] * rt->extent;
+        my.scount = recvcounts[cr];
+        my.sdesc = rt;
+        my.stype = recvtype;
+    } else {
+        my.sbuf = stage_in(ss, sendbuf, st->lb + (long long)sendcount * st->extent, true);
+        my.scount = sendcount;
+        my.sdesc = st;
+        my.stype = sendtype;
+    }
+    my.rbuf = grb;
+    CollArgs a;
+    a.kind = JOB_ALLGATHERV;
+    a.count = 0;
+    a.dt = recvtype;
+    a.op = 0;
+    a.root = 0;
+    a.esize = 0;
+    a.ufn = nullptr;
+    a.est_piece = (long long)my.scount * my.sdesc->size;
+    a.variant = -1;
+    int rc = coll_run(c, my, a, __LINE__);
+    stage_out(ss, false);
+    stage_out(rs, true);
+    stage_out(s3, false);
+    stage_out(s4, false);
+    return rc;
+}
+
+__device__ int MPI_Gatherv(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf,
+                           const int recvcounts[], const int displs[], MPI_Datatype recvtype, int root, MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (root < 0 || root >= c->size) return GPUMPI_ERR_ROOT;
+    const int n = c->size;
+    const int cr = comm_rank_of(c, me());
+    const TypeDesc* st = sendbuf == MPI_IN_PLACE ? nullptr : tdesc(sendtype);
+    const TypeDesc* rt = cr == root ? tdesc(recvtype) : nullptr;
+    if ((sendbuf != MPI_IN_PLACE && !st) || (cr == root && !rt)) return GPUMPI_ERR_TYPE;
+    Stage s3, s4;
+    CollSlot my{};
+    my.sbuf = sendbuf;
+    my.scount = sendcount;
+    my.sdesc = st ? st : rt;
+    my.stype = sendtype;
+    long long rspan = 0;
+    if (cr == root) {
+        for (int i = 0; i < n; i++) {
+            long long e = rt->lb + ((long long)displs[i] + recvcounts[i]) * rt->extent;
+            rspan = e > rspan ? e : rspan;
+        }
+        my.rbuf = recvbuf;
+        my.rcounts = stage_ints(s3, recvcounts, n);
+        my.rdispls = stage_ints(s4, displs, n);
+        my.rdesc = rt;
+        my.rtype = recvtype;
+    } else {
+        my.rdesc = st;
+    }
+    long long sspan = st ? st->lb + (long long)sendcount * st->extent : 0;
+    int rc = pull_collective(JOB_GATHERV, c, my, sspan, cr == root ? rspan : 0,
+                             st ? (long long)sendcount * st->size : 0, root);
+    stage_out(s3, false);
+    stage_out(s4, false);
+    return rc;
+}
+
+__device__ int MPI_Gather(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf, int recvcount,
+                          MPI_Datatype recvtype, int root, MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (root < 0 || root >= c->size) return GPUMPI_ERR_ROOT;
+    const int n = c->size;
+    const int cr = comm_rank_of(c, me());
+    const TypeDesc* st = sendbuf == MPI_IN_PLACE ? nullptr : tdesc(sendtype);
+    const TypeDesc* rt = cr == root ? tdesc(recvtype) : nullptr;
+    if ((sendbuf != MPI_IN_PLACE && !st) || (cr == root && !rt)) return GPUMPI_ERR_TYPE;
+    CollSlot my{};
+    my.sbuf = sendbuf;
+    my.scount = sendcount;
+    my.sdesc = st ? st : rt;
+    my.stype = sendtype;
+    long long rspan = 0;
+    if (cr == root) {
+        my.rbuf = recvbuf;
+        my.rcount = recvcount;
+        my.rdesc = rt;
+        my.rtype = recvtype;
+        rspan = rt->lb + (long long)n * recvcount * rt->extent;
+    } else {
+        my.rdesc = st;
+    }
+    long long sspan = st ? st->lb + (long long)sendcount * st->extent : 0;
+    return pull_collective(JOB_GATHERV, c, my, sspan, rspan, st ? (long long)sendcount * st->size : 0, root);
+}
+
+__device__ int MPI_Scatterv(const void* sendbuf, const int sendcounts[], const int displs[], MPI_Datatype sendtype,
+                            void* recvbuf, int recvcount, MPI_Datatype recvtype, int root, MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (root < 0 || root >= c->size) return GPUMPI_ERR_ROOT;
+    const int n = c->size;
+    const int cr = comm_rank_of(c, me());
+    const TypeDesc* st = cr == root ? tdesc(sendtype) : nullptr;
+    const TypeDesc* rt = recvbuf == MPI_IN_PLACE ? nullptr : tdesc(recvtype);
+    if ((cr == root && !st) || (recvbuf != MPI_IN_PLACE && !rt)) return GPUMPI_ERR_TYPE;
+    Stage s1, s2;
+    CollSlot my{};
+    my.rbuf = recvbuf;
+    my.rcount = recvcount;
+    my.rdesc = rt ? rt : st;
+    my.rtype = recvtype;
+    long long sspan = 0;
+    if (cr == root) {
+        for (int i = 0; i < n; i++) {
+            long long e = st->lb + ((long long)displs[i] + sendcounts[i]) * st->extent;
+            sspan = e > sspan ? e : sspan;
+        }
+        my.sbuf = sendbuf;
+        my.scounts = stage_ints(s1, sendcounts, n);
+        my.sdispls = stage_ints(s2, displs, n);
+        my.sdesc = st;
+        my.stype = sendtype;
+    } else {
+        my.sdesc = rt;
+    }
+    long long rspan = rt ? rt->lb + (long long)recvcount * rt->extent : 0;
+    int rc = pull_collective(JOB_SCATTERV, c, my, sspan, rspan, rt ? (long long)recvcount * rt->size : 0, root);
+    stage_out(s1, false);
+    stage_out(s2, false);
+    return rc;
+}
+
+__device__ int MPI_Scatter(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf, int recvcount,
+                           MPI_Datatype recvtype, int root, MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (root < 0 || root >= c->size) return GPUMPI_ERR_ROOT;
+    const int n = c->size;
+    const int cr = comm_rank_of(c, me());
+    const TypeDesc* st = cr == root ? tdesc(sendtype) : nullptr;
+    const TypeDesc* rt = recvbuf == MPI_IN_PLACE ? nullptr : tdesc(recvtype);
+    if ((cr == root && !st) || (recvbuf != MPI_IN_PLACE && !rt)) return GPUMPI_ERR_TYPE;
+    CollSlot my{};
+    my.rbuf = recvbuf;
+    my.rcount = recvcount;
+    my.rdesc = rt ? rt : st;
+    my.rtype = recvtype;
+    long long sspan = 0;
+    if (cr == root) {
+        my.sbuf = sendbuf;
+        my.scount = sendcount;
+        my.sdesc = st;
+        my.stype = sendtype;
+        sspan = st->lb + (long long)n * sendcount * st->extent;
+    } else {
+        my.sdesc = rt;
+    }
+    long long rspan = rt ? rt->lb + (long long)recvcount * rt->extent : 0;
+    return pull_collective(JOB_SCATTERV, c, my, sspan, rspan, rt ? (long long)recvcount * rt->size : 0, root);
+}
+
+// ------------------------------------------------------------------------------------------------
+// operators
+// ------------------------------------------------------------------------------------------------
+__device__ int MPI_Op_create(MPI_User_function* user_fn, int commute, MPI_Op* op) {
+    MPI_Op o = (MPI_Op)malloc(sizeof(MPI_Op_impl));
+    if (!o) return GPUMPI_ERR_NO_MEM;
+    o->code = GPUMPI_OP_USER;
+    o->fn = user_fn;
+    o->commute = commute;
+    *op = o;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Op_free(MPI_Op* op) {
+    if (op && *op && (*op)->code == GPUMPI_OP_USER) free(*op);
+    if (op) *op = MPI_OP_NULL;
+    return MPI_SUCCESS;
+}
+
+// ------------------------------------------------------------------------------------------------
+// datatypes
+// ------------------------------------------------------------------------------------------------
+__device__ int MPI_Type_size(MPI_Datatype datatype, int* size) {
+    const TypeDesc* t = tdesc(datatype);
+    if (!t) return GPUMPI_ERR_TYPE;
+    *size = (int)t->size;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Type_get_extent(MPI_Datatype datatype, MPI_Aint* lb, MPI_Aint* extent) {
+    const TypeDesc* t = tdesc(datatype);
+    if (!t) return GPUMPI_ERR_TYPE;
+    *lb = 0;
+    *extent = t->extent;
+    return MPI_SUCCESS;
+}
+namespace {
+__device__ int new_type(const TypeDesc& d, MPI_Datatype* out) {
+    TypeDesc* slot;
+    int h = type_alloc(&slot);
+    if (h < 0) return GPUMPI_ERR_NO_MEM;
+    int in_use = 1;
+    *slot = d;
+    slot->in_use = in_use;
+    slot->committed = 0;
+    *out = (MPI_Datatype)h;
+    return MPI_SUCCESS;
+}
+}  // namespace
+__device__ int MPI_Type_contiguous(int count, MPI_Datatype oldtype, MPI_Datatype* newtype) {
+    const TypeDesc* o = tdesc(oldtype);
+    if (!o) return GPUMPI_ERR_TYPE;
+    TypeDesc d;
+    int rc = type_hvector_desc(count, 1, o->extent, o, &d);
+    if (rc) return rc;
+    d.base = o->base;
+    return new_type(d, newtype);
+}
+__device__ int MPI_Type_vector(int count, int blocklength, int stride, MPI_Datatype oldtype, MPI_Datatype* newtype) {
+    const TypeDesc* o = tdesc(oldtype);
+    if (!o) return GPUMPI_ERR_TYPE;
+    if (stride < 0) return GPUMPI_ERR_ARG;
+    TypeDesc d;
+    int rc = type_hvector_desc(count, blocklength, (long long)stride * o->extent, o, &d);
+    if (rc) return rc;
+    d.base = o->base;
+    return new_type(d, newtype);
+}
+__device__ int MPI_Type_create_hvector(int count, int blocklength, MPI_Aint stride, MPI_Datatype oldtype,
+                                       MPI_Datatype* newtype) {
+    const TypeDesc* o = tdesc(oldtype);
+    if (!o) return GPUMPI_ERR_TYPE;
+    if (stride < 0) return GPUMPI_ERR_ARG;
+    TypeDesc d;
+    int rc = type_hvector_desc(count, blocklength, stride, o, &d);
+    if (rc) return rc;
+    d.base = o->base;
+    return new_type(d, newtype);
+}
+__device__ int MPI_Type_create_subarray(int ndims, const int sizes[], const int subsizes[], const int starts[],
+                                        int order, MPI_Datatype oldtype, MPI_Datatype* newtype) {
+    const TypeDesc* o = tdesc(oldtype);
+    if (!o) return GPUMPI_ERR_TYPE;
+    TypeDesc d;
+    int rc = type_subarray_desc(ndims, sizes, subsizes, starts, order, o, &d);
+    if (rc) return rc;
+    d.base = o->base;
+    return new_type(d, newtype);
+}
+__device__ int MPI_Type_commit(MPI_Datatype* datatype) {
+    if (!datatype) return GPUMPI_ERR_TYPE;
+    if (!is_derived(*datatype)) return MPI_SUCCESS;
+    TypeDesc* t = (TypeDesc*)tdesc(*datatype);
+    if (!t) return GPUMPI_ERR_TYPE;
+    t->committed = 1;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Type_free(MPI_Datatype* datatype) {
+    if (!datatype || !is_derived(*datatype)) return GPUMPI_ERR_TYPE;
+    TypeDesc* t = (TypeDesc*)tdesc(*datatype);
+    if (t) t->in_use = 0;
+    *datatype = MPI_DATATYPE_NULL;
+    return MPI_SUCCESS;
+}
+
+// ------------------------------------------------------------------------------------------------
+// communicators and groups
+// ------------------------------------------------------------------------------------------------
+__device__ int MPI_Comm_size(MPI_Comm comm, int* size) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    *size = c->size;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Comm_rank(MPI_Comm comm, int* rank) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    *rank = comm_rank_of(c, me());
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Comm_split(MPI_Comm comm, int color, int key, MPI_Comm* newcomm) {
+    return comm_split_impl(comm, color, key, newcomm);
+}
+__device__ int MPI_Comm_dup(MPI_Comm comm, MPI_Comm* newcomm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_FAILURE;  // reference returns MPI_FAILURE for MPI_COMM_NULL (communicator.cu:118-121)
+    return comm_split_impl(comm, 0, comm_rank_of(c, me()), newcomm);
+}
+__device__ int MPI_Comm_create(MPI_Comm comm, MPI_Group group, MPI_Comm* newcomm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    int grank = MPI_UNDEFINED;
+    if (group) MPI_Group_rank(group, &grank);
+    return comm_split_impl(comm, grank == MPI_UNDEFINED ? GPUMPI_UNDEFINED : 0, grank, newcomm);
+}
+__device__ int MPI_Comm_free(MPI_Comm* comm) {
+    // communicator objects live in the run's arena and are reclaimed when the launch ends
+    if (comm) *comm = MPI_COMM_NULL;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Comm_group(MPI_Comm comm, MPI_Group* group) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (c->is_world) {
+        *group = MPI_GROUP_WORLD;
+        return MPI_SUCCESS;
+    }
+    MPI_Group g = group_new(c->size);
+    if (!g) return GPUMPI_ERR_NO_MEM;
+    for (int i = 0; i < c->size; i++) g->ranks[i] = c->members[i];
+    *group = g;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Group_incl(MPI_Group group, int n, const int ranks[], MPI_Group* newgroup) {
+    if (!group) return GPUMPI_ERR_ARG;
+    MPI_Group g = group_new(n);
+    if (!g) return GPUMPI_ERR_NO_MEM;
+    for (int i = 0; i < n; i++) {
+        if (ranks[i] < 0 || ranks[i] >= group->size) {
+            free(g);
+            return GPUMPI_ERR_RANK;
+        }
+        g->ranks[i] = group->ranks[ranks[i]];
+    }
+    *newgroup = g;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Group_range_incl(MPI_Group group, int n, int ranges[][3], MPI_Group* newgroup) {
+    if (!group) return GPUMPI_ERR_ARG;
+    int total = 0;
+    for (int i = 0; i < n; i++) {
+        int first = ranges[i][0], last = ranges[i][1], stride = ranges[i][2];
+        if (stride == 0) return GPUMPI_ERR_ARG;
+        int cnt = (last - first) / stride + 1;
+        if (cnt < 0) cnt = 0;
+        total += cnt;
+    }
+    MPI_Group g = group_new(total);
+    if (!g) return GPUMPI_ERR_NO_MEM;
+    int k = 0;
+    for (int i = 0; i < n; i++) {
+        int first = ranges[i][0], last = ranges[i][1], stride = ranges[i][2];
+        for (int r = first; stride > 0 ? r <= last : r >= last; r += stride) {
+            if (r < 0 || r >= group->size) {
+                free(g);
+                return GPUMPI_ERR_RANK;
+            }
+            g->ranks[k++] = group->ranks[r];
+        }
+    }
+    *newgroup = g;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Group_free(MPI_Group* group) {
+    if (group && *group && !(*group)->is_static) {
+        if (--(*group)->refcount <= 0) free(*group);
+    }
+    if (group) *group = MPI_GROUP_NULL;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Group_size(MPI_Group group, int* size) {
+    if (!group) return GPUMPI_ERR_ARG;
+    *size = group->size;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Group_rank(MPI_Group group, int* rank) {
+    // MPI semantics: MPI_UNDEFINED in *rank when the caller is not a member (the reference returns
+    // MPI_UNDEFINED as the function result and leaves *rank untouched, group.cu:110-122)
+    if (!group) return GPUMPI_ERR_ARG;
+    *rank = MPI_UNDEFINED;
+    for (int i = 0; i < group->size; i++)
+        if (group->ranks[i] == me()) {
+            *rank = i;
+            break;
+        }
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Group_translate_ranks(MPI_Group g1, int n, const int ranks1[], MPI_Group g2, int ranks2[]) {
+    if (!g1 || !g2) return GPUMPI_ERR_ARG;
+    for (int i = 0; i < n; i++) {
+        ranks2[i] = MPI_UNDEFINED;
+        if (ranks1[i] < 0 || ranks1[i] >= g1->size) return GPUMPI_ERR_RANK;
+        int w = g1->ranks[ranks1[i]];
+        for (int k = 0; k < g2->size; k++)
+            if (g2->ranks[k] == w) {
+                ranks2[i] = k;
+                break;
+            }
+    }
+    return MPI_SUCCESS;
+}
+
+// ------------------------------------------------------------------------------------------------
+// host side of this translation unit: install a runtime before a launch
+// ------------------------------------------------------------------------------------------------
+extern "C" cudaError_t gpumpi_internal_install(Runtime* d_rt, MPI_Comm world, MPI_Group gworld, MPI_Group gempty,
+                                                cudaStream_t stream) {
+    cudaError_t e;
+    if ((e = cudaMemcpyToSymbolAsync(g_rt, &d_rt, sizeof(d_rt), 0, cudaMemcpyHostToDevice, stream))) return e;
+    if ((e = cudaMemcpyToSymbolAsync(MPI_COMM_WORLD, &world, sizeof(world), 0, cudaMemcpyHostToDevice, stream))) return e;
+    if ((e = cudaMemcpyToSymbolAsync(MPI_GROUP_WORLD, &gworld, sizeof(gworld), 0, cudaMemcpyHostToDevice, stream))) return e;
+    if ((e = cudaMemcpyToSymbolAsync(MPI_GROUP_EMPTY, &gempty, sizeof(gempty), 0, cudaMemcpyHostToDevice, stream))) return e;
+    return cudaSuccess;
+}
+
+__device__ MPI_Op gpumpi_predefined_op(int code) {
+    return (code >= 0 && code < GPUMPI_NUM_PREDEFINED_OPS) ? &g_predef_ops[code] : nullptr;
+}
+
+namespace gpumpi {
+__device__ int mlp_select(int kind, long long bytes, int n, int dt, int op) {
+    (void)kind; (void)bytes; (void)n; (void)dt; (void)op;
+    return GPUMPI_VARIANT_DIRECT;
+}
+}  // namespace gpumpi

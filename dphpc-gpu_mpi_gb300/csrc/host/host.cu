@@ -1,0 +1,692 @@
+// host.cu — host side of libgpumpi.so: the C ABI of include/gpumpi.h.
+//
+// Replaces the reference's host launcher and harness (gpu_libs/gpu_main/main.cu:133-320,
+// tests/test_runner.cuh:26-86): option parsing, device-memory layout of all runtime state (no managed
+// memory), per-launch reset, cooperative launch of the persistent rank kernel with occupancy-derived
+// geometry, collection of device-side error records, and staging of host buffers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../programs/rt_kernel.cuh"
+#include "../runtime/rt_core.cuh"
+
+using gpumpi::Runtime;
+
+extern const gpumpi_prog_entry g_test_programs[];
+extern const int g_num_test_programs;
+extern const gpumpi_prog_entry g_hot_programs[];
+extern const int g_num_hot_programs;
+extern const gpumpi_prog_entry g_app_programs[];
+extern const int g_num_app_programs;
+
+extern "C" cudaError_t gpumpi_internal_install(Runtime* d_rt, MPI_Comm world, MPI_Group gworld, MPI_Group gempty,
+                                                cudaStream_t stream);
+
+namespace {
+
+std::atomic<long long> g_launches{0};
+std::string g_create_error;
+std::mutex g_limits_mu;
+bool g_limits_set = false;
+
+const gpumpi_prog_entry* find_program(int id) {
+    for (int i = 0; i < g_num_test_programs; i++)
+        if (g_test_programs[i].id == id) return &g_test_programs[i];
+    for (int i = 0; i < g_num_hot_programs; i++)
+        if (g_hot_programs[i].id == id) return &g_hot_programs[i];
+    for (int i = 0; i < g_num_app_programs; i++)
+        if (g_app_programs[i].id == id) return &g_app_programs[i];
+    return nullptr;
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// carve sub-allocations out of one region
+struct Carver {
+    size_t off = 0;
+    template <class T>
+    size_t take(size_t count, size_t align = 256) {
+        off = align_up(off, align);
+        size_t o = off;
+        off += sizeof(T) * count;
+        return o;
+    }
+};
+
+// small state re-uploaded before every launch (everything else in the control region is zeroed)
+struct FixedImage {
+    MPI_Comm_impl world;
+    gpumpi::Board board;
+    MPI_Group_impl gworld;
+    MPI_Group_impl gempty;
+    unsigned ctx_counter;
+};
+
+}  // namespace
+
+struct gpumpi_world {
+    gpumpi_config cfg;
+    int device = 0, sm_count = 0, max_blocks = 0;
+    int T = 0, nengines = 0, blocks_per_sm = 0;
+    Runtime h_rt;
+    Runtime* d_rt = nullptr;
+    char* d_ctrl = nullptr;
+    size_t ctrl_bytes = 0;
+    char* d_data = nullptr;
+    size_t data_bytes = 0;
+    FixedImage* d_fixed = nullptr;
+    FixedImage h_fixed;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0;
+    int variant_override = -1, selector_mode = 0;
+    signed char* d_table = nullptr;
+    float* d_mlp = nullptr;
+    // scratch for host-buffer staging
+    void* d_stage[8] = {};
+    size_t stage_bytes[8] = {};
+    // host mirrors of the error/exit records
+    std::vector<gpumpi::ErrorRecord> h_err;
+    std::vector<int> h_exit;
+};
+
+#define CK(expr)                                                                               \
+    do {                                                                                       \
+        cudaError_t e_ = (expr);                                                               \
+        if (e_ != cudaSuccess) {                                                               \
+            if (w) w->err = std::string(#expr) + ": " + cudaGetErrorString(e_);                \
+            return GPUMPI_ERR_CUDA;                                                            \
+        }                                                                                      \
+    } while (0)
+
+extern "C" {
+
+int gpumpi_config_init(gpumpi_config* c) {
+    if (!c) return GPUMPI_ERR_ARG;
+    memset(c, 0, sizeof(*c));
+    c->nranks = 1;
+    c->threads_per_block = 0;
+    c->engine_blocks = -1;
+    c->pending_requests = 1024;   // reference CLI default (main.cu:76)
+    c->mailbox_depth = 64;
+    c->unexpected_depth = 256;
+    c->eager_bytes = 1024;
+    c->max_types = 16;
+    c->posted_depth = 1024;
+    c->device = 0;
+    c->stack_bytes = 8192;
+    c->heap_bytes = 0;
+    c->arena_bytes = 64ull << 20;
+    c->copy_chunk_bytes = 256 << 10;
+    c->engine_min_bytes = 256 << 10;
+    c->timeout_s = 20.0;
+    c->trace_capacity = 0;
+    return GPUMPI_SUCCESS;
+}
+
+// ---gpumpi -n <ranks> -g <blocks> -b <threads> -s <stack> -p <heap> -e <pending>  (main.cu:70-78)
+int gpumpi_parse_args(int argc, char** argv, gpumpi_config* cfg) {
+    int pos = -1;
+    for (int i = 0; i < argc; i++)
+        if (strcmp(argv[i], "---gpumpi") == 0) pos = i;
+    if (pos < 0) return -1;
+    long long g = 0;
+    for (int i = pos + 1; i + 1 < argc; i += 2) {
+        const char* k = argv[i];
+        long long v = atoll(argv[i + 1]);
+        if (!strcmp(k, "-n") || !strcmp(k, "--numProcs")) cfg->nranks = (int)v;
+        else if (!strcmp(k, "-g") || !strcmp(k, "--blocksPerGrid")) g = v;
+        else if (!strcmp(k, "-b") || !strcmp(k, "--threadsPerBlock")) cfg->threads_per_block = (int)v;
+        else if (!strcmp(k, "-s") || !strcmp(k, "--stackSize")) cfg->stack_bytes = (size_t)v;
+        else if (!strcmp(k, "-p") || !strcmp(k, "--heapSize")) cfg->heap_bytes = (size_t)v;
+        else if (!strcmp(k, "-e") || !strcmp(k, "--pendingBufferSize")) cfg->pending_requests = (int)v;
+        else if (!strcmp(k, "--engines")) cfg->engine_blocks = (int)v;
+        else if (!strcmp(k, "--timeout")) cfg->timeout_s = atof(argv[i + 1]);
+    }
+    // a rank is a block here, so -g alone (the reference's blocks-per-grid) also gives the rank count
+    if (cfg->nranks <= 1 && g > 0) cfg->nranks = (int)g;
+    return pos;
+}
+
+const char* gpumpi_last_error(gpumpi_world* w) { return w ? w->err.c_str() : g_create_error.c_str(); }
+
+long long gpumpi_kernel_launches(void) { return g_launches.load(); }
+
+int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
+    gpumpi_world* w = nullptr;
+    if (!cfg_in || !out) return GPUMPI_ERR_ARG;
+    gpumpi_config cfg = *cfg_in;
+    if (cfg.nranks < 1) {
+        g_create_error = "nranks must be >= 1";
+        return GPUMPI_ERR_ARG;
+    }
+    if (cfg.eager_bytes < 16) cfg.eager_bytes = 16;
+    cfg.eager_bytes = (cfg.eager_bytes + 15) & ~15;
+    int md = 1;
+    while (md < cfg.mailbox_depth) md <<= 1;
+    cfg.mailbox_depth = md;
+    if (cfg.unexpected_depth < 1) cfg.unexpected_depth = 1;
+    if (cfg.posted_depth < 1) cfg.posted_depth = 1;
+    if (cfg.pending_requests < 1) cfg.pending_requests = 1;
+    if (cfg.max_types < 1) cfg.max_types = 1;
+    if (cfg.timeout_s <= 0) cfg.timeout_s = 20.0;
+
+    cudaError_t e = cudaSetDevice(cfg.device);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+        return GPUMPI_ERR_CUDA;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_limits_mu);
+        if (!g_limits_set) {
+            cudaDeviceSetLimit(cudaLimitStackSize, cfg.stack_bytes);
+            cudaDeviceSetLimit(cudaLimitMallocHeapSize, cfg.heap_bytes ? cfg.heap_bytes : (1ull << 30));
+            cudaGetLastError();
+            g_limits_set = true;
+        }
+    }
+    w = new gpumpi_world();
+    w->cfg = cfg;
+    w->device = cfg.device;
+    CK(cudaDeviceGetAttribute(&w->sm_count, cudaDevAttrMultiProcessorCount, cfg.device));
+    w->max_blocks = w->sm_count * 32;
+    const int n = cfg.nranks;
+    const int nb = w->max_blocks > n ? w->max_blocks : n;
+
+    // ---- control region: zeroed before every launch ----
+    Carver cc;
+    size_t o_ranks = cc.take<gpumpi::RankState>(n);
+    size_t o_ring = cc.take<gpumpi::Envelope>((size_t)n * cfg.mailbox_depth);
+    size_t o_types = cc.take<gpumpi::TypeDesc>((size_t)n * cfg.max_types);
+    size_t o_errors = cc.take<gpumpi::ErrorRecord>(nb);
+    size_t o_exit = cc.take<int>(n);
+    size_t o_arena_top = cc.take<unsigned long long>(1);
+    size_t o_done = cc.take<unsigned>(1);
+    size_t o_abort = cc.take<unsigned>(1);
+    size_t o_trace_count = cc.take<unsigned long long>(1);
+    w->ctrl_bytes = align_up(cc.off, 256);
+
+    // ---- data region ----
+    Carver dc;
+    size_t o_ring_pl = dc.take<unsigned char>((size_t)n * cfg.mailbox_depth * cfg.eager_bytes);
+    size_t o_uq = dc.take<gpumpi::UqEntry>((size_t)n * cfg.unexpected_depth);
+    size_t o_uq_pl = dc.take<unsigned char>((size_t)n * cfg.unexpected_depth * cfg.eager_bytes);
+    size_t o_uq_free = dc.take<int>((size_t)n * cfg.unexpected_depth);
+    size_t o_reqs = dc.take<MPI_Request_impl>((size_t)n * cfg.pending_requests);
+    size_t o_req_free = dc.take<int>((size_t)n * cfg.pending_requests);
+    size_t o_posted = dc.take<int>((size_t)n * cfg.posted_depth);
+    size_t o_tasks = dc.take<gpumpi::Task>(nb);
+    size_t o_wmembers = dc.take<int>(n);
+    size_t o_wslots = dc.take<gpumpi::CollSlot>(n);
+    size_t o_board_ring = dc.take<gpumpi::BoardEntry>(4096);
+    size_t o_trace = dc.take<gpumpi::TraceRec>(cfg.trace_capacity > 0 ? cfg.trace_capacity : 1);
+    size_t o_arena = dc.take<unsigned char>(cfg.arena_bytes);
+    w->data_bytes = align_up(dc.off, 256);
+
+    CK(cudaMalloc(&w->d_ctrl, w->ctrl_bytes));
+    CK(cudaMalloc(&w->d_data, w->data_bytes));
+    CK(cudaMalloc(&w->d_fixed, sizeof(FixedImage)));
+    CK(cudaMalloc(&w->d_rt, sizeof(Runtime)));
+    CK(cudaMemset(w->d_data, 0, w->data_bytes));
+    CK(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&w->ev0));
+    CK(cudaEventCreate(&w->ev1));
+
+    // identity member list of the world
+    std::vector<int> ident(n);
+    for (int i = 0; i < n; i++) ident[i] = i;
+    CK(cudaMemcpy(w->d_data + o_wmembers, ident.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+
+    Runtime& r = w->h_rt;
+    memset(&r, 0, sizeof(r));
+    r.nranks = n;
+    r.pending = cfg.pending_requests;
+    r.mbox_depth = cfg.mailbox_depth;
+    r.uq_depth = cfg.unexpected_depth;
+    r.eager = cfg.eager_bytes;
+    r.posted_cap = cfg.posted_depth;
+    r.max_types = cfg.max_types;
+    r.uq_payload_slots = cfg.unexpected_depth;
+    r.timeout_ns = (long long)(cfg.timeout_s * 1e9);
+    r.copy_chunk_bytes = cfg.copy_chunk_bytes;
+    r.engine_min_bytes = cfg.engine_min_bytes;
+    r.variant_override = -1;
+    r.selector_mode = 0;
+    r.trace_cap = cfg.trace_capacity;
+    r.trace_enabled = cfg.trace_capacity > 0;
+    r.ranks = (gpumpi::RankState*)(w->d_ctrl + o_ranks);
+    r.ring = (gpumpi::Envelope*)(w->d_ctrl + o_ring);
+    r.types = (gpumpi::TypeDesc*)(w->d_ctrl + o_types);
+    r.errors = (gpumpi::ErrorRecord*)(w->d_ctrl + o_errors);
+    r.exit_codes = (int*)(w->d_ctrl + o_exit);
+    r.arena_top = (unsigned long long*)(w->d_ctrl + o_arena_top);
+    r.ranks_done = (unsigned*)(w->d_ctrl + o_done);
+    r.abort_flag = (unsigned*)(w->d_ctrl + o_abort);
+    r.trace_count = (unsigned long long*)(w->d_ctrl + o_trace_count);
+    r.ring_payload = (unsigned char*)(w->d_data + o_ring_pl);
+    r.uq = (gpumpi::UqEntry*)(w->d_data + o_uq);
+    r.uq_payload = (unsigned char*)(w->d_data + o_uq_pl);
+    r.uq_free = (int*)(w->d_data + o_uq_free);
+    r.reqs = (MPI_Request_impl*)(w->d_data + o_reqs);
+    r.req_free = (int*)(w->d_data + o_req_free);
+    r.posted = (int*)(w->d_data + o_posted);
+    r.tasks = (gpumpi::Task*)(w->d_data + o_tasks);
+    r.world_members = (int*)(w->d_data + o_wmembers);
+    r.world_slots = (gpumpi::CollSlot*)(w->d_data + o_wslots);
+    r.trace = (gpumpi::TraceRec*)(w->d_data + o_trace);
+    r.arena = (unsigned char*)(w->d_data + o_arena);
+    r.arena_bytes = cfg.arena_bytes;
+    r.world = &w->d_fixed->world;
+    r.board = &w->d_fixed->board;
+    r.ctx_counter = &w->d_fixed->ctx_counter;
+
+    FixedImage& f = w->h_fixed;
+    memset(&f, 0, sizeof(f));
+    f.world.size = n;
+    f.world.ctx = 1;  // the reference's MPI_COMM_WORLD context (communicator.cu:60)
+    f.world.is_world = 1;
+    f.world.magic = gpumpi::COMM_MAGIC;
+    f.world.members = r.world_members;
+    f.world.rank_of = nullptr;
+    f.world.slots = r.world_slots;
+    f.board.ring = (gpumpi::BoardEntry*)(w->d_data + o_board_ring);
+    f.board.cap = 4096;
+    f.gworld.size = n;
+    f.gworld.ranks = r.world_members;
+    f.gworld.refcount = 1;
+    f.gworld.is_static = 1;
+    f.gempty.size = 0;
+    f.gempty.ranks = nullptr;
+    f.gempty.refcount = 1;
+    f.gempty.is_static = 1;
+    f.ctx_counter = 2;
+    w->h_err.resize(nb);
+    w->h_exit.resize(n);
+    *out = w;
+    return GPUMPI_SUCCESS;
+}
+
+int gpumpi_world_destroy(gpumpi_world* w) {
+    if (!w) return GPUMPI_SUCCESS;
+    cudaSetDevice(w->device);
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    cudaFree(w->d_ctrl);
+    cudaFree(w->d_data);
+    cudaFree(w->d_fixed);
+    cudaFree(w->d_rt);
+    cudaFree(w->d_table);
+    cudaFree(w->d_mlp);
+    for (auto& p : w->d_stage) cudaFree(p);
+    if (w->ev0) cudaEventDestroy(w->ev0);
+    if (w->ev1) cudaEventDestroy(w->ev1);
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+    return GPUMPI_SUCCESS;
+}
+
+int gpumpi_world_get_info(gpumpi_world* w, gpumpi_world_info* info) {
+    if (!w || !info) return GPUMPI_ERR_ARG;
+    info->nranks = w->cfg.nranks;
+    info->threads_per_block = w->T;
+    info->engine_blocks = w->nengines;
+    info->blocks_per_sm = w->blocks_per_sm;
+    info->sm_count = w->sm_count;
+    info->device = w->device;
+    info->device_bytes = w->ctrl_bytes + w->data_bytes;
+    return GPUMPI_SUCCESS;
+}
+
+int gpumpi_set_policy(gpumpi_world* w, int variant, int mode) {
+    if (!w) return GPUMPI_ERR_ARG;
+    w->variant_override = variant;
+    w->selector_mode = mode;
+    return GPUMPI_SUCCESS;
+}
+
+int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes) {
+    if (!w || !table || bytes != 2 * 32 * 16) return GPUMPI_ERR_ARG;
+    cudaSetDevice(w->device);
+    if (!w->d_table) CK(cudaMalloc(&w->d_table, bytes));
+    CK(cudaMemcpy(w->d_table, table, bytes, cudaMemcpyHostToDevice));
+    return GPUMPI_SUCCESS;
+}
+
+int gpumpi_set_mlp(gpumpi_world* w, const float* params, size_t count) {
+    if (!w || !params || count != GPUMPI_MLP_NPARAMS) return GPUMPI_ERR_ARG;
+    cudaSetDevice(w->device);
+    if (!w->d_mlp) CK(cudaMalloc(&w->d_mlp, sizeof(float) * count));
+    CK(cudaMemcpy(w->d_mlp, params, sizeof(float) * count, cudaMemcpyHostToDevice));
+    return GPUMPI_SUCCESS;
+}
+
+int gpumpi_read_trace(gpumpi_world* w, void* host_out, size_t cap, size_t* nout) {
+    if (!w || !nout) return GPUMPI_ERR_ARG;
+    unsigned long long cnt = 0;
+    CK(cudaMemcpy(&cnt, w->h_rt.trace_count, sizeof(cnt), cudaMemcpyDeviceToHost));
+    size_t n = std::min<size_t>({(size_t)cnt, cap, (size_t)std::max(0, w->cfg.trace_capacity)});
+    if (n && host_out) CK(cudaMemcpy(host_out, w->h_rt.trace, n * sizeof(gpumpi::TraceRec), cudaMemcpyDeviceToHost));
+    *nout = n;
+    return GPUMPI_SUCCESS;
+}
+
+double gpumpi_last_kernel_ms(gpumpi_world* w) { return w ? w->last_ms : 0.0; }
+
+// Picks the block size and engine count for program `pe` (largest of 256/128/64 threads whose
+// occupancy co-hosts all ranks, unless the configuration fixes it).
+static int choose_geometry(gpumpi_world* w, const gpumpi_prog_entry* pe) {
+    const int n = w->cfg.nranks;
+    int cands[3] = {256, 128, 64};
+    int chosen = 0, bps = 0;
+    for (int k = 0; k < 3; k++) {
+        int T = cands[k];
+        if (w->cfg.threads_per_block > 0 && T != w->cfg.threads_per_block) continue;
+        int b = 0;
+        CK(pe->occupancy(&b, T, 0));
+        if ((long long)b * w->sm_count >= n) {
+            chosen = T;
+            bps = b;
+            break;
+        }
+    }
+    if (!chosen && w->cfg.threads_per_block > 0) {
+        int b = 0;
+        CK(pe->occupancy(&b, w->cfg.threads_per_block, 0));
+        if ((long long)b * w->sm_count >= n) {
+            chosen = w->cfg.threads_per_block;
+            bps = b;
+        }
+    }
+    if (!chosen) {
+        int b = 0;
+        pe->occupancy(&b, 32, 0);
+        w->err = "cannot co-host " + std::to_string(n) + " rank blocks on " + std::to_string(w->sm_count) +
+                 " SMs (max " + std::to_string((long long)b * w->sm_count) + " blocks of 32 threads)";
+        return GPUMPI_ERR_LAUNCH;
+    }
+    int cap = bps * w->sm_count;
+    int eng = cap - n;
+    if (w->cfg.engine_blocks >= 0) eng = std::min(eng, w->cfg.engine_blocks);
+    w->T = chosen;
+    w->blocks_per_sm = bps;
+    w->nengines = std::max(0, eng);
+    return GPUMPI_SUCCESS;
+}
+
+int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params, void* stream_v, int sync) {
+    if (!w || !params) return GPUMPI_ERR_ARG;
+    const gpumpi_prog_entry* pe = find_program(program);
+    if (!pe) {
+        w->err = "unknown program " + std::to_string(program);
+        return GPUMPI_ERR_ARG;
+    }
+    CK(cudaSetDevice(w->device));
+    int rc = choose_geometry(w, pe);
+    if (rc) return rc;
+    cudaStream_t s = stream_v ? (cudaStream_t)stream_v : w->stream;
+    Runtime& r = w->h_rt;
+    r.T = w->T;
+    r.nengines = w->nengines;
+    r.variant_override = w->variant_override;
+    r.selector_mode = w->selector_mode;
+    r.tuned_table = w->d_table;
+    r.mlp_params = w->d_mlp;
+    CK(cudaMemsetAsync(w->d_ctrl, 0, w->ctrl_bytes, s));
+    CK(cudaMemcpyAsync(w->d_fixed, &w->h_fixed, sizeof(FixedImage), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(w->d_rt, &r, sizeof(Runtime), cudaMemcpyHostToDevice, s));
+    CK(gpumpi_internal_install(w->d_rt, &w->d_fixed->world, &w->d_fixed->gworld, &w->d_fixed->gempty, s));
+    CK(cudaEventRecord(w->ev0, s));
+    cudaError_t le = pe->launch(w->cfg.nranks + w->nengines, w->T, 0, s, params);
+    if (le != cudaSuccess) {
+        w->err = std::string("launch of ") + pe->name + ": " + cudaGetErrorString(le);
+        cudaGetLastError();
+        return GPUMPI_ERR_LAUNCH;
+    }
+    g_launches++;
+    CK(cudaEventRecord(w->ev1, s));
+    if (!sync) return GPUMPI_SUCCESS;
+    CK(cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+    w->last_ms = ms;
+    // collect device-side error records
+    const int nb = w->cfg.nranks + w->nengines;
+    CK(cudaMemcpy(w->h_err.data(), r.errors, sizeof(gpumpi::ErrorRecord) * nb, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(w->h_exit.data(), r.exit_codes, sizeof(int) * w->cfg.nranks, cudaMemcpyDeviceToHost));
+    for (int b = 0; b < nb; b++) {
+        const gpumpi::ErrorRecord& e = w->h_err[b];
+        if (e.code) {
+            char buf[256];
+            snprintf(buf, sizeof buf, "rank %d: MPI error %d (detail %d) at runtime line %d, info %lld", e.rank,
+                     e.code, e.detail, e.line, e.info);
+            w->err = buf;
+            return e.detail == GPUMPI_ERR_TIMEOUT ? GPUMPI_ERR_TIMEOUT : e.code;
+        }
+    }
+    for (int i = 0; i < w->cfg.nranks; i++)
+        if (w->h_exit[i] != 0) {
+            w->err = "rank " + std::to_string(i) + " returned " + std::to_string(w->h_exit[i]);
+            return w->h_exit[i];
+        }
+    return GPUMPI_SUCCESS;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// host-buffer staging and the hot-path entry points
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+bool is_device_ptr(const void* p) {
+    if (!p) return true;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// device buffer for slot k holding `bytes`; copies host data in when `in` is non-null
+int stage(gpumpi_world* w, int k, const void* host, size_t bytes, bool copy_in, cudaStream_t s, void** dev) {
+    if (w->stage_bytes[k] < bytes) {
+        cudaFree(w->d_stage[k]);
+        w->d_stage[k] = nullptr;
+        w->stage_bytes[k] = 0;
+        CK(cudaMalloc(&w->d_stage[k], bytes));
+        w->stage_bytes[k] = bytes;
+    }
+    if (copy_in && host && bytes) CK(cudaMemcpyAsync(w->d_stage[k], host, bytes, cudaMemcpyHostToDevice, s));
+    *dev = w->d_stage[k];
+    return GPUMPI_SUCCESS;
+}
+
+struct Buf {
+    const void* user;
+    size_t bytes;
+    bool in, out;
+    void* dev;
+    bool staged;
+};
+
+int run_with_buffers(gpumpi_world* w, int program, gpumpi_params& prm, Buf* bufs, int nbufs, int iters,
+                     uint64_t* iter_ns, void* stream_v) {
+    cudaStream_t s = stream_v ? (cudaStream_t)stream_v : w->stream;
+    CK(cudaSetDevice(w->device));
+    for (int k = 0; k < nbufs; k++) {
+        Buf& b = bufs[k];
+        b.staged = false;
+        b.dev = (void*)b.user;
+        if (b.user && !is_device_ptr(b.user)) {
+            int rc = stage(w, k, b.user, b.bytes, b.in, s, &b.dev);
+            if (rc) return rc;
+            b.staged = true;
+        }
+    }
+    uint64_t* d_ns = nullptr;
+    if (iter_ns && iters > 0) {
+        void* d;
+        int rc = stage(w, 7, nullptr, sizeof(uint64_t) * iters, false, s, &d);
+        if (rc) return rc;
+        d_ns = (uint64_t*)d;
+    }
+    for (int k = 0; k < nbufs; k++) prm.p[k] = bufs[k].dev;
+    prm.p[6] = d_ns;
+    int rc = gpumpi_run_program(w, program, &prm, s, 1);
+    for (int k = 0; k < nbufs; k++)
+        if (bufs[k].staged && bufs[k].out) CK(cudaMemcpyAsync((void*)bufs[k].user, bufs[k].dev, bufs[k].bytes, cudaMemcpyDeviceToHost, s));
+    if (d_ns) CK(cudaMemcpyAsync(iter_ns, d_ns, sizeof(uint64_t) * iters, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return rc;
+}
+
+size_t type_bytes(int dt) {
+    static const int sizes[GPUMPI_NUM_PREDEFINED_TYPES] = {1, 2, 4, 8, 8, 8, 1, 1, 2, 4, 8, 8, 4, 8, 8, 4, 1, 1,
+                                                           2, 4, 8, 1, 2, 4, 8, 8, 8, 16, 16, 1, 8, 8, 16, 16, 8, 16};
+    return (dt >= 0 && dt < GPUMPI_NUM_PREDEFINED_TYPES) ? (size_t)sizes[dt] : 0;
+}
+
+int coll_call(gpumpi_world* w, int kind, const void* sb, size_t sbytes, long long sstride, void* rb, size_t rbytes,
+              long long rstride, long long count, int dt, int op, int root, int iters, uint64_t* iter_ns,
+              void* stream, const int* mats[4], size_t mat_bytes) {
+    if (!w) return GPUMPI_ERR_ARG;
+    if (!type_bytes(dt)) {
+        w->err = "unsupported datatype for the host entry points";
+        return GPUMPI_ERR_TYPE;
+    }
+    gpumpi_params prm;
+    memset(&prm, 0, sizeof(prm));
+    prm.i[0] = kind;
+    prm.i[1] = count;
+    prm.i[2] = dt;
+    prm.i[3] = op;
+    prm.i[4] = root;
+    prm.i[5] = iters;
+    prm.i[6] = sstride;
+    prm.i[7] = rstride;
+    Buf b[6] = {{sb, sbytes, true, false, nullptr, false},
+                {rb, rbytes, kind == GPUMPI_COLL_BCAST, true, nullptr, false},
+                {mats ? mats[0] : nullptr, mat_bytes, true, false, nullptr, false},
+                {mats ? mats[1] : nullptr, mat_bytes, true, false, nullptr, false},
+                {mats ? mats[2] : nullptr, mat_bytes, true, false, nullptr, false},
+                {mats ? mats[3] : nullptr, mat_bytes, true, false, nullptr, false}};
+    return run_with_buffers(w, GPUMPI_P_COLL, prm, b, 6, iters, iter_ns, stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int gpumpi_test_run(gpumpi_world* w, int test, uint8_t* ok, int64_t* outi, double* outd) {
+    if (!w) return GPUMPI_ERR_ARG;
+    const int n = w->cfg.nranks;
+    gpumpi_params prm;
+    memset(&prm, 0, sizeof(prm));
+    std::vector<uint8_t> hok(n, 0);
+    std::vector<int64_t> hi((size_t)n * 64, 0);
+    std::vector<double> hd((size_t)n * 64, 0.0);
+    Buf b[3] = {{hok.data(), (size_t)n, true, true, nullptr, false},
+                {hi.data(), sizeof(int64_t) * n * 64, true, true, nullptr, false},
+                {hd.data(), sizeof(double) * n * 64, true, true, nullptr, false}};
+    int rc = run_with_buffers(w, test, prm, b, 3, 0, nullptr, nullptr);
+    if (ok) memcpy(ok, hok.data(), n);
+    if (outi) memcpy(outi, hi.data(), sizeof(int64_t) * n * 64);
+    if (outd) memcpy(outd, hd.data(), sizeof(double) * n * 64);
+    return rc;
+}
+
+int gpumpi_allreduce(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long count, int dt, int op, int iters,
+                     uint64_t* iter_ns, void* stream) {
+    if (!w) return GPUMPI_ERR_ARG;
+    size_t per = (size_t)count * type_bytes(dt);
+    size_t all = per * w->cfg.nranks;
+    return coll_call(w, GPUMPI_COLL_ALLREDUCE, sendbuf, all, (long long)per, recvbuf, all, (long long)per, count, dt,
+                     op, 0, iters, iter_ns, stream, nullptr, 0);
+}
+
+int gpumpi_reduce(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long count, int dt, int op, int root,
+                  int iters, uint64_t* iter_ns, void* stream) {
+    if (!w) return GPUMPI_ERR_ARG;
+    size_t per = (size_t)count * type_bytes(dt);
+    size_t all = per * w->cfg.nranks;
+    // recvbuf is rank-major too (only root's slot is written)
+    return coll_call(w, GPUMPI_COLL_REDUCE, sendbuf, all, (long long)per, recvbuf, all, (long long)per, count, dt, op,
+                     root, iters, iter_ns, stream, nullptr, 0);
+}
+
+int gpumpi_bcast(gpumpi_world* w, void* buf, long long count, int dt, int root, int iters, uint64_t* iter_ns,
+                 void* stream) {
+    if (!w) return GPUMPI_ERR_ARG;
+    size_t per = (size_t)count * type_bytes(dt);
+    size_t all = per * w->cfg.nranks;
+    return coll_call(w, GPUMPI_COLL_BCAST, nullptr, 0, 0, buf, all, (long long)per, count, dt, 0, root, iters, iter_ns,
+                     stream, nullptr, 0);
+}
+
+int gpumpi_alltoall(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long cpp, int dt, int iters,
+                    uint64_t* iter_ns, void* stream) {
+    if (!w) return GPUMPI_ERR_ARG;
+    size_t per = (size_t)cpp * type_bytes(dt) * w->cfg.nranks;
+    size_t all = per * w->cfg.nranks;
+    return coll_call(w, GPUMPI_COLL_ALLTOALL, sendbuf, all, (long long)per, recvbuf, all, (long long)per, cpp, dt, 0,
+                     0, iters, iter_ns, stream, nullptr, 0);
+}
+
+int gpumpi_allgather(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long count, int dt, int iters,
+                     uint64_t* iter_ns, void* stream) {
+    if (!w) return GPUMPI_ERR_ARG;
+    size_t per = (size_t)count * type_bytes(dt);
+    return coll_call(w, GPUMPI_COLL_ALLGATHER, sendbuf, per * w->cfg.nranks, (long long)per, recvbuf,
+                     per * w->cfg.nranks * w->cfg.nranks, (long long)(per * w->cfg.nranks), count, dt, 0, 0, iters,
+                     iter_ns, stream, nullptr, 0);
+}
+
+int gpumpi_alltoallv(gpumpi_world* w, const void* sendbuf, long long send_stride, const int* sendcounts,
+                     const int* sdispls, void* recvbuf, long long recv_stride, const int* recvcounts, const int* rdispls,
+                     int dt, int iters, uint64_t* iter_ns, void* stream) {
+    if (!w) return GPUMPI_ERR_ARG;
+    const int* mats[4] = {sendcounts, sdispls, recvcounts, rdispls};
+    size_t n = (size_t)w->cfg.nranks;
+    return coll_call(w, GPUMPI_COLL_ALLTOALLV, sendbuf, (size_t)send_stride * n, send_stride, recvbuf,
+                     (size_t)recv_stride * n, recv_stride, 0, dt, 0, 0, iters, iter_ns, stream, mats,
+                     sizeof(int) * n * n);
+}
+
+int gpumpi_pingpong(gpumpi_world* w, void* bufs, long long bytes, int pairs, int iters, int nonblocking,
+                    uint64_t* iter_ns, void* stream) {
+    if (!w) return GPUMPI_ERR_ARG;
+    gpumpi_params prm;
+    memset(&prm, 0, sizeof(prm));
+    prm.i[0] = bytes;
+    prm.i[1] = iters;
+    prm.i[2] = nonblocking;
+    prm.i[3] = pairs;
+    prm.i[4] = bytes;
+    Buf b[1] = {{bufs, (size_t)bytes * w->cfg.nranks, true, true, nullptr, false}};
+    return run_with_buffers(w, GPUMPI_P_PINGPONG, prm, b, 1, iters, iter_ns, stream);
+}
+
+int gpumpi_ring(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long bytes, int iters, int nonblocking,
+                uint64_t* iter_ns, void* stream) {
+    if (!w) return GPUMPI_ERR_ARG;
+    gpumpi_params prm;
+    memset(&prm, 0, sizeof(prm));
+    prm.i[0] = bytes;
+    prm.i[1] = iters;
+    prm.i[2] = nonblocking;
+    prm.i[4] = bytes;
+    Buf b[2] = {{sendbuf, (size_t)bytes * w->cfg.nranks, true, false, nullptr, false},
+                {recvbuf, (size_t)bytes * w->cfg.nranks, false, true, nullptr, false}};
+    return run_with_buffers(w, GPUMPI_P_RING, prm, b, 2, iters, iter_ns, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,671 @@
+// prog_tests.cu — device programs that mirror the reference's GPU tests.
+//
+// Each program does what the corresponding reference test does (same ranks, same buffers on the
+// rank's stack or device heap, same values), written against the MPI surface instead of the
+// reference's CudaMPI:: internals, and reports per rank: ok flag (the reference's REQUIRE(ok[i])),
+// plus the received values so the host can compare them with the golden vectors.
+//   p[0] = uint8 ok[nranks], p[1] = int64 outi[nranks*64], p[2] = double outd[nranks*64]
+#include "rt_kernel.cuh"
+
+namespace {
+
+__device__ __forceinline__ int wrank() {
+    int r = -1;
+    MPI_Comm_rank(MPI_COMM_WORLD, &r);
+    return r;
+}
+__device__ __forceinline__ unsigned char* okp(const gpumpi_params& p) { return (unsigned char*)p.p[0]; }
+__device__ __forceinline__ long long* outi(const gpumpi_params& p, int r) { return (long long*)p.p[1] + (long long)r * 64; }
+__device__ __forceinline__ double* outd(const gpumpi_params& p, int r) { return (double*)p.p[2] + (long long)r * 64; }
+
+// tests/cuda_mpi_test.cu:5-36
+struct SingleInt {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        bool ok = true;
+        if (rank == 0) {
+            int x = 3456;
+            MPI_Request r;
+            ok = MPI_Isend(&x, 1, MPI_INT, 1, 15, MPI_COMM_WORLD, &r) == MPI_SUCCESS;
+            ok = ok && MPI_Wait(&r, MPI_STATUS_IGNORE) == MPI_SUCCESS;
+        } else if (rank == 1) {
+            int x = 0;
+            MPI_Request r;
+            MPI_Irecv(&x, 1, MPI_INT, 0, 15, MPI_COMM_WORLD, &r);
+            MPI_Wait(&r, MPI_STATUS_IGNORE);
+            ok = x == 3456;
+            outi(p, rank)[0] = x;
+        }
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// tests/cuda_mpi_test.cu:38-73
+struct TransferArray {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        bool ok = true;
+        if (rank == 0) {
+            int x[16];
+            for (int i = 0; i < 16; i++) x[i] = i;
+            MPI_Send(x, 16, MPI_INT, 1, 15, MPI_COMM_WORLD);
+        } else if (rank == 1) {
+            int x[16] = {};
+            MPI_Recv(x, 16, MPI_INT, 0, 15, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
+            for (int i = 0; i < 16; i++) {
+                ok = ok && x[i] == i;
+                outi(p, rank)[i] = x[i];
+            }
+        }
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// tests/cuda_mpi_test.cu:75-127 — both ranks post the receive, then the send
+struct SendRecv {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        int other = 1 - rank;
+        int x[16], y[16] = {};
+        for (int i = 0; i < 16; i++) x[i] = rank == 0 ? i : -i;
+        MPI_Request rq[2];
+        MPI_Irecv(y, 16, MPI_INT, other, 15, MPI_COMM_WORLD, &rq[0]);
+        MPI_Isend(x, 16, MPI_INT, other, 15, MPI_COMM_WORLD, &rq[1]);
+        MPI_Wait(&rq[0], MPI_STATUS_IGNORE);
+        bool ok = true;
+        for (int i = 0; i < 16; i++) {
+            ok = ok && y[i] == (rank == 0 ? -i : i);
+            outi(p, rank)[i] = y[i];
+        }
+        MPI_Wait(&rq[1], MPI_STATUS_IGNORE);
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// tests/cuda_mpi_test.cu:129-174 — five messages of 1,2,4,8,16 ints, tags 10..14, one buffer
+struct RepeatSendRecv {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        int other = (rank + 1) % 2;
+        int local[16], remote[16] = {};
+        for (int i = 0; i < 16; i++) local[i] = (rank + 1) * i;
+        MPI_Request s[5], r[5];
+        for (int i = 0; i < 5; i++) {
+            MPI_Isend(local, 1 << i, MPI_INT, other, 10 + i, MPI_COMM_WORLD, &s[i]);
+            MPI_Irecv(remote, 1 << i, MPI_INT, other, 10 + i, MPI_COMM_WORLD, &r[i]);
+        }
+        for (int i = 0; i < 5; i++) {
+            MPI_Wait(&s[i], MPI_STATUS_IGNORE);
+            MPI_Wait(&r[i], MPI_STATUS_IGNORE);
+        }
+        bool ok = true;
+        for (int i = 0; i < 16; i++) {
+            ok = ok && remote[i] == (other + 1) * i;
+            outi(p, rank)[i] = remote[i];
+        }
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// tests/cuda_mpi_test.cu:177-233 — 3-rank ring, both directions, 5 sizes
+struct NetworkFlood {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        const int n = 3;
+        int next = (rank + 1) % n, prev = (rank + n - 1) % n;
+        int local[16], prevd[16] = {}, nextd[16] = {};
+        for (int i = 0; i < 16; i++) local[i] = (rank + 1) * i;
+        MPI_Request sn[5], rn[5], sp[5], rp[5];
+        for (int i = 0; i < 5; i++) {
+            int tag = 10 + i;
+            MPI_Isend(local, 1 << i, MPI_INT, next, tag, MPI_COMM_WORLD, &sn[i]);
+            MPI_Irecv(nextd, 1 << i, MPI_INT, next, tag, MPI_COMM_WORLD, &rn[i]);
+            MPI_Isend(local, 1 << i, MPI_INT, prev, tag, MPI_COMM_WORLD, &sp[i]);
+            MPI_Irecv(prevd, 1 << i, MPI_INT, prev, tag, MPI_COMM_WORLD, &rp[i]);
+        }
+        for (int i = 0; i < 5; i++) {
+            MPI_Wait(&rp[i], MPI_STATUS_IGNORE);
+            MPI_Wait(&sn[i], MPI_STATUS_IGNORE);
+            MPI_Wait(&sp[i], MPI_STATUS_IGNORE);
+            MPI_Wait(&rn[i], MPI_STATUS_IGNORE);
+        }
+        bool ok = true;
+        for (int i = 0; i < 16; i++) {
+            ok = ok && prevd[i] == (prev + 1) * i && nextd[i] == (next + 1) * i;
+            outi(p, rank)[i] = prevd[i];
+            outi(p, rank)[16 + i] = nextd[i];
+        }
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// tests/cuda_mpi_test.cu:235-317 — 10 ranks x 20 repeats x 16 ints to every other rank, heap buffers
+struct AllToAll {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        int n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        const int reps = 20, ds = 16;
+        int* local = (int*)malloc(sizeof(int) * ds * reps * n);
+        int* remote = (int*)malloc(sizeof(int) * ds * reps * n);
+        MPI_Request* sreq = (MPI_Request*)malloc(sizeof(MPI_Request) * reps * n);
+        MPI_Request* rreq = (MPI_Request*)malloc(sizeof(MPI_Request) * reps * n);
+        bool ok = local && remote && sreq && rreq;
+        if (!ok) {
+            okp(p)[rank] = 0;
+            return MPI_ERR_NO_MEM;
+        }
+        for (int r = 0; r < n; r++)
+            for (int k = 0; k < reps; k++)
+                for (int i = 0; i < ds; i++) {
+                    int idx = i + k * ds + r * ds * reps;
+                    local[idx] = i * k * r;
+                    remote[idx] = 0;
+                }
+        for (int k = 0; k < reps; k++)
+            for (int r = 0; r < n; r++)
+                if (r != rank) {
+                    int idx = k * ds + r * ds * reps;
+                    MPI_Isend(local + idx, ds, MPI_INT, r, 15, MPI_COMM_WORLD, &sreq[r + k * n]);
+                    MPI_Irecv(remote + idx, ds, MPI_INT, r, 15, MPI_COMM_WORLD, &rreq[r + k * n]);
+                }
+        for (int k = 0; k < reps; k++)
+            for (int r = 0; r < n; r++)
+                if (r != rank) {
+                    MPI_Wait(&sreq[r + k * n], MPI_STATUS_IGNORE);
+                    MPI_Wait(&rreq[r + k * n], MPI_STATUS_IGNORE);
+                }
+        long long bad = 0, sum = 0;
+        for (int k = 0; k < reps; k++)
+            for (int r = 0; r < n; r++)
+                if (r != rank)
+                    for (int i = 0; i < ds; i++) {
+                        int v = remote[i + k * ds + r * ds * reps];
+                        sum += v;
+                        if (v != i * k * rank) bad++;
+                    }
+        outi(p, rank)[0] = bad;
+        outi(p, rank)[1] = sum;
+        okp(p)[rank] = bad == 0;
+        free(local);
+        free(remote);
+        free(sreq);
+        free(rreq);
+        return MPI_Finalize();
+    }
+};
+
+// tests/collectives_test.cu:6-54 — MPI_Reduce int16 PROD on 5 ranks, 14 stack elements
+struct ReduceInt16Prod {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        short buf[14], rb[14] = {};
+        for (int i = 0; i < 14; i++) buf[i] = (short)((rank + 1) * (i + 1));
+        int rc = MPI_Reduce(buf, rb, 14, MPI_INT16_T, MPI_PROD, 0, MPI_COMM_WORLD);
+        bool ok = rc == MPI_SUCCESS;
+        if (rank == 0) {
+            for (int i = 0; i < 14; i++) {
+                short e = 1;
+                for (int r = 0; r < n; r++) e = (short)(e * (short)((r + 1) * (i + 1)));
+                ok = ok && rb[i] == e;
+                outi(p, rank)[i] = rb[i];
+            }
+        }
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// tests/collectives_test.cu:57-98 — MPI_Allreduce fp64 SUM on 7 ranks, 17 stack elements
+struct AllreduceF64 {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        double buf[17], rb[17] = {};
+        for (int i = 0; i < 17; i++) buf[i] = (double)((rank + 1) * (i + 1));
+        int rc = MPI_Allreduce(buf, rb, 17, MPI_DOUBLE, MPI_SUM, MPI_COMM_WORLD);
+        bool ok = rc == MPI_SUCCESS;
+        for (int i = 0; i < 17; i++) {
+            double e = 0;
+            for (int r = 0; r < n; r++) e += (double)((r + 1) * (i + 1));
+            ok = ok && fabs(rb[i] - e) <= 1e-5;
+            outd(p, rank)[i] = rb[i];
+        }
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// tests/collectives_test.cu:100-141 — MPI_Allgather 7 ranks x 7 ints (device-heap vectors there)
+struct Allgather {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        const int bs = 7;
+        int* buf = (int*)malloc(sizeof(int) * bs);
+        int* rb = (int*)malloc(sizeof(int) * bs * n);
+        for (int i = 0; i < bs; i++) buf[i] = (rank + 1) * (i + 1);
+        for (int i = 0; i < bs * n; i++) rb[i] = 0;
+        int rc = MPI_Allgather(buf, bs, MPI_INT, rb, bs, MPI_INT, MPI_COMM_WORLD);
+        bool ok = rc == MPI_SUCCESS;
+        for (int r = 0; r < n; r++)
+            for (int i = 0; i < bs; i++) {
+                ok = ok && rb[r * bs + i] == (r + 1) * (i + 1);
+                if (r * bs + i < 64) outi(p, rank)[r * bs + i] = rb[r * bs + i];
+            }
+        okp(p)[rank] = ok;
+        free(buf);
+        free(rb);
+        return MPI_Finalize();
+    }
+};
+
+// tests/collectives_test.cu:144-196 — MPI_Scatter root 2, 4 ints per rank
+struct Scatter {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        const int root = 2, bs = 4;
+        int* sb = (int*)malloc(sizeof(int) * bs * n);
+        int* rb = (int*)malloc(sizeof(int) * bs);
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < bs; i++) sb[i + j * bs] = rank == root ? j : -2;
+        for (int i = 0; i < bs; i++) rb[i] = -1;
+        int rc = MPI_Scatter(sb, bs, MPI_INT, rb, bs, MPI_INT, root, MPI_COMM_WORLD);
+        bool ok = rc == MPI_SUCCESS;
+        for (int i = 0; i < bs; i++) {
+            ok = ok && rb[i] == rank;
+            outi(p, rank)[i] = rb[i];
+        }
+        okp(p)[rank] = ok;
+        free(sb);
+        free(rb);
+        return MPI_Finalize();
+    }
+};
+
+// tests/collectives_test.cu:199-288 — MPI_Scatterv root 2, sizes i+1, packed displacements
+struct Scatterv {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        const int root = 2;
+        int* sizes = (int*)malloc(sizeof(int) * n);
+        int* displs = (int*)malloc(sizeof(int) * n);
+        for (int i = 0; i < n; i++) {
+            sizes[i] = i + 1;
+            displs[i] = i == 0 ? 0 : displs[i - 1] + sizes[i - 1];
+        }
+        int total = displs[n - 1] + sizes[n - 1];
+        int* sb = (int*)malloc(sizeof(int) * total);
+        int* rb = (int*)malloc(sizeof(int) * sizes[rank]);
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < sizes[j]; i++) sb[displs[j] + i] = rank == root ? j : -2;
+        for (int i = 0; i < sizes[rank]; i++) rb[i] = -1;
+        int rc = MPI_Scatterv(sb, sizes, displs, MPI_INT, rb, sizes[rank], MPI_INT, root, MPI_COMM_WORLD);
+        MPI_Barrier(MPI_COMM_WORLD);
+        bool ok = rc == MPI_SUCCESS;
+        for (int i = 0; i < sizes[rank]; i++) {
+            ok = ok && rb[i] == rank;
+            outi(p, rank)[i] = rb[i];
+        }
+        okp(p)[rank] = ok;
+        free(sizes);
+        free(displs);
+        free(sb);
+        free(rb);
+        return MPI_Finalize();
+    }
+};
+
+// tests/communicator_test.cu:5-25
+struct CommRank {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        okp(p)[rank] = rank == gpumpi_world_rank();
+        outi(p, rank)[0] = rank;
+        return MPI_Finalize();
+    }
+};
+
+// tests/communicator_test.cu:27-90 — three dup'ed communicators, same tag, crossing order
+struct CommDup {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        MPI_Comm c1, c2, c3;
+        MPI_Comm_dup(MPI_COMM_WORLD, &c1);
+        MPI_Comm_dup(MPI_COMM_WORLD, &c2);
+        MPI_Comm_dup(c2, &c3);
+        MPI_Request rq[3] = {nullptr, nullptr, nullptr};
+        short data[30] = {};
+        if (rank == 0) {
+            for (int i = 0; i < 30; i++) data[i] = (short)(i + 1);
+            MPI_Isend(data + 0, 10, MPI_INT16_T, 1, 17, c1, &rq[0]);
+            MPI_Irecv(data + 10, 10, MPI_INT16_T, 1, 17, c2, &rq[1]);
+            MPI_Isend(data + 20, 10, MPI_INT16_T, 1, 17, c3, &rq[2]);
+        } else if (rank == 1) {
+            for (int i = 0; i < 30; i++) data[i] = (short)-(i + 1);
+            MPI_Irecv(data + 20, 10, MPI_INT16_T, 0, 17, c3, &rq[2]);
+            MPI_Irecv(data + 0, 10, MPI_INT16_T, 0, 17, c1, &rq[0]);
+            MPI_Isend(data + 10, 10, MPI_INT16_T, 0, 17, c2, &rq[1]);
+        }
+        MPI_Status st[3];
+        MPI_Waitall(3, rq, st);
+        bool ok = true;
+        if (rank == 0) {
+            for (int i = 10; i < 20; i++) ok = ok && data[i] == -(i + 1);
+        } else if (rank == 1) {
+            for (int i = 0; i < 10; i++) ok = ok && data[i] == i + 1;
+            for (int i = 20; i < 30; i++) ok = ok && data[i] == i + 1;
+        }
+        for (int i = 0; i < 30; i++) outi(p, rank)[i] = data[i];
+        MPI_Comm_free(&c1);
+        MPI_Comm_free(&c2);
+        MPI_Comm_free(&c3);
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// tests/communicator_test.cu:93-152 — Comm_split colours/keys over 10 ranks
+struct CommSplit {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        int color, key;
+        if (rank < 3) { color = 0; key = rank; }
+        else if (rank < 6) { color = 1; key = 6 - rank; }
+        else if (rank < 9) { color = 2; key = 1; }
+        else { color = 2; key = 0; }
+        MPI_Comm c;
+        int rc = MPI_Comm_split(MPI_COMM_WORLD, color, key, &c);
+        int nr = -1, ns = -1;
+        MPI_Comm_rank(c, &nr);
+        MPI_Comm_size(c, &ns);
+        bool ok = rc == MPI_SUCCESS;
+        if (rank < 3) ok = ok && nr == rank && ns == 3;
+        else if (rank < 6) ok = ok && nr == 5 - rank && ns == 3;
+        else if (rank < 9) ok = ok && nr == rank - 5 && ns == 4;
+        else ok = ok && nr == 0 && ns == 4;
+        // traffic on the new communicator uses its ranks (the reference sends to global indices, H1)
+        int token = rank, got = -1;
+        int next = (nr + 1) % ns, prev = (nr + ns - 1) % ns;
+        MPI_Sendrecv(&token, 1, MPI_INT, next, 5, &got, 1, MPI_INT, prev, 5, c, MPI_STATUS_IGNORE);
+        int expect_prev_world = -1;
+        // world rank of my predecessor in the new communicator
+        MPI_Group g, wg;
+        MPI_Comm_group(c, &g);
+        MPI_Comm_group(MPI_COMM_WORLD, &wg);
+        MPI_Group_translate_ranks(g, 1, &prev, wg, &expect_prev_world);
+        ok = ok && got == expect_prev_world;
+        MPI_Group_free(&g);
+        MPI_Group_free(&wg);
+        outi(p, rank)[0] = nr;
+        outi(p, rank)[1] = ns;
+        outi(p, rank)[2] = got;
+        MPI_Comm_free(&c);
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// tests/sample_test.cu
+struct Sample {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        okp(p)[wrank()] = 1;
+        return MPI_Finalize();
+    }
+};
+
+// ---- beyond the reference's tests ----
+
+// wildcard receives posted after the send (the reference matches them only when posted first,
+// cuda_mpi.cu:300-303), non-overtaking order, Iprobe/Probe/Get_count, Sendrecv, MPI_PROC_NULL,
+// Ssend, truncation error.  Ranks: >= 3.
+struct P2PMatching {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        bool ok = true;
+        long long* o = outi(p, rank);
+        if (rank == 1 || rank == 2) {
+            // 4 messages each, alternating tags; payload encodes (sender, sequence)
+            for (int k = 0; k < 4; k++) {
+                int v = rank * 100 + k;
+                MPI_Send(&v, 1, MPI_INT, 0, 7 + (k & 1), MPI_COMM_WORLD);
+            }
+        }
+        MPI_Barrier(MPI_COMM_WORLD);  // all small sends are now queued at rank 0
+        if (rank == 1 || rank == 2) {
+            int* big = (int*)malloc(sizeof(int) * 300);
+            for (int i = 0; i < 300; i++) big[i] = rank * 1000 + i;
+            int rc = MPI_Ssend(big, 300, MPI_INT, 0, 99, MPI_COMM_WORLD);
+            ok = ok && rc == 0;
+            free(big);
+        } else if (rank == 0) {
+            // probe then receive with wildcards: per sender, values must arrive in send order
+            int last[3] = {-1, -1, -1};
+            for (int m = 0; m < 8; m++) {
+                MPI_Status st;
+                int rc = MPI_Probe(MPI_ANY_SOURCE, MPI_ANY_TAG, MPI_COMM_WORLD, &st);
+                int cnt = -1;
+                MPI_Get_count(&st, MPI_INT, &cnt);
+                ok = ok && rc == 0 && cnt == 1;
+                int v = -1;
+                MPI_Status st2;
+                MPI_Recv(&v, 1, MPI_INT, st.MPI_SOURCE, st.MPI_TAG, MPI_COMM_WORLD, &st2);
+                int s = v / 100, k = v % 100;
+                ok = ok && s == st2.MPI_SOURCE && (s == 1 || s == 2) && k > last[s] && st2.MPI_TAG == 7 + (k & 1);
+                if (s == 1 || s == 2) last[s] = k;
+                o[m] = v;
+            }
+            ok = ok && last[1] == 3 && last[2] == 3;
+            // synchronous (rendezvous) sends; the second one is truncated on purpose
+            int* big = (int*)malloc(sizeof(int) * 300);
+            MPI_Status st;
+            int rc = MPI_Recv(big, 300, MPI_INT, 1, 99, MPI_COMM_WORLD, &st);
+            ok = ok && rc == 0 && big[0] == 1000 && big[299] == 1299;
+            rc = MPI_Recv(big, 10, MPI_INT, 2, 99, MPI_COMM_WORLD, &st);
+            ok = ok && rc == MPI_ERR_TRUNCATE && big[9] == 2009 && big[10] == 1010;
+            o[8] = rc;
+            free(big);
+        }
+        // Sendrecv ring + PROC_NULL
+        int tok = rank * 7, got = -1;
+        MPI_Sendrecv(&tok, 1, MPI_INT, (rank + 1) % n, 3, &got, 1, MPI_INT, (rank + n - 1) % n, 3, MPI_COMM_WORLD,
+                     MPI_STATUS_IGNORE);
+        ok = ok && got == ((rank + n - 1) % n) * 7;
+        MPI_Status stn;
+        int dummy = 5;
+        int rc = MPI_Recv(&dummy, 1, MPI_INT, MPI_PROC_NULL, 0, MPI_COMM_WORLD, &stn);
+        ok = ok && rc == 0 && dummy == 5 && stn.MPI_SOURCE == MPI_PROC_NULL;
+        rc = MPI_Send(&dummy, 1, MPI_INT, MPI_PROC_NULL, 0, MPI_COMM_WORLD);
+        ok = ok && rc == 0;
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// Failure detection without a GPU fault: rank 0 waits for a message nobody sends.  The bounded wait
+// must end with MPI_ERR_OTHER; the other ranks skip the final barrier so the kernel ends.
+struct Timeout {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        if (rank == 0) {
+            int x = 0;
+            int rc = MPI_Recv(&x, 1, MPI_INT, 1, 1234, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
+            outi(p, rank)[0] = rc;
+            okp(p)[rank] = rc == MPI_ERR_OTHER;
+        } else {
+            okp(p)[rank] = 1;
+        }
+        return 0;
+    }
+};
+
+// Derived datatypes: vector columns, subarray faces and contiguous blocks sent between ranks 0 and 1,
+// checked element by element (results also copied out for a host-side check).
+struct Datatypes {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank();
+        bool ok = true;
+        double* grid = (double*)malloc(sizeof(double) * 6 * 6 * 6);
+        double* recv = (double*)malloc(sizeof(double) * 64);
+        for (int i = 0; i < 216; i++) grid[i] = rank * 1000.0 + i;
+        for (int i = 0; i < 64; i++) recv[i] = -1;
+        // column of a 6x6 matrix: vector(6, 1, 6)
+        MPI_Datatype col, face, blk;
+        MPI_Type_vector(6, 1, 6, MPI_DOUBLE, &col);
+        MPI_Type_commit(&col);
+        int sizes[3] = {6, 6, 6}, subs[3] = {4, 4, 1}, starts[3] = {1, 1, 4};
+        MPI_Type_create_subarray(3, sizes, subs, starts, MPI_ORDER_C, MPI_DOUBLE, &face);
+        MPI_Type_commit(&face);
+        MPI_Type_contiguous(5, MPI_DOUBLE, &blk);
+        MPI_Type_commit(&blk);
+        int sz = 0;
+        MPI_Type_size(face, &sz);
+        ok = ok && sz == 16 * 8;
+        if (rank == 0) {
+            MPI_Send(grid + 2, 1, col, 1, 1, MPI_COMM_WORLD);     // column 2 of the first 6x6 plane
+            MPI_Send(grid, 1, face, 1, 2, MPI_COMM_WORLD);        // x = 4 face of the interior
+            MPI_Send(grid + 100, 2, blk, 1, 3, MPI_COMM_WORLD);   // 10 contiguous doubles
+            // typed receive side: 16 contiguous doubles scattered into a face of my grid
+            double packed[16];
+            for (int i = 0; i < 16; i++) packed[i] = 5000.0 + i;
+            MPI_Send(packed, 16, MPI_DOUBLE, 1, 4, MPI_COMM_WORLD);
+        } else if (rank == 1) {
+            MPI_Status st;
+            MPI_Recv(recv, 6, MPI_DOUBLE, 0, 1, MPI_COMM_WORLD, &st);
+            for (int i = 0; i < 6; i++) ok = ok && recv[i] == 2 + 6 * i;
+            MPI_Recv(recv + 6, 16, MPI_DOUBLE, 0, 2, MPI_COMM_WORLD, &st);
+            for (int z = 0; z < 4; z++)
+                for (int y = 0; y < 4; y++) ok = ok && recv[6 + z * 4 + y] == (z + 1) * 36 + (y + 1) * 6 + 4;
+            MPI_Recv(recv + 22, 10, MPI_DOUBLE, 0, 3, MPI_COMM_WORLD, &st);
+            for (int i = 0; i < 10; i++) ok = ok && recv[22 + i] == 100 + i;
+            MPI_Recv(grid, 1, face, 0, 4, MPI_COMM_WORLD, &st);
+            for (int z = 0; z < 4; z++)
+                for (int y = 0; y < 4; y++) ok = ok && grid[(z + 1) * 36 + (y + 1) * 6 + 4] == 5000.0 + z * 4 + y;
+            ok = ok && grid[0] == 1000.0 && grid[4] == 1004.0;
+            for (int i = 0; i < 32; i++) outd(p, rank)[i] = recv[i];
+        }
+        MPI_Type_free(&col);
+        MPI_Type_free(&face);
+        MPI_Type_free(&blk);
+        free(grid);
+        free(recv);
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// Collectives on split communicators of uneven sizes (the reference has Bcast via p2p with wrong
+// rank translation there, H1, and no sub-communicator Barrier).
+struct SubcommColl {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        int color = rank % 3;
+        MPI_Comm c;
+        MPI_Comm_split(MPI_COMM_WORLD, color, -rank, &c);
+        int cr = -1, cs = -1;
+        MPI_Comm_rank(c, &cr);
+        MPI_Comm_size(c, &cs);
+        long long v[5], s[5];
+        for (int i = 0; i < 5; i++) v[i] = rank * 10 + i;
+        int rc = MPI_Allreduce(v, s, 5, MPI_LONG_LONG, MPI_SUM, c);
+        bool ok = rc == 0;
+        for (int i = 0; i < 5; i++) {
+            long long e = 0;
+            for (int q = color; q < n; q += 3) e += q * 10 + i;
+            ok = ok && s[i] == e;
+        }
+        int b[4] = {0, 0, 0, 0};
+        if (cr == cs - 1)
+            for (int i = 0; i < 4; i++) b[i] = rank + i;
+        rc = MPI_Bcast(b, 4, MPI_INT, cs - 1, c);
+        int root_world = color;  // highest key -rank -> comm rank cs-1 is the smallest world rank
+        ok = ok && rc == 0 && b[0] == root_world && b[3] == root_world + 3;
+        rc = MPI_Barrier(c);
+        ok = ok && rc == 0;
+        int* g = (int*)malloc(sizeof(int) * cs);
+        rc = MPI_Allgather(&rank, 1, MPI_INT, g, 1, MPI_INT, c);
+        for (int i = 0; i < cs; i++) ok = ok && g[i] == color + 3 * (cs - 1 - i);
+        free(g);
+        outi(p, rank)[0] = cr;
+        outi(p, rank)[1] = cs;
+        outi(p, rank)[2] = s[0];
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+// Argument errors come back as MPI error codes; nothing traps.
+struct Errors {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        bool ok = true;
+        int x = 0;
+        ok = ok && MPI_Send(&x, 1, MPI_INT, n + 5, 0, MPI_COMM_WORLD) == MPI_ERR_RANK;
+        ok = ok && MPI_Send(&x, 1, (MPI_Datatype)999, 0, 0, MPI_COMM_WORLD) == MPI_ERR_TYPE;
+        ok = ok && MPI_Send(&x, -1, MPI_INT, 0, 0, MPI_COMM_WORLD) == MPI_ERR_COUNT;
+        ok = ok && MPI_Send(&x, 1, MPI_INT, 0, 0, (MPI_Comm)nullptr) == MPI_ERR_COMM;
+        float f = 1.f, g = 0.f;
+        // BAND is not defined on float (operators.cu IsTypeOpAllowed)
+        ok = ok && MPI_Allreduce(&f, &g, 1, MPI_FLOAT, MPI_BAND, MPI_COMM_WORLD) == MPI_ERR_OP;
+        ok = ok && MPI_Reduce(&f, &g, 1, MPI_FLOAT, MPI_SUM, n + 1, MPI_COMM_WORLD) == MPI_ERR_ROOT;
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
+}  // namespace
+
+extern const gpumpi_prog_entry g_test_programs[] = {
+    GPUMPI_PROGRAM(GPUMPI_T_SINGLE_INT, "single_int", SingleInt),
+    GPUMPI_PROGRAM(GPUMPI_T_TRANSFER_ARRAY, "transfer_array", TransferArray),
+    GPUMPI_PROGRAM(GPUMPI_T_SEND_RECV, "send_recv", SendRecv),
+    GPUMPI_PROGRAM(GPUMPI_T_REPEAT_SEND_RECV, "repeat_send_recv", RepeatSendRecv),
+    GPUMPI_PROGRAM(GPUMPI_T_NETWORK_FLOOD, "network_flood", NetworkFlood),
+    GPUMPI_PROGRAM(GPUMPI_T_ALL_TO_ALL, "all_to_all", AllToAll),
+    GPUMPI_PROGRAM(GPUMPI_T_REDUCE_INT16_PROD, "reduce_int16_prod", ReduceInt16Prod),
+    GPUMPI_PROGRAM(GPUMPI_T_ALLREDUCE_F64, "allreduce_f64_sum", AllreduceF64),
+    GPUMPI_PROGRAM(GPUMPI_T_ALLGATHER, "allgather_int", Allgather),
+    GPUMPI_PROGRAM(GPUMPI_T_SCATTER, "scatter_int", Scatter),
+    GPUMPI_PROGRAM(GPUMPI_T_SCATTERV, "scatterv_int", Scatterv),
+    GPUMPI_PROGRAM(GPUMPI_T_COMM_RANK, "comm_rank", CommRank),
+    GPUMPI_PROGRAM(GPUMPI_T_COMM_DUP, "comm_dup_isolation", CommDup),
+    GPUMPI_PROGRAM(GPUMPI_T_COMM_SPLIT, "comm_split", CommSplit),
+    GPUMPI_PROGRAM(GPUMPI_T_SAMPLE, "sample", Sample),
+    GPUMPI_PROGRAM(GPUMPI_T_P2P_MATCHING, "p2p_matching", P2PMatching),
+    GPUMPI_PROGRAM(GPUMPI_T_TIMEOUT, "timeout", Timeout),
+    GPUMPI_PROGRAM(GPUMPI_T_DATATYPES, "datatypes", Datatypes),
+    GPUMPI_PROGRAM(GPUMPI_T_SUBCOMM_COLL, "subcomm_coll", SubcommColl),
+    GPUMPI_PROGRAM(GPUMPI_T_ERRORS, "errors", Errors),
+};
+extern const int g_num_test_programs = sizeof(g_test_programs) / sizeof(g_test_programs[0]);

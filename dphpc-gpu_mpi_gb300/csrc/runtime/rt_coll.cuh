@@ -1,0 +1,522 @@
+// rt_coll.cuh — collectives as single-pass chunked jobs.
+//
+// Reference behaviour being replaced:
+//   * MPI_Reduce: root gathers n-1 buffers by point-to-point, then one thread folds them in rank
+//     order (gpu_libs/gpu_mpi/mpi.cu:181-235); world + MPI_DOUBLE + MPI_SUM uses atomicAdd
+//     (mpi.cu:148-179, order non-deterministic);
+//   * MPI_Allreduce = Reduce(root 0) + Bcast(root 0) (mpi.cu:276-282);
+//   * MPI_Bcast: staging buffer + two grid barriers on the world, n-1 sends otherwise (mpi.cu:86-140);
+//   * MPI_Alltoall(v): n-1 Isend + n-1 Irecv + local memcpy + waits (mpi.cu:333-408);
+//   * MPI_Gather(v) / Scatter(v) / Allgather: root loops of blocking Send/Recv (mpi.cu:291-322,410-517).
+//
+// Here every collective is: publish my arguments in the communicator's slot table -> one barrier
+// (the last arriver opens a job of N chunks) -> every member block, plus any copy-engine block, claims
+// chunks with one atomic each and executes them -> wait until all N chunks are done.  Data moves
+// exactly once: folds read every member's input once and write every output once, pulls copy each
+// block once.  The canonical reduction order of the reference (result = x_0, then op(x_s, result) for
+// s = 1..n-1) is kept per element by the DIRECT and STAGED variants, so results are bit-identical.
+#pragma once
+#include "rt_core.cuh"
+#include "rt_types.cuh"
+#include "rt_ops.cuh"
+#include "rt_copy.cuh"
+
+namespace gpumpi {
+
+// shared-memory pointer tile used by the fold executors (one per block)
+constexpr int PTILE = 256;
+__shared__ unsigned long long s_ptile[PTILE];
+__shared__ unsigned char s_acc[256 * 16];   // generic-path accumulators, one 16-byte element per thread
+
+__device__ __forceinline__ int comm_rank_of(const MPI_Comm_impl* c, int world) {
+    return c->is_world ? world : c->rank_of[world];
+}
+
+// ------------------------------------------------------------------------------------------------
+// job lifecycle
+// ------------------------------------------------------------------------------------------------
+// Opens a new epoch of job j with n chunks.  Caller has written the job's parameters already.
+__device__ __forceinline__ unsigned job_open(Job* j, int n) {
+    unsigned e = j->epoch + 1;
+    j->epoch = e;
+    j->nchunks = n;
+    st_relaxed64(&j->done, (unsigned long long)e << 32);
+    st_relaxed64(&j->limit, ((unsigned long long)e << 32) | (unsigned)n);
+    atom_exch_release64(&j->next, (unsigned long long)e << 32);
+    return e;
+}
+
+// Claims one chunk; returns its index or -1 once the current epoch is exhausted.
+__device__ __forceinline__ long long job_claim(Job* j) {
+    unsigned long long t = atom_add_acqrel64(&j->next, 1ULL);
+    unsigned e = (unsigned)(t >> 32);
+    unsigned idx = (unsigned)t;
+    unsigned long long lim = ld_acquire64(&j->limit);
+    if ((unsigned)(lim >> 32) != e || idx >= (unsigned)lim) return -1;
+    return idx;
+}
+
+__device__ __forceinline__ void job_finish(Job* j) { atom_add_acqrel64(&j->done, 1ULL); }
+
+// Posts job j (epoch e) on the board so copy-engine blocks help with it.
+__device__ __forceinline__ void board_post(Job* j, unsigned e) {
+    Board* b = g_rt->board;
+    if (!b || g_rt->nengines <= 0) return;
+    unsigned long long i = atomicAdd(&b->reserve, 1ULL);
+    BoardEntry* en = &b->ring[i % (unsigned long long)b->cap];
+    en->job = j;
+    en->epoch = e;
+    st_release(&en->seq, (unsigned)(i + 1));
+}
+
+// Thread 0: claims and executes chunks of j until none is left, then waits for all to finish.
+__device__ __noinline__ int job_run_and_wait(Job* j, int line) {
+    long long idx;
+    while ((idx = job_claim(j)) >= 0) {
+        Task t;
+        t.kind = TASK_CHUNK;
+        t.p0 = j;
+        t.n0 = idx;
+        dispatch(t);
+        job_finish(j);
+    }
+    unsigned long long target = ((unsigned long long)j->epoch << 32) | (unsigned)j->nchunks;
+    if (ld_acquire64(&j->done) == target) return 0;
+    Deadline d = make_deadline();
+    while (ld_acquire64(&j->done) != target) {
+        if (int e = wait_tick(d, line, 128)) return e;
+    }
+    return 0;
+}
+
+// ------------------------------------------------------------------------------------------------
+// communicator barrier: generation counter; the last arriver runs `setup` before releasing
+// ------------------------------------------------------------------------------------------------
+template <class F>
+__device__ int comm_barrier(MPI_Comm_impl* c, F&& setup, int line) {
+    unsigned g = ld_acquire(&c->bar_gen);
+    unsigned a = atom_add_acqrel(&c->bar_count, 1u);
+    if (a == (unsigned)c->size - 1) {
+        c->bar_count = 0;
+        setup();
+        st_release(&c->bar_gen, g + 1);
+        return 0;
+    }
+    Deadline d = make_deadline();
+    while (ld_acquire(&c->bar_gen) == g) {
+        if (int e = wait_tick(d, line, 64)) return e;
+    }
+    return 0;
+}
+
+// ------------------------------------------------------------------------------------------------
+// fold executors (Allreduce / Reduce)
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ const void* slot_in(const CollSlot* s) {
+    return (const void*)__ldcg((const unsigned long long*)&s->sbuf);
+}
+__device__ __forceinline__ void* slot_out(const CollSlot* s) {
+    return (void*)__ldcg((const unsigned long long*)&s->rbuf);
+}
+
+// loads pointer field `which` (0 = sbuf, 1 = rbuf) of members [r0, r0+m) into s_ptile
+__device__ __forceinline__ void load_ptile(const CollSlot* slots, int r0, int m, int which, int tid, int nt) {
+    bar_sync(BAR_TASK, nt);
+    for (int i = tid; i < m; i += nt)
+        s_ptile[i] = __ldcg(which == 0 ? (const unsigned long long*)&slots[r0 + i].sbuf
+                                        : (const unsigned long long*)&slots[r0 + i].rbuf);
+    bar_sync(BAR_TASK, nt);
+}
+
+template <class T, int V>
+__device__ __forceinline__ void ld_elems(const T* p, T (&v)[V], int nv, bool vec16) {
+    if constexpr ((V * sizeof(T)) % 16 == 0) {
+        if (vec16 && nv == V) {
+#pragma unroll
+            for (int q = 0; q < (int)(V * sizeof(T) / 16); q++) {
+                uint4 w = __ldcg((const uint4*)p + q);
+                *reinterpret_cast<uint4*>(&v[q * (16 / sizeof(T))]) = w;
+            }
+            return;
+        }
+    } else if constexpr ((V * sizeof(T)) == 8 && sizeof(T) < 8) {
+        if (vec16 && nv == V) {
+            unsigned long long w = __ldcg((const unsigned long long*)p);
+            *reinterpret_cast<unsigned long long*>(&v[0]) = w;
+            return;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < V; k++)
+        if (k < nv) v[k] = __ldcg(p + k);
+}
+
+template <class T, int V>
+__device__ __forceinline__ void st_elems(T* p, const T (&v)[V], int nv, bool vec16) {
+    if constexpr ((V * sizeof(T)) % 16 == 0) {
+        if (vec16 && nv == V) {
+#pragma unroll
+            for (int q = 0; q < (int)(V * sizeof(T) / 16); q++)
+                __stcg((uint4*)p + q, *reinterpret_cast<const uint4*>(&v[q * (16 / sizeof(T))]));
+            return;
+        }
+    } else if constexpr ((V * sizeof(T)) == 8 && sizeof(T) < 8) {
+        if (vec16 && nv == V) {
+            __stcg((unsigned long long*)p, *reinterpret_cast<const unsigned long long*>(&v[0]));
+            return;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < V; k++)
+        if (k < nv) __stcg(p + k, v[k]);
+}
+
+// Canonical-order fold of elements [e0, e0 + nt*V): thread tid owns V consecutive elements.
+// order: acc = x_0; acc = op(x_s, acc) for s = 1..n-1 (in comm-rank order).
+template <class T, int OP, int V>
+__device__ __noinline__ void fold_fast(const Job* j, long long e0, int tid, int nt) {
+    constexpr int BYTES = V * (int)sizeof(T);
+    // ranks folded per step: ~64 bytes of loads in flight per thread without spilling
+    constexpr int U = 64 / BYTES > 8 ? 8 : 64 / BYTES < 1 ? 1 : 64 / BYTES;
+    const MPI_Comm_impl* c = j->comm;
+    const CollSlot* slots = c->slots;
+    const int n = c->size;
+    const long long count = j->count;
+    const long long e = e0 + (long long)tid * V;
+    const int nv = e < count ? (int)min((long long)V, count - e) : 0;
+    const bool vec16 = j->aligned16 >= (int)((V * sizeof(T)) >= 16 ? 16 : (V * sizeof(T)));
+    T acc[V];
+#pragma unroll
+    for (int k = 0; k < V; k++) acc[k] = T();
+    for (int r0 = 0; r0 < n; r0 += PTILE) {
+        const int m = min(PTILE, n - r0);
+        load_ptile(slots, r0, m, 0, tid, nt);
+        if (nv > 0) {
+            int i = 0;
+            if (r0 == 0) {
+                ld_elems<T, V>((const T*)s_ptile[0] + e, acc, nv, vec16);
+                i = 1;
+            }
+            for (; i + U <= m; i += U) {
+                T v[U][V];
+#pragma unroll
+                for (int u = 0; u < U; u++) ld_elems<T, V>((const T*)s_ptile[i + u] + e, v[u], nv, vec16);
+#pragma unroll
+                for (int u = 0; u < U; u++)
+#pragma unroll
+                    for (int k = 0; k < V; k++) acc[k] = op_apply<OP, T>(v[u][k], acc[k]);
+            }
+            for (; i < m; i++) {
+                T v[V];
+                ld_elems<T, V>((const T*)s_ptile[i] + e, v, nv, vec16);
+#pragma unroll
+                for (int k = 0; k < V; k++) acc[k] = op_apply<OP, T>(v[k], acc[k]);
+            }
+        }
+    }
+    if (j->kind == JOB_REDUCE) {
+        if (nv > 0) {
+            T* out = (T*)slot_out(&slots[j->root]);
+            st_elems<T, V>(out + e, acc, nv, vec16);
+        }
+        return;
+    }
+    for (int r0 = 0; r0 < n; r0 += PTILE) {
+        const int m = min(PTILE, n - r0);
+        load_ptile(slots, r0, m, 1, tid, nt);
+        if (nv > 0)
+            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_ptile[i] + e, acc, nv, vec16);
+    }
+}
+
+// Any legal (op, type) and user-defined ops, one element per thread, same canonical order.
+__device__ __noinline__ void fold_generic(const Job* j, long long e0, int tid, int nt) {
+    const MPI_Comm_impl* c = j->comm;
+    const CollSlot* slots = c->slots;
+    const int n = c->size;
+    const int es = j->esize;
+    const long long e = e0 + tid;
+    const bool act = e < j->count;
+    unsigned char* acc = s_acc + tid * 16;
+    MPI_Datatype dtv = (MPI_Datatype)j->dt;
+    int one = 1;
+    for (int r0 = 0; r0 < n; r0 += PTILE) {
+        const int m = min(PTILE, n - r0);
+        load_ptile(slots, r0, m, 0, tid, nt);
+        if (act) {
+            for (int i = 0; i < m; i++) {
+                const unsigned char* src = (const unsigned char*)s_ptile[i] + e * es;
+                if (r0 == 0 && i == 0) {
+                    for (int b = 0; b < es; b++) acc[b] = src[b];
+                } else if (j->ufn) {
+                    j->ufn((void*)src, acc, &one, &dtv);
+                } else {
+                    apply_elem(j->op, j->dt, src, acc);
+                }
+            }
+        }
+    }
+    if (j->kind == JOB_REDUCE) {
+        if (act) {
+            unsigned char* out = (unsigned char*)slot_out(&slots[j->root]) + e * es;
+            for (int b = 0; b < es; b++) out[b] = acc[b];
+        }
+        return;
+    }
+    for (int r0 = 0; r0 < n; r0 += PTILE) {
+        const int m = min(PTILE, n - r0);
+        load_ptile(slots, r0, m, 1, tid, nt);
+        if (act)
+            for (int i = 0; i < m; i++) {
+                unsigned char* out = (unsigned char*)s_ptile[i] + e * es;
+                for (int b = 0; b < es; b++) out[b] = acc[b];
+            }
+    }
+}
+
+// storage-type / op dispatch of the fast path; returns false if no fast instantiation exists
+// vec choices: 16/sizeof(T) (one 16-byte vector), 8/sizeof(T) (4-byte types), 1
+template <class T, int OP>
+__device__ __forceinline__ void fold_fast_v(const Job* j, long long e0, int tid, int nt) {
+    constexpr int VW = 16 / sizeof(T);
+    if (j->vec >= VW) fold_fast<T, OP, VW>(j, e0, tid, nt);
+    else if constexpr (sizeof(T) == 4) {
+        if (j->vec >= 2) fold_fast<T, OP, 2>(j, e0, tid, nt);
+        else fold_fast<T, OP, 1>(j, e0, tid, nt);
+    } else fold_fast<T, OP, 1>(j, e0, tid, nt);
+}
+
+template <class T>
+__device__ __forceinline__ bool fold_fast_arith(const Job* j, long long e0, int tid, int nt) {
+    switch (j->op) {
+    case GPUMPI_OP_SUM: fold_fast_v<T, GPUMPI_OP_SUM>(j, e0, tid, nt); return true;
+    case GPUMPI_OP_MAX: fold_fast_v<T, GPUMPI_OP_MAX>(j, e0, tid, nt); return true;
+    case GPUMPI_OP_MIN: fold_fast_v<T, GPUMPI_OP_MIN>(j, e0, tid, nt); return true;
+    case GPUMPI_OP_PROD: fold_fast_v<T, GPUMPI_OP_PROD>(j, e0, tid, nt); return true;
+    default: return false;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ bool fold_fast_int(const Job* j, long long e0, int tid, int nt) {
+    switch (j->op) {
+    case GPUMPI_OP_BAND: fold_fast_v<T, GPUMPI_OP_BAND>(j, e0, tid, nt); return true;
+    case GPUMPI_OP_BOR: fold_fast_v<T, GPUMPI_OP_BOR>(j, e0, tid, nt); return true;
+    case GPUMPI_OP_BXOR: fold_fast_v<T, GPUMPI_OP_BXOR>(j, e0, tid, nt); return true;
+    default: return fold_fast_arith<T>(j, e0, tid, nt);
+    }
+}
+
+// true if the (dt, op) pair has a templated fast path
+__device__ __forceinline__ bool fold_has_fast(int dt, int op, MPI_User_function* ufn) {
+#ifdef GPUMPI_NO_FAST_FOLD
+    return false;
+#endif
+    if (ufn) return false;
+    switch (dt) {
+    case GPUMPI_FLOAT: case GPUMPI_DOUBLE: case GPUMPI_LONG_DOUBLE:
+        return op == GPUMPI_OP_SUM || op == GPUMPI_OP_MAX || op == GPUMPI_OP_MIN || op == GPUMPI_OP_PROD;
+    case GPUMPI_INT: case GPUMPI_INT32_T: case GPUMPI_UNSIGNED: case GPUMPI_UINT32_T: case GPUMPI_LONG:
+    case GPUMPI_LONG_LONG_INT: case GPUMPI_LONG_LONG: case GPUMPI_INT64_T: case GPUMPI_UNSIGNED_LONG:
+    case GPUMPI_UNSIGNED_LONG_LONG: case GPUMPI_UINT64_T:
+        return op == GPUMPI_OP_SUM || op == GPUMPI_OP_MAX || op == GPUMPI_OP_MIN || op == GPUMPI_OP_PROD ||
+               op == GPUMPI_OP_BAND || op == GPUMPI_OP_BOR || op == GPUMPI_OP_BXOR;
+    default: return false;
+    }
+}
+
+__device__ __noinline__ void fold_chunk(const Job* j, long long idx, int tid, int nt) {
+    const long long e0 = idx * j->chunk;
+    bool done = false;
+#ifndef GPUMPI_NO_FAST_FOLD
+    if (fold_has_fast(j->dt, j->op, j->ufn)) {
+        switch (j->dt) {
+        case GPUMPI_FLOAT: done = fold_fast_arith<float>(j, e0, tid, nt); break;
+        case GPUMPI_DOUBLE: case GPUMPI_LONG_DOUBLE: done = fold_fast_arith<double>(j, e0, tid, nt); break;
+        case GPUMPI_INT: case GPUMPI_INT32_T: done = fold_fast_int<int>(j, e0, tid, nt); break;
+        case GPUMPI_UNSIGNED: case GPUMPI_UINT32_T: done = fold_fast_int<unsigned>(j, e0, tid, nt); break;
+        case GPUMPI_LONG: case GPUMPI_LONG_LONG_INT: case GPUMPI_LONG_LONG: case GPUMPI_INT64_T:
+            done = fold_fast_int<long long>(j, e0, tid, nt); break;
+        default: done = fold_fast_int<unsigned long long>(j, e0, tid, nt); break;
+        }
+    }
+#endif
+    if (!done) fold_generic(j, e0, tid, nt);
+}
+
+// ------------------------------------------------------------------------------------------------
+// pull executors (Bcast / Alltoall(v) / Allgather(v) / Gather(v) / Scatter(v))
+//   piece p -> (receiver r, sender s); the chunk covers `tile` consecutive pieces (warp per piece),
+//   or, when pieces are large, one byte range of one piece (`vec` parts per piece, whole block).
+// ------------------------------------------------------------------------------------------------
+struct Piece {
+    const char* src;
+    char* dst;
+    const TypeDesc* sdesc;   // nullptr: contiguous
+    const TypeDesc* rdesc;
+    long long bytes;         // packed bytes to move
+    int trunc;
+};
+
+__device__ __forceinline__ int ldcg_int(const int* p) { return __ldcg(p); }
+
+__device__ __forceinline__ void piece_of(const Job* j, long long p, Piece& pc) {
+    const MPI_Comm_impl* c = j->comm;
+    const CollSlot* S = c->slots;
+    const int n = c->size;
+    int r, s;
+    switch (j->kind) {
+    case JOB_ALLTOALLV: case JOB_ALLGATHERV: r = (int)(p / n); s = (int)(p % n); break;
+    case JOB_GATHERV: r = j->root; s = (int)p; break;
+    default: r = (int)p; s = j->root; break;  // SCATTERV, BCAST
+    }
+    const CollSlot* ss = &S[s];
+    const CollSlot* rs = &S[r];
+    const char* sbuf = (const char*)__ldcg((const unsigned long long*)&ss->sbuf);
+    char* rbuf = (char*)__ldcg((const unsigned long long*)&rs->rbuf);
+    const TypeDesc* sd = (const TypeDesc*)__ldcg((const unsigned long long*)&ss->sdesc);
+    const TypeDesc* rd = (const TypeDesc*)__ldcg((const unsigned long long*)&rs->rdesc);
+    long long sext = __ldcg(&sd->extent), rext = __ldcg(&rd->extent);
+    long long ssz = __ldcg(&sd->size), rsz = __ldcg(&rd->size);
+    long long scount, rcount, soff, roff;
+    switch (j->kind) {
+    case JOB_ALLTOALLV: {
+        const int* sc = (const int*)__ldcg((const unsigned long long*)&ss->scounts);
+        const int* sdp = (const int*)__ldcg((const unsigned long long*)&ss->sdispls);
+        const int* rc = (const int*)__ldcg((const unsigned long long*)&rs->rcounts);
+        const int* rdp = (const int*)__ldcg((const unsigned long long*)&rs->rdispls);
+        long long sct = __ldcg(&ss->scount), rct = __ldcg(&rs->rcount);
+        scount = sc ? ldcg_int(sc + r) : sct;
+        soff = sdp ? (long long)ldcg_int(sdp + r) * sext : (long long)r * sct * sext;
+        rcount = rc ? ldcg_int(rc + s) : rct;
+        roff = rdp ? (long long)ldcg_int(rdp + s) * rext : (long long)s * rct * rext;
+        break;
+    }
+    case JOB_ALLGATHERV: case JOB_GATHERV: {
+        const int* rc = (const int*)__ldcg((const unsigned long long*)&rs->rcounts);
+        const int* rdp = (const int*)__ldcg((const unsigned long long*)&rs->rdispls);
+        long long rct = __ldcg(&rs->rcount);
+        scount = __ldcg(&ss->scount);
+        soff = 0;
+        rcount = rc ? ldcg_int(rc + s) : rct;
+        roff = rdp ? (long long)ldcg_int(rdp + s) * rext : (long long)s * rct * rext;
+        break;
+    }
+    case JOB_SCATTERV: {
+        const int* sc = (const int*)__ldcg((const unsigned long long*)&ss->scounts);
+        const int* sdp = (const int*)__ldcg((const unsigned long long*)&ss->sdispls);
+        long long sct = __ldcg(&ss->scount);
+        scount = sc ? ldcg_int(sc + r) : sct;
+        soff = sdp ? (long long)ldcg_int(sdp + r) * sext : (long long)r * sct * sext;
+        rcount = __ldcg(&rs->rcount);
+        roff = 0;
+        break;
+    }
+    default: {  // BCAST: root's buffer (published as sbuf) into every member's buffer (rbuf)
+        scount = __ldcg(&ss->scount);
+        rcount = __ldcg(&rs->rcount);
+        soff = 0;
+        roff = 0;
+        break;
+    }
+    }
+    long long sbytes = scount * ssz, rbytes = rcount * rsz;
+    pc.trunc = sbytes > rbytes;
+    pc.bytes = sbytes < rbytes ? sbytes : rbytes;
+    // in-place / self pieces move nothing
+    if (sbuf == (const char*)MPI_IN_PLACE || rbuf == (char*)MPI_IN_PLACE ||
+        (j->kind == JOB_BCAST && r == s) || (sbuf + soff == rbuf + roff && sd == rd))
+        pc.bytes = 0;
+    pc.src = sbuf + soff;
+    pc.dst = rbuf + roff;
+    pc.sdesc = desc_contiguous(sd) ? nullptr : sd;
+    pc.rdesc = desc_contiguous(rd) ? nullptr : rd;
+}
+
+__device__ __forceinline__ void piece_copy(const Piece& pc, long long b0, long long b1, int lane, int nl) {
+    if (b1 <= b0) return;
+    if (!pc.sdesc && !pc.rdesc) copy_bytes(pc.dst + b0, pc.src + b0, b1 - b0, lane, nl);
+    else typed_copy(pc.dst, pc.rdesc, pc.src, pc.sdesc, b0, b1, lane, nl);
+}
+
+__device__ __noinline__ void pull_chunk(Job* j, long long idx, int tid, int nt) {
+    const long long npieces = j->count;
+    if (j->vec > 1) {  // byte range `part` of one piece, whole block
+        const long long p = idx / j->vec;
+        const int part = (int)(idx % j->vec);
+        Piece pc;
+        piece_of(j, p, pc);
+        long long per = ((pc.bytes + j->vec - 1) / j->vec + 15) & ~15LL;
+        long long b0 = per * part, b1 = min(pc.bytes, b0 + per);
+        piece_copy(pc, b0, b1, tid, nt);
+        if (tid == 0 && part == 0 && pc.trunc) atomicOr(&j->err, 1u);
+        return;
+    }
+    const int lane = tid & 31, warp = tid >> 5, nwarps = (nt + 31) >> 5;
+    const long long p0 = idx * j->tile;
+    const long long p1 = min(npieces, p0 + j->tile);
+    for (long long p = p0 + warp; p < p1; p += nwarps) {
+        Piece pc;
+        piece_of(j, p, pc);
+        piece_copy(pc, 0, pc.bytes, lane, 32);
+        if (lane == 0 && pc.trunc) atomicOr(&j->err, 1u);
+    }
+}
+
+__device__ __noinline__ void copy_chunk(const Job* j, long long idx, int tid, int nt) {
+    long long off = idx * j->chunk;
+    long long len = min(j->chunk, j->count - off);
+    copy_bytes((char*)j->dst + off, (const char*)j->src + off, len, tid, nt);
+}
+
+__device__ __noinline__ void exec_chunk(Job* j, long long idx, int tid, int nt) {
+    switch (j->kind) {
+    case JOB_COPY: copy_chunk(j, idx, tid, nt); break;
+    case JOB_ALLREDUCE: case JOB_REDUCE: fold_chunk(j, idx, tid, nt); break;
+    default: pull_chunk(j, idx, tid, nt); break;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// copy-engine loop (blocks >= nranks): claim chunks of any job posted on the board
+// ------------------------------------------------------------------------------------------------
+__device__ void engine_loop() {
+    Board* b = g_rt->board;
+    const unsigned long long cap = (unsigned long long)b->cap;
+    unsigned long long cursor = 0;
+    unsigned ns = 32;
+    for (;;) {
+        bool worked = false;
+        unsigned long long res = ld_acquire64(&b->reserve);
+        if (res > cap && res - cap > cursor) cursor = res - cap;
+        for (unsigned long long i = cursor; i < res; i++) {
+            BoardEntry* en = &b->ring[i % cap];
+            unsigned seq = ld_acquire(&en->seq);
+            int diff = (int)(seq - (unsigned)(i + 1));
+            if (diff < 0) break;             // not written yet
+            if (diff == 0) {
+                Job* j = (Job*)__ldcg((const unsigned long long*)&en->job);
+                long long idx;
+                while ((idx = job_claim(j)) >= 0) {
+                    Task t;
+                    t.kind = TASK_CHUNK;
+                    t.p0 = j;
+                    t.n0 = idx;
+                    dispatch(t);
+                    job_finish(j);
+                    worked = true;
+                }
+            }
+            if (i == cursor) cursor++;
+        }
+        if (ld_relaxed(g_rt->ranks_done) >= (unsigned)g_rt->nranks || ld_relaxed(g_rt->abort_flag)) return;
+        if (!worked) {
+            __nanosleep(ns);
+            ns = ns * 2 > 1024 ? 1024 : ns * 2;
+        } else {
+            ns = 32;
+        }
+    }
+}
+
+}  // namespace gpumpi

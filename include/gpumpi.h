@@ -1,0 +1,186 @@
+/*
+ * gpumpi.h — host C ABI of the block-rank MPI runtime (libgpumpi.so).
+ *
+ * Plain C: opaque handles, plain pointers and sizes, no CUDA or torch types in the signatures
+ * (streams are passed as void*, a cudaStream_t or NULL for the world's own stream).
+ *
+ * What each entry point replaces in the reference (lilyyangyn/dphpc-gpu_mpi):
+ *   gpumpi_config_init / gpumpi_parse_args  <- parseGPUMPIArgs and its defaults,
+ *                                               gpu_libs/gpu_main/main.cu:48-97 (---gpumpi -n -g -b -s -p -e)
+ *   gpumpi_world_create / _destroy          <- SharedState::Holder + ThreadPrivateState::Context set-up,
+ *                                               gpu_libs/gpu_libc/cuda_mpi.cuh:459-502, main.cu:210-278
+ *   gpumpi_run_program                      <- the launch of __gpu_main_caller and the host wait loop,
+ *                                               main.cu:280-320 (co-residency check main.cu:188-208)
+ *   gpumpi_test_run                         <- TestRunner::run<Kernel>(), tests/test_runner.cuh:26-86
+ *   gpumpi_allreduce / _reduce / _bcast /   <- one MPI_Allreduce / MPI_Reduce / MPI_Bcast / MPI_Alltoall /
+ *   _alltoall / _alltoallv / _allgather        MPI_Alltoallv / MPI_Allgather call made by every rank of a
+ *                                               launch (gpu_libs/gpu_mpi/mpi.cu:276-282,181-235,101-140,
+ *                                               333-408,410-419) — the hot path, callable from the host
+ *   gpumpi_pingpong / gpumpi_ring           <- MPI_Send/MPI_Recv loops of benchmarks/mpi_communication/
+ *                                               mpi_communication.c:10-55 (point-to-point benchmark)
+ *   gpumpi_last_error                       <- CudaMPI::printLastError, gpu_libs/gpu_libc/assert.cu:58-71
+ *
+ * Buffers: every data pointer may be device memory or host memory (pageable or pinned); host memory
+ * is staged through device memory inside the call (the host<->device copies are part of the call).
+ * Rank-major layout: rank r's buffer starts at base + r * stride_bytes.
+ * Return value: GPUMPI_SUCCESS (0) or an error code from gpumpi_abi.h; never aborts the process.
+ */
+#ifndef GPUMPI_H
+#define GPUMPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "gpumpi_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gpumpi_world gpumpi_world;
+
+typedef struct gpumpi_config {
+    int nranks;               /* -n: MPI ranks = thread blocks */
+    int threads_per_block;    /* -b: 0 = pick from occupancy (largest of 256/128/64 that fits) */
+    int engine_blocks;        /* copy-engine blocks beside the ranks; -1 = fill the GPU, 0 = none */
+    int pending_requests;     /* -e: request slots per rank (reference default 1024) */
+    int mailbox_depth;        /* envelope ring slots per rank (power of two) */
+    int unexpected_depth;     /* unexpected-message queue depth per rank */
+    int eager_bytes;          /* messages up to this size travel inline (multiple of 16) */
+    int max_types;            /* derived datatypes per rank */
+    int posted_depth;         /* posted receives per rank */
+    int device;               /* CUDA device ordinal */
+    size_t stack_bytes;       /* -s: per-thread stack limit */
+    size_t heap_bytes;        /* -p: device malloc heap (0 = 1 GiB) */
+    size_t arena_bytes;       /* communicator objects created at run time */
+    long long copy_chunk_bytes;   /* chunk of large point-to-point copies shared with engines */
+    long long engine_min_bytes;   /* jobs smaller than this are not offered to engine blocks */
+    double timeout_s;         /* bound on every device-side wait */
+    int trace_capacity;       /* per-call timing records kept (0 = tracing off) */
+} gpumpi_config;
+
+typedef struct gpumpi_world_info {
+    int nranks, threads_per_block, engine_blocks, blocks_per_sm, sm_count, device;
+    size_t device_bytes;      /* device memory held by the world */
+} gpumpi_world_info;
+
+/* generic parameters of a built-in device program */
+typedef struct gpumpi_params {
+    long long i[16];
+    double d[4];
+    void* p[16];
+} gpumpi_params;
+
+/* built-in device programs (each runs on every rank of a launch) */
+enum gpumpi_program {
+    /* mirrors of the reference's GPU tests (tests/cuda_mpi_test.cu, collectives_test.cu, communicator_test.cu,
+     * sample_test.cu): p[0] = uint8 ok[nranks], p[1] = int64 out[nranks * 64], p[2] = double out[nranks * 64] */
+    GPUMPI_T_SINGLE_INT = 1,
+    GPUMPI_T_TRANSFER_ARRAY,
+    GPUMPI_T_SEND_RECV,
+    GPUMPI_T_REPEAT_SEND_RECV,
+    GPUMPI_T_NETWORK_FLOOD,
+    GPUMPI_T_ALL_TO_ALL,
+    GPUMPI_T_REDUCE_INT16_PROD,
+    GPUMPI_T_ALLREDUCE_F64,
+    GPUMPI_T_ALLGATHER,
+    GPUMPI_T_SCATTER,
+    GPUMPI_T_SCATTERV,
+    GPUMPI_T_COMM_RANK,
+    GPUMPI_T_COMM_DUP,
+    GPUMPI_T_COMM_SPLIT,
+    GPUMPI_T_SAMPLE,
+    GPUMPI_T_P2P_MATCHING,     /* wildcards, ordering, probe, sendrecv, proc_null */
+    GPUMPI_T_TIMEOUT,          /* a receive nobody sends to: bounded wait returns MPI_ERR_OTHER */
+    GPUMPI_T_DATATYPES,        /* vector / subarray / contiguous send-recv round trips */
+    GPUMPI_T_SUBCOMM_COLL,     /* collectives on split communicators */
+    GPUMPI_T_ERRORS,           /* argument errors return codes, never trap */
+    /* hot-path programs */
+    GPUMPI_P_COLL = 100,       /* i[0]=kind i[1]=count i[2]=dt i[3]=op i[4]=root i[5]=iters i[6]=send stride
+                                  i[7]=recv stride i[8]=variant p[0]=send p[1]=recv p[2..5]=count/displ matrices
+                                  p[6]=uint64 iter_ns[iters] p[7]=int rc[nranks] */
+    GPUMPI_P_PINGPONG,         /* i[0]=bytes i[1]=iters i[2]=mode(0 blocking,1 nonblocking) i[3]=pairs
+                                  p[0]=buffers (rank-major, stride i[4]) p[6]=iter_ns p[7]=rc */
+    GPUMPI_P_RING,             /* i[0]=bytes i[1]=iters i[2]=mode i[4]=stride p[0]=send p[1]=recv p[6] p[7] */
+    GPUMPI_P_PI,               /* i[0]=seed i[1]=pairs per rank p[0]=int64 hits[nranks] p[1]=int64 total p[7]=rc */
+    GPUMPI_P_BUCKET_SORT,      /* see bench / tests */
+    GPUMPI_P_HALO,
+    GPUMPI_P_BATCH,
+};
+
+/* collective kinds for GPUMPI_P_COLL */
+enum gpumpi_coll_kind {
+    GPUMPI_COLL_ALLREDUCE = 0,
+    GPUMPI_COLL_REDUCE,
+    GPUMPI_COLL_BCAST,
+    GPUMPI_COLL_ALLTOALL,
+    GPUMPI_COLL_ALLTOALLV,
+    GPUMPI_COLL_ALLGATHER,
+    GPUMPI_COLL_GATHER,
+    GPUMPI_COLL_SCATTER,
+    GPUMPI_COLL_BARRIER,
+    GPUMPI_COLL_ALLGATHERV,
+    GPUMPI_COLL_GATHERV,
+    GPUMPI_COLL_SCATTERV,
+};
+
+int gpumpi_config_init(gpumpi_config* cfg);
+/* Parses the options after "---gpumpi" into cfg; returns the index of "---gpumpi" (= the user's argc)
+ * or -1 when it is absent. */
+int gpumpi_parse_args(int argc, char** argv, gpumpi_config* cfg);
+
+int gpumpi_world_create(const gpumpi_config* cfg, gpumpi_world** out);
+int gpumpi_world_destroy(gpumpi_world* w);
+int gpumpi_world_get_info(gpumpi_world* w, gpumpi_world_info* info);
+/* Text of the last error of this world (or of the last failed create when w is NULL). */
+const char* gpumpi_last_error(gpumpi_world* w);
+
+/* Variant policy for reductions: variant >= 0 forces one, -1 lets the selector decide;
+ * mode 0 = plain (DIRECT), 1 = tuned table, 2 = learned MLP. */
+int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
+/* Tuned table: int8 [2][32][16] (kind, log2 bytes per rank, log2 ranks) -> variant, host memory. */
+int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes);
+/* Learned selector weights: float[GPUMPI_MLP_NPARAMS] in the layout of the training kernels. */
+int gpumpi_set_mlp(gpumpi_world* w, const float* params, size_t count);
+/* Timing trace: copies up to `cap` records {log2 bytes, log2 ranks, kind, variant, dt, op, us, pad}
+ * (32 bytes each) into host memory; returns the number of records written in *n. */
+int gpumpi_read_trace(gpumpi_world* w, void* host_out, size_t cap, size_t* n);
+
+/* Runs built-in program `program` on all ranks; blocks until it finished when sync != 0. */
+int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params, void* stream, int sync);
+/* Launch-time of the last run in milliseconds (CUDA events around the kernel). */
+double gpumpi_last_kernel_ms(gpumpi_world* w);
+/* How many kernels the library launched so far (all worlds). */
+long long gpumpi_kernel_launches(void);
+
+/* TestRunner equivalent: runs test program `test` on the world's ranks; ok[nranks] (host) receives
+ * each rank's flag; outi/outd (host, nranks*64 each, may be NULL) receive the test's values. */
+int gpumpi_test_run(gpumpi_world* w, int test, uint8_t* ok, int64_t* outi, double* outd);
+
+/* Hot path from the host: every rank calls the collective `iters` times on its slice of the
+ * rank-major buffers.  iter_ns (host, may be NULL) receives rank 0's per-call durations. */
+int gpumpi_allreduce(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long count, int datatype,
+                     int op, int iters, uint64_t* iter_ns, void* stream);
+int gpumpi_reduce(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long count, int datatype, int op,
+                  int root, int iters, uint64_t* iter_ns, void* stream);
+int gpumpi_bcast(gpumpi_world* w, void* buf, long long count, int datatype, int root, int iters,
+                 uint64_t* iter_ns, void* stream);
+int gpumpi_alltoall(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long count_per_pair, int datatype,
+                    int iters, uint64_t* iter_ns, void* stream);
+/* counts/displs: int32 [nranks][nranks] (row r = rank r's array); buffers with strides in bytes */
+int gpumpi_alltoallv(gpumpi_world* w, const void* sendbuf, long long send_stride, const int* sendcounts,
+                     const int* sdispls, void* recvbuf, long long recv_stride, const int* recvcounts,
+                     const int* rdispls, int datatype, int iters, uint64_t* iter_ns, void* stream);
+int gpumpi_allgather(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long count, int datatype,
+                     int iters, uint64_t* iter_ns, void* stream);
+int gpumpi_pingpong(gpumpi_world* w, void* bufs, long long bytes, int pairs, int iters, int nonblocking,
+                    uint64_t* iter_ns, void* stream);
+int gpumpi_ring(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long bytes, int iters, int nonblocking,
+                uint64_t* iter_ns, void* stream);
+
+#define GPUMPI_MLP_NPARAMS (64 * 12 + 64 + 64 * 64 + 64 + 4 * 64 + 4)
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUMPI_H */

@@ -1,0 +1,241 @@
+// mpi.h.cuh — the __device__ MPI surface of the block-rank runtime.
+//
+// Drop-in for the reference's gpu_libs/gpu_mpi/mpi.h.cuh (which includes mpi.cuh, mpi_common.cuh,
+// group.cuh, communicator.cuh, datatypes.cuh, operators.cuh): same type names, same handle kinds
+// (opaque pointers for MPI_Comm / MPI_Group / MPI_Op / MPI_Request, an enum for MPI_Datatype with the
+// reference's value order), same constants, same function signatures.  Code converted for the
+// reference (every function __device__, main renamed __gpu_main) compiles against this header.
+//
+// Calling convention: an MPI rank is one thread block; the user program runs on thread 0 of the block
+// (scalar code, exactly as in the reference) and MPI calls use the rest of the block internally.
+// Call MPI functions from thread 0 of a rank block only.
+#pragma once
+
+#include <stdint.h>
+#include <stddef.h>
+
+#include "gpumpi_abi.h"
+
+// ---- constants (reference gpu_libs/gpu_mpi/mpi.cuh:4-9, mpi_common.cuh:3-9) ----
+#define MPI_MAX_PROCESSOR_NAME 256
+#define MPI_ANY_TAG (-1)
+#define MPI_ANY_SOURCE (-1)
+#define MPI_PROC_NULL (-2)
+#define MPI_TAG_UB ((1 << 15) - 1)
+#define MPI_SUCCESS 0
+#define MPI_FAILURE -1
+#define MPI_ERR_OTHER 1
+#define MPI_ERR_BUFFER GPUMPI_ERR_BUFFER
+#define MPI_ERR_COUNT GPUMPI_ERR_COUNT
+#define MPI_ERR_TYPE GPUMPI_ERR_TYPE
+#define MPI_ERR_TAG GPUMPI_ERR_TAG
+#define MPI_ERR_COMM GPUMPI_ERR_COMM
+#define MPI_ERR_RANK GPUMPI_ERR_RANK
+#define MPI_ERR_ROOT GPUMPI_ERR_ROOT
+#define MPI_ERR_OP GPUMPI_ERR_OP
+#define MPI_ERR_ARG GPUMPI_ERR_ARG
+#define MPI_ERR_REQUEST GPUMPI_ERR_REQUEST
+#define MPI_ERR_TRUNCATE GPUMPI_ERR_TRUNCATE
+#define MPI_ERR_NO_MEM GPUMPI_ERR_NO_MEM
+#define MPI_ERR_INTERN GPUMPI_ERR_INTERN
+#define MPI_UNDEFINED -1
+#define MPI_THREAD_SINGLE 1
+#define MPI_THREAD_FUNNELED 2
+#define MPI_THREAD_SERIALIZED 3
+#define MPI_THREAD_MULTIPLE 4
+#define MPI_IN_PLACE ((void*)(intptr_t)1)
+#define MPI_BOTTOM ((void*)0)
+
+// ---- datatypes: the reference's enum (gpu_libs/gpu_mpi/datatypes.cuh:12-14) with a fixed
+//      underlying type so derived-type handles can share it ----
+enum MPI_Datatype : int {
+    MPI_CHAR = GPUMPI_CHAR,
+    MPI_SHORT = GPUMPI_SHORT,
+    MPI_INT = GPUMPI_INT,
+    MPI_LONG = GPUMPI_LONG,
+    MPI_LONG_LONG_INT = GPUMPI_LONG_LONG_INT,
+    MPI_LONG_LONG = GPUMPI_LONG_LONG,
+    MPI_SIGNED_CHAR = GPUMPI_SIGNED_CHAR,
+    MPI_UNSIGNED_CHAR = GPUMPI_UNSIGNED_CHAR,
+    MPI_UNSIGNED_SHORT = GPUMPI_UNSIGNED_SHORT,
+    MPI_UNSIGNED = GPUMPI_UNSIGNED,
+    MPI_UNSIGNED_LONG = GPUMPI_UNSIGNED_LONG,
+    MPI_UNSIGNED_LONG_LONG = GPUMPI_UNSIGNED_LONG_LONG,
+    MPI_FLOAT = GPUMPI_FLOAT,
+    MPI_DOUBLE = GPUMPI_DOUBLE,
+    MPI_LONG_DOUBLE = GPUMPI_LONG_DOUBLE,
+    MPI_WCHAR = GPUMPI_WCHAR,
+    MPI_C_BOOL = GPUMPI_C_BOOL,
+    MPI_INT8_T = GPUMPI_INT8_T,
+    MPI_INT16_T = GPUMPI_INT16_T,
+    MPI_INT32_T = GPUMPI_INT32_T,
+    MPI_INT64_T = GPUMPI_INT64_T,
+    MPI_UINT8_T = GPUMPI_UINT8_T,
+    MPI_UINT16_T = GPUMPI_UINT16_T,
+    MPI_UINT32_T = GPUMPI_UINT32_T,
+    MPI_UINT64_T = GPUMPI_UINT64_T,
+    MPI_C_COMPLEX = GPUMPI_C_COMPLEX,
+    MPI_C_FLOAT_COMPLEX = GPUMPI_C_FLOAT_COMPLEX,
+    MPI_C_DOUBLE_COMPLEX = GPUMPI_C_DOUBLE_COMPLEX,
+    MPI_C_LONG_DOUBLE_COMPLEX = GPUMPI_C_LONG_DOUBLE_COMPLEX,
+    MPI_BYTE = GPUMPI_BYTE,
+    MPI_2INT = GPUMPI_2INT,
+    MPI_FLOAT_INT = GPUMPI_FLOAT_INT,
+    MPI_DOUBLE_INT = GPUMPI_DOUBLE_INT,
+    MPI_LONG_INT = GPUMPI_LONG_INT,
+    MPI_SHORT_INT = GPUMPI_SHORT_INT,
+    MPI_LONG_DOUBLE_INT = GPUMPI_LONG_DOUBLE_INT,
+    MPI_DATATYPE_NULL = GPUMPI_DATATYPE_NULL,
+};
+#define MPI_ORDER_C 56
+#define MPI_ORDER_FORTRAN 57
+
+// ---- opaque handles (reference: communicator.cuh:6-8, group.cuh:4-5, operators.cuh:7-8, mpi.cuh:26-29) ----
+struct MPI_Comm_impl;
+using MPI_Comm = MPI_Comm_impl*;
+struct MPI_Group_impl;
+typedef MPI_Group_impl* MPI_Group;
+struct MPI_Op_impl;
+using MPI_Op = MPI_Op_impl*;
+struct MPI_Request_impl;
+using MPI_Request = MPI_Request_impl*;
+#define MPI_REQUEST_NULL nullptr
+#define MPI_OP_NULL nullptr
+
+typedef void MPI_User_function(void* invec, void* inoutvec, int* len, MPI_Datatype* datatype);
+
+__device__ extern MPI_Comm MPI_COMM_WORLD;
+__device__ extern MPI_Comm MPI_COMM_NULL;
+__device__ extern MPI_Comm MPI_COMM_SELF;
+__device__ extern MPI_Group MPI_GROUP_WORLD;
+__device__ extern MPI_Group MPI_GROUP_NULL;
+__device__ extern MPI_Group MPI_GROUP_EMPTY;
+
+__device__ extern MPI_Op MPI_MAX;
+__device__ extern MPI_Op MPI_MIN;
+__device__ extern MPI_Op MPI_SUM;
+__device__ extern MPI_Op MPI_PROD;
+__device__ extern MPI_Op MPI_LAND;
+__device__ extern MPI_Op MPI_BAND;
+__device__ extern MPI_Op MPI_LOR;
+__device__ extern MPI_Op MPI_BOR;
+__device__ extern MPI_Op MPI_LXOR;
+__device__ extern MPI_Op MPI_BXOR;
+__device__ extern MPI_Op MPI_MAXLOC;
+__device__ extern MPI_Op MPI_MINLOC;
+
+struct MPI_Status {
+    int MPI_SOURCE = MPI_ANY_SOURCE;
+    int MPI_TAG = MPI_ANY_TAG;
+    int MPI_ERROR = MPI_SUCCESS;
+    long long count_bytes = 0;
+};
+#define MPI_STATUSES_IGNORE ((MPI_Status*)nullptr)
+#define MPI_STATUS_IGNORE ((MPI_Status*)nullptr)
+
+typedef long long MPI_Aint;
+typedef long long MPI_Count;
+
+// ---- environment (reference mpi.cuh:39-46,49,63,66,121) ----
+__device__ int MPI_Init(int* argc, char*** argv);
+__device__ int MPI_Init_thread(int* argc, char*** argv, int required, int* provided);
+__device__ int MPI_Initialized(int* flag);
+__device__ int MPI_Finalize(void);
+__device__ int MPI_Finalized(int* flag);
+__device__ int MPI_Abort(MPI_Comm comm, int errorcode);
+__device__ int MPI_Get_processor_name(char* name, int* resultlen);
+__device__ double MPI_Wtime(void);
+__device__ double MPI_Wtick(void);
+
+// ---- point-to-point (reference mpi.cuh:55-62,113-128) ----
+__device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int dest, int tag, MPI_Comm comm);
+__device__ int MPI_Ssend(const void* buf, int count, MPI_Datatype datatype, int dest, int tag, MPI_Comm comm);
+__device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source, int tag, MPI_Comm comm,
+                        MPI_Status* status);
+__device__ int MPI_Sendrecv(const void* sendbuf, int sendcount, MPI_Datatype sendtype, int dest, int sendtag,
+                            void* recvbuf, int recvcount, MPI_Datatype recvtype, int source, int recvtag,
+                            MPI_Comm comm, MPI_Status* status);
+__device__ int MPI_Isend(const void* buf, int count, MPI_Datatype datatype, int dest, int tag, MPI_Comm comm,
+                         MPI_Request* request);
+__device__ int MPI_Issend(const void* buf, int count, MPI_Datatype datatype, int dest, int tag, MPI_Comm comm,
+                          MPI_Request* request);
+__device__ int MPI_Irecv(void* buf, int count, MPI_Datatype datatype, int source, int tag, MPI_Comm comm,
+                         MPI_Request* request);
+__device__ int MPI_Wait(MPI_Request* request, MPI_Status* status);
+__device__ int MPI_Waitall(int count, MPI_Request array_of_requests[], MPI_Status* array_of_statuses);
+__device__ int MPI_Waitany(int count, MPI_Request array_of_requests[], int* index, MPI_Status* status);
+__device__ int MPI_Waitsome(int incount, MPI_Request array_of_requests[], int* outcount, int array_of_indices[],
+                            MPI_Status array_of_statuses[]);
+__device__ int MPI_Test(MPI_Request* request, int* flag, MPI_Status* status);
+__device__ int MPI_Testall(int count, MPI_Request array_of_requests[], int* flag, MPI_Status array_of_statuses[]);
+__device__ int MPI_Request_free(MPI_Request* request);
+__device__ int MPI_Iprobe(int source, int tag, MPI_Comm comm, int* flag, MPI_Status* status);
+__device__ int MPI_Probe(int source, int tag, MPI_Comm comm, MPI_Status* status);
+__device__ int MPI_Get_count(const MPI_Status* status, MPI_Datatype datatype, int* count);
+
+// ---- collectives (reference mpi.cuh:47-94) ----
+__device__ int MPI_Barrier(MPI_Comm comm);
+__device__ int MPI_Bcast(void* buffer, int count, MPI_Datatype datatype, int root, MPI_Comm comm);
+__device__ int MPI_Reduce(const void* sendbuf, void* recvbuf, int count, MPI_Datatype datatype, MPI_Op op, int root,
+                          MPI_Comm comm);
+__device__ int MPI_Allreduce(const void* sendbuf, void* recvbuf, int count, MPI_Datatype datatype, MPI_Op op,
+                             MPI_Comm comm);
+__device__ int MPI_Gather(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf, int recvcount,
+                          MPI_Datatype recvtype, int root, MPI_Comm comm);
+__device__ int MPI_Gatherv(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf,
+                           const int recvcounts[], const int displs[], MPI_Datatype recvtype, int root, MPI_Comm comm);
+__device__ int MPI_Scatter(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf, int recvcount,
+                           MPI_Datatype recvtype, int root, MPI_Comm comm);
+__device__ int MPI_Scatterv(const void* sendbuf, const int sendcounts[], const int displs[], MPI_Datatype sendtype,
+                            void* recvbuf, int recvcount, MPI_Datatype recvtype, int root, MPI_Comm comm);
+__device__ int MPI_Allgather(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf, int recvcount,
+                             MPI_Datatype recvtype, MPI_Comm comm);
+__device__ int MPI_Allgatherv(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf,
+                              const int recvcounts[], const int displs[], MPI_Datatype recvtype, MPI_Comm comm);
+__device__ int MPI_Alltoall(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf, int recvcount,
+                            MPI_Datatype recvtype, MPI_Comm comm);
+__device__ int MPI_Alltoallv(const void* sendbuf, const int sendcounts[], const int sdispls[], MPI_Datatype sendtype,
+                             void* recvbuf, const int recvcounts[], const int rdispls[], MPI_Datatype recvtype,
+                             MPI_Comm comm);
+
+// ---- operators (reference operators.cuh:18-20, mpi.cuh:43-44) ----
+__device__ int MPI_Op_create(MPI_User_function* user_fn, int commute, MPI_Op* op);
+__device__ int MPI_Op_free(MPI_Op* op);
+
+// ---- datatypes (reference mpi.cuh:53-54,67 are stubs there; implemented here per the MPI standard) ----
+__device__ int MPI_Type_size(MPI_Datatype datatype, int* size);
+__device__ int MPI_Type_get_extent(MPI_Datatype datatype, MPI_Aint* lb, MPI_Aint* extent);
+__device__ int MPI_Type_contiguous(int count, MPI_Datatype oldtype, MPI_Datatype* newtype);
+__device__ int MPI_Type_vector(int count, int blocklength, int stride, MPI_Datatype oldtype, MPI_Datatype* newtype);
+__device__ int MPI_Type_create_hvector(int count, int blocklength, MPI_Aint stride, MPI_Datatype oldtype,
+                                       MPI_Datatype* newtype);
+__device__ int MPI_Type_create_subarray(int ndims, const int array_of_sizes[], const int array_of_subsizes[],
+                                        const int array_of_starts[], int order, MPI_Datatype oldtype,
+                                        MPI_Datatype* newtype);
+__device__ int MPI_Type_commit(MPI_Datatype* datatype);
+__device__ int MPI_Type_free(MPI_Datatype* datatype);
+
+// ---- communicators and groups (reference communicator.cuh:23-49, group.cuh:21-31) ----
+__device__ int MPI_Comm_size(MPI_Comm comm, int* size);
+__device__ int MPI_Comm_rank(MPI_Comm comm, int* rank);
+__device__ int MPI_Comm_group(MPI_Comm comm, MPI_Group* group);
+__device__ int MPI_Comm_create(MPI_Comm comm, MPI_Group group, MPI_Comm* newcomm);
+__device__ int MPI_Comm_dup(MPI_Comm comm, MPI_Comm* newcomm);
+__device__ int MPI_Comm_split(MPI_Comm comm, int color, int key, MPI_Comm* newcomm);
+__device__ int MPI_Comm_free(MPI_Comm* comm);
+__device__ int MPI_Group_incl(MPI_Group group, int n, const int ranks[], MPI_Group* newgroup);
+__device__ int MPI_Group_range_incl(MPI_Group group, int n, int ranges[][3], MPI_Group* newgroup);
+__device__ int MPI_Group_free(MPI_Group* group);
+__device__ int MPI_Group_size(MPI_Group group, int* size);
+__device__ int MPI_Group_rank(MPI_Group group, int* rank);
+__device__ int MPI_Group_translate_ranks(MPI_Group group1, int n, const int ranks1[], MPI_Group group2, int ranks2[]);
+
+// ---- block-rank extensions (no counterpart in the reference) ----
+// Rank of the calling block in MPI_COMM_WORLD, usable anywhere in the rank's block.
+__device__ int gpumpi_world_rank(void);
+// Run fn(arg, tid, nthreads) on every thread of the calling rank's block (called from thread 0);
+// gives scalar user code the data-parallel width of its block between MPI calls.
+__device__ int gpumpi_block_parallel(void (*fn)(void* arg, int tid, int nthreads), void* arg);
+// Per-rank copy of a converted program's global variable (reference global_vars.cuh:15 indexes by
+// the global thread id; a rank here is a block, so the index is the rank).
+#define __gpu_global(var) (var[gpumpi_world_rank()])
