@@ -1,0 +1,311 @@
+#!/usr/bin/env python
+"""Benchmark of the intra-GPU MPI hot path (one JSON line on stdout).
+
+Default workload: MPI_Allreduce(SUM, fp32) among 1024 block-ranks, 1 MiB per rank (262144 floats),
+canonical rank order, inputs resident in HBM (1 GiB of inputs + 1 GiB of outputs: larger than the
+129 MB L2, so no L2 flush is needed between steps).  A "step" is one MPI_Allreduce call by every rank;
+K steps run inside one persistent launch of the rank kernel, timed with CUDA events on its stream.
+
+Reported:
+  value      algorithmic GB/s = 2 * ranks * bytes_per_rank / step time (every input read once, every
+             output written once), summed over replicas when run on N GPUs (replicas only);
+  e2e        the same metric through the C ABI with pinned HOST buffers: host->device copy of the
+             inputs, the collective, device->host copy of all outputs, every step;
+  roofline   against the measured HBM copy bandwidth (MEASURED_PEAKS.json, "of measured");
+  cpu_baseline  the CPU oracle's multi-threaded allreduce on a bounded sample, on this host's cores;
+  extra      p50/p99 per-call latency, Alltoallv GB/s on the bucket-sort shape, per-variant GB/s.
+
+--impl reference: the reference's algorithm for this path restated on the CPU (the oracle port:
+canonical-order fold, all host threads) on the same workload; the reference's own gpu_mpi runtime
+cannot run on the GPU machine.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "dphpc-gpu_mpi_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "intra-GPU Allreduce/Alltoallv GB/s & p50 latency: learned vs tuned vs plain"
+WORKLOAD = {"workload": "allreduce_sum_f32_1024ranks_1MiB", "ranks": 1024, "bytes_per_rank": 1 << 20,
+            "dtype": "f32", "op": "sum", "order": "canonical", "l2": "inputs 1 GiB > L2, no flush"}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1
+    import torch.distributed as dist
+    import torch
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    dist.init_process_group(backend=backend)
+    return dist, dist.get_rank(), ws
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-i", str(index), "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per step of the allreduce from the committed ncu summary (scaled to the bench size)."""
+    p = ROOT / "profiles" / "allreduce_fold_1024ranks.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_step_full_size:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(threads: int):
+    from oracle import oracle
+    import numpy as np
+    n, count = 1024, 16384  # 64 KiB per rank: same rank count, bounded sample
+    x = oracle.fill_f32(7, n * count).reshape(n, count)
+    oracle.allreduce(x, 12, 2, threads=threads)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        oracle.allreduce(x, 12, 2, threads=threads)
+        reps += 1
+        if time.perf_counter() - t0 > 4.0 or reps >= 200:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    gbs = 2.0 * n * count * 4 / dt / 1e9
+    return {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"oracle allreduce fp32 SUM, 1024 ranks x 64 KiB, {reps} reps, {threads} threads"}
+
+
+def run_reference(args, dist, rank, ws):
+    """The reference's CPU restatement (oracle port) on the same workload, all host threads."""
+    if rank != 0:
+        return
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    n, count = WORKLOAD["ranks"], WORKLOAD["bytes_per_rank"] // 4
+    x = oracle.fill_f32(1, n * count).reshape(n, count)
+    for _ in range(max(0, min(args.warmup, 1))):
+        oracle.allreduce(x, 12, 2, threads=threads)
+    steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        oracle.allreduce(x, 12, 2, threads=threads)
+    dt = (time.perf_counter() - t0) / steps
+    gbs = 2.0 * n * count * 4 / dt / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": ws, "steps": steps,
+            "warmup": min(args.warmup, 1), "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (LCG)",
+            "config": dict(WORKLOAD),
+            "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+                             "sample": f"full workload, {steps} steps (bounded), {threads} threads"},
+            "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def pct(v, q):
+    v = sorted(v)
+    if not v:
+        return None
+    k = min(len(v) - 1, max(0, int(round(q * (len(v) - 1)))))
+    return v[k]
+
+
+def bench_alltoallv(gpumpi, torch, w_kw):
+    """Bucket-sort shape: 2^25 int32 keys over 256 ranks, keys ~ mean of four U(0,1), bucketed by range."""
+    import numpy as np
+    n, kpr = 256, (1 << 25) // 256
+    g = torch.Generator(device="cuda").manual_seed(1234)
+    keys = (torch.rand((n, kpr, 4), generator=g, device="cuda", dtype=torch.float64).sum(-1) * (1 << 19)).floor()
+    keys = keys.to(torch.int32)
+    dest = (keys.to(torch.int64) * n) >> 21
+    order = torch.argsort(dest, dim=1, stable=True)
+    send = torch.gather(keys, 1, order).contiguous()
+    sc = torch.stack([torch.bincount(dest[r], minlength=n) for r in range(n)]).to(torch.int32)
+    rc = sc.t().contiguous()
+    sd = torch.cumsum(sc, 1, dtype=torch.int32) - sc
+    rd = torch.cumsum(rc, 1, dtype=torch.int32) - rc
+    R = int(rc.sum(1).max().item())
+    recv = torch.zeros((n, R), dtype=torch.int32, device="cuda")
+    total_bytes = int(sc.sum().item()) * 4
+    with gpumpi.World(n, **w_kw) as w:
+        w.alltoallv(send, kpr * 4, sc, sd, recv, R * 4, rc, rd, gpumpi.INT, iters=3)
+        iters = 20
+        ns = np.zeros(iters, dtype=np.uint64)
+        w.alltoallv(send, kpr * 4, sc, sd, recv, R * 4, rc, rd, gpumpi.INT, iters=iters, iter_ns=ns)
+        ms = w.last_kernel_ms() / iters
+    return {"ranks": n, "keys": 1 << 25, "bytes_moved_per_call": total_bytes,
+            "gbs": 2.0 * total_bytes / (ms * 1e-3) / 1e9, "ms_per_call": ms,
+            "p50_us": float(pct(list(ns), 0.5)) / 1e3, "p99_us": float(pct(list(ns), 0.99)) / 1e3}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extra", action="store_true")
+    args = ap.parse_args()
+    dist, rank, ws = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, dist, rank, ws)
+        return
+    import numpy as np
+    import torch
+    import gpumpi
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    gpumpi.build()
+    n, per = WORKLOAD["ranks"], WORKLOAD["bytes_per_rank"]
+    count = per // 4
+    K, W = max(1, args.steps), max(3, args.warmup)
+    w_kw = {"device": local, "timeout_s": 30.0}
+    g = torch.Generator(device="cuda").manual_seed(2026 + rank)
+    send = (torch.rand((n, count), generator=g, device="cuda") * 2 - 1).contiguous()
+    recv = torch.empty_like(send)
+    world = gpumpi.World(n, **w_kw)
+    world.allreduce(send, recv, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=W)
+    torch.cuda.synchronize()
+    # canonical-order result is identical on every rank
+    assert torch.equal(recv[0], recv[n - 1]), "allreduce results differ between ranks"
+
+    ns = np.zeros(K, dtype=np.uint64)
+    clocks = ClockSampler(local)
+    time.sleep(0.2)
+    barrier(dist)
+    torch.cuda.synchronize()
+    l0 = gpumpi.kernel_launches()
+    world.allreduce(send, recv, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=K, iter_ns=ns)
+    torch.cuda.synchronize()
+    launches = gpumpi.kernel_launches() - l0
+    barrier(dist)
+    ms_total = world.last_kernel_ms()
+    clk = clocks.stop()
+    ms_step = max_over_ranks(dist, ms_total / K)
+    algo_bytes = 2.0 * n * per
+    value = ws * algo_bytes / (ms_step * 1e-3) / 1e9
+    p50, p99 = float(pct(list(ns), 0.5)) / 1e3, float(pct(list(ns), 0.99)) / 1e3
+
+    # end to end through the C ABI with pinned host buffers (H2D + collective + D2H every step)
+    hs = send.cpu().pin_memory()
+    hr = torch.empty_like(hs).pin_memory()
+    ke = max(1, min(K, 10))
+    world.allreduce(hs.numpy(), hr.numpy(), count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=1)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        world.allreduce(hs.numpy(), hr.numpy(), count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=1)
+    e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / ke)
+    assert torch.equal(hr[0], recv[0].cpu())
+    e2e = {"value": ws * algo_bytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": n * per,
+           "d2h_bytes_per_step": n * per, "ms_per_step": e2e_s * 1e3}
+
+    peak, peak_kind = measured_peak()
+    achieved = algo_bytes / (ms_total / K * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"hbm_gbs of {peak_kind}", "traffic": traffic_from_profile(),
+                "algorithmic_bytes_per_step": algo_bytes, "kernel": "gpumpi_rank_kernel<Coll> (fold_fast<float,SUM>)"}
+
+    extra = {"p50_us": p50, "p99_us": p99, "world": world.info()}
+    if not args.no_extra and rank == 0:
+        try:
+            extra["alltoallv_bucket_sort"] = bench_alltoallv(gpumpi, torch, w_kw)
+        except Exception as e:  # reported, not hidden
+            extra["alltoallv_bucket_sort"] = {"error": str(e)}
+        variants = {}
+        for v in range(4):
+            world.set_policy(v, 0)
+            world.allreduce(send, recv, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=20)
+            variants[gpumpi.VARIANT_NAMES[v]] = algo_bytes / (world.last_kernel_ms() / 20 * 1e-3) / 1e9
+        world.set_policy(-1, 0)
+        extra["allreduce_variants_gbs"] = variants
+    world.close()
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": ws, "steps": K, "warmup": W,
+                "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic (torch.rand uniform [-1,1), seeded)",
+                "config": dict(WORKLOAD, parallelism=f"replicas x{ws}"),
+                "roofline": roofline, "e2e": e2e,
+                "cpu_baseline": cpu_baseline(os.cpu_count() or 1),
+                "clocks": clk, "gpu_launches": launches, "extra": extra}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -80,7 +80,7 @@ __device__ __noinline__ int job_run_and_wait(Job* j, int line) {
         dispatch(t);
         job_finish(j);
     }
-    unsigned long long target = ((unsigned long long)j->epoch << 32) | (unsigned)j->nchunks;
+    const unsigned long long target = ld_acquire64(&j->limit);  // (epoch << 32) | nchunks
     if (ld_acquire64(&j->done) == target) return 0;
     Deadline d = make_deadline();
     while (ld_acquire64(&j->done) != target) {
@@ -107,6 +107,34 @@ __device__ int comm_barrier(MPI_Comm_impl* c, F&& setup, int line) {
         if (int e = wait_tick(d, line, 64)) return e;
     }
     return 0;
+}
+
+// Parameters of the job epoch being executed, read once per chunk with L2-only loads (the Job
+// struct is rewritten by every epoch, so no executing block may keep it in L1).
+struct JobParams {
+    int kind, dt, op, root, esize, vec, tile, aligned16;
+    long long count, chunk;
+    const MPI_Comm_impl* comm;
+    const void* src;
+    void* dst;
+    MPI_User_function* ufn;
+};
+
+__device__ __forceinline__ void load_params(const Job* j, JobParams& P) {
+    P.kind = __ldcg(&j->kind);
+    P.dt = __ldcg(&j->dt);
+    P.op = __ldcg(&j->op);
+    P.root = __ldcg(&j->root);
+    P.esize = __ldcg(&j->esize);
+    P.vec = __ldcg(&j->vec);
+    P.tile = __ldcg(&j->tile);
+    P.aligned16 = __ldcg(&j->aligned16);
+    P.count = __ldcg(&j->count);
+    P.chunk = __ldcg(&j->chunk);
+    P.comm = (const MPI_Comm_impl*)__ldcg((const unsigned long long*)&j->comm);
+    P.src = (const void*)__ldcg((const unsigned long long*)&j->src);
+    P.dst = (void*)__ldcg((const unsigned long long*)&j->dst);
+    P.ufn = (MPI_User_function*)__ldcg((const unsigned long long*)&j->ufn);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -174,7 +202,7 @@ __device__ __forceinline__ void st_elems(T* p, const T (&v)[V], int nv, bool vec
 // Canonical-order fold of elements [e0, e0 + nt*V): thread tid owns V consecutive elements.
 // order: acc = x_0; acc = op(x_s, acc) for s = 1..n-1 (in comm-rank order).
 template <class T, int OP, int V>
-__device__ __noinline__ void fold_fast(const Job* j, long long e0, int tid, int nt) {
+__device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid, int nt) {
     constexpr int BYTES = V * (int)sizeof(T);
     // ranks folded per step: ~64 bytes of loads in flight per thread without spilling
     constexpr int U = 64 / BYTES > 8 ? 8 : 64 / BYTES < 1 ? 1 : 64 / BYTES;
@@ -230,7 +258,7 @@ __device__ __noinline__ void fold_fast(const Job* j, long long e0, int tid, int 
 }
 
 // Any legal (op, type) and user-defined ops, one element per thread, same canonical order.
-__device__ __noinline__ void fold_generic(const Job* j, long long e0, int tid, int nt) {
+__device__ __noinline__ void fold_generic(const JobParams* j, long long e0, int tid, int nt) {
     const MPI_Comm_impl* c = j->comm;
     const CollSlot* slots = c->slots;
     const int n = c->size;
@@ -277,7 +305,7 @@ __device__ __noinline__ void fold_generic(const Job* j, long long e0, int tid, i
 // storage-type / op dispatch of the fast path; returns false if no fast instantiation exists
 // vec choices: 16/sizeof(T) (one 16-byte vector), 8/sizeof(T) (4-byte types), 1
 template <class T, int OP>
-__device__ __forceinline__ void fold_fast_v(const Job* j, long long e0, int tid, int nt) {
+__device__ __forceinline__ void fold_fast_v(const JobParams* j, long long e0, int tid, int nt) {
     constexpr int VW = 16 / sizeof(T);
     if (j->vec >= VW) fold_fast<T, OP, VW>(j, e0, tid, nt);
     else if constexpr (sizeof(T) == 4) {
@@ -287,7 +315,7 @@ __device__ __forceinline__ void fold_fast_v(const Job* j, long long e0, int tid,
 }
 
 template <class T>
-__device__ __forceinline__ bool fold_fast_arith(const Job* j, long long e0, int tid, int nt) {
+__device__ __forceinline__ bool fold_fast_arith(const JobParams* j, long long e0, int tid, int nt) {
     switch (j->op) {
     case GPUMPI_OP_SUM: fold_fast_v<T, GPUMPI_OP_SUM>(j, e0, tid, nt); return true;
     case GPUMPI_OP_MAX: fold_fast_v<T, GPUMPI_OP_MAX>(j, e0, tid, nt); return true;
@@ -298,7 +326,7 @@ __device__ __forceinline__ bool fold_fast_arith(const Job* j, long long e0, int 
 }
 
 template <class T>
-__device__ __forceinline__ bool fold_fast_int(const Job* j, long long e0, int tid, int nt) {
+__device__ __forceinline__ bool fold_fast_int(const JobParams* j, long long e0, int tid, int nt) {
     switch (j->op) {
     case GPUMPI_OP_BAND: fold_fast_v<T, GPUMPI_OP_BAND>(j, e0, tid, nt); return true;
     case GPUMPI_OP_BOR: fold_fast_v<T, GPUMPI_OP_BOR>(j, e0, tid, nt); return true;
@@ -325,7 +353,7 @@ __device__ __forceinline__ bool fold_has_fast(int dt, int op, MPI_User_function*
     }
 }
 
-__device__ __noinline__ void fold_chunk(const Job* j, long long idx, int tid, int nt) {
+__device__ __noinline__ void fold_chunk(const JobParams* j, long long idx, int tid, int nt) {
     const long long e0 = idx * j->chunk;
     bool done = false;
 #ifndef GPUMPI_NO_FAST_FOLD
@@ -360,7 +388,7 @@ struct Piece {
 
 __device__ __forceinline__ int ldcg_int(const int* p) { return __ldcg(p); }
 
-__device__ __forceinline__ void piece_of(const Job* j, long long p, Piece& pc) {
+__device__ __forceinline__ void piece_of(const JobParams* j, long long p, Piece& pc) {
     const MPI_Comm_impl* c = j->comm;
     const CollSlot* S = c->slots;
     const int n = c->size;
@@ -439,7 +467,7 @@ __device__ __forceinline__ void piece_copy(const Piece& pc, long long b0, long l
     else typed_copy(pc.dst, pc.rdesc, pc.src, pc.sdesc, b0, b1, lane, nl);
 }
 
-__device__ __noinline__ void pull_chunk(Job* j, long long idx, int tid, int nt) {
+__device__ __noinline__ void pull_chunk(const JobParams* j, Job* jg, long long idx, int tid, int nt) {
     const long long npieces = j->count;
     if (j->vec > 1) {  // byte range `part` of one piece, whole block
         const long long p = idx / j->vec;
@@ -449,7 +477,7 @@ __device__ __noinline__ void pull_chunk(Job* j, long long idx, int tid, int nt) 
         long long per = ((pc.bytes + j->vec - 1) / j->vec + 15) & ~15LL;
         long long b0 = per * part, b1 = min(pc.bytes, b0 + per);
         piece_copy(pc, b0, b1, tid, nt);
-        if (tid == 0 && part == 0 && pc.trunc) atomicOr(&j->err, 1u);
+        if (tid == 0 && part == 0 && pc.trunc) atomicOr(&jg->err, 1u);
         return;
     }
     const int lane = tid & 31, warp = tid >> 5, nwarps = (nt + 31) >> 5;
@@ -459,21 +487,24 @@ __device__ __noinline__ void pull_chunk(Job* j, long long idx, int tid, int nt) 
         Piece pc;
         piece_of(j, p, pc);
         piece_copy(pc, 0, pc.bytes, lane, 32);
-        if (lane == 0 && pc.trunc) atomicOr(&j->err, 1u);
+        if (lane == 0 && pc.trunc) atomicOr(&jg->err, 1u);
     }
 }
 
-__device__ __noinline__ void copy_chunk(const Job* j, long long idx, int tid, int nt) {
+__device__ __noinline__ void copy_chunk(const JobParams* j, long long idx, int tid, int nt) {
     long long off = idx * j->chunk;
     long long len = min(j->chunk, j->count - off);
     copy_bytes((char*)j->dst + off, (const char*)j->src + off, len, tid, nt);
 }
 
-__device__ __noinline__ void exec_chunk(Job* j, long long idx, int tid, int nt) {
+__device__ __noinline__ void exec_chunk(Job* jg, long long idx, int tid, int nt) {
+    JobParams P;
+    load_params(jg, P);
+    const JobParams* j = &P;
     switch (j->kind) {
     case JOB_COPY: copy_chunk(j, idx, tid, nt); break;
     case JOB_ALLREDUCE: case JOB_REDUCE: fold_chunk(j, idx, tid, nt); break;
-    default: pull_chunk(j, idx, tid, nt); break;
+    default: pull_chunk(j, jg, idx, tid, nt); break;
     }
 }
 

@@ -1,0 +1,213 @@
+"""GPU parity of the hot path against the CPU oracle, through the C ABI: bit-exact for integer and
+byte data and for floating-point reductions in the canonical rank order."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+ALLREDUCE_CASES = [
+    # ranks, count, dt, op, numpy dtype
+    (2, 1, 2, 2, np.int32),
+    (7, 17, 13, 2, np.float64),
+    (32, 1000, 12, 2, np.float32),
+    (64, 4096, 12, 2, np.float32),
+    (128, 3333, 2, 2, np.int32),
+    (256, 1 << 14, 13, 2, np.float64),
+    (64, 2048, 12, 0, np.float32),
+    (64, 2048, 2, 1, np.int32),
+    (48, 777, 20, 3, np.int64),
+    (33, 1025, 2, 9, np.int32),
+    (16, 100, 18, 3, np.int16),      # generic path, wraps
+    (16, 64, 16, 8, np.uint8),       # bool LXOR (reference semantics)
+    (1024, 1 << 12, 12, 2, np.float32),
+]
+
+
+def make_input(oracle, n, count, npdt, seed):
+    if np.issubdtype(npdt, np.floating):
+        x = oracle.fill_f64(seed, n * count).astype(npdt)
+    else:
+        x = oracle.fill_i32(seed, n * count)
+        if npdt == np.uint8:
+            x = (x & 1).astype(npdt)
+        else:
+            x = (x % 1000).astype(npdt)
+    return x.reshape(n, count)
+
+
+@pytest.mark.parametrize("n,count,dt,op,npdt", ALLREDUCE_CASES)
+def test_allreduce_matches_oracle_bit_exact(gpulib, oracle, n, count, dt, op, npdt):
+    x = make_input(oracle, n, count, npdt, 1000 + n + count)
+    ref = oracle.allreduce(x, dt, op)
+    with gpulib.World(n, timeout_s=10.0) as w:
+        s, r = dev(x), dev(np.zeros_like(x))
+        w.allreduce(s, r, count, dt, op)
+        got = host(r)
+    assert np.array_equal(got.view(np.uint8), ref.view(np.uint8))
+
+
+def test_allreduce_host_buffers_and_in_place(gpulib, oracle):
+    n, count = 24, 5000
+    x = make_input(oracle, n, count, np.float32, 5)
+    ref = oracle.allreduce(x, 12, 2)
+    with gpulib.World(n, timeout_s=10.0) as w:
+        out = np.zeros_like(x)
+        w.allreduce(x, out, count, 12, 2)          # host (numpy) buffers, staged by the library
+        assert np.array_equal(out, ref)
+        buf = dev(x)
+        import ctypes
+        rc = w.coll("allreduce", 1, buf, count, 12, 2, send_stride=0, recv_stride=count * 4)  # MPI_IN_PLACE
+        assert rc == 0, w.last_error()
+        assert np.array_equal(host(buf), ref)
+
+
+def test_allreduce_variants_agree(gpulib, oracle):
+    n, count = 64, 1 << 14
+    x = make_input(oracle, n, count, np.float32, 9)
+    ref = oracle.allreduce(x, 12, 2)
+    ref64 = x.astype(np.float64).sum(0)
+    with gpulib.World(n, timeout_s=10.0) as w:
+        for v in range(4):
+            w.set_policy(v, 0)
+            s, r = dev(x), dev(np.zeros_like(x))
+            w.allreduce(s, r, count, 12, 2)
+            got = host(r)
+            if v in (0, 3):   # canonical order: bit-exact
+                assert np.array_equal(got, ref), v
+            else:             # reordered: within 1e-6 relative of the fp64 sum (scaled by sum |x|)
+                scale = np.abs(x).astype(np.float64).sum(0) + 1e-30
+                assert (np.abs(got[0] - ref64) / scale).max() <= 1e-6, v
+                assert (got == got[0]).all()
+
+
+@pytest.mark.parametrize("n,count,root,dt", [(5, 14, 0, 2), (33, 1000, 7, 13), (100, 4096, 99, 12)])
+def test_reduce_matches_oracle(gpulib, oracle, n, count, root, dt):
+    npdt = {2: np.int32, 12: np.float32, 13: np.float64}[dt]
+    x = make_input(oracle, n, count, npdt, 77)
+    ref = oracle.reduce(x, dt, 2)
+    with gpulib.World(n, timeout_s=10.0) as w:
+        s, r = dev(x), dev(np.zeros_like(x))
+        w.reduce(s, r, count, dt, 2, root)
+        got = host(r)
+    assert np.array_equal(got[root], ref)
+
+
+@pytest.mark.parametrize("n,count,root", [(2, 1, 1), (7, 10, 3), (64, 1 << 16, 5), (300, 333, 299)])
+def test_bcast(gpulib, oracle, n, count, root):
+    x = np.zeros((n, count), np.int32)
+    x[root] = oracle.fill_i32(3, count)
+    with gpulib.World(n, timeout_s=10.0) as w:
+        b = dev(x)
+        w.bcast(b, count, 2, root)
+        got = host(b)
+    assert (got == x[root]).all()
+
+
+@pytest.mark.parametrize("n,c", [(3, 1), (10, 16), (64, 256), (256, 37), (32, 20000)])
+def test_alltoall(gpulib, oracle, n, c):
+    x = oracle.fill_i32(11 + n, n * n * c).reshape(n, n * c)
+    sc = np.full((n, n), c, np.int32)
+    d = np.tile(np.arange(n, dtype=np.int32) * c, (n, 1))
+    ref = oracle.alltoallv(x, sc, d, n * c, sc, d)
+    with gpulib.World(n, timeout_s=10.0) as w:
+        s, r = dev(x), dev(np.zeros_like(x))
+        w.alltoall(s, r, c, 2)
+        got = host(r)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("n,maxc,zero_frac", [(4, 5, 0.3), (37, 40, 0.5), (256, 300, 0.2), (128, 3, 0.9)])
+def test_alltoallv_uneven_and_zero_counts(gpulib, oracle, n, maxc, zero_frac):
+    # zero-count pairs abort the reference (hazard H2: assert(dataSize > 0), mpi.cu:548-549)
+    rng = np.random.default_rng(n)
+    sc = rng.integers(1, maxc + 1, (n, n)).astype(np.int32)
+    sc[rng.random((n, n)) < zero_frac] = 0
+    rc = sc.T.copy()
+    sd = np.concatenate([np.zeros((n, 1), np.int32), np.cumsum(sc, 1)[:, :-1]], 1).astype(np.int32)
+    rd = np.concatenate([np.zeros((n, 1), np.int32), np.cumsum(rc, 1)[:, :-1]], 1).astype(np.int32)
+    S = int(sc.sum(1).max()) + 1
+    R = int(rc.sum(1).max()) + 1
+    x = oracle.fill_i32(n, n * S).reshape(n, S)
+    ref = oracle.alltoallv(x, sc, sd, R, rc, rd)
+    with gpulib.World(n, timeout_s=10.0) as w:
+        s, r = dev(x), dev(np.zeros((n, R), np.int32))
+        w.alltoallv(s, S * 4, dev(sc), dev(sd), r, R * 4, dev(rc), dev(rd), 2)
+        got = host(r)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("n,c", [(7, 7), (100, 64), (512, 3)])
+def test_allgather(gpulib, oracle, n, c):
+    x = oracle.fill_i32(5, n * c).reshape(n, c)
+    with gpulib.World(n, timeout_s=10.0) as w:
+        s, r = dev(x), dev(np.zeros((n, n * c), np.int32))
+        w.allgather(s, r, c, 2)
+        got = host(r)
+    assert (got == x.reshape(1, -1)).all()
+
+
+@pytest.mark.parametrize("n,nbytes,nb", [(2, 8, False), (4, 4096, True), (8, 1 << 20, False), (256, 1 << 16, True),
+                                         (128, 1 << 24, True)])
+def test_ring_bytes_exact(gpulib, oracle, n, nbytes, nb):
+    x = oracle.fill_i32(n, n * nbytes // 4).view(np.uint8).reshape(n, nbytes)
+    with gpulib.World(n, timeout_s=20.0) as w:
+        s, r = dev(x), dev(np.zeros_like(x))
+        w.ring(s, r, nbytes, iters=2, nonblocking=nb)
+        got = host(r)
+    assert np.array_equal(got, np.roll(x, 1, axis=0))
+
+
+@pytest.mark.parametrize("nbytes", [8, 1024, 1 << 20, 1 << 26])
+def test_pingpong_round_trip_exact(gpulib, oracle, nbytes):
+    n = 4
+    x = oracle.fill_i32(nbytes, n * nbytes // 4).view(np.uint8).reshape(n, nbytes)
+    with gpulib.World(n, timeout_s=20.0) as w:
+        b = dev(x)
+        w.pingpong(b, nbytes, 2, iters=3)
+        got = host(b)
+    # after each round trip both ranks of a pair hold the even rank's data
+    for p in range(2):
+        assert np.array_equal(got[2 * p], x[2 * p]) and np.array_equal(got[2 * p + 1], x[2 * p])
+
+
+def test_pi_bit_exact(gpulib, oracle):
+    n, pairs, seed = 64, 1 << 14, 20251203
+    with gpulib.World(n, timeout_s=20.0) as w:
+        hits = np.zeros(n, np.int64)
+        tot = np.zeros(1, np.int64)
+        hd, td = dev(hits), dev(tot)
+        rc = w.run_program(gpulib.P_PI, i=(seed, pairs), p=(hd, td))
+        assert rc == 0, w.last_error()
+        hits, tot = host(hd), host(td)
+    ref = [oracle.pi_hits(seed, r, pairs) for r in range(n)]
+    assert hits.tolist() == ref and int(tot[0]) == sum(ref)
+
+
+@pytest.mark.parametrize("name,n", [("p2p_matching", 5), ("datatypes", 2), ("subcomm_coll", 13), ("errors", 4)])
+def test_extended_programs(gpulib, name, n):
+    with gpulib.World(n, timeout_s=10.0) as w:
+        rc, ok, oi, od = w.run_test(name)
+    assert rc == 0 and ok.all(), (name, ok, oi[:, :10])
+
+
+def test_timeout_returns_error_not_hang(gpulib):
+    # failure detection without a GPU fault: a receive that nobody matches ends in MPI_ERR_OTHER
+    with gpulib.World(3, timeout_s=0.5) as w:
+        rc, ok, oi, od = w.run_test("timeout")
+        assert ok.all() and oi[0, 0] == gpulib.ERR_OTHER
+        assert rc == gpulib.ERR_TIMEOUT
+        # the world is still usable afterwards
+        rc2, ok2, _, _ = w.run_test("sample")
+        assert rc2 == 0 and ok2.all()
