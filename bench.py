@@ -210,6 +210,22 @@ def bench_alltoallv(gpumpi, torch, w_kw):
             "p50_us": float(pct(list(ns), 0.5)) / 1e3, "p99_us": float(pct(list(ns), 0.99)) / 1e3}
 
 
+def small_case(args, gpumpi, torch, local):
+    """Allreduce fp32 SUM, 1024 ranks x 256 KiB (512 MiB of traffic per call): the profiled case."""
+    n, count = 1024, 65536
+    g = torch.Generator(device="cuda").manual_seed(7)
+    send = (torch.rand((n, count), generator=g, device="cuda") * 2 - 1).contiguous()
+    recv = torch.empty_like(send)
+    with gpumpi.World(n, device=local, timeout_s=120.0) as w:
+        w.allreduce(send, recv, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=max(1, args.warmup))
+        w.allreduce(send, recv, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=max(1, args.steps))
+        ms = w.last_kernel_ms() / max(1, args.steps)
+        info = w.info()
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "small", "ranks": n, "bytes_per_rank": count * 4, "ms_per_step": ms,
+                      "gbs": 2.0 * n * count * 4 / (ms * 1e-3) / 1e9, "world": info}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -217,6 +233,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--case", default="full", choices=["full", "small"],
+                    help="small: 1024 ranks x 256 KiB, device timing only (the ncu capture case)")
     args = ap.parse_args()
     dist, rank, ws = dist_setup()
     if args.impl == "reference":
@@ -229,6 +247,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     gpumpi.build()
+    if args.case == "small":
+        small_case(args, gpumpi, torch, local)
+        return
     n, per = WORKLOAD["ranks"], WORKLOAD["bytes_per_rank"]
     count = per // 4
     K, W = max(1, args.steps), max(3, args.warmup)

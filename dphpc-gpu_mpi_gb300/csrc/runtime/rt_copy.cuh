@@ -3,27 +3,41 @@
 // Replaces the reference's single-thread byte memcpy (gpu_libs/gpu_libc/cuda_mpi.cu:168,323 and the
 // __gpu_memcpy byte loop of gpu_libs/gpu_libc/string.cu:185-192): nl cooperating threads move the
 // message with 16-byte vector accesses (8/4/1-byte when the two addresses disagree modulo 16),
-// four independent loads in flight per thread, L2-only loads (ld.global.cg) so a block never reads
-// a stale L1 line written by another SM.
+// four independent loads in flight per thread, L2-only loads (ld.global.cg) for global buffers so a
+// block never reads a stale L1 line written by another SM (generic accesses for thread-local and
+// shared buffers, where the .global forms would be illegal).
 #pragma once
 #include "rt_core.cuh"
 
 namespace gpumpi {
 
-template <class V>
+// CG: both addresses are global, so L2-only accesses (ld/st.global.cg) are legal; otherwise
+// (thread-local or shared buffers) plain generic accesses are used.
+template <class V, bool CG>
+__device__ __forceinline__ V ldv(const V* p) {
+    if constexpr (CG) return __ldcg(p);
+    else return *p;
+}
+template <class V, bool CG>
+__device__ __forceinline__ void stv(V* p, V v) {
+    if constexpr (CG) __stcg(p, v);
+    else *p = v;
+}
+
+template <class V, bool CG>
 __device__ __forceinline__ void copy_vec_body(V* d, const V* s, long long nv, int lane, int nl) {
     long long i = lane;
     for (; i + 3LL * nl < nv; i += 4LL * nl) {
-        V a = __ldcg(s + i);
-        V b = __ldcg(s + i + nl);
-        V c = __ldcg(s + i + 2LL * nl);
-        V e = __ldcg(s + i + 3LL * nl);
-        __stcg(d + i, a);
-        __stcg(d + i + nl, b);
-        __stcg(d + i + 2LL * nl, c);
-        __stcg(d + i + 3LL * nl, e);
+        V a = ldv<V, CG>(s + i);
+        V b = ldv<V, CG>(s + i + nl);
+        V c = ldv<V, CG>(s + i + 2LL * nl);
+        V e = ldv<V, CG>(s + i + 3LL * nl);
+        stv<V, CG>(d + i, a);
+        stv<V, CG>(d + i + nl, b);
+        stv<V, CG>(d + i + 2LL * nl, c);
+        stv<V, CG>(d + i + 3LL * nl, e);
     }
-    for (; i < nv; i += nl) __stcg(d + i, __ldcg(s + i));
+    for (; i < nv; i += nl) stv<V, CG>(d + i, ldv<V, CG>(s + i));
 }
 
 __device__ __forceinline__ void copy_bytes_slow(char* d, const char* s, long long n, int lane, int nl) {
@@ -46,9 +60,16 @@ __device__ __noinline__ void copy_bytes(void* dst, const void* src, long long n,
     long long body = (n - head) & ~(long long)(w - 1);
     long long tail = n - head - body;
     for (long long i = lane; i < head; i += nl) d[i] = s[i];
-    if (w == 16) copy_vec_body<uint4>((uint4*)(d + head), (const uint4*)(s + head), body / 16, lane, nl);
-    else if (w == 8) copy_vec_body<unsigned long long>((unsigned long long*)(d + head), (const unsigned long long*)(s + head), body / 8, lane, nl);
-    else copy_vec_body<unsigned>((unsigned*)(d + head), (const unsigned*)(s + head), body / 4, lane, nl);
+    const bool cg = is_global_ptr(d) && is_global_ptr(s);
+    if (cg) {
+        if (w == 16) copy_vec_body<uint4, true>((uint4*)(d + head), (const uint4*)(s + head), body / 16, lane, nl);
+        else if (w == 8) copy_vec_body<unsigned long long, true>((unsigned long long*)(d + head), (const unsigned long long*)(s + head), body / 8, lane, nl);
+        else copy_vec_body<unsigned, true>((unsigned*)(d + head), (const unsigned*)(s + head), body / 4, lane, nl);
+    } else {
+        if (w == 16) copy_vec_body<uint4, false>((uint4*)(d + head), (const uint4*)(s + head), body / 16, lane, nl);
+        else if (w == 8) copy_vec_body<unsigned long long, false>((unsigned long long*)(d + head), (const unsigned long long*)(s + head), body / 8, lane, nl);
+        else copy_vec_body<unsigned, false>((unsigned*)(d + head), (const unsigned*)(s + head), body / 4, lane, nl);
+    }
     for (long long i = lane; i < tail; i += nl) d[head + body + i] = s[head + body + i];
 }
 

@@ -94,22 +94,32 @@ __device__ __forceinline__ int typed_unit(const TypeDesc* s, const void* sb, con
     return (int)u;
 }
 
-template <int U>
+template <int U, bool CG>
 __device__ __forceinline__ void copy_unit(char* d, const char* s) {
-    if constexpr (U == 16) __stcg((uint4*)d, __ldcg((const uint4*)s));
-    else if constexpr (U == 8) __stcg((unsigned long long*)d, __ldcg((const unsigned long long*)s));
-    else if constexpr (U == 4) __stcg((unsigned*)d, __ldcg((const unsigned*)s));
-    else if constexpr (U == 2) *(unsigned short*)d = *(const volatile unsigned short*)s;
-    else *d = *(const volatile char*)s;
+    if constexpr (U == 16) {
+        if constexpr (CG) __stcg((uint4*)d, __ldcg((const uint4*)s));
+        else *(uint4*)d = *(const uint4*)s;
+    } else if constexpr (U == 8) {
+        if constexpr (CG) __stcg((unsigned long long*)d, __ldcg((const unsigned long long*)s));
+        else *(unsigned long long*)d = *(const unsigned long long*)s;
+    } else if constexpr (U == 4) {
+        if constexpr (CG) __stcg((unsigned*)d, __ldcg((const unsigned*)s));
+        else *(unsigned*)d = *(const unsigned*)s;
+    } else if constexpr (U == 2) {
+        *(unsigned short*)d = *(const volatile unsigned short*)s;
+    } else {
+        *d = *(const volatile char*)s;
+    }
 }
 
-template <int U>
+// CG selects L2-only accesses; legal only when both buffers are in global memory.
+template <int U, bool CG>
 __device__ __noinline__ void typed_copy_u(char* db, const TypeDesc* dt_, const char* sb, const TypeDesc* st_,
-                                             long long b0, long long b1, int lane, int nl) {
+                                          long long b0, long long b1, int lane, int nl) {
     for (long long off = b0 + (long long)lane * U; off < b1; off += (long long)nl * U) {
         long long sa = st_ ? desc_map(st_, off) : off;
         long long da = dt_ ? desc_map(dt_, off) : off;
-        copy_unit<U>(db + da, sb + sa);
+        copy_unit<U, CG>(db + da, sb + sa);
     }
 }
 
@@ -122,12 +132,21 @@ __device__ __noinline__ void typed_copy(void* db, const TypeDesc* dt_, const voi
     u = min(u, (int)pow2_div(b1));
     char* d = (char*)db;
     const char* s = (const char*)sb;
-    switch (u) {
-    case 16: typed_copy_u<16>(d, dt_, s, st_, b0, b1, lane, nl); break;
-    case 8: typed_copy_u<8>(d, dt_, s, st_, b0, b1, lane, nl); break;
-    case 4: typed_copy_u<4>(d, dt_, s, st_, b0, b1, lane, nl); break;
-    case 2: typed_copy_u<2>(d, dt_, s, st_, b0, b1, lane, nl); break;
-    default: typed_copy_u<1>(d, dt_, s, st_, b0, b1, lane, nl); break;
+    if (is_global_ptr(db) && is_global_ptr(sb)) {
+        switch (u) {
+        case 16: typed_copy_u<16, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
+        case 8: typed_copy_u<8, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
+        case 4: typed_copy_u<4, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
+        case 2: typed_copy_u<2, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
+        default: typed_copy_u<1, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
+        }
+    } else {
+        switch (u) {
+        case 16: typed_copy_u<16, false>(d, dt_, s, st_, b0, b1, lane, nl); break;
+        case 8: typed_copy_u<8, false>(d, dt_, s, st_, b0, b1, lane, nl); break;
+        case 4: typed_copy_u<4, false>(d, dt_, s, st_, b0, b1, lane, nl); break;
+        default: typed_copy_u<1, false>(d, dt_, s, st_, b0, b1, lane, nl); break;
+        }
     }
 }
 
