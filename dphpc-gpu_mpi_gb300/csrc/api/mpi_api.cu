@@ -204,11 +204,32 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         j->count = a.count;
         bytes = a.count * a.esize * (long long)n;
         int variant = select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, a.variant);
-        j->variant = variant;
         may_post = may_post && bytes >= g_rt->engine_min_bytes;
         long long target = n + (may_post ? g_rt->nengines : 0);
         int vec = 1;
-        if (fold_has_fast(a.dt, a.op, a.ufn)) {
+        j->tile = 0;
+        if (variant == GPUMPI_VARIANT_STAGED) {
+            // canonical order through shared-memory stages: needs 16-byte aligned buffers and room for
+            // two stages of at least one rank
+            const int es = a.esize;
+            const int stage_room = g_rt->dyn_smem - 128;
+            if (!fold_has_staged(a.dt, a.op, a.ufn) || j->aligned16 < 16 || stage_room < 2 * T * es) {
+                variant = GPUMPI_VARIANT_DIRECT;
+            } else {
+                int cands[3] = {16 / es, es == 4 ? 2 : 1, 1};
+                for (int k = 0; k < 3; k++) {
+                    int v = cands[k];
+                    if (stage_room < 2 * T * v * es) continue;
+                    long long nch = (a.count + (long long)T * v - 1) / ((long long)T * v);
+                    if (nch >= target || v == 1) { vec = v; break; }
+                }
+                int G = stage_room / (2 * T * vec * es);
+                j->tile = G < 1 ? 1 : G > 64 ? 64 : G;
+            }
+        }
+        if (variant == GPUMPI_VARIANT_TREE || variant == GPUMPI_VARIANT_RING) variant = GPUMPI_VARIANT_DIRECT;
+        j->variant = variant;
+        if (variant == GPUMPI_VARIANT_DIRECT && fold_has_fast(a.dt, a.op, a.ufn)) {
             int es = a.esize;
             int cands[3] = {16 / es, es == 4 ? 2 : 1, 1};
             for (int k = 0; k < 3; k++) {
@@ -220,7 +241,6 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             }
         }
         j->vec = vec;
-        j->tile = 0;
         j->chunk = (long long)T * vec;
         nchunks = (int)((a.count + j->chunk - 1) / j->chunk);
     } else if (a.kind == JOB_BARRIER) {

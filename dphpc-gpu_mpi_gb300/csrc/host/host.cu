@@ -76,6 +76,7 @@ struct gpumpi_world {
     gpumpi_config cfg;
     int device = 0, sm_count = 0, max_blocks = 0;
     int T = 0, nengines = 0, blocks_per_sm = 0;
+    size_t dyn_smem = 0;
     Runtime h_rt;
     Runtime* d_rt = nullptr;
     char* d_ctrl = nullptr;
@@ -88,7 +89,7 @@ struct gpumpi_world {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0;
-    int variant_override = -1, selector_mode = 0;
+    int variant_override = -1, selector_mode = 3;
     signed char* d_table = nullptr;
     float* d_mlp = nullptr;
     // scratch for host-buffer staging
@@ -382,20 +383,45 @@ double gpumpi_last_kernel_ms(gpumpi_world* w) { return w ? w->last_ms : 0.0; }
 
 // Picks the block size and engine count for program `pe` (largest of 256/128/64 threads whose
 // occupancy co-hosts all ranks, unless the configuration fixes it).
+// Dynamic shared memory for T-thread blocks when `bps` blocks share an SM: what is left of the SM's
+// shared memory after each block's static allocation and the per-block reservation, capped at the
+// 48 KiB that needs no opt-in.  Used for the STAGED fold's TMA stages.
+static size_t dyn_smem_for(gpumpi_world* w, const gpumpi_prog_entry* pe, int bps) {
+    int smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, w->device);
+    cudaFuncAttributes fa;
+    if (pe->attributes(&fa) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    long long per = (long long)smem_sm / (bps > 0 ? bps : 1) - (long long)fa.sharedSizeBytes - 1024;
+    if (per > 48 * 1024) per = 48 * 1024;
+    per &= ~127LL;
+    return per >= 4096 ? (size_t)per : 0;
+}
+
 static int choose_geometry(gpumpi_world* w, const gpumpi_prog_entry* pe) {
     const int n = w->cfg.nranks;
     int cands[3] = {256, 128, 64};
     int chosen = 0, bps = 0;
-    for (int k = 0; k < 3; k++) {
+    size_t dyn = 0;
+    for (int k = 0; k < 3 && !chosen; k++) {
         int T = cands[k];
         if (w->cfg.threads_per_block > 0 && T != w->cfg.threads_per_block) continue;
         int b = 0;
-        CK(pe->occupancy(&b, T, 0));
-        if ((long long)b * w->sm_count >= n) {
-            chosen = T;
-            bps = b;
-            break;
+        CK(pe->occupancy(&b, T, 0));  // register-limited occupancy
+        if ((long long)b * w->sm_count < n) continue;
+        // keep that occupancy and give each block the shared memory that is left over
+        size_t d = dyn_smem_for(w, pe, b);
+        int b2 = 0;
+        CK(pe->occupancy(&b2, T, d));
+        while (d > 0 && b2 < b) {
+            d = d > 4096 + 1024 ? d - 1024 : 0;
+            CK(pe->occupancy(&b2, T, d));
         }
+        chosen = T;
+        bps = b2;
+        dyn = d;
     }
     if (!chosen && w->cfg.threads_per_block > 0) {
         int b = 0;
@@ -405,6 +431,7 @@ static int choose_geometry(gpumpi_world* w, const gpumpi_prog_entry* pe) {
             bps = b;
         }
     }
+    w->dyn_smem = dyn;
     if (!chosen) {
         int b = 0;
         pe->occupancy(&b, 32, 0);
@@ -423,6 +450,7 @@ static int choose_geometry(gpumpi_world* w, const gpumpi_prog_entry* pe) {
 
 int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params, void* stream_v, int sync) {
     if (!w || !params) return GPUMPI_ERR_ARG;
+    w->err.clear();
     const gpumpi_prog_entry* pe = find_program(program);
     if (!pe) {
         w->err = "unknown program " + std::to_string(program);
@@ -439,12 +467,13 @@ int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params
     r.selector_mode = w->selector_mode;
     r.tuned_table = w->d_table;
     r.mlp_params = w->d_mlp;
+    r.dyn_smem = (int)w->dyn_smem;
     CK(cudaMemsetAsync(w->d_ctrl, 0, w->ctrl_bytes, s));
     CK(cudaMemcpyAsync(w->d_fixed, &w->h_fixed, sizeof(FixedImage), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(w->d_rt, &r, sizeof(Runtime), cudaMemcpyHostToDevice, s));
     CK(gpumpi_internal_install(w->d_rt, &w->d_fixed->world, &w->d_fixed->gworld, &w->d_fixed->gempty, s));
     CK(cudaEventRecord(w->ev0, s));
-    cudaError_t le = pe->launch(w->cfg.nranks + w->nengines, w->T, 0, s, params);
+    cudaError_t le = pe->launch(w->cfg.nranks + w->nengines, w->T, w->dyn_smem, s, params);
     if (le != cudaSuccess) {
         w->err = std::string("launch of ") + pe->name + ": " + cudaGetErrorString(le);
         cudaGetLastError();
@@ -461,16 +490,21 @@ int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params
     const int nb = w->cfg.nranks + w->nengines;
     CK(cudaMemcpy(w->h_err.data(), r.errors, sizeof(gpumpi::ErrorRecord) * nb, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(w->h_exit.data(), r.exit_codes, sizeof(int) * w->cfg.nranks, cudaMemcpyDeviceToHost));
+    // Error records describe what went wrong inside MPI calls; the calls also returned the codes to the
+    // program, so only a run that hit a bounded-wait timeout fails here (other errors surface through
+    // the ranks' exit codes).
+    int timeout = 0;
     for (int b = 0; b < nb; b++) {
         const gpumpi::ErrorRecord& e = w->h_err[b];
         if (e.code) {
             char buf[256];
             snprintf(buf, sizeof buf, "rank %d: MPI error %d (detail %d) at runtime line %d, info %lld", e.rank,
                      e.code, e.detail, e.line, e.info);
-            w->err = buf;
-            return e.detail == GPUMPI_ERR_TIMEOUT ? GPUMPI_ERR_TIMEOUT : e.code;
+            if (w->err.empty() || e.detail == GPUMPI_ERR_TIMEOUT) w->err = buf;
+            if (e.detail == GPUMPI_ERR_TIMEOUT) timeout = 1;
         }
     }
+    if (timeout) return GPUMPI_ERR_TIMEOUT;
     for (int i = 0; i < w->cfg.nranks; i++)
         if (w->h_exit[i] != 0) {
             w->err = "rank " + std::to_string(i) + " returned " + std::to_string(w->h_exit[i]);

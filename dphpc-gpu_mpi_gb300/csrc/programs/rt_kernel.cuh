@@ -37,12 +37,14 @@ __global__ void __launch_bounds__(256) gpumpi_rank_kernel(gpumpi_params prm) {
 
 typedef cudaError_t (*gpumpi_launch_fn)(int grid, int block, size_t smem, cudaStream_t s, const gpumpi_params* p);
 typedef cudaError_t (*gpumpi_occ_fn)(int* blocks_per_sm, int block, size_t smem);
+typedef cudaError_t (*gpumpi_attr_fn)(cudaFuncAttributes* attr);
 
 struct gpumpi_prog_entry {
     int id;
     const char* name;
     gpumpi_launch_fn launch;
     gpumpi_occ_fn occupancy;
+    gpumpi_attr_fn attributes;
 };
 
 template <class P>
@@ -57,5 +59,10 @@ cudaError_t gpumpi_occ_prog(int* blocks_per_sm, int block, size_t smem) {
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gpumpi_rank_kernel<P>, block, smem);
 }
 
+template <class P>
+cudaError_t gpumpi_attr_prog(cudaFuncAttributes* attr) {
+    return cudaFuncGetAttributes(attr, gpumpi_rank_kernel<P>);
+}
+
 #define GPUMPI_PROGRAM(ID, NAME, TYPE) \
-    { ID, NAME, &gpumpi_launch_prog<TYPE>, &gpumpi_occ_prog<TYPE> }
+    { ID, NAME, &gpumpi_launch_prog<TYPE>, &gpumpi_occ_prog<TYPE>, &gpumpi_attr_prog<TYPE> }

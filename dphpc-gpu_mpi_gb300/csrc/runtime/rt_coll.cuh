@@ -20,6 +20,7 @@
 #include "rt_types.cuh"
 #include "rt_ops.cuh"
 #include "rt_copy.cuh"
+#include "rt_tma.cuh"
 
 namespace gpumpi {
 
@@ -112,7 +113,7 @@ __device__ int comm_barrier(MPI_Comm_impl* c, F&& setup, int line) {
 // Parameters of the job epoch being executed, read once per chunk with L2-only loads (the Job
 // struct is rewritten by every epoch, so no executing block may keep it in L1).
 struct JobParams {
-    int kind, dt, op, root, esize, vec, tile, aligned16;
+    int kind, dt, op, root, esize, vec, tile, aligned16, variant;
     long long count, chunk;
     const MPI_Comm_impl* comm;
     const void* src;
@@ -122,6 +123,7 @@ struct JobParams {
 
 __device__ __forceinline__ void load_params(const Job* j, JobParams& P) {
     P.kind = __ldcg(&j->kind);
+    P.variant = __ldcg(&j->variant);
     P.dt = __ldcg(&j->dt);
     P.op = __ldcg(&j->op);
     P.root = __ldcg(&j->root);
@@ -257,6 +259,115 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
     }
 }
 
+// STAGED variant: canonical-order fold with the inputs streamed through shared memory by TMA bulk
+// copies.  Chunk = nt*V elements; thread 0 keeps two stages of G ranks x chunk bytes in flight
+// (mbarrier transaction counts); every thread folds its V elements from shared memory in rank order.
+// Same operation order as fold_fast, so results are bit-identical to DIRECT and the reference order.
+// Requires 16-byte aligned buffers and a chunk byte count that is a multiple of 16 (checked by caller).
+__shared__ int s_stage_abort;
+
+template <class T, int OP, int V>
+__device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int tid, int nt) {
+    constexpr int S = 2;
+    const MPI_Comm_impl* c = j->comm;
+    const CollSlot* slots = c->slots;
+    const int n = c->size;
+    const long long E = j->chunk;
+    const long long e0 = idx * E;
+    const long long ne = min(E, j->count - e0);
+    const unsigned CB = (unsigned)(ne * (long long)sizeof(T));
+    const int G = j->tile;
+    const int ngroups = (n + G - 1) / G;
+    unsigned long long* full = (unsigned long long*)g_dyn_smem;
+    T* stage = (T*)(g_dyn_smem + 128);
+    const long long stage_elems = (long long)G * E;
+    if (tid == 0) {
+        for (int q = 0; q < S; q++) mbar_init(&full[q], 1);
+        fence_mbar_init();
+        s_stage_abort = 0;
+    }
+    bar_sync(BAR_TASK, nt);
+    if (tid == 0) {
+        for (int g = 0; g < S && g < ngroups; g++) {
+            const int r0 = g * G, m = min(G, n - r0);
+            mbar_expect_tx(&full[g], (unsigned)m * CB);
+            for (int k = 0; k < m; k++) {
+                const T* src = (const T*)__ldcg((const unsigned long long*)&slots[r0 + k].sbuf) + e0;
+                tma_load_1d(stage + (long long)g * stage_elems + (long long)k * E, src, CB, &full[g]);
+            }
+        }
+    }
+    const long long my = (long long)tid * V;
+    const int nv = my < ne ? (int)min((long long)V, ne - my) : 0;
+    T acc[V];
+#pragma unroll
+    for (int q = 0; q < V; q++) acc[q] = T();
+    for (int g = 0; g < ngroups; g++) {
+        const int sidx = g % S;
+        const unsigned par = (unsigned)((g / S) & 1);
+        if (!mbar_wait_bounded(&full[sidx], par)) {
+            s_stage_abort = 1;
+            if (tid == 0) record_error(GPUMPI_ERR_OTHER, GPUMPI_ERR_TIMEOUT, __LINE__, idx);
+        }
+        bar_sync(BAR_TASK, nt);  // (a) everyone waited; abort flag visible
+        if (s_stage_abort) break;
+        const int m = min(G, n - g * G);
+        const T* st = stage + (long long)sidx * stage_elems + my;
+        if (nv > 0) {
+            int k = 0;
+            if (g == 0) {
+                if (nv == V) {
+#pragma unroll
+                    for (int q = 0; q < V; q++) acc[q] = st[q];
+                } else {
+                    for (int q = 0; q < nv; q++) acc[q] = st[q];
+                }
+                k = 1;
+            }
+            if (nv == V) {
+                for (; k < m; k++) {
+                    const T* p = st + (long long)k * E;
+#pragma unroll
+                    for (int q = 0; q < V; q++) acc[q] = op_apply<OP, T>(p[q], acc[q]);
+                }
+            } else {
+                for (; k < m; k++) {
+                    const T* p = st + (long long)k * E;
+                    for (int q = 0; q < nv; q++) acc[q] = op_apply<OP, T>(p[q], acc[q]);
+                }
+            }
+        }
+        bar_sync(BAR_TASK, nt);  // (b) stage consumed by every thread
+        if (tid == 0 && g + S < ngroups) {
+            const int gg = g + S, r0 = gg * G, mm = min(G, n - r0);
+            mbar_expect_tx(&full[sidx], (unsigned)mm * CB);
+            for (int k = 0; k < mm; k++) {
+                const T* src = (const T*)__ldcg((const unsigned long long*)&slots[r0 + k].sbuf) + e0;
+                tma_load_1d(stage + (long long)sidx * stage_elems + (long long)k * E, src, CB, &full[sidx]);
+            }
+        }
+    }
+    if (s_stage_abort) return;
+    // every issued copy was waited for: the barriers can be retired (re-initialised by the next chunk)
+    if (tid == 0)
+        for (int q = 0; q < S; q++) mbar_inval(&full[q]);
+    if (j->kind == JOB_REDUCE) {
+        if (nv > 0) {
+            T* out = (T*)slot_out(&slots[j->root]) + e0 + my;
+            for (int q = 0; q < nv; q++) __stcg(out + q, acc[q]);
+        }
+        return;
+    }
+    const long long e = e0 + my;
+    const bool vec16 = (V * sizeof(T)) % 16 == 0 || (V * sizeof(T)) == 8;
+    for (int r0 = 0; r0 < n; r0 += PTILE) {
+        const int m = min(PTILE, n - r0);
+        load_ptile(slots, r0, m, 1, tid, nt);
+        if (nv > 0)
+            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_ptile[i] + e, acc, nv, vec16);
+    }
+}
+
 // Any legal (op, type) and user-defined ops, one element per thread, same canonical order.
 __device__ __noinline__ void fold_generic(const JobParams* j, long long e0, int tid, int nt) {
     const MPI_Comm_impl* c = j->comm;
@@ -353,11 +464,50 @@ __device__ __forceinline__ bool fold_has_fast(int dt, int op, MPI_User_function*
     }
 }
 
+template <class T, int OP>
+__device__ __forceinline__ void fold_staged_v(const JobParams* j, long long idx, int tid, int nt) {
+    if (j->vec >= 16 / (int)sizeof(T)) fold_staged<T, OP, 16 / sizeof(T)>(j, idx, tid, nt);
+    else if constexpr (sizeof(T) == 4) {
+        if (j->vec >= 2) fold_staged<T, OP, 2>(j, idx, tid, nt);
+        else fold_staged<T, OP, 1>(j, idx, tid, nt);
+    } else fold_staged<T, OP, 1>(j, idx, tid, nt);
+}
+
+template <class T>
+__device__ __forceinline__ bool fold_staged_t(const JobParams* j, long long idx, int tid, int nt) {
+    switch (j->op) {
+    case GPUMPI_OP_SUM: fold_staged_v<T, GPUMPI_OP_SUM>(j, idx, tid, nt); return true;
+    case GPUMPI_OP_MAX: fold_staged_v<T, GPUMPI_OP_MAX>(j, idx, tid, nt); return true;
+    case GPUMPI_OP_MIN: fold_staged_v<T, GPUMPI_OP_MIN>(j, idx, tid, nt); return true;
+    default: return false;
+    }
+}
+
+// true if (dt, op) has a STAGED instantiation
+__device__ __forceinline__ bool fold_has_staged(int dt, int op, MPI_User_function* ufn) {
+    if (ufn || !(op == GPUMPI_OP_SUM || op == GPUMPI_OP_MAX || op == GPUMPI_OP_MIN)) return false;
+    switch (dt) {
+    case GPUMPI_FLOAT: case GPUMPI_DOUBLE: case GPUMPI_LONG_DOUBLE: case GPUMPI_INT: case GPUMPI_INT32_T:
+    case GPUMPI_LONG: case GPUMPI_LONG_LONG_INT: case GPUMPI_LONG_LONG: case GPUMPI_INT64_T:
+        return true;
+    default: return false;
+    }
+}
+
 __device__ __noinline__ void fold_chunk(const JobParams* j, long long idx, int tid, int nt) {
     const long long e0 = idx * j->chunk;
     bool done = false;
 #ifndef GPUMPI_NO_FAST_FOLD
-    if (fold_has_fast(j->dt, j->op, j->ufn)) {
+    if (j->variant == GPUMPI_VARIANT_STAGED && j->tile > 0 &&
+        ((min(j->chunk, j->count - e0) * j->esize) & 15) == 0) {
+        switch (j->dt) {
+        case GPUMPI_FLOAT: done = fold_staged_t<float>(j, idx, tid, nt); break;
+        case GPUMPI_DOUBLE: case GPUMPI_LONG_DOUBLE: done = fold_staged_t<double>(j, idx, tid, nt); break;
+        case GPUMPI_INT: case GPUMPI_INT32_T: done = fold_staged_t<int>(j, idx, tid, nt); break;
+        default: done = fold_staged_t<long long>(j, idx, tid, nt); break;
+        }
+    }
+    if (!done && fold_has_fast(j->dt, j->op, j->ufn)) {
         switch (j->dt) {
         case GPUMPI_FLOAT: done = fold_fast_arith<float>(j, e0, tid, nt); break;
         case GPUMPI_DOUBLE: case GPUMPI_LONG_DOUBLE: done = fold_fast_arith<double>(j, e0, tid, nt); break;

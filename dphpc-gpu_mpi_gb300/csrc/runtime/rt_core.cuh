@@ -350,7 +350,8 @@ struct Runtime {
     long long copy_chunk_bytes;       // chunk size of point-to-point copy jobs
     long long engine_min_bytes;       // smaller jobs are not posted to the engines
     int variant_override;             // -1: selector decides
-    int selector_mode;                // 0 plain (direct), 1 tuned table, 2 learned
+    int selector_mode;                // 0 plain (DIRECT), 1 tuned table, 2 learned MLP, 3 heuristic
+    int dyn_smem;                     // dynamic shared memory bytes of this launch (STAGED stages)
     int trace_enabled;
     int trace_cap;
     // state arrays (device global memory)

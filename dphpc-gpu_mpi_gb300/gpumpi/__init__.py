@@ -206,7 +206,8 @@ class World:
         lib().gpumpi_world_get_info(self.h, ctypes.byref(i))
         return {f: getattr(i, f) for f, _ in WorldInfo._fields_}
 
-    def set_policy(self, variant: int = -1, mode: int = 0):
+    def set_policy(self, variant: int = -1, mode: int = 3):
+        """variant >= 0 forces one; mode 0 plain (DIRECT), 1 tuned table, 2 learned MLP, 3 heuristic."""
         self._check(lib().gpumpi_set_policy(self.h, variant, mode), "set_policy")
 
     def set_tuned_table(self, table: np.ndarray):
