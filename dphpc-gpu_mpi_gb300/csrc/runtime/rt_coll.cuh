@@ -259,114 +259,11 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
     }
 }
 
-// STAGED variant: canonical-order fold with the inputs streamed through shared memory by TMA bulk
-// copies.  Chunk = nt*V elements; thread 0 keeps two stages of G ranks x chunk bytes in flight
-// (mbarrier transaction counts); every thread folds its V elements from shared memory in rank order.
-// Same operation order as fold_fast, so results are bit-identical to DIRECT and the reference order.
-// Requires 16-byte aligned buffers and a chunk byte count that is a multiple of 16 (checked by caller).
-__shared__ int s_stage_abort;
+}  // namespace gpumpi
 
-template <class T, int OP, int V>
-__device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int tid, int nt) {
-    constexpr int S = 2;
-    const MPI_Comm_impl* c = j->comm;
-    const CollSlot* slots = c->slots;
-    const int n = c->size;
-    const long long E = j->chunk;
-    const long long e0 = idx * E;
-    const long long ne = min(E, j->count - e0);
-    const unsigned CB = (unsigned)(ne * (long long)sizeof(T));
-    const int G = j->tile;
-    const int ngroups = (n + G - 1) / G;
-    unsigned long long* full = (unsigned long long*)g_dyn_smem;
-    T* stage = (T*)(g_dyn_smem + 128);
-    const long long stage_elems = (long long)G * E;
-    if (tid == 0) {
-        for (int q = 0; q < S; q++) mbar_init(&full[q], 1);
-        fence_mbar_init();
-        s_stage_abort = 0;
-    }
-    bar_sync(BAR_TASK, nt);
-    if (tid == 0) {
-        for (int g = 0; g < S && g < ngroups; g++) {
-            const int r0 = g * G, m = min(G, n - r0);
-            mbar_expect_tx(&full[g], (unsigned)m * CB);
-            for (int k = 0; k < m; k++) {
-                const T* src = (const T*)__ldcg((const unsigned long long*)&slots[r0 + k].sbuf) + e0;
-                tma_load_1d(stage + (long long)g * stage_elems + (long long)k * E, src, CB, &full[g]);
-            }
-        }
-    }
-    const long long my = (long long)tid * V;
-    const int nv = my < ne ? (int)min((long long)V, ne - my) : 0;
-    T acc[V];
-#pragma unroll
-    for (int q = 0; q < V; q++) acc[q] = T();
-    for (int g = 0; g < ngroups; g++) {
-        const int sidx = g % S;
-        const unsigned par = (unsigned)((g / S) & 1);
-        if (!mbar_wait_bounded(&full[sidx], par)) {
-            s_stage_abort = 1;
-            if (tid == 0) record_error(GPUMPI_ERR_OTHER, GPUMPI_ERR_TIMEOUT, __LINE__, idx);
-        }
-        bar_sync(BAR_TASK, nt);  // (a) everyone waited; abort flag visible
-        if (s_stage_abort) break;
-        const int m = min(G, n - g * G);
-        const T* st = stage + (long long)sidx * stage_elems + my;
-        if (nv > 0) {
-            int k = 0;
-            if (g == 0) {
-                if (nv == V) {
-#pragma unroll
-                    for (int q = 0; q < V; q++) acc[q] = st[q];
-                } else {
-                    for (int q = 0; q < nv; q++) acc[q] = st[q];
-                }
-                k = 1;
-            }
-            if (nv == V) {
-                for (; k < m; k++) {
-                    const T* p = st + (long long)k * E;
-#pragma unroll
-                    for (int q = 0; q < V; q++) acc[q] = op_apply<OP, T>(p[q], acc[q]);
-                }
-            } else {
-                for (; k < m; k++) {
-                    const T* p = st + (long long)k * E;
-                    for (int q = 0; q < nv; q++) acc[q] = op_apply<OP, T>(p[q], acc[q]);
-                }
-            }
-        }
-        bar_sync(BAR_TASK, nt);  // (b) stage consumed by every thread
-        if (tid == 0 && g + S < ngroups) {
-            const int gg = g + S, r0 = gg * G, mm = min(G, n - r0);
-            mbar_expect_tx(&full[sidx], (unsigned)mm * CB);
-            for (int k = 0; k < mm; k++) {
-                const T* src = (const T*)__ldcg((const unsigned long long*)&slots[r0 + k].sbuf) + e0;
-                tma_load_1d(stage + (long long)sidx * stage_elems + (long long)k * E, src, CB, &full[sidx]);
-            }
-        }
-    }
-    if (s_stage_abort) return;
-    // every issued copy was waited for: the barriers can be retired (re-initialised by the next chunk)
-    if (tid == 0)
-        for (int q = 0; q < S; q++) mbar_inval(&full[q]);
-    if (j->kind == JOB_REDUCE) {
-        if (nv > 0) {
-            T* out = (T*)slot_out(&slots[j->root]) + e0 + my;
-            for (int q = 0; q < nv; q++) __stcg(out + q, acc[q]);
-        }
-        return;
-    }
-    const long long e = e0 + my;
-    const bool vec16 = (V * sizeof(T)) % 16 == 0 || (V * sizeof(T)) == 8;
-    for (int r0 = 0; r0 < n; r0 += PTILE) {
-        const int m = min(PTILE, n - r0);
-        load_ptile(slots, r0, m, 1, tid, nt);
-        if (nv > 0)
-            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_ptile[i] + e, acc, nv, vec16);
-    }
-}
+#include "rt_staged.cuh"
+
+namespace gpumpi {
 
 // Any legal (op, type) and user-defined ops, one element per thread, same canonical order.
 __device__ __noinline__ void fold_generic(const JobParams* j, long long e0, int tid, int nt) {

@@ -1,0 +1,120 @@
+// rt_staged.cuh — STAGED variant of the fold (Allreduce / Reduce): canonical rank order, inputs
+// streamed through shared memory by TMA bulk copies.
+//
+// Chunk = nt*V elements.  For each tile of up to 256 ranks the block first stages the tile's input
+// pointers in shared memory (so issuing a copy costs no global round trip), then thread 0 keeps S
+// stages of G ranks x chunk bytes in flight (one mbarrier per stage, transaction-count completion)
+// while every thread folds its V elements of the ready stage in rank order.  The operation order is
+// exactly fold_fast's, so results are bit-identical to DIRECT and to the reference's fold
+// (gpu_libs/gpu_mpi/mpi.cu:209-225).  Needs 16-byte aligned buffers and a chunk byte count that is a
+// multiple of 16 (the caller checks); the output is written with L2-only vector stores.
+#pragma once
+#include "rt_core.cuh"
+#include "rt_tma.cuh"
+
+namespace gpumpi {
+
+__shared__ int s_stage_abort;
+
+template <class T, int OP, int V>
+__device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int tid, int nt) {
+    constexpr int S = 2;
+    const MPI_Comm_impl* c = j->comm;
+    const CollSlot* slots = c->slots;
+    const int n = c->size;
+    const long long E = j->chunk;
+    const long long e0 = idx * E;
+    const long long ne = min(E, j->count - e0);
+    const unsigned CB = (unsigned)(ne * (long long)sizeof(T));
+    const int G = j->tile;
+    unsigned long long* full = (unsigned long long*)g_dyn_smem;
+    T* stage = (T*)(g_dyn_smem + 128);
+    const long long stage_elems = (long long)G * E;
+    if (tid == 0) {
+        for (int q = 0; q < S; q++) mbar_init(&full[q], 1);
+        fence_mbar_init();
+        s_stage_abort = 0;
+    }
+    const long long my = (long long)tid * V;
+    const int nv = my < ne ? (int)min((long long)V, ne - my) : 0;
+    T acc[V];
+#pragma unroll
+    for (int q = 0; q < V; q++) acc[q] = T();
+    unsigned gi = 0;  // groups issued/consumed so far (stage = gi % S, phase parity = (gi / S) & 1)
+    bool first = true;
+    for (int r0 = 0; r0 < n && !s_stage_abort; r0 += PTILE) {
+        const int m = min(PTILE, n - r0);
+        load_ptile(slots, r0, m, 0, tid, nt);  // two block barriers; previous stages all consumed
+        const int ng = (m + G - 1) / G;
+        if (tid == 0) {
+            for (int g = 0; g < S && g < ng; g++) {
+                const unsigned sidx = (gi + g) % S;
+                const int k0 = g * G, mm = min(G, m - k0);
+                mbar_expect_tx(&full[sidx], (unsigned)mm * CB);
+                for (int k = 0; k < mm; k++)
+                    tma_load_1d(stage + (long long)sidx * stage_elems + (long long)k * E,
+                                (const T*)s_ptile[k0 + k] + e0, CB, &full[sidx]);
+            }
+        }
+        for (int g = 0; g < ng; g++, gi++) {
+            const unsigned sidx = gi % S;
+            const unsigned par = (gi / S) & 1u;
+            if (!mbar_wait_bounded(&full[sidx], par)) {
+                s_stage_abort = 1;
+                if (tid == 0) record_error(GPUMPI_ERR_OTHER, GPUMPI_ERR_TIMEOUT, __LINE__, idx);
+            }
+            bar_sync(BAR_TASK, nt);  // (a) everyone waited; abort flag visible
+            if (s_stage_abort) break;
+            const int mm = min(G, m - g * G);
+            const T* st = stage + (long long)sidx * stage_elems + my;
+            if (nv > 0) {
+                int k = 0;
+                if (first) {
+                    for (int q = 0; q < nv; q++) acc[q] = st[q];
+                    k = 1;
+                }
+                if (nv == V) {
+                    for (; k < mm; k++) {
+                        const T* p = st + (long long)k * E;
+#pragma unroll
+                        for (int q = 0; q < V; q++) acc[q] = op_apply<OP, T>(p[q], acc[q]);
+                    }
+                } else {
+                    for (; k < mm; k++) {
+                        const T* p = st + (long long)k * E;
+                        for (int q = 0; q < nv; q++) acc[q] = op_apply<OP, T>(p[q], acc[q]);
+                    }
+                }
+            }
+            first = false;
+            bar_sync(BAR_TASK, nt);  // (b) stage consumed by every thread
+            if (tid == 0 && g + S < ng) {
+                const int gg = g + S, k0 = gg * G, m2 = min(G, m - k0);
+                mbar_expect_tx(&full[sidx], (unsigned)m2 * CB);
+                for (int k = 0; k < m2; k++)
+                    tma_load_1d(stage + (long long)sidx * stage_elems + (long long)k * E,
+                                (const T*)s_ptile[k0 + k] + e0, CB, &full[sidx]);
+            }
+        }
+    }
+    if (s_stage_abort) return;
+    // every issued copy was waited for: retire the barriers (the next chunk initialises them again)
+    if (tid == 0)
+        for (int q = 0; q < S; q++) mbar_inval(&full[q]);
+    if (j->kind == JOB_REDUCE) {
+        if (nv > 0) {
+            T* out = (T*)slot_out(&slots[j->root]) + e0 + my;
+            for (int q = 0; q < nv; q++) __stcg(out + q, acc[q]);
+        }
+        return;
+    }
+    const long long e = e0 + my;
+    for (int r0 = 0; r0 < n; r0 += PTILE) {
+        const int m = min(PTILE, n - r0);
+        load_ptile(slots, r0, m, 1, tid, nt);
+        if (nv > 0)
+            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_ptile[i] + e, acc, nv, true);
+    }
+}
+
+}  // namespace gpumpi
