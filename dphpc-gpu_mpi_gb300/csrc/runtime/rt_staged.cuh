@@ -16,6 +16,30 @@ namespace gpumpi {
 
 __shared__ int s_stage_abort;
 
+// Issues the bulk copies of one group (ranks k0 .. k0+mm-1 of the current pointer tile) into the stage
+// at sdst, after checking what the hardware requires of every copy: 16-byte aligned global source,
+// 16-byte aligned destination inside this launch's dynamic shared memory, non-zero size that is a
+// multiple of 16.  On a violation nothing is issued: the error is recorded, the abort flag is set and
+// the stage barrier is completed with a plain arrival so no thread waits for bytes that never come.
+template <class T>
+__device__ __forceinline__ void stage_issue(unsigned long long* bar, T* sdst, long long E, int k0, int mm, long long e0,
+                                            unsigned CB) {
+    for (int k = 0; k < mm; k++) {
+        const T* src = (const T*)s_ptile[k0 + k] + e0;
+        const unsigned long long s_off = (unsigned long long)((const unsigned char*)(sdst + (long long)k * E) - g_dyn_smem);
+        const bool ok = (((unsigned long long)(size_t)src | s_off) & 15ull) == 0 && CB > 0 && (CB & 15u) == 0 &&
+                        s_off + CB <= (unsigned long long)g_rt->dyn_smem && is_global_ptr(src);
+        if (!ok) {
+            record_error(GPUMPI_ERR_INTERN, 2, __LINE__, (long long)s_off);
+            s_stage_abort = 1;
+            mbar_expect_tx(bar, 0);
+            return;
+        }
+    }
+    mbar_expect_tx(bar, (unsigned)mm * CB);
+    for (int k = 0; k < mm; k++) tma_load_1d(sdst + (long long)k * E, (const T*)s_ptile[k0 + k] + e0, CB, bar);
+}
+
 template <class T, int OP, int V>
 __device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int tid, int nt) {
     constexpr int S = 2;
@@ -42,7 +66,8 @@ __device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int 
     for (int q = 0; q < V; q++) acc[q] = T();
     unsigned gi = 0;  // groups issued/consumed so far (stage = gi % S, phase parity = (gi / S) & 1)
     bool first = true;
-    for (int r0 = 0; r0 < n && !s_stage_abort; r0 += PTILE) {
+    bool aborted = false;  // only ever read right after a block barrier, so every thread agrees
+    for (int r0 = 0; r0 < n && !aborted; r0 += PTILE) {
         const int m = min(PTILE, n - r0);
         load_ptile(slots, r0, m, 0, tid, nt);  // two block barriers; previous stages all consumed
         const int ng = (m + G - 1) / G;
@@ -50,10 +75,7 @@ __device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int 
             for (int g = 0; g < S && g < ng; g++) {
                 const unsigned sidx = (gi + g) % S;
                 const int k0 = g * G, mm = min(G, m - k0);
-                mbar_expect_tx(&full[sidx], (unsigned)mm * CB);
-                for (int k = 0; k < mm; k++)
-                    tma_load_1d(stage + (long long)sidx * stage_elems + (long long)k * E,
-                                (const T*)s_ptile[k0 + k] + e0, CB, &full[sidx]);
+                stage_issue<T>(&full[sidx], stage + (long long)sidx * stage_elems, E, k0, mm, e0, CB);
             }
         }
         for (int g = 0; g < ng; g++, gi++) {
@@ -64,7 +86,8 @@ __device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int 
                 if (tid == 0) record_error(GPUMPI_ERR_OTHER, GPUMPI_ERR_TIMEOUT, __LINE__, idx);
             }
             bar_sync(BAR_TASK, nt);  // (a) everyone waited; abort flag visible
-            if (s_stage_abort) break;
+            aborted = s_stage_abort != 0;
+            if (aborted) break;
             const int mm = min(G, m - g * G);
             const T* st = stage + (long long)sidx * stage_elems + my;
             if (nv > 0) {
@@ -90,14 +113,11 @@ __device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int 
             bar_sync(BAR_TASK, nt);  // (b) stage consumed by every thread
             if (tid == 0 && g + S < ng) {
                 const int gg = g + S, k0 = gg * G, m2 = min(G, m - k0);
-                mbar_expect_tx(&full[sidx], (unsigned)m2 * CB);
-                for (int k = 0; k < m2; k++)
-                    tma_load_1d(stage + (long long)sidx * stage_elems + (long long)k * E,
-                                (const T*)s_ptile[k0 + k] + e0, CB, &full[sidx]);
+                stage_issue<T>(&full[sidx], stage + (long long)sidx * stage_elems, E, k0, m2, e0, CB);
             }
         }
     }
-    if (s_stage_abort) return;
+    if (aborted) return;
     // every issued copy was waited for: retire the barriers (the next chunk initialises them again)
     if (tid == 0)
         for (int q = 0; q < S; q++) mbar_inval(&full[q]);
