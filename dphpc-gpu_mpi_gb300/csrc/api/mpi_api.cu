@@ -180,6 +180,38 @@ struct CollArgs {
     int variant;
 };
 
+// Elements per thread for a fold chunk (chunk = T * v elements).  Candidates: one 16-byte vector,
+// 8 bytes (4-byte types), one element.  Score = blocks busy per wave x bytes in flight per thread
+// (the rank-unrolled loads of fold_fast keep ~64 bytes in flight, at most 8 loads): the canonical
+// order makes every element a sequential chain over all ranks, so memory parallelism comes only from
+// elements in flight.  A tuning override (gpumpi_set_tuning) takes precedence when it is legal.
+__device__ int pick_vec(long long count, int T, int es, long long target, int aligned, int stage_room) {
+    int cands[3] = {16 / es, es == 4 ? 2 : 1, 1};
+    int best = 1;
+    double best_score = -1.0;
+    for (int k = 0; k < 3; k++) {
+        const int v = cands[k];
+        const int need = v * es >= 16 ? 16 : v * es;
+        if (v > 1 && aligned < need) continue;
+        if (stage_room < 2 * T * v * es) continue;
+        if (g_rt->tune_vec > 0) {
+            if (v == g_rt->tune_vec) return v;
+            continue;
+        }
+        const long long nch = (count + (long long)T * v - 1) / ((long long)T * v);
+        const long long waves = (nch + target - 1) / (target > 0 ? target : 1);
+        const double busy = (double)nch / (double)(waves > 0 ? waves : 1);
+        int u = 64 / (v * es);
+        u = u < 1 ? 1 : u > 8 ? 8 : u;
+        const double score = busy * (double)(v * es * u);
+        if (score > best_score + 1e-9) {
+            best_score = score;
+            best = v;
+        }
+    }
+    return best;
+}
+
 __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, unsigned e_next) {
     Job* j = &c->job;
     unsigned mis = ld_relaxed(&c->misalign[e_next & 1]);
@@ -216,14 +248,9 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             if (!fold_has_staged(a.dt, a.op, a.ufn) || j->aligned16 < 16 || stage_room < 2 * T * es) {
                 variant = GPUMPI_VARIANT_DIRECT;
             } else {
-                int cands[3] = {16 / es, es == 4 ? 2 : 1, 1};
-                for (int k = 0; k < 3; k++) {
-                    int v = cands[k];
-                    if (stage_room < 2 * T * v * es) continue;
-                    long long nch = (a.count + (long long)T * v - 1) / ((long long)T * v);
-                    if (nch >= target || v == 1) { vec = v; break; }
-                }
+                vec = pick_vec(a.count, T, es, target, 16, stage_room);
                 int G = stage_room / (2 * T * vec * es);
+                if (g_rt->tune_group > 0 && g_rt->tune_group < G) G = g_rt->tune_group;
                 j->tile = G < 1 ? 1 : G > 64 ? 64 : G;
             }
         }
@@ -231,14 +258,7 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         j->variant = variant;
         if (variant == GPUMPI_VARIANT_DIRECT && fold_has_fast(a.dt, a.op, a.ufn)) {
             int es = a.esize;
-            int cands[3] = {16 / es, es == 4 ? 2 : 1, 1};
-            for (int k = 0; k < 3; k++) {
-                int v = cands[k];
-                int need = v * es >= 16 ? 16 : v * es;
-                if (v > 1 && j->aligned16 < need) continue;
-                long long nch = (a.count + (long long)T * v - 1) / ((long long)T * v);
-                if (nch >= target || v == 1) { vec = v; break; }
-            }
+            vec = pick_vec(a.count, T, es, target, j->aligned16, 1 << 30);
         }
         j->vec = vec;
         j->chunk = (long long)T * vec;

@@ -90,6 +90,7 @@ struct gpumpi_world {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0;
     int variant_override = -1, selector_mode = 3;
+    int tune_vec = 0, tune_group = 0;
     signed char* d_table = nullptr;
     float* d_mlp = nullptr;
     // scratch for host-buffer staging
@@ -353,6 +354,18 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode) {
     return GPUMPI_SUCCESS;
 }
 
+int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
+    if (!w) return GPUMPI_ERR_ARG;
+    switch (key) {
+    case GPUMPI_TUNE_VEC: w->tune_vec = (int)value; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_STAGE_GROUP: w->tune_group = (int)value; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_ENGINES: w->cfg.engine_blocks = (int)value; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_COPY_CHUNK: w->h_rt.copy_chunk_bytes = value; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_ENGINE_MIN_BYTES: w->h_rt.engine_min_bytes = value; return GPUMPI_SUCCESS;
+    default: return GPUMPI_ERR_ARG;
+    }
+}
+
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes) {
     if (!w || !table || bytes != 2 * 32 * 16) return GPUMPI_ERR_ARG;
     cudaSetDevice(w->device);
@@ -468,6 +481,8 @@ int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params
     r.tuned_table = w->d_table;
     r.mlp_params = w->d_mlp;
     r.dyn_smem = (int)w->dyn_smem;
+    r.tune_vec = w->tune_vec;
+    r.tune_group = w->tune_group;
     CK(cudaMemsetAsync(w->d_ctrl, 0, w->ctrl_bytes, s));
     CK(cudaMemcpyAsync(w->d_fixed, &w->h_fixed, sizeof(FixedImage), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(w->d_rt, &r, sizeof(Runtime), cudaMemcpyHostToDevice, s));

@@ -352,6 +352,8 @@ struct Runtime {
     int variant_override;             // -1: selector decides
     int selector_mode;                // 0 plain (DIRECT), 1 tuned table, 2 learned MLP, 3 heuristic
     int dyn_smem;                     // dynamic shared memory bytes of this launch (STAGED stages)
+    int tune_vec;                     // autotuner override: elements per thread of fold chunks (0 = auto)
+    int tune_group;                   // autotuner override: ranks per STAGED stage (0 = auto)
     int trace_enabled;
     int trace_cap;
     // state arrays (device global memory)

@@ -31,6 +31,7 @@ VARIANT_AUTO, VARIANT_DIRECT, VARIANT_TREE, VARIANT_RING, VARIANT_STAGED = -1, 0
 VARIANT_NAMES = ["direct", "tree", "ring", "staged"]
 
 ERR_OTHER, ERR_TRUNCATE, ERR_TIMEOUT = 1, 12, 15
+TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES = 1, 2, 3, 4, 5
 
 TESTS = {
     "single_int": 1, "transfer_array": 2, "send_recv": 3, "repeat_send_recv": 4, "network_flood": 5,
@@ -54,7 +55,7 @@ MLP_NPARAMS = 64 * 12 + 64 + 64 * 64 + 64 + 4 * 64 + 4
 # symbols include/gpumpi.h declares (checked by the CPU test suite)
 EXPORTS = [
     "gpumpi_config_init", "gpumpi_parse_args", "gpumpi_world_create", "gpumpi_world_destroy",
-    "gpumpi_world_get_info", "gpumpi_last_error", "gpumpi_set_policy", "gpumpi_set_tuned_table",
+    "gpumpi_world_get_info", "gpumpi_last_error", "gpumpi_set_policy", "gpumpi_set_tuning", "gpumpi_set_tuned_table",
     "gpumpi_set_mlp", "gpumpi_read_trace", "gpumpi_run_program", "gpumpi_last_kernel_ms",
     "gpumpi_kernel_launches", "gpumpi_test_run", "gpumpi_allreduce", "gpumpi_reduce", "gpumpi_bcast",
     "gpumpi_alltoall", "gpumpi_alltoallv", "gpumpi_allgather", "gpumpi_pingpong", "gpumpi_ring",
@@ -114,6 +115,7 @@ def lib():
         L.gpumpi_last_error.argtypes = [vp]
         L.gpumpi_last_error.restype = ctypes.c_char_p
         L.gpumpi_set_policy.argtypes = [vp, i32, i32]
+        L.gpumpi_set_tuning.argtypes = [vp, i32, i64]
         L.gpumpi_set_tuned_table.argtypes = [vp, vp, ctypes.c_size_t]
         L.gpumpi_set_mlp.argtypes = [vp, vp, ctypes.c_size_t]
         L.gpumpi_read_trace.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
@@ -209,6 +211,10 @@ class World:
     def set_policy(self, variant: int = -1, mode: int = 3):
         """variant >= 0 forces one; mode 0 plain (DIRECT), 1 tuned table, 2 learned MLP, 3 heuristic."""
         self._check(lib().gpumpi_set_policy(self.h, variant, mode), "set_policy")
+
+    def set_tuning(self, key: int, value: int):
+        """Autotuner knobs (TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES)."""
+        self._check(lib().gpumpi_set_tuning(self.h, key, value), "set_tuning")
 
     def set_tuned_table(self, table: np.ndarray):
         t = np.ascontiguousarray(table, dtype=np.int8)

@@ -138,6 +138,15 @@ const char* gpumpi_last_error(gpumpi_world* w);
 /* Variant policy for reductions: variant >= 0 forces one, -1 lets the selector decide;
  * mode 0 = plain (DIRECT), 1 = tuned table, 2 = learned MLP. */
 int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
+/* Autotuner knobs: GPUMPI_TUNE_VEC (elements per thread of fold chunks, 0 = auto),
+ * GPUMPI_TUNE_STAGE_GROUP (ranks per STAGED stage, 0 = auto), GPUMPI_TUNE_ENGINES (copy-engine blocks,
+ * -1 = fill the GPU), GPUMPI_TUNE_COPY_CHUNK (bytes), GPUMPI_TUNE_ENGINE_MIN_BYTES (bytes). */
+#define GPUMPI_TUNE_VEC 1
+#define GPUMPI_TUNE_STAGE_GROUP 2
+#define GPUMPI_TUNE_ENGINES 3
+#define GPUMPI_TUNE_COPY_CHUNK 4
+#define GPUMPI_TUNE_ENGINE_MIN_BYTES 5
+int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Tuned table: int8 [2][32][16] (kind, log2 bytes per rank, log2 ranks) -> variant, host memory. */
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes);
 /* Learned selector weights: float[GPUMPI_MLP_NPARAMS] in the layout of the training kernels. */
