@@ -182,11 +182,39 @@ struct CollArgs {
 
 // Elements per thread for a fold chunk (chunk = T * v elements).  Candidates: one 16-byte vector,
 // 8 bytes (4-byte types), one element.  Score = blocks busy per wave x bytes in flight per thread
-// (the rank-unrolled loads of fold_fast keep ~64 bytes in flight, at most 8 loads): the canonical
+// (the rank-unrolled loads of fold_fast keep ~128 bytes in flight, at most 16 loads): the canonical
 // order makes every element a sequential chain over all ranks, so memory parallelism comes only from
 // elements in flight.  A tuning override (gpumpi_set_tuning) takes precedence when it is legal.
 __device__ int pick_vec(long long count, int T, int es, long long target, int aligned, int stage_room) {
     int cands[3] = {16 / es, es == 4 ? 2 : 1, 1};
+    double score_of[3] = {-1.0, -1.0, -1.0}, busy_of[3] = {0, 0, 0};
+    for (int k = 0; k < 3; k++) {
+        const int v = cands[k];
+        const int need = v * es >= 16 ? 16 : v * es;
+        if (v > 1 && aligned < need) continue;
+        if (stage_room < 2 * T * v * es) continue;
+        if (g_rt->tune_vec > 0) {
+            if (v == g_rt->tune_vec) return v;
+            continue;
+        }
+        const long long nch = (count + (long long)T * v - 1) / ((long long)T * v);
+        const long long waves = (nch + target - 1) / (target > 0 ? target : 1);
+        busy_of[k] = (double)nch / (double)(waves > 0 ? waves : 1);
+        int u = 128 / (v * es);
+        u = u < 1 ? 1 : u > 16 ? 16 : u;
+        score_of[k] = busy_of[k] * (double)(v * es * u);
+    }
+    // among candidates within 5% of the best score: most busy blocks, then the widest vector
+    double top = -1.0;
+    for (int k = 0; k < 3; k++) top = score_of[k] > top ? score_of[k] : top;
+    int pick = -1;
+    for (int k = 0; k < 3; k++) {
+        if (score_of[k] < 0.95 * top || score_of[k] < 0) continue;
+        if (pick < 0 || busy_of[k] > busy_of[pick] * 1.01 ||
+            (busy_of[k] >= busy_of[pick] * 0.99 && cands[k] > cands[pick]))
+            pick = k;
+    }
+    if (pick >= 0) return cands[pick];
     int best = 1;
     double best_score = -1.0;
     for (int k = 0; k < 3; k++) {
@@ -201,8 +229,8 @@ __device__ int pick_vec(long long count, int T, int es, long long target, int al
         const long long nch = (count + (long long)T * v - 1) / ((long long)T * v);
         const long long waves = (nch + target - 1) / (target > 0 ? target : 1);
         const double busy = (double)nch / (double)(waves > 0 ? waves : 1);
-        int u = 64 / (v * es);
-        u = u < 1 ? 1 : u > 8 ? 8 : u;
+        int u = 128 / (v * es);
+        u = u < 1 ? 1 : u > 16 ? 16 : u;
         const double score = busy * (double)(v * es * u);
         if (score > best_score + 1e-9) {
             best_score = score;

@@ -206,8 +206,8 @@ __device__ __forceinline__ void st_elems(T* p, const T (&v)[V], int nv, bool vec
 template <class T, int OP, int V>
 __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid, int nt) {
     constexpr int BYTES = V * (int)sizeof(T);
-    // ranks folded per step: ~64 bytes of loads in flight per thread without spilling
-    constexpr int U = 64 / BYTES > 8 ? 8 : 64 / BYTES < 1 ? 1 : 64 / BYTES;
+    // ranks folded per step: ~128 bytes of loads in flight per thread (at most 16 loads)
+    constexpr int U = 128 / BYTES > 16 ? 16 : 128 / BYTES < 1 ? 1 : 128 / BYTES;
     const MPI_Comm_impl* c = j->comm;
     const CollSlot* slots = c->slots;
     const int n = c->size;

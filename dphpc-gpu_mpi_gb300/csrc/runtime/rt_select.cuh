@@ -28,7 +28,6 @@ __device__ int select_variant(int kind, long long bytes_per_rank, int n, int dt,
         if (v >= 0 && v < GPUMPI_NUM_VARIANTS) return v;
     }
     if (g_rt->selector_mode == 2 && g_rt->mlp_params) return mlp_select(kind, bytes_per_rank, n, dt, op);
-    if (g_rt->selector_mode == 3 && bytes_per_rank >= 4096) return GPUMPI_VARIANT_STAGED;
     return GPUMPI_VARIANT_DIRECT;
 }
 
