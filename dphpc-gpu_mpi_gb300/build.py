@@ -23,6 +23,7 @@ SOURCES = [
     CSRC / "programs" / "prog_hot.cu",
     CSRC / "programs" / "prog_apps.cu",
     CSRC / "host" / "host.cu",
+    CSRC / "host" / "noalloc.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

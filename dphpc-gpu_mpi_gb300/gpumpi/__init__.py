@@ -59,6 +59,7 @@ EXPORTS = [
     "gpumpi_set_mlp", "gpumpi_read_trace", "gpumpi_run_program", "gpumpi_last_kernel_ms",
     "gpumpi_kernel_launches", "gpumpi_test_run", "gpumpi_allreduce", "gpumpi_reduce", "gpumpi_bcast",
     "gpumpi_alltoall", "gpumpi_alltoallv", "gpumpi_allgather", "gpumpi_pingpong", "gpumpi_ring",
+    "gpumpi_allreduce_noalloc",
 ]
 
 

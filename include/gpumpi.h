@@ -187,6 +187,21 @@ int gpumpi_pingpong(gpumpi_world* w, void* bufs, long long bytes, int pairs, int
 int gpumpi_ring(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long bytes, int iters, int nonblocking,
                 uint64_t* iter_ns, void* stream);
 
+/* Allocation-free MPI_Allreduce among `nranks` block-ranks (no counterpart in the reference).
+ * For callers that cannot allocate device memory when they reduce — inside stream capture, inside an
+ * allocator or memory-pool callback, or under a fixed device-memory budget — this call allocates
+ * nothing: its scratch (rank table, barrier words, chunk counter) is a fixed static device array of
+ * GPUMPI_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until exit.  sendbuf/recvbuf are
+ * rank-major DEVICE buffers of nranks * count elements; nranks <= GPUMPI_NOALLOC_MAX_RANKS (else
+ * GPUMPI_ERR_ARG); float/double/int32/int64 with SUM/MAX/MIN/PROD (else GPUMPI_ERR_TYPE).  Asynchronous
+ * on `stream`; canonical rank order, bit-identical to gpumpi_allreduce.  All calls share the array:
+ * calls that overlap on the GPU race.  The first call on a device looks up the array's address with
+ * that device current; make it before any stream capture. */
+#define GPUMPI_NOALLOC_MAX_RANKS 4096
+#define GPUMPI_NOALLOC_SCRATCH_BYTES (64 * 1024 + 256)
+int gpumpi_allreduce_noalloc(const void* sendbuf, void* recvbuf, long long count, int datatype, int op, int nranks,
+                             void* stream);
+
 #define GPUMPI_MLP_NPARAMS (64 * 12 + 64 + 64 * 64 + 64 + 4 * 64 + 4)
 
 #ifdef __cplusplus
