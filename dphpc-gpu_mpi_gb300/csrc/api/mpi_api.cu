@@ -282,7 +282,27 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
                 j->tile = G < 1 ? 1 : G > 64 ? 64 : G;
             }
         }
-        if (variant == GPUMPI_VARIANT_TREE || variant == GPUMPI_VARIANT_RING) variant = GPUMPI_VARIANT_DIRECT;
+        if (variant == GPUMPI_VARIANT_TREE) {
+            // two-level rank split on the world communicator: R groups (power of two, >= 8 ranks each)
+            // so that chunks x groups covers the blocks; partials and flags must fit the tree scratch
+            const int es = a.esize;
+            int v = (j->aligned16 >= 16) ? 16 / es : 1;
+            if (g_rt->tune_vec > 0) v = g_rt->tune_vec == 16 / es ? v : 1;
+            const long long E = (long long)T * v;
+            const long long C = (a.count + E - 1) / E;
+            int R = 2;
+            while (R < 16 && R * 2 <= n / 8 && C * R < target) R *= 2;
+            if (g_rt->tune_group > 0) R = g_rt->tune_group;
+            const bool ok = fold_has_tree(a.dt, a.op, a.ufn) && c->is_world && n >= 16 && R >= 2 && R <= n &&
+                            (long long)R * a.count * es <= g_rt->tree_scratch_bytes && C * R <= g_rt->tree_flags_cap &&
+                            g_rt->tree_scratch && g_rt->tree_flags;
+            if (ok) {
+                vec = v;
+                j->tile = R;
+            } else {
+                variant = GPUMPI_VARIANT_DIRECT;
+            }
+        }
         j->variant = variant;
         if (variant == GPUMPI_VARIANT_DIRECT && fold_has_fast(a.dt, a.op, a.ufn)) {
             int es = a.esize;
@@ -291,6 +311,7 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         j->vec = vec;
         j->chunk = (long long)T * vec;
         nchunks = (int)((a.count + j->chunk - 1) / j->chunk);
+        if (variant == GPUMPI_VARIANT_TREE) nchunks *= (j->tile + 1);  // C*R phase-1 + C phase-2 chunks
     } else if (a.kind == JOB_BARRIER) {
         nchunks = 0;
     } else {

@@ -215,6 +215,8 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     size_t o_done = cc.take<unsigned>(1);
     size_t o_abort = cc.take<unsigned>(1);
     size_t o_trace_count = cc.take<unsigned long long>(1);
+    const int tree_flags_cap = 1 << 16;
+    size_t o_tree_flags = cc.take<unsigned>(tree_flags_cap);
     w->ctrl_bytes = align_up(cc.off, 256);
 
     // ---- data region ----
@@ -232,6 +234,8 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     size_t o_board_ring = dc.take<gpumpi::BoardEntry>(4096);
     size_t o_trace = dc.take<gpumpi::TraceRec>(cfg.trace_capacity > 0 ? cfg.trace_capacity : 1);
     size_t o_arena = dc.take<unsigned char>(cfg.arena_bytes);
+    const size_t tree_bytes = 64ull << 20;
+    size_t o_tree = dc.take<unsigned char>(tree_bytes);
     w->data_bytes = align_up(dc.off, 256);
 
     CK(cudaMalloc(&w->d_ctrl, w->ctrl_bytes));
@@ -287,6 +291,10 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     r.trace = (gpumpi::TraceRec*)(w->d_data + o_trace);
     r.arena = (unsigned char*)(w->d_data + o_arena);
     r.arena_bytes = cfg.arena_bytes;
+    r.tree_scratch = (unsigned char*)(w->d_data + o_tree);
+    r.tree_scratch_bytes = (long long)tree_bytes;
+    r.tree_flags = (unsigned*)(w->d_ctrl + o_tree_flags);
+    r.tree_flags_cap = tree_flags_cap;
     r.world = &w->d_fixed->world;
     r.board = &w->d_fixed->board;
     r.ctx_counter = &w->d_fixed->ctx_counter;

@@ -114,6 +114,7 @@ __device__ int comm_barrier(MPI_Comm_impl* c, F&& setup, int line) {
 // struct is rewritten by every epoch, so no executing block may keep it in L1).
 struct JobParams {
     int kind, dt, op, root, esize, vec, tile, aligned16, variant;
+    unsigned epoch;
     long long count, chunk;
     const MPI_Comm_impl* comm;
     const void* src;
@@ -124,6 +125,7 @@ struct JobParams {
 __device__ __forceinline__ void load_params(const Job* j, JobParams& P) {
     P.kind = __ldcg(&j->kind);
     P.variant = __ldcg(&j->variant);
+    P.epoch = __ldcg(&j->epoch);
     P.dt = __ldcg(&j->dt);
     P.op = __ldcg(&j->op);
     P.root = __ldcg(&j->root);
@@ -150,11 +152,15 @@ __device__ __forceinline__ void* slot_out(const CollSlot* s) {
 }
 
 // loads pointer field `which` (0 = sbuf, 1 = rbuf) of members [r0, r0+m) into s_ptile
-__device__ __forceinline__ void load_ptile(const CollSlot* slots, int r0, int m, int which, int tid, int nt) {
+// With rot != 0 the tile holds members (r0 + i + rot) mod n: the RING variant's rotated fold order.
+__device__ __forceinline__ void load_ptile(const CollSlot* slots, int r0, int m, int which, int tid, int nt,
+                                           int rot = 0, int n = 1) {
     bar_sync(BAR_TASK, nt);
-    for (int i = tid; i < m; i += nt)
-        s_ptile[i] = __ldcg(which == 0 ? (const unsigned long long*)&slots[r0 + i].sbuf
-                                        : (const unsigned long long*)&slots[r0 + i].rbuf);
+    for (int i = tid; i < m; i += nt) {
+        const int r = rot ? (r0 + i + rot) % n : r0 + i;
+        s_ptile[i] = __ldcg(which == 0 ? (const unsigned long long*)&slots[r].sbuf
+                                        : (const unsigned long long*)&slots[r].rbuf);
+    }
     bar_sync(BAR_TASK, nt);
 }
 
@@ -215,12 +221,14 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
     const long long e = e0 + (long long)tid * V;
     const int nv = e < count ? (int)min((long long)V, count - e) : 0;
     const bool vec16 = j->aligned16 >= (int)((V * sizeof(T)) >= 16 ? 16 : (V * sizeof(T)));
+    // RING: chunk k folds members k+1, k+2, ..., k (mod n), the order a ring reduce-scatter produces
+    const int rot = j->variant == GPUMPI_VARIANT_RING ? (int)((e0 / j->chunk + 1) % n) : 0;
     T acc[V];
 #pragma unroll
     for (int k = 0; k < V; k++) acc[k] = T();
     for (int r0 = 0; r0 < n; r0 += PTILE) {
         const int m = min(PTILE, n - r0);
-        load_ptile(slots, r0, m, 0, tid, nt);
+        load_ptile(slots, r0, m, 0, tid, nt, rot, n);
         if (nv > 0) {
             int i = 0;
             if (r0 == 0) {
@@ -262,6 +270,7 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
 }  // namespace gpumpi
 
 #include "rt_staged.cuh"
+#include "rt_tree.cuh"
 
 namespace gpumpi {
 
@@ -395,6 +404,10 @@ __device__ __noinline__ void fold_chunk(const JobParams* j, long long idx, int t
     const long long e0 = idx * j->chunk;
     bool done = false;
 #ifndef GPUMPI_NO_FAST_FOLD
+    // TREE chunks are numbered by phase (see rt_tree.cuh), not by element range
+    if (j->variant == GPUMPI_VARIANT_TREE && j->tile > 0) {
+        if (fold_tree_dispatch(j, idx, tid, nt)) return;
+    }
     if (j->variant == GPUMPI_VARIANT_STAGED && j->tile > 0 &&
         ((min(j->chunk, j->count - e0) * j->esize) & 15) == 0) {
         switch (j->dt) {

@@ -354,6 +354,10 @@ struct Runtime {
     int dyn_smem;                     // dynamic shared memory bytes of this launch (STAGED stages)
     int tune_vec;                     // autotuner override: elements per thread of fold chunks (0 = auto)
     int tune_group;                   // autotuner override: ranks per STAGED stage (0 = auto)
+    unsigned char* tree_scratch;      // TREE partials (world communicator)
+    long long tree_scratch_bytes;
+    unsigned* tree_flags;             // TREE partial-ready flags, tagged with the job epoch
+    int tree_flags_cap;
     int trace_enabled;
     int trace_cap;
     // state arrays (device global memory)
