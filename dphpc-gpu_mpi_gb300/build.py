@@ -24,6 +24,7 @@ SOURCES = [
     CSRC / "programs" / "prog_apps.cu",
     CSRC / "host" / "host.cu",
     CSRC / "host" / "noalloc.cu",
+    CSRC / "selector" / "mlp.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -43,7 +44,7 @@ def common_flags() -> list[str]:
 
 def _deps() -> list[Path]:
     out = list(SOURCES)
-    for d in ("runtime", "programs", "api", "host"):
+    for d in ("runtime", "programs", "api", "host", "selector"):
         out += list((CSRC / d).glob("*.cuh"))
     out += list((ROOT / "include").glob("*.h")) + list((ROOT / "include").glob("*.cuh"))
     return out

@@ -370,6 +370,75 @@ __device__ __forceinline__ int op_code_of(MPI_Op op, MPI_User_function** ufn) {
     return op->code;
 }
 
+// ---- learned selector: in-kernel inference of the MLP trained by csrc/selector/mlp.cu ----
+// Features (same formula as gpumpi/selector.py): log2 bytes per rank, log2 ranks, datatype one-hot
+// (f32, f64, i32, i64), operator one-hot (SUM, MAX, MIN, PROD), rank share of the launch's blocks, kind.
+struct MlpWork {
+    float f[12];
+    float h1[64];
+    float h2[64];
+    float y[4];
+};
+__shared__ MlpWork s_mlp;
+
+__device__ void mlp_infer_task(void* arg, int tid, int nt) {
+    MlpWork* w = (MlpWork*)arg;
+    const float* p = g_rt->mlp_params;
+    constexpr int W1 = 0, B1 = 64 * 12, W2 = B1 + 64, B2 = W2 + 64 * 64, W3 = B2 + 64, B3 = W3 + 4 * 64;
+    if (tid < 64) {
+        float z = __ldcg(p + B1 + tid);
+        for (int i = 0; i < 12; i++) z = fmaf(__ldcg(p + W1 + tid * 12 + i), w->f[i], z);
+        w->h1[tid] = z > 0.f ? z : 0.f;
+    }
+    bar_sync(BAR_TASK, nt);
+    if (tid < 64) {
+        float z = __ldcg(p + B2 + tid);
+        for (int i = 0; i < 64; i++) z = fmaf(__ldcg(p + W2 + tid * 64 + i), w->h1[i], z);
+        w->h2[tid] = z > 0.f ? z : 0.f;
+    }
+    bar_sync(BAR_TASK, nt);
+    if (tid < 4) {
+        float z = __ldcg(p + B3 + tid);
+        for (int i = 0; i < 64; i++) z = fmaf(__ldcg(p + W3 + tid * 64 + i), w->h2[i], z);
+        w->y[tid] = z;
+    }
+}
+
+// Variant with the smallest predicted time; every member computes it from the same inputs with the
+// same operation order, so all members agree.  Cached per rank for repeated calls of one shape.
+__device__ __noinline__ int learned_variant(int kind, long long bytes, int n, int dt, int op) {
+    RankState* R = &g_rt->ranks[me()];
+    if (R->sel_key_kind == kind && R->sel_key_bytes == bytes && R->sel_key_n == n && R->sel_key_dt == dt &&
+        R->sel_key_op == op)
+        return R->sel_variant;
+    MlpWork* w = &s_mlp;
+    for (int i = 0; i < 12; i++) w->f[i] = 0.f;
+    w->f[0] = (log2f((float)(bytes > 0 ? bytes : 1)) - 16.f) / 8.f;
+    w->f[1] = (log2f((float)n) - 8.f) / 3.f;
+    const int dslot = dt == GPUMPI_FLOAT ? 2 : (dt == GPUMPI_DOUBLE || dt == GPUMPI_LONG_DOUBLE) ? 3
+                      : (dt == GPUMPI_INT || dt == GPUMPI_INT32_T) ? 4 : 5;
+    w->f[dslot] = 1.f;
+    const int oslot = op == GPUMPI_OP_SUM ? 6 : op == GPUMPI_OP_MAX ? 7 : op == GPUMPI_OP_MIN ? 8 : 9;
+    w->f[oslot] = 1.f;
+    w->f[10] = (float)n / (float)(g_rt->nranks + g_rt->nengines);
+    w->f[11] = kind == JOB_REDUCE ? 1.f : 0.f;
+    Task t;
+    t.kind = TASK_USER;
+    t.p0 = (const void*)&mlp_infer_task;
+    t.p1 = w;
+    dispatch(t);
+    int best = 0;
+    for (int v = 1; v < 4; v++)
+        if (w->y[v] < w->y[best]) best = v;
+    R->sel_key_kind = kind;
+    R->sel_key_bytes = bytes;
+    R->sel_key_n = n;
+    R->sel_key_dt = dt;
+    R->sel_key_op = op;
+    R->sel_variant = best;
+    return best;
+}
+
 __device__ __noinline__ int fold_collective(int kind, const void* sendbuf, void* recvbuf, int count, MPI_Datatype dt, MPI_Op op,
                                int root, MPI_Comm comm) {
     MPI_Comm_impl* c = check_comm(comm);
@@ -412,6 +481,8 @@ __device__ __noinline__ int fold_collective(int kind, const void* sendbuf, void*
     a.ufn = ufn;
     a.est_piece = 0;
     a.variant = g_rt->variant_override;
+    if (a.variant < 0 && g_rt->selector_mode == 2 && g_rt->mlp_params)
+        a.variant = learned_variant(kind, bytes, c->size, dt, opc);
     int rc = coll_run(c, my, a, __LINE__);
     stage_out(ss, false);
     stage_out(rs, has_out);

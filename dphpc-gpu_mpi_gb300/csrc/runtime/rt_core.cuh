@@ -284,6 +284,8 @@ struct alignas(128) RankState {
     int sel_key_kind;
     long long sel_key_bytes;
     int sel_key_n;
+    int sel_key_dt;
+    int sel_key_op;
     int sel_variant;
     unsigned long long coll_calls;
     Job p2p_job;

@@ -59,7 +59,7 @@ EXPORTS = [
     "gpumpi_set_mlp", "gpumpi_read_trace", "gpumpi_run_program", "gpumpi_last_kernel_ms",
     "gpumpi_kernel_launches", "gpumpi_test_run", "gpumpi_allreduce", "gpumpi_reduce", "gpumpi_bcast",
     "gpumpi_alltoall", "gpumpi_alltoallv", "gpumpi_allgather", "gpumpi_pingpong", "gpumpi_ring",
-    "gpumpi_allreduce_noalloc",
+    "gpumpi_allreduce_noalloc", "gpumpi_mlp_forward", "gpumpi_mlp_loss_grad", "gpumpi_mlp_adam_step",
 ]
 
 
@@ -133,6 +133,9 @@ def lib():
         L.gpumpi_allgather.argtypes = [vp, vp, vp, i64, i32, i32, u64p, vp]
         L.gpumpi_pingpong.argtypes = [vp, vp, i64, i32, i32, i32, u64p, vp]
         L.gpumpi_ring.argtypes = [vp, vp, vp, i64, i32, i32, u64p, vp]
+        L.gpumpi_mlp_forward.argtypes = [vp, vp, i32, vp, vp]
+        L.gpumpi_mlp_loss_grad.argtypes = [vp, vp, vp, vp, i32, vp, vp, vp]
+        L.gpumpi_mlp_adam_step.argtypes = [vp, vp, vp, vp, i32, ctypes.c_float, ctypes.c_float, vp]
         _lib = L
     return _lib
 

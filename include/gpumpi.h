@@ -204,6 +204,16 @@ int gpumpi_allreduce_noalloc(const void* sendbuf, void* recvbuf, long long count
 
 #define GPUMPI_MLP_NPARAMS (64 * 12 + 64 + 64 * 64 + 64 + 4 * 64 + 4)
 
+/* The learned selector's network (12 -> 64 -> 64 -> 4, ReLU), trained on the GPU by these kernels.
+ * All pointers are device buffers; params use the layout W1[64][12] b1[64] W2[64][64] b2[64] W3[4][64] b3[4].
+ * x: [batch][12] features, t: [batch][4] target log-times, mask: [batch][4] (1 where measured).
+ * No counterpart in the reference (it has one algorithm per collective). */
+int gpumpi_mlp_forward(const float* params, const float* x, int batch, float* y, void* stream);
+int gpumpi_mlp_loss_grad(const float* params, const float* x, const float* t, const float* mask, int batch,
+                         float* grads, float* loss, void* stream);
+int gpumpi_mlp_adam_step(float* params, const float* grads, float* m, float* v, int step, float lr, float wd,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif

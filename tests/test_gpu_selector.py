@@ -1,0 +1,98 @@
+"""GPU: the learned selector's network trained by the library's own kernels — forward and gradients
+against the CPU oracle's fp64 restatement, training, what the trained network gains over the plain
+policy, and the tuned-table / learned policies driving real collectives."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def rand_problem(seed, batch):
+    rng = np.random.default_rng(seed)
+    p = (rng.standard_normal(64 * 12 + 64 + 64 * 64 + 64 + 4 * 64 + 4) * 0.2).astype(np.float32)
+    x = rng.standard_normal((batch, 12)).astype(np.float32)
+    t = rng.standard_normal((batch, 4)).astype(np.float32)
+    m = (rng.random((batch, 4)) > 0.4).astype(np.float32)
+    return p, x, t, m
+
+
+def test_mlp_forward_and_gradients_match_fp64_oracle(gpulib, oracle):
+    from gpumpi.selector import MLP
+    p, x, t, m = rand_problem(1, 77)
+    mlp = MLP(params=p)
+    y = mlp.predict(x)
+    y_ref = oracle.mlp_forward(p.astype(np.float64), x.astype(np.float64))
+    assert np.allclose(y, y_ref, rtol=1e-4, atol=1e-4)
+    loss, g = mlp.loss_grad(*(torch.from_numpy(a).cuda() for a in (x, t, m)))
+    torch.cuda.synchronize()
+    l_ref, g_ref = oracle.mlp_loss_grad(p, x, t, m)
+    assert abs(float(loss.item()) - l_ref) <= 1e-4 * max(1.0, abs(l_ref))
+    g = g.cpu().numpy()
+    # fp32 accumulation with atomics vs fp64: relative to the gradient's scale
+    scale = np.abs(g_ref).max()
+    assert np.abs(g - g_ref).max() <= 1e-4 * scale + 1e-6
+
+
+def synthetic_times(X):
+    """A timing model with crossovers: log-time per variant from (log2 bytes, log2 ranks)."""
+    lb = X[:, 0] * 8 + 16
+    lr = X[:, 1] * 3 + 8
+    base = np.log(5.0 + 2.0 ** (lb + lr - 32.0) * 1e3)
+    t = np.stack([base,
+                  base - 0.3 * (lb < 16) * (lr > 7) + 0.1,      # tree wins: small messages, many ranks
+                  base + 0.05 * np.sin(lb) + 0.02,               # ring ~ direct
+                  base + 0.2 - 0.35 * (lb > 20) * (lr < 7)], 1)  # staged wins: big messages, few ranks
+    return t.astype(np.float32)
+
+
+def test_training_gains_over_plain_policy(gpulib):
+    from gpumpi.selector import MLP, features
+    rng = np.random.default_rng(5)
+    n = 8000
+    feats = np.stack([features(2, 2 ** rng.uniform(6, 25), int(2 ** rng.uniform(4, 11)),
+                               int(rng.choice([12, 2, 13])), 2, rng.uniform(0.5, 1.0)) for _ in range(n)])
+    T_all = synthetic_times(feats)
+    M = np.zeros_like(T_all)
+    M[np.arange(n), rng.integers(0, 4, n)] = 1.0            # one measured variant per sample
+    T = T_all * M
+    mlp = MLP(seed=3)
+    hist = mlp.train(feats[:6000], T[:6000], M[:6000], epochs=40, batch=256, lr=3e-3)
+    assert hist[-1] < 0.25 * hist[0]
+    held = feats[6000:]
+    truth = np.exp(T_all[6000:])
+    pick = np.argmin(mlp.predict(held), axis=1)
+    best = truth.min(1)
+    learned = truth[np.arange(len(pick)), pick].sum() / best.sum() - 1.0
+    plain = truth[:, 0].sum() / best.sum() - 1.0
+    assert learned < 0.5 * plain, (learned, plain)   # the network recovers most of the available gain
+
+
+def test_learned_and_tuned_policies_drive_allreduce(gpulib, oracle):
+    from gpumpi.selector import MLP
+    n, count = 128, 5000
+    x = oracle.fill_i32(77, n * count).reshape(n, count) % 1000
+    ref = oracle.allreduce(x, 2, 2)
+    with gpulib.World(n, timeout_s=20.0, trace_capacity=64) as w:
+        # tuned table that picks RING everywhere
+        table = np.full((2, 32, 16), 2, np.int8)
+        w.set_tuned_table(table)
+        w.set_policy(-1, 1)
+        s, r = torch.from_numpy(x).cuda(), torch.zeros((n, count), dtype=torch.int32, device="cuda")
+        w.allreduce(s, r, count, 2, 2)
+        torch.cuda.synchronize()
+        assert np.array_equal(r.cpu().numpy(), ref)
+        assert set(w.read_trace()["variant"].tolist()) == {2}
+        # learned policy with a network whose output bias prefers TREE
+        p = np.zeros(64 * 12 + 64 + 64 * 64 + 64 + 4 * 64 + 4, np.float32)
+        p[-4:] = [1.0, -1.0, 0.5, 0.7]
+        w.set_mlp(p)
+        w.set_policy(-1, 2)
+        r.zero_()
+        w.allreduce(s, r, count, 2, 2, iters=3)
+        torch.cuda.synchronize()
+        assert np.array_equal(r.cpu().numpy(), ref)
+        assert set(w.read_trace()["variant"].tolist()) == {1}
