@@ -210,6 +210,69 @@ def bench_alltoallv(gpumpi, torch, w_kw):
             "p50_us": float(pct(list(ns), 0.5)) / 1e3, "p99_us": float(pct(list(ns), 0.99)) / 1e3}
 
 
+def bench_alltoallv_1024(gpumpi, torch, w_kw, uniform: bool):
+    """Alltoall(v) among 1024 ranks, 1 MiB sent per rank: int32 pieces of 256 elements (uniform), or
+    uneven counts uniform in [0, 512] elements per pair (seeded; displacements packed, so most pieces
+    start at a different 16-byte alignment in the sender and the receiver).  GB/s per piece order."""
+    import numpy as np
+    n = 1024
+    rng = np.random.default_rng(4242)
+    sc = np.full((n, n), 256, np.int32) if uniform else rng.integers(0, 513, (n, n)).astype(np.int32)
+    rc = sc.T.copy()
+    sd = (np.cumsum(sc, 1) - sc).astype(np.int32)
+    rd = (np.cumsum(rc, 1) - rc).astype(np.int32)
+    S, R = int(sc.sum(1).max()), int(rc.sum(1).max())
+    g = torch.Generator(device="cuda").manual_seed(99)
+    send = torch.randint(-2**31, 2**31 - 1, (n, S), generator=g, device="cuda", dtype=torch.int32)
+    recv = torch.zeros((n, R), dtype=torch.int32, device="cuda")
+    dsc, dsd, drc, drd = (torch.from_numpy(a).cuda() for a in (sc, sd, rc, rd))
+    total = int(sc.sum()) * 4
+    out = {"ranks": n, "bytes_moved_per_call": total, "counts": "uniform 256" if uniform else "uniform [0,512]"}
+    with gpumpi.World(n, **w_kw) as w:
+        for v, name in ((0, "direct"), (1, "tree"), (2, "ring"), (3, "staged")):
+            w.set_policy(v, 0)
+            w.alltoallv(send, S * 4, dsc, dsd, recv, R * 4, drc, drd, gpumpi.INT, iters=3)
+            iters = 20
+            ns = np.zeros(iters, dtype=np.uint64)
+            w.alltoallv(send, S * 4, dsc, dsd, recv, R * 4, drc, drd, gpumpi.INT, iters=iters, iter_ns=ns)
+            ms = w.last_kernel_ms() / iters
+            out[name] = {"gbs": 2.0 * total / (ms * 1e-3) / 1e9, "ms_per_call": ms,
+                         "p50_us": float(pct(list(ns), 0.5)) / 1e3}
+    # spot check: receiver 5's block from sender 7 equals sender 7's block for receiver 5
+    r5 = recv[5, int(rd[5, 7]):int(rd[5, 7]) + int(rc[5, 7])]
+    s7 = send[7, int(sd[7, 5]):int(sd[7, 5]) + int(sc[7, 5])]
+    assert torch.equal(r5, s7), "alltoallv placement"
+    return out
+
+
+def small_alltoallv_case(args, gpumpi, torch, local):
+    """Alltoallv int32 among 1024 ranks, 256 KiB sent per rank, counts uniform in [0, 128] per pair
+    (seeded; 256 MiB read + 256 MiB written per call): the profiled pull case."""
+    import numpy as np
+    n = 1024
+    rng = np.random.default_rng(4242)
+    sc = rng.integers(0, 129, (n, n)).astype(np.int32)
+    rc = sc.T.copy()
+    sd = (np.cumsum(sc, 1) - sc).astype(np.int32)
+    rd = (np.cumsum(rc, 1) - rc).astype(np.int32)
+    S, R = int(sc.sum(1).max()), int(rc.sum(1).max())
+    g = torch.Generator(device="cuda").manual_seed(99)
+    send = torch.randint(-2**31, 2**31 - 1, (n, S), generator=g, device="cuda", dtype=torch.int32)
+    recv = torch.zeros((n, R), dtype=torch.int32, device="cuda")
+    dsc, dsd, drc, drd = (torch.from_numpy(a).cuda() for a in (sc, sd, rc, rd))
+    total = int(sc.sum()) * 4
+    with gpumpi.World(n, device=local, timeout_s=120.0) as w:
+        if args.variant >= 0:
+            w.set_policy(args.variant, 0)
+        w.alltoallv(send, S * 4, dsc, dsd, recv, R * 4, drc, drd, gpumpi.INT, iters=max(1, args.warmup))
+        w.alltoallv(send, S * 4, dsc, dsd, recv, R * 4, drc, drd, gpumpi.INT, iters=max(1, args.steps))
+        ms = w.last_kernel_ms() / max(1, args.steps)
+        info = w.info()
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "alltoallv_small", "variant": args.variant, "ranks": n, "bytes_moved": total,
+                      "ms_per_step": ms, "gbs": 2.0 * total / (ms * 1e-3) / 1e9, "world": info}), flush=True)
+
+
 def small_case(args, gpumpi, torch, local):
     """Allreduce fp32 SUM, 1024 ranks x 256 KiB (512 MiB of traffic per call): the profiled case."""
     n, count = 1024, 65536
@@ -233,8 +296,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extra", action="store_true")
-    ap.add_argument("--case", default="full", choices=["full", "small"],
-                    help="small: 1024 ranks x 256 KiB, device timing only (the ncu capture case)")
+    ap.add_argument("--case", default="full", choices=["full", "small", "alltoallv_small"],
+                    help="small: Allreduce 1024 ranks x 256 KiB; alltoallv_small: Alltoallv 1024 ranks x "
+                         "256 KiB; device timing only (the ncu capture cases)")
+    ap.add_argument("--variant", type=int, default=-1, help="variant override for the small cases")
     args = ap.parse_args()
     dist, rank, ws = dist_setup()
     if args.impl == "reference":
@@ -249,6 +314,9 @@ def main():
     gpumpi.build()
     if args.case == "small":
         small_case(args, gpumpi, torch, local)
+        return
+    if args.case == "alltoallv_small":
+        small_alltoallv_case(args, gpumpi, torch, local)
         return
     n, per = WORKLOAD["ranks"], WORKLOAD["bytes_per_rank"]
     count = per // 4
@@ -302,10 +370,13 @@ def main():
 
     extra = {"p50_us": p50, "p99_us": p99, "world": world.info()}
     if not args.no_extra and rank == 0:
-        try:
-            extra["alltoallv_bucket_sort"] = bench_alltoallv(gpumpi, torch, w_kw)
-        except Exception as e:  # reported, not hidden
-            extra["alltoallv_bucket_sort"] = {"error": str(e)}
+        for key, fn in (("alltoallv_bucket_sort", lambda: bench_alltoallv(gpumpi, torch, w_kw)),
+                        ("alltoallv_1024ranks_1MiB", lambda: bench_alltoallv_1024(gpumpi, torch, w_kw, False)),
+                        ("alltoall_1024ranks_1MiB", lambda: bench_alltoallv_1024(gpumpi, torch, w_kw, True))):
+            try:
+                extra[key] = fn()
+            except Exception as e:  # reported, not hidden
+                extra[key] = {"error": str(e)}
         variants = {}
         for v in range(4):
             world.set_policy(v, 0)

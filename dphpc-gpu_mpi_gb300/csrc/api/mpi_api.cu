@@ -255,7 +255,6 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
     j->aligned16 = (mis & 15) == 0 ? 16 : (mis & 7) == 0 ? 8 : (mis & 3) == 0 ? 4 : 0;
     j->t_setup = now_ns();
     const int T = nthreads();
-    const int W = (T + 31) / 32;
     const int n = c->size;
     int nchunks = 0;
     long long bytes = 0;
@@ -315,9 +314,18 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
     } else if (a.kind == JOB_BARRIER) {
         nchunks = 0;
     } else {
-        long long P = (a.kind == JOB_ALLTOALLV || a.kind == JOB_ALLGATHERV) ? (long long)n * n : (long long)n;
+        const bool matrix = a.kind == JOB_ALLTOALLV || a.kind == JOB_ALLGATHERV;
+        long long P = matrix ? (long long)n * n : (long long)n;
         j->count = P;
-        j->variant = GPUMPI_VARIANT_DIRECT;
+        // piece order (DIRECT / TREE / RING, see piece_of) or bulk-copy staging (STAGED)
+        int variant = a.kind == JOB_ALLTOALLV
+                          ? select_variant(a.kind, a.est_piece * n, n, a.dt, -1, a.variant)
+                          : (matrix && a.variant >= 0 && a.variant < GPUMPI_NUM_VARIANTS ? a.variant
+                                                                                          : GPUMPI_VARIANT_DIRECT);
+        // STAGED needs shared memory for two bulk-copy stages of at least 512 bytes per warp
+        if (variant == GPUMPI_VARIANT_STAGED && (!matrix || staged_pull_stage_bytes(T) < 512))
+            variant = GPUMPI_VARIANT_DIRECT;
+        j->variant = variant;
         bytes = a.est_piece * P;
         may_post = may_post && bytes >= g_rt->engine_min_bytes;
         long long target = n + (may_post ? g_rt->nengines : 0);
@@ -327,9 +335,10 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             j->tile = 1;
             nchunks = (int)(P * parts);
         } else {
-            long long tile = P / (target > 0 ? target : 1);
+            // one piece per thread of the block prepares the chunk; about two chunks per worker block
+            long long tile = P / (2 * (target > 0 ? target : 1));
             if (tile < 1) tile = 1;
-            if (tile > 4 * W) tile = 4 * W;
+            if (tile > T) tile = T;
             j->vec = 1;
             j->tile = (int)tile;
             nchunks = (int)((P + tile - 1) / tile);
@@ -418,10 +427,12 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     const int dslot = dt == GPUMPI_FLOAT ? 2 : (dt == GPUMPI_DOUBLE || dt == GPUMPI_LONG_DOUBLE) ? 3
                       : (dt == GPUMPI_INT || dt == GPUMPI_INT32_T) ? 4 : 5;
     w->f[dslot] = 1.f;
-    const int oslot = op == GPUMPI_OP_SUM ? 6 : op == GPUMPI_OP_MAX ? 7 : op == GPUMPI_OP_MIN ? 8 : 9;
-    w->f[oslot] = 1.f;
+    if (op >= 0) {  // pulls (Alltoall(v)) have no operator: all four slots stay 0
+        const int oslot = op == GPUMPI_OP_SUM ? 6 : op == GPUMPI_OP_MAX ? 7 : op == GPUMPI_OP_MIN ? 8 : 9;
+        w->f[oslot] = 1.f;
+    }
     w->f[10] = (float)n / (float)(g_rt->nranks + g_rt->nengines);
-    w->f[11] = kind == JOB_REDUCE ? 1.f : 0.f;
+    w->f[11] = kind == JOB_REDUCE ? 1.f : kind == JOB_ALLTOALLV ? -1.f : 0.f;
     Task t;
     t.kind = TASK_USER;
     t.p0 = (const void*)&mlp_infer_task;
@@ -512,7 +523,9 @@ __device__ __noinline__ int pull_collective(int kind, MPI_Comm_impl* c, CollSlot
     a.esize = 0;
     a.ufn = nullptr;
     a.est_piece = est_piece;
-    a.variant = -1;
+    a.variant = g_rt->variant_override;
+    if (a.variant < 0 && kind == JOB_ALLTOALLV && g_rt->selector_mode == 2 && g_rt->mlp_params)
+        a.variant = learned_variant(kind, est_piece * c->size, c->size, my.stype, -1);
     int rc = coll_run(c, my, a, __LINE__);
     stage_out(ss, false);
     stage_out(rs, true);

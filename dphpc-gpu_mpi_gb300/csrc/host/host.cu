@@ -171,6 +171,11 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
         g_create_error = "nranks must be >= 1";
         return GPUMPI_ERR_ARG;
     }
+    if (cfg.threads_per_block > 0 && (cfg.threads_per_block % 32 != 0 || cfg.threads_per_block > 256)) {
+        // block tasks scan and copy with whole warps; the kernel is compiled for at most 256 threads
+        g_create_error = "threads_per_block must be a multiple of 32 in [32, 256]";
+        return GPUMPI_ERR_ARG;
+    }
     if (cfg.eager_bytes < 16) cfg.eager_bytes = 16;
     cfg.eager_bytes = (cfg.eager_bytes + 15) & ~15;
     int md = 1;
@@ -375,9 +380,11 @@ int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
 }
 
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes) {
-    if (!w || !table || bytes != 2 * 32 * 16) return GPUMPI_ERR_ARG;
+    // [kinds][32][16]: kinds 0 Allreduce, 1 Reduce, 2 Alltoall(v); a two-kind table leaves kind 2 unset
+    if (!w || !table || (bytes != 2 * 32 * 16 && bytes != 3 * 32 * 16)) return GPUMPI_ERR_ARG;
     cudaSetDevice(w->device);
-    if (!w->d_table) CK(cudaMalloc(&w->d_table, bytes));
+    if (!w->d_table) CK(cudaMalloc(&w->d_table, 3 * 32 * 16));
+    CK(cudaMemset(w->d_table, 0xff, 3 * 32 * 16));
     CK(cudaMemcpy(w->d_table, table, bytes, cudaMemcpyHostToDevice));
     return GPUMPI_SUCCESS;
 }

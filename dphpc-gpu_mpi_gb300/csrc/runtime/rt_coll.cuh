@@ -24,10 +24,25 @@
 
 namespace gpumpi {
 
-// shared-memory pointer tile used by the fold executors (one per block)
+// Per-block chunk scratch.  Folds use the pointer tile (member buffers of up to PTILE ranks) and the
+// generic path's accumulators; pulls use the piece table of rt_pull.cuh.  A block runs one chunk
+// at a time and every chunk starts with a block barrier before it writes here (load_ptile, pull_tile,
+// pull_part), so the two views never overlap in time.
 constexpr int PTILE = 256;
-__shared__ unsigned long long s_ptile[PTILE];
-__shared__ unsigned char s_acc[256 * 16];   // generic-path accumulators, one 16-byte element per thread
+union ChunkScratch {
+    struct {
+        unsigned long long ptile[PTILE];
+        unsigned char acc[256 * 16];     // generic-path accumulators, one 16-byte element per thread
+    } f;
+    struct {
+        long long d[PTILE];              // destination start of the piece
+        long long e[PTILE];              // destination end
+        long long delta[PTILE];          // source address - destination address
+        long long pref[PTILE / 32][33];  // per warp: exclusive prefix of full 16-byte units, then the total
+        unsigned char flag[PTILE];       // PF_* bits
+    } p;
+};
+__shared__ __align__(16) ChunkScratch s_chunk;
 
 __device__ __forceinline__ int comm_rank_of(const MPI_Comm_impl* c, int world) {
     return c->is_world ? world : c->rank_of[world];
@@ -70,16 +85,16 @@ __device__ __forceinline__ void board_post(Job* j, unsigned e) {
     st_release(&en->seq, (unsigned)(i + 1));
 }
 
-// Thread 0: claims and executes chunks of j until none is left, then waits for all to finish.
+// Thread 0: executes chunks of j until none is left (one block task claims them in a loop and finishes
+// each), then waits for all chunks to finish.
 __device__ __noinline__ int job_run_and_wait(Job* j, int line) {
-    long long idx;
-    while ((idx = job_claim(j)) >= 0) {
+    const long long idx = job_claim(j);
+    if (idx >= 0) {
         Task t;
         t.kind = TASK_CHUNK;
         t.p0 = j;
         t.n0 = idx;
         dispatch(t);
-        job_finish(j);
     }
     const unsigned long long target = ld_acquire64(&j->limit);  // (epoch << 32) | nchunks
     if (ld_acquire64(&j->done) == target) return 0;
@@ -151,14 +166,14 @@ __device__ __forceinline__ void* slot_out(const CollSlot* s) {
     return (void*)__ldcg((const unsigned long long*)&s->rbuf);
 }
 
-// loads pointer field `which` (0 = sbuf, 1 = rbuf) of members [r0, r0+m) into s_ptile
+// loads pointer field `which` (0 = sbuf, 1 = rbuf) of members [r0, r0+m) into s_chunk.f.ptile
 // With rot != 0 the tile holds members (r0 + i + rot) mod n: the RING variant's rotated fold order.
 __device__ __forceinline__ void load_ptile(const CollSlot* slots, int r0, int m, int which, int tid, int nt,
                                            int rot = 0, int n = 1) {
     bar_sync(BAR_TASK, nt);
     for (int i = tid; i < m; i += nt) {
         const int r = rot ? (r0 + i + rot) % n : r0 + i;
-        s_ptile[i] = __ldcg(which == 0 ? (const unsigned long long*)&slots[r].sbuf
+        s_chunk.f.ptile[i] = __ldcg(which == 0 ? (const unsigned long long*)&slots[r].sbuf
                                         : (const unsigned long long*)&slots[r].rbuf);
     }
     bar_sync(BAR_TASK, nt);
@@ -232,13 +247,13 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
         if (nv > 0) {
             int i = 0;
             if (r0 == 0) {
-                ld_elems<T, V>((const T*)s_ptile[0] + e, acc, nv, vec16);
+                ld_elems<T, V>((const T*)s_chunk.f.ptile[0] + e, acc, nv, vec16);
                 i = 1;
             }
             for (; i + U <= m; i += U) {
                 T v[U][V];
 #pragma unroll
-                for (int u = 0; u < U; u++) ld_elems<T, V>((const T*)s_ptile[i + u] + e, v[u], nv, vec16);
+                for (int u = 0; u < U; u++) ld_elems<T, V>((const T*)s_chunk.f.ptile[i + u] + e, v[u], nv, vec16);
 #pragma unroll
                 for (int u = 0; u < U; u++)
 #pragma unroll
@@ -246,7 +261,7 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
             }
             for (; i < m; i++) {
                 T v[V];
-                ld_elems<T, V>((const T*)s_ptile[i] + e, v, nv, vec16);
+                ld_elems<T, V>((const T*)s_chunk.f.ptile[i] + e, v, nv, vec16);
 #pragma unroll
                 for (int k = 0; k < V; k++) acc[k] = op_apply<OP, T>(v[k], acc[k]);
             }
@@ -263,7 +278,7 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
         const int m = min(PTILE, n - r0);
         load_ptile(slots, r0, m, 1, tid, nt);
         if (nv > 0)
-            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_ptile[i] + e, acc, nv, vec16);
+            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_chunk.f.ptile[i] + e, acc, nv, vec16);
     }
 }
 
@@ -282,7 +297,7 @@ __device__ __noinline__ void fold_generic(const JobParams* j, long long e0, int 
     const int es = j->esize;
     const long long e = e0 + tid;
     const bool act = e < j->count;
-    unsigned char* acc = s_acc + tid * 16;
+    unsigned char* acc = s_chunk.f.acc + tid * 16;
     MPI_Datatype dtv = (MPI_Datatype)j->dt;
     int one = 1;
     for (int r0 = 0; r0 < n; r0 += PTILE) {
@@ -290,7 +305,7 @@ __device__ __noinline__ void fold_generic(const JobParams* j, long long e0, int 
         load_ptile(slots, r0, m, 0, tid, nt);
         if (act) {
             for (int i = 0; i < m; i++) {
-                const unsigned char* src = (const unsigned char*)s_ptile[i] + e * es;
+                const unsigned char* src = (const unsigned char*)s_chunk.f.ptile[i] + e * es;
                 if (r0 == 0 && i == 0) {
                     for (int b = 0; b < es; b++) acc[b] = src[b];
                 } else if (j->ufn) {
@@ -313,7 +328,7 @@ __device__ __noinline__ void fold_generic(const JobParams* j, long long e0, int 
         load_ptile(slots, r0, m, 1, tid, nt);
         if (act)
             for (int i = 0; i < m; i++) {
-                unsigned char* out = (unsigned char*)s_ptile[i] + e * es;
+                unsigned char* out = (unsigned char*)s_chunk.f.ptile[i] + e * es;
                 for (int b = 0; b < es; b++) out[b] = acc[b];
             }
     }
@@ -454,7 +469,19 @@ __device__ __forceinline__ void piece_of(const JobParams* j, long long p, Piece&
     const int n = c->size;
     int r, s;
     switch (j->kind) {
-    case JOB_ALLTOALLV: case JOB_ALLGATHERV: r = (int)(p / n); s = (int)(p % n); break;
+    case JOB_ALLTOALLV: case JOB_ALLGATHERV:
+        // piece order of the variant: DIRECT receiver-major (each chunk fills one receiver's buffer),
+        // TREE sender-major (each chunk drains one sender's buffer), RING receiver-major with the
+        // senders rotated so receiver r starts at itself (no sender is read by every block at once)
+        if (j->variant == GPUMPI_VARIANT_TREE) {
+            s = (int)(p / n);
+            r = (int)(p % n);
+        } else {
+            r = (int)(p / n);
+            s = (int)(p % n);
+            if (j->variant == GPUMPI_VARIANT_RING) s = (s + r) % n;
+        }
+        break;
     case JOB_GATHERV: r = j->root; s = (int)p; break;
     default: r = (int)p; s = j->root; break;  // SCATTERV, BCAST
     }
@@ -527,29 +554,11 @@ __device__ __forceinline__ void piece_copy(const Piece& pc, long long b0, long l
     else typed_copy(pc.dst, pc.rdesc, pc.src, pc.sdesc, b0, b1, lane, nl);
 }
 
-__device__ __noinline__ void pull_chunk(const JobParams* j, Job* jg, long long idx, int tid, int nt) {
-    const long long npieces = j->count;
-    if (j->vec > 1) {  // byte range `part` of one piece, whole block
-        const long long p = idx / j->vec;
-        const int part = (int)(idx % j->vec);
-        Piece pc;
-        piece_of(j, p, pc);
-        long long per = ((pc.bytes + j->vec - 1) / j->vec + 15) & ~15LL;
-        long long b0 = per * part, b1 = min(pc.bytes, b0 + per);
-        piece_copy(pc, b0, b1, tid, nt);
-        if (tid == 0 && part == 0 && pc.trunc) atomicOr(&jg->err, 1u);
-        return;
-    }
-    const int lane = tid & 31, warp = tid >> 5, nwarps = (nt + 31) >> 5;
-    const long long p0 = idx * j->tile;
-    const long long p1 = min(npieces, p0 + j->tile);
-    for (long long p = p0 + warp; p < p1; p += nwarps) {
-        Piece pc;
-        piece_of(j, p, pc);
-        piece_copy(pc, 0, pc.bytes, lane, 32);
-        if (lane == 0 && pc.trunc) atomicOr(&jg->err, 1u);
-    }
-}
+}  // namespace gpumpi
+
+#include "rt_pull.cuh"
+
+namespace gpumpi {
 
 __device__ __noinline__ void copy_chunk(const JobParams* j, long long idx, int tid, int nt) {
     long long off = idx * j->chunk;
@@ -557,14 +566,51 @@ __device__ __noinline__ void copy_chunk(const JobParams* j, long long idx, int t
     copy_bytes((char*)j->dst + off, (const char*)j->src + off, len, tid, nt);
 }
 
+// The block's copy of the executing job's parameters: one thread reads them per chunk; every executor
+// then reads shared memory instead of a per-thread stack copy (which would live in local memory and,
+// with most of the SM's L1 given to shared memory, cost L2 traffic on every access).  Thread 0 starts a
+// chunk only after every helper finished the previous task, so no reader of the old values remains.
+__shared__ JobParams s_jp;
+
+__shared__ long long s_next_chunk;
+
+// Runs chunk idx of job jg, then keeps claiming and running chunks of the same job epoch until none is
+// left; thread 0 marks each chunk finished once every thread of the block is done with it (the barrier
+// orders the block's writes before thread 0's release).  One task per job and block keeps the call chain
+// (and its saved registers) out of the per-chunk path.
+template <class F>
+__device__ __forceinline__ void chunk_loop(Job* jg, long long idx, int tid, int nt, F&& body) {
+    for (;;) {
+        body(idx);
+        bar_sync(BAR_TASK, nt);
+        if (tid == 0) {
+            job_finish(jg);
+            s_next_chunk = job_claim(jg);
+        }
+        bar_sync(BAR_TASK, nt);
+        idx = s_next_chunk;
+        if (idx < 0) return;
+    }
+}
+
+__device__ __noinline__ void pull_run(const JobParams* j, Job* jg, long long idx, int tid, int nt) {
+    chunk_loop(jg, idx, tid, nt, [&](long long i) { pull_chunk(j, jg, i, tid, nt); });
+}
+__device__ __noinline__ void fold_run(const JobParams* j, Job* jg, long long idx, int tid, int nt) {
+    chunk_loop(jg, idx, tid, nt, [&](long long i) { fold_chunk(j, i, tid, nt); });
+}
+__device__ __noinline__ void copy_run(const JobParams* j, Job* jg, long long idx, int tid, int nt) {
+    chunk_loop(jg, idx, tid, nt, [&](long long i) { copy_chunk(j, i, tid, nt); });
+}
+
 __device__ __noinline__ void exec_chunk(Job* jg, long long idx, int tid, int nt) {
-    JobParams P;
-    load_params(jg, P);
-    const JobParams* j = &P;
+    if (tid == 0) load_params(jg, s_jp);
+    bar_sync(BAR_TASK, nt);
+    const JobParams* j = &s_jp;
     switch (j->kind) {
-    case JOB_COPY: copy_chunk(j, idx, tid, nt); break;
-    case JOB_ALLREDUCE: case JOB_REDUCE: fold_chunk(j, idx, tid, nt); break;
-    default: pull_chunk(j, jg, idx, tid, nt); break;
+    case JOB_COPY: copy_run(j, jg, idx, tid, nt); break;
+    case JOB_ALLREDUCE: case JOB_REDUCE: fold_run(j, jg, idx, tid, nt); break;
+    default: pull_run(j, jg, idx, tid, nt); break;
     }
 }
 
@@ -587,14 +633,13 @@ __device__ void engine_loop() {
             if (diff < 0) break;             // not written yet
             if (diff == 0) {
                 Job* j = (Job*)__ldcg((const unsigned long long*)&en->job);
-                long long idx;
-                while ((idx = job_claim(j)) >= 0) {
+                const long long idx = job_claim(j);
+                if (idx >= 0) {  // the task claims the job's remaining chunks itself
                     Task t;
                     t.kind = TASK_CHUNK;
                     t.p0 = j;
                     t.n0 = idx;
                     dispatch(t);
-                    job_finish(j);
                     worked = true;
                 }
             }

@@ -13,13 +13,13 @@ __device__ __forceinline__ int clamp_i(int v, int lo, int hi) { return v < lo ? 
 __device__ __forceinline__ int ilog2_ll(long long v) { return v <= 1 ? 0 : 63 - __clzll(v); }
 
 // tuned table layout: [kind 0..1][log2 bytes-per-rank 0..31][log2 ranks 0..15] -> variant
-constexpr int SEL_KINDS = 2, SEL_BYTES = 32, SEL_RANKS = 16;
+constexpr int SEL_KINDS = 3, SEL_BYTES = 32, SEL_RANKS = 16;
 
 __device__ int mlp_select(int kind, long long bytes, int n, int dt, int op);
 
 __device__ int select_variant(int kind, long long bytes_per_rank, int n, int dt, int op, int override_v) {
     if (override_v >= 0 && override_v < GPUMPI_NUM_VARIANTS) return override_v;
-    const int k = kind == JOB_ALLREDUCE ? 0 : kind == JOB_REDUCE ? 1 : -1;
+    const int k = kind == JOB_ALLREDUCE ? 0 : kind == JOB_REDUCE ? 1 : kind == JOB_ALLTOALLV ? 2 : -1;
     if (k < 0) return GPUMPI_VARIANT_DIRECT;
     if (g_rt->selector_mode == 1 && g_rt->tuned_table) {
         int b = clamp_i(ilog2_ll(bytes_per_rank), 0, SEL_BYTES - 1);

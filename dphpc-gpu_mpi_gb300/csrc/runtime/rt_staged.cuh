@@ -25,7 +25,7 @@ template <class T>
 __device__ __forceinline__ void stage_issue(unsigned long long* bar, T* sdst, long long E, int k0, int mm, long long e0,
                                             unsigned CB) {
     for (int k = 0; k < mm; k++) {
-        const T* src = (const T*)s_ptile[k0 + k] + e0;
+        const T* src = (const T*)s_chunk.f.ptile[k0 + k] + e0;
         const unsigned long long s_off = (unsigned long long)((const unsigned char*)(sdst + (long long)k * E) - g_dyn_smem);
         const bool ok = (((unsigned long long)(size_t)src | s_off) & 15ull) == 0 && CB > 0 && (CB & 15u) == 0 &&
                         s_off + CB <= (unsigned long long)g_rt->dyn_smem && is_global_ptr(src);
@@ -37,7 +37,7 @@ __device__ __forceinline__ void stage_issue(unsigned long long* bar, T* sdst, lo
         }
     }
     mbar_expect_tx(bar, (unsigned)mm * CB);
-    for (int k = 0; k < mm; k++) tma_load_1d(sdst + (long long)k * E, (const T*)s_ptile[k0 + k] + e0, CB, bar);
+    for (int k = 0; k < mm; k++) tma_load_1d(sdst + (long long)k * E, (const T*)s_chunk.f.ptile[k0 + k] + e0, CB, bar);
 }
 
 template <class T, int OP, int V>
@@ -133,7 +133,7 @@ __device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int 
         const int m = min(PTILE, n - r0);
         load_ptile(slots, r0, m, 1, tid, nt);
         if (nv > 0)
-            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_ptile[i] + e, acc, nv, true);
+            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_chunk.f.ptile[i] + e, acc, nv, true);
     }
 }
 

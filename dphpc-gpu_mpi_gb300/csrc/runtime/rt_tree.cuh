@@ -28,13 +28,13 @@ __device__ __forceinline__ void tree_fold_range(const CollSlot* slots, int g0, i
         if (nv == 0) continue;
         int i = 0;
         if (r0 == g0) {
-            ld_elems<T, V>((const T*)s_ptile[0] + e, acc, nv, vec);
+            ld_elems<T, V>((const T*)s_chunk.f.ptile[0] + e, acc, nv, vec);
             i = 1;
         }
         for (; i + U <= m; i += U) {
             T v[U][V];
 #pragma unroll
-            for (int u = 0; u < U; u++) ld_elems<T, V>((const T*)s_ptile[i + u] + e, v[u], nv, vec);
+            for (int u = 0; u < U; u++) ld_elems<T, V>((const T*)s_chunk.f.ptile[i + u] + e, v[u], nv, vec);
 #pragma unroll
             for (int u = 0; u < U; u++)
 #pragma unroll
@@ -42,7 +42,7 @@ __device__ __forceinline__ void tree_fold_range(const CollSlot* slots, int g0, i
         }
         for (; i < m; i++) {
             T v[V];
-            ld_elems<T, V>((const T*)s_ptile[i] + e, v, nv, vec);
+            ld_elems<T, V>((const T*)s_chunk.f.ptile[i] + e, v, nv, vec);
 #pragma unroll
             for (int q = 0; q < V; q++) acc[q] = op_apply<OP, T>(v[q], acc[q]);
         }
@@ -116,7 +116,7 @@ __device__ __noinline__ void fold_tree(const JobParams* j, long long idx, int ti
         const int m = min(PTILE, n - r0);
         load_ptile(slots, r0, m, 1, tid, nt);
         if (nv > 0)
-            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_ptile[i] + e, acc, nv, vec);
+            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_chunk.f.ptile[i] + e, acc, nv, vec);
     }
 }
 

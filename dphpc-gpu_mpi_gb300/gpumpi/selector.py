@@ -32,7 +32,7 @@ if __package__ in (None, ""):
 import gpumpi  # noqa: E402
 
 NVAR = 4
-KIND_ALLREDUCE, KIND_REDUCE = 2, 3          # JOB_ALLREDUCE / JOB_REDUCE codes of the runtime
+KIND_ALLREDUCE, KIND_REDUCE, KIND_ALLTOALLV = 2, 3, 5   # JOB_* codes of the runtime
 DT_SLOT = {gpumpi.FLOAT: 2, gpumpi.DOUBLE: 3, gpumpi.INT: 4, gpumpi.INT64_T: 5}
 OP_SLOT = {gpumpi.OP_SUM: 6, gpumpi.OP_MAX: 7, gpumpi.OP_MIN: 8, gpumpi.OP_PROD: 9}
 DT_SIZE = {gpumpi.FLOAT: 4, gpumpi.DOUBLE: 8, gpumpi.INT: 4, gpumpi.INT64_T: 8}
@@ -45,9 +45,10 @@ def features(kind: int, bytes_per_rank: float, n: int, dt: int, op: int, rank_sh
     f[0] = (math.log2(max(bytes_per_rank, 1.0)) - 16.0) / 8.0
     f[1] = (math.log2(n) - 8.0) / 3.0
     f[DT_SLOT.get(dt, 5)] = 1.0
-    f[OP_SLOT.get(op, 9)] = 1.0
+    if op >= 0:                              # Alltoall(v) has no operator: op = -1, slots stay 0
+        f[OP_SLOT.get(op, 9)] = 1.0
     f[10] = rank_share
-    f[11] = 1.0 if kind == KIND_REDUCE else 0.0
+    f[11] = 1.0 if kind == KIND_REDUCE else -1.0 if kind == KIND_ALLTOALLV else 0.0
     return f
 
 

@@ -147,7 +147,8 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
 #define GPUMPI_TUNE_COPY_CHUNK 4
 #define GPUMPI_TUNE_ENGINE_MIN_BYTES 5
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
-/* Tuned table: int8 [2][32][16] (kind, log2 bytes per rank, log2 ranks) -> variant, host memory. */
+/* Tuned table: int8 [3][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; log2 bytes per
+ * rank; log2 ranks) -> variant or -1, host memory; a [2][32][16] table leaves Alltoall(v) untuned. */
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes);
 /* Learned selector weights: float[GPUMPI_MLP_NPARAMS] in the layout of the training kernels. */
 int gpumpi_set_mlp(gpumpi_world* w, const float* params, size_t count);

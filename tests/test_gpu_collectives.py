@@ -165,6 +165,36 @@ def test_alltoallv_uneven_and_zero_counts(gpulib, oracle, n, maxc, zero_frac):
     assert np.array_equal(got, ref)
 
 
+def uneven_exchange(rng, n, maxc, zero_frac, min_c=1):
+    sc = rng.integers(min_c, maxc + 1, (n, n)).astype(np.int32)
+    sc[rng.random((n, n)) < zero_frac] = 0
+    rc = sc.T.copy()
+    sd = np.concatenate([np.zeros((n, 1), np.int32), np.cumsum(sc, 1)[:, :-1]], 1).astype(np.int32)
+    rd = np.concatenate([np.zeros((n, 1), np.int32), np.cumsum(rc, 1)[:, :-1]], 1).astype(np.int32)
+    return sc, sd, rc, rd, int(sc.sum(1).max()) + 1, int(rc.sum(1).max()) + 1
+
+
+@pytest.mark.parametrize("n,maxc,dt,npdt", [(64, 3000, 0, np.int8),       # CHAR: every byte shift 0..15
+                                            (48, 700, 2, np.int32),       # int32: shifts 0/4/8/12
+                                            (96, 13, 13, np.float64),     # tiny pieces, edges only
+                                            (8, 40000, 2, np.int32)])     # >= 64 KiB pieces: split parts
+def test_alltoallv_piece_orders_and_shifts(gpulib, oracle, n, maxc, dt, npdt):
+    """Every pull variant (receiver-major, sender-major and rotated piece orders; bulk-copy staging) on
+    displacements that put source and destination at every relative alignment."""
+    rng = np.random.default_rng(maxc + n)
+    sc, sd, rc, rd, S, R = uneven_exchange(rng, n, maxc, 0.1, min_c=0)
+    x = oracle.fill_i32(n + 1, n * S).astype(npdt).reshape(n, S)
+    ref = oracle.alltoallv(x, sc, sd, R, rc, rd)
+    with gpulib.World(n, timeout_s=20.0, trace_capacity=64) as w:
+        for v in range(4):
+            w.set_policy(v, 0)
+            s, r = dev(x), dev(np.zeros((n, R), npdt))
+            w.alltoallv(s, S * x.itemsize, dev(sc), dev(sd), r, R * x.itemsize, dev(rc), dev(rd), dt)
+            got = host(r)
+            assert np.array_equal(got.view(np.uint8), ref.view(np.uint8)), v
+            assert set(w.read_trace()["variant"].tolist()) == {v}   # the trace covers the last launch
+
+
 @pytest.mark.parametrize("n,c", [(7, 7), (100, 64), (512, 3)])
 def test_allgather(gpulib, oracle, n, c):
     x = oracle.fill_i32(5, n * c).reshape(n, c)
