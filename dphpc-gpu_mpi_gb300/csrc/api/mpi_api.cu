@@ -591,6 +591,11 @@ __device__ int gpumpi_block_parallel(void (*fn)(void*, int, int), void* arg) {
     dispatch(t);
     return MPI_SUCCESS;
 }
+__device__ void gpumpi_block_sync(int nthreads) { bar_sync(BAR_TASK, nthreads); }
+__device__ void* gpumpi_block_scratch(size_t* bytes) {
+    if (bytes) *bytes = (size_t)g_rt->dyn_smem;
+    return g_rt->dyn_smem > 0 ? (void*)g_dyn_smem : nullptr;
+}
 
 // ------------------------------------------------------------------------------------------------
 // point-to-point

@@ -1,7 +1,381 @@
-// prog_apps.cu — application programs built on the MPI surface (filled in below).
+// prog_apps.cu — application programs on the MPI surface: the distributed bucket sort of integer keys
+// and the 3D halo exchange with derived-datatype faces.
+//
+// Scalar per-rank logic runs on each rank block's thread 0, like converted MPI code; the data-parallel
+// loops between MPI calls use the block's threads through gpumpi_block_parallel.
 #include "rt_kernel.cuh"
 
-extern const gpumpi_prog_entry g_app_programs[] = {
-    {-1, "none", nullptr, nullptr, nullptr},
+namespace {
+
+__device__ __forceinline__ unsigned long long gtime() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+constexpr unsigned long long LCG_A = 6364136223846793005ULL, LCG_C = 1442695040888963407ULL;
+
+// LCG state after k steps from s (affine map (A, C) raised to the k-th power by repeated squaring)
+__device__ unsigned long long lcg_jump(unsigned long long s, unsigned long long k) {
+    unsigned long long A = 1, C = 0, ak = LCG_A, ck = LCG_C;
+    while (k) {
+        if (k & 1) {
+            A = ak * A;
+            C = ak * C + ck;
+        }
+        ck = ak * ck + ck;
+        ak = ak * ak;
+        k >>= 1;
+    }
+    return A * s + C;
+}
+
+__device__ __forceinline__ double lcg_u01(unsigned long long& s) {
+    s = s * LCG_A + LCG_C;
+    return (double)(s >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__shared__ int s_scan[257];
+
+// Exclusive prefix of the nt per-thread sums in s_scan; s_scan[nt] = total.
+__device__ void scan_thread_sums(int tid, int nt) {
+    gpumpi_block_sync(nt);
+    if (tid == 0) {
+        int run = 0;
+        for (int t = 0; t < nt; t++) {
+            const int v = s_scan[t];
+            s_scan[t] = run;
+            run += v;
+        }
+        s_scan[nt] = run;
+    }
+    gpumpi_block_sync(nt);
+}
+
+// exclusive prefix sum of a[0..m) in place (a may be shared or global); returns the total to every thread
+__device__ int block_exclusive_scan(int* a, int m, int tid, int nt) {
+    const int seg = (m + nt - 1) / nt;
+    const int lo = min(m, tid * seg), hi = min(m, lo + seg);
+    int s = 0;
+    for (int i = lo; i < hi; i++) s += a[i];
+    s_scan[tid] = s;
+    scan_thread_sums(tid, nt);
+    int acc = s_scan[tid];
+    for (int i = lo; i < hi; i++) {
+        const int v = a[i];
+        a[i] = acc;
+        acc += v;
+    }
+    const int total = s_scan[nt];
+    gpumpi_block_sync(nt);
+    return total;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Distributed bucket sort (the call pattern of an integer sort benchmark: bucket counts by
+// MPI_Alltoall, keys by MPI_Alltoallv, then a local counting sort).  Keys: key = floor(2^21 * mean of
+// four U(0,1) draws) from the 64-bit LCG seeded seed + rank; bucket of key k on n ranks: (k * n) >> 21,
+// so rank r receives exactly the keys in [ceil(r 2^21 / n), ceil((r + 1) 2^21 / n)).
+//   i[0] seed  i[1] keys per rank  i[2] iterations  i[3] receive capacity per rank (keys)
+//   i[4] 1: generate the keys on the device  i[5] per-rank stride of the global histogram scratch
+//   p[0] keys [n][kpr]  p[1] send buffer [n][kpr]  p[2] receive buffer [n][cap]  p[3] sorted [n][cap]
+//   p[4] int64 received count [n]  p[5] int32 scratch [n][4n]  p[6] int32 histogram scratch [n][i[5]]
+//   p[7] int rc [n]  p[8] int64 per-iteration ns (rank 0)
+// ------------------------------------------------------------------------------------------------
+constexpr int KEY_BITS = 21;
+
+struct SortWork {
+    unsigned long long seed;
+    long long kpr;
+    int rank, n;
+    int* keys;
+    int* send;
+    int* recv;
+    int* out;
+    int* sc;  // send counts [n], then send displacements, receive counts, receive displacements
+    int* hist_global;
+    long long nrecv;
+    int lo, range;
+    int err;
 };
-extern const int g_num_app_programs = 0;
+__shared__ SortWork s_sort;
+
+__device__ void sort_gen_task(void* arg, int tid, int nt) {
+    SortWork* w = (SortWork*)arg;
+    const long long per = (w->kpr + nt - 1) / nt;
+    const long long lo = min(w->kpr, per * tid), hi = min(w->kpr, lo + per);
+    unsigned long long s = lcg_jump(w->seed + (unsigned long long)w->rank, 4ULL * (unsigned long long)lo);
+    for (long long i = lo; i < hi; i++) {
+        const double a = lcg_u01(s), b = lcg_u01(s), c = lcg_u01(s), d = lcg_u01(s);
+        const double sum = __dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d);
+        w->keys[i] = (int)floor(__dmul_rn(sum, 524288.0));  // 2^21 * sum / 4
+    }
+}
+
+// bucket counts, send displacements and the packed send buffer (keys grouped by destination rank)
+__device__ void sort_pack_task(void* arg, int tid, int nt) {
+    SortWork* w = (SortWork*)arg;
+    const int n = w->n;
+    size_t sbytes = 0;
+    int* bins = (int*)gpumpi_block_scratch(&sbytes);
+    const bool in_smem = bins && sbytes >= (size_t)n * sizeof(int);
+    if (!in_smem) bins = w->sc;
+    for (int d = tid; d < n; d += nt) bins[d] = 0;
+    gpumpi_block_sync(nt);
+    for (long long i = tid; i < w->kpr; i += nt) atomicAdd(&bins[((long long)w->keys[i] * n) >> KEY_BITS], 1);
+    gpumpi_block_sync(nt);
+    int* sd = w->sc + n;
+    for (int d = tid; d < n; d += nt) {
+        const int c = bins[d];
+        w->sc[d] = c;
+        sd[d] = c;
+    }
+    gpumpi_block_sync(nt);
+    block_exclusive_scan(sd, n, tid, nt);
+    // cursors start at the displacements; the order inside a bucket does not matter (sorted later)
+    int* cur = in_smem ? bins : w->sc + 3 * n;  // spare n ints of the scratch row when not in shared memory
+    for (int d = tid; d < n; d += nt) cur[d] = sd[d];
+    gpumpi_block_sync(nt);
+    for (long long i = tid; i < w->kpr; i += nt) {
+        const int k = w->keys[i];
+        const int pos = atomicAdd(&cur[((long long)k * n) >> KEY_BITS], 1);
+        w->send[pos] = k;
+    }
+}
+
+__device__ void sort_rdispl_task(void* arg, int tid, int nt) {
+    SortWork* w = (SortWork*)arg;
+    const int n = w->n;
+    const int* rc = w->sc + 2 * n;
+    int* rd = w->sc + 3 * n;
+    for (int d = tid; d < n; d += nt) rd[d] = rc[d];
+    gpumpi_block_sync(nt);
+    const int total = block_exclusive_scan(rd, n, tid, nt);
+    if (tid == 0) w->nrecv = total;
+}
+
+// counting sort of the received keys (all in [lo, lo + range))
+__device__ void sort_local_task(void* arg, int tid, int nt) {
+    SortWork* w = (SortWork*)arg;
+    size_t sbytes = 0;
+    int* hist = (int*)gpumpi_block_scratch(&sbytes);
+    if (!hist || sbytes < (size_t)w->range * sizeof(int)) hist = w->hist_global;
+    for (int k = tid; k < w->range; k += nt) hist[k] = 0;
+    gpumpi_block_sync(nt);
+    for (long long i = tid; i < w->nrecv; i += nt) {
+        const int k = w->recv[i] - w->lo;
+        if (k >= 0 && k < w->range) atomicAdd(&hist[k], 1);
+        else w->err = 1;
+    }
+    gpumpi_block_sync(nt);
+    // positions: exclusive prefix of the histogram by segments, then each thread writes its values' runs
+    const int seg = (w->range + nt - 1) / nt;
+    const int a = min(w->range, tid * seg), b = min(w->range, a + seg);
+    int s = 0;
+    for (int k = a; k < b; k++) s += hist[k];
+    s_scan[tid] = s;
+    scan_thread_sums(tid, nt);
+    int pos = s_scan[tid];
+    for (int k = a; k < b; k++) {
+        const int c = hist[k];
+        for (int q = 0; q < c; q++) w->out[pos + q] = w->lo + k;
+        pos += c;
+    }
+}
+
+struct BucketSort {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = -1, n = 0;
+        MPI_Comm_rank(MPI_COMM_WORLD, &rank);
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        const long long kpr = p.i[1], cap = p.i[3];
+        const int iters = (int)p.i[2];
+        SortWork* w = &s_sort;
+        w->seed = (unsigned long long)p.i[0];
+        w->kpr = kpr;
+        w->rank = rank;
+        w->n = n;
+        w->keys = (int*)p.p[0] + (long long)rank * kpr;
+        w->send = (int*)p.p[1] + (long long)rank * kpr;
+        w->recv = (int*)p.p[2] + (long long)rank * cap;
+        w->out = (int*)p.p[3] + (long long)rank * cap;
+        w->sc = (int*)p.p[5] + (long long)rank * 4 * n;
+        w->hist_global = (int*)p.p[6] + (long long)rank * p.i[5];
+        const long long max_key = 1LL << KEY_BITS;
+        w->lo = (int)((max_key * rank + n - 1) / n);
+        w->range = (int)((max_key * (rank + 1) + n - 1) / n) - w->lo;
+        w->err = 0;
+        w->nrecv = 0;
+        long long* iter_ns = (long long*)p.p[8];
+        int rc = (w->range > p.i[5]) ? MPI_ERR_COUNT : MPI_SUCCESS;
+        if (p.i[4]) gpumpi_block_parallel(&sort_gen_task, w);
+        int brc = MPI_Barrier(MPI_COMM_WORLD);
+        if (!rc) rc = brc;
+        int* sc = w->sc;
+        for (int it = 0; it < iters && rc == 0; it++) {
+            const unsigned long long t0 = gtime();
+            gpumpi_block_parallel(&sort_pack_task, w);
+            rc = MPI_Alltoall(sc, 1, MPI_INT, sc + 2 * n, 1, MPI_INT, MPI_COMM_WORLD);
+            if (rc) break;
+            gpumpi_block_parallel(&sort_rdispl_task, w);
+            int overflow = 0;
+            if (w->nrecv > cap) {
+                // the receive buffer cannot hold this rank's bucket: receive nothing (the senders' pieces
+                // are reported truncated) and fail after the collective every rank takes part in
+                for (int d = 0; d < n; d++) sc[2 * n + d] = 0;
+                w->nrecv = 0;
+                overflow = 1;
+            }
+            rc = MPI_Alltoallv(w->send, sc, sc + n, MPI_INT, w->recv, sc + 2 * n, sc + 3 * n, MPI_INT,
+                               MPI_COMM_WORLD);
+            if (overflow) rc = MPI_ERR_COUNT;
+            if (rc) break;
+            gpumpi_block_parallel(&sort_local_task, w);
+            if (w->err) rc = MPI_ERR_OTHER;
+            if (rank == 0 && iter_ns) iter_ns[it] = (long long)(gtime() - t0);
+        }
+        ((long long*)p.p[4])[rank] = w->nrecv;
+        if (p.p[7]) ((int*)p.p[7])[rank] = rc;
+        return rc ? rc : MPI_Finalize();
+    }
+};
+
+// ------------------------------------------------------------------------------------------------
+// 3D halo exchange: global grid G^3, G = P * L, periodic, on P^3 ranks (rank = (pz * P + py) * P + px);
+// each rank holds an (L + 2)^3 block of doubles whose interior is its L^3 sub-grid and whose one-cell
+// faces are filled from the six neighbours every iteration (edges and corners are not exchanged).  The
+// faces are derived datatypes: z faces MPI_Type_vector(L, L, W), y faces MPI_Type_vector(L, L, W * W),
+// x faces an hvector over z of the columns MPI_Type_vector(L, 1, W) (mode 0), or all twelve face
+// positions as MPI_Type_create_subarray of the block (mode 1).  Isend/Irecv + Waitall, 12 requests.
+//   i[0] P  i[1] L  i[2] iterations  i[3] face type mode  p[0] blocks [P^3][(L + 2)^3]
+//   p[6] int64 per-iteration ns (rank 0)  p[7] int rc [n]
+// Cell value: (gz * 1000003 + gy * 1009 + gx) * 0.125 (exact in double); halos start at -1.
+// ------------------------------------------------------------------------------------------------
+struct HaloWork {
+    double* blk;
+    int L, P, px, py, pz;
+};
+__shared__ HaloWork s_halo;
+
+__device__ void halo_fill_task(void* arg, int tid, int nt) {
+    HaloWork* w = (HaloWork*)arg;
+    const long long W = w->L + 2;
+    const long long cells = W * W * W;
+    for (long long c = tid; c < cells; c += nt) {
+        const long long z = c / (W * W), y = (c / W) % W, x = c % W;
+        const bool halo = z == 0 || z == W - 1 || y == 0 || y == W - 1 || x == 0 || x == W - 1;
+        double v = -1.0;
+        if (!halo) {  // interior cell: global coordinates are inside [0, G)
+            const long long gz = (long long)w->pz * w->L + z - 1, gy = (long long)w->py * w->L + y - 1,
+                            gx = (long long)w->px * w->L + x - 1;
+            v = (double)(gz * 1000003 + gy * 1009 + gx) * 0.125;
+        }
+        w->blk[c] = v;
+    }
+}
+
+struct Halo {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = -1, n = 0;
+        MPI_Comm_rank(MPI_COMM_WORLD, &rank);
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        const int P = (int)p.i[0], L = (int)p.i[1], iters = (int)p.i[2], mode = (int)p.i[3];
+        const int W = L + 2;
+        if (P * P * P != n || L < 1) {
+            if (p.p[7]) ((int*)p.p[7])[rank] = MPI_ERR_ARG;
+            return MPI_ERR_ARG;
+        }
+        HaloWork* w = &s_halo;
+        w->L = L;
+        w->P = P;
+        w->px = rank % P;
+        w->py = (rank / P) % P;
+        w->pz = rank / (P * P);
+        w->blk = (double*)p.p[0] + (long long)rank * W * W * W;
+        gpumpi_block_parallel(&halo_fill_task, w);
+
+        // mode 0: face[d] is one face normal to dimension d (0 = x, 1 = y, 2 = z), placed by its address;
+        // mode 1: sub[d][k] is the face at position k (send low, send high, recv low, recv high) of the block
+        MPI_Datatype face[3] = {MPI_DATATYPE_NULL, MPI_DATATYPE_NULL, MPI_DATATYPE_NULL};
+        MPI_Datatype sub[3][4];
+        int rc = MPI_SUCCESS;
+        if (mode == 0) {
+            MPI_Datatype col;
+            rc |= MPI_Type_vector(L, 1, W, MPI_DOUBLE, &col);
+            rc |= MPI_Type_create_hvector(L, 1, (MPI_Aint)W * W * (MPI_Aint)sizeof(double), col, &face[0]);
+            rc |= MPI_Type_vector(L, L, W * W, MPI_DOUBLE, &face[1]);
+            rc |= MPI_Type_vector(L, L, W, MPI_DOUBLE, &face[2]);
+            for (int d = 0; d < 3; d++) rc |= MPI_Type_commit(&face[d]);
+            rc |= MPI_Type_free(&col);
+        } else {
+            const int sizes[3] = {W, W, W};  // C order: z, y, x
+            for (int d = 0; d < 3; d++) {
+                const int axis = 2 - d;  // array axis of dimension d
+                int sub_sizes[3] = {L, L, L};
+                sub_sizes[axis] = 1;
+                const int pos[4] = {1, L, 0, L + 1};
+                for (int k = 0; k < 4; k++) {
+                    int starts[3] = {1, 1, 1};
+                    starts[axis] = pos[k];
+                    rc |= MPI_Type_create_subarray(3, sizes, sub_sizes, starts, MPI_ORDER_C, MPI_DOUBLE, &sub[d][k]);
+                    rc |= MPI_Type_commit(&sub[d][k]);
+                }
+            }
+        }
+        const int brc = MPI_Barrier(MPI_COMM_WORLD);
+        if (!rc) rc = brc;
+        const int pc[3] = {w->px, w->py, w->pz};
+        long long* iter_ns = (long long*)p.p[6];
+        for (int it = 0; it < iters && rc == 0; it++) {
+            const unsigned long long t0 = gtime();
+            MPI_Request rq[12];
+            int nr = 0;
+            for (int d = 0; d < 3 && !rc; d++) {
+                const long long stride = d == 0 ? 1 : d == 1 ? W : (long long)W * W;
+                int up[3] = {pc[0], pc[1], pc[2]}, dn[3] = {pc[0], pc[1], pc[2]};
+                up[d] = (pc[d] + 1) % P;
+                dn[d] = (pc[d] + P - 1) % P;
+                const int rup = (up[2] * P + up[1]) * P + up[0], rdn = (dn[2] * P + dn[1]) * P + dn[0];
+                double* b = w->blk;
+                // tag 2d: a high face travelling up; tag 2d+1: a low face travelling down
+                if (mode == 0) {
+                    // address of the face at coordinate 0 of dimension d; coordinate c adds c * stride
+                    const long long base = d == 0 ? (long long)W * W + W : d == 1 ? (long long)W * W + 1 : W + 1;
+                    rc |= MPI_Irecv(b + base, 1, face[d], rdn, 2 * d, MPI_COMM_WORLD, &rq[nr++]);
+                    rc |= MPI_Irecv(b + base + (L + 1) * stride, 1, face[d], rup, 2 * d + 1, MPI_COMM_WORLD, &rq[nr++]);
+                    rc |= MPI_Isend(b + base + L * stride, 1, face[d], rup, 2 * d, MPI_COMM_WORLD, &rq[nr++]);
+                    rc |= MPI_Isend(b + base + stride, 1, face[d], rdn, 2 * d + 1, MPI_COMM_WORLD, &rq[nr++]);
+                } else {
+                    rc |= MPI_Irecv(b, 1, sub[d][2], rdn, 2 * d, MPI_COMM_WORLD, &rq[nr++]);
+                    rc |= MPI_Irecv(b, 1, sub[d][3], rup, 2 * d + 1, MPI_COMM_WORLD, &rq[nr++]);
+                    rc |= MPI_Isend(b, 1, sub[d][1], rup, 2 * d, MPI_COMM_WORLD, &rq[nr++]);
+                    rc |= MPI_Isend(b, 1, sub[d][0], rdn, 2 * d + 1, MPI_COMM_WORLD, &rq[nr++]);
+                }
+            }
+            if (nr) {
+                const int wrc = MPI_Waitall(nr, rq, MPI_STATUSES_IGNORE);
+                if (!rc) rc = wrc;
+            }
+            if (rank == 0 && iter_ns) iter_ns[it] = (long long)(gtime() - t0);
+        }
+        if (mode == 0) {
+            for (int d = 0; d < 3; d++)
+                if (face[d] != MPI_DATATYPE_NULL) MPI_Type_free(&face[d]);
+        } else {
+            for (int d = 0; d < 3; d++)
+                for (int k = 0; k < 4; k++) MPI_Type_free(&sub[d][k]);
+        }
+        if (p.p[7]) ((int*)p.p[7])[rank] = rc;
+        return rc ? rc : MPI_Finalize();
+    }
+};
+
+}  // namespace
+
+extern const gpumpi_prog_entry g_app_programs[] = {
+    GPUMPI_PROGRAM(GPUMPI_P_BUCKET_SORT, "bucket_sort", BucketSort),
+    GPUMPI_PROGRAM(GPUMPI_P_HALO, "halo", Halo),
+};
+extern const int g_num_app_programs = sizeof(g_app_programs) / sizeof(g_app_programs[0]);

@@ -21,8 +21,11 @@ __device__ void engine_main();
 
 __device__ MPI_Op gpumpi_predefined_op(int code);
 
+// At most 64 registers per thread (256 threads x 4 blocks, or 128 x 8, fill an SM's register file):
+// the rank count a launch can co-host is set by this.  The runtime's device functions are compiled
+// with the same cap; the bound keeps a program's own code (inlined into the kernel) from raising it.
 template <class P>
-__global__ void __launch_bounds__(256) gpumpi_rank_kernel(gpumpi_params prm) {
+__global__ void __launch_bounds__(256, 4) gpumpi_rank_kernel(gpumpi_params prm) {
     if (threadIdx.x != 0) {
         gpumpi::helper_loop();
         return;

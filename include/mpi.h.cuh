@@ -236,6 +236,11 @@ __device__ int gpumpi_world_rank(void);
 // Run fn(arg, tid, nthreads) on every thread of the calling rank's block (called from thread 0);
 // gives scalar user code the data-parallel width of its block between MPI calls.
 __device__ int gpumpi_block_parallel(void (*fn)(void* arg, int tid, int nthreads), void* arg);
+// Inside such a function: a barrier over the block's nthreads threads.
+__device__ void gpumpi_block_sync(int nthreads);
+// The block's dynamic shared memory (size in *bytes, 0 when the launch has none); free for the rank's
+// own block-parallel functions between MPI calls.
+__device__ void* gpumpi_block_scratch(size_t* bytes);
 // Per-rank copy of a converted program's global variable (reference global_vars.cuh:15 indexes by
 // the global thread id; a rank here is a block, so the index is the rank).
 #define __gpu_global(var) (var[gpumpi_world_rank()])

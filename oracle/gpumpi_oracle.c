@@ -461,31 +461,29 @@ void orc_bucket_keys(uint64_t seed, int rank, int64_t nkeys, int32_t* keys) {
 }
 
 int orc_bucket_sort(const int32_t* keys, int n, int64_t kpr, int32_t* out, int64_t cap, int64_t* out_counts) {
+    /* bucket of key k on n ranks: (k * n) >> 21, so rank r receives exactly the keys in
+     * [ceil(r 2^21 / n), ceil((r + 1) 2^21 / n)); its sorted output is that range of the global
+     * histogram expanded in increasing key order */
     const int64_t max_key = (int64_t)1 << 21;
-    for (int r = 0; r < n; r++) out_counts[r] = 0;
-    /* counts per destination */
+    int64_t* hist = (int64_t*)calloc((size_t)max_key, sizeof(int64_t));
+    if (!hist) return GPUMPI_ERR_NO_MEM;
     for (int64_t i = 0; i < (int64_t)n * kpr; i++) {
-        int d = (int)(((int64_t)keys[i] * n) >> 21);
-        out_counts[d]++;
+        const int64_t k = keys[i];
+        if (k < 0 || k >= max_key) { free(hist); return GPUMPI_ERR_ARG; }
+        hist[k]++;
     }
-    for (int r = 0; r < n; r++) if (out_counts[r] > cap) return GPUMPI_ERR_COUNT;
-    /* counting sort of each destination's key range */
     for (int r = 0; r < n; r++) {
-        int64_t lo = (max_key * r + n - 1) / n, hi = (max_key * (r + 1) + n - 1) / n;
-        /* keys k with (k*n)>>21 == r are exactly those with ceil(r*2^21/n) <= k < ceil((r+1)*2^21/n) */
-        int64_t range = hi - lo;
-        int64_t* hist = (int64_t*)calloc((size_t)(range > 0 ? range : 1), sizeof(int64_t));
-        if (!hist) return GPUMPI_ERR_NO_MEM;
-        for (int64_t i = 0; i < (int64_t)n * kpr; i++) {
-            int64_t k = keys[i];
-            if (k >= lo && k < hi) hist[k - lo]++;
-        }
-        int64_t pos = 0;
+        const int64_t lo = (max_key * r + n - 1) / n, hi = (max_key * (r + 1) + n - 1) / n;
+        int64_t cnt = 0;
+        for (int64_t k = lo; k < hi; k++) cnt += hist[k];
+        out_counts[r] = cnt;
+        if (cnt > cap) { free(hist); return GPUMPI_ERR_COUNT; }
         int32_t* o = out + (int64_t)r * cap;
-        for (int64_t k = 0; k < range; k++)
-            for (int64_t c = 0; c < hist[k]; c++) o[pos++] = (int32_t)(k + lo);
-        free(hist);
+        int64_t pos = 0;
+        for (int64_t k = lo; k < hi; k++)
+            for (int64_t c = 0; c < hist[k]; c++) o[pos++] = (int32_t)k;
     }
+    free(hist);
     return 0;
 }
 
