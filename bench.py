@@ -273,6 +273,43 @@ def small_alltoallv_case(args, gpumpi, torch, local):
                       "ms_per_step": ms, "gbs": 2.0 * total / (ms * 1e-3) / 1e9, "world": info}), flush=True)
 
 
+def bench_bucket_sort(gpumpi, torch, w_kw):
+    """Distributed bucket sort: 2^25 int32 keys over 256 ranks, 10 iterations of Alltoall(counts) +
+    Alltoallv(keys) + local counting sort, keys generated on the device from the seeded LCG."""
+    import numpy as np
+    from gpumpi import apps
+    n, total, iters = 256, 1 << 25, 10
+    ns = np.zeros(iters, dtype=np.uint64)
+    with gpumpi.World(n, **w_kw) as w:
+        rc, _, _, counts = apps.bucket_sort(w, 20251203, total, iters=iters, iter_ns=ns)
+        if rc:
+            return {"error": f"rc={rc}: {w.last_error()}"}
+        ms_total = w.last_kernel_ms()
+    it_ms = float(np.median(ns[1:])) / 1e6
+    return {"ranks": n, "keys": total, "iterations": iters, "ms_per_iteration_p50": it_ms,
+            "mkeys_per_s": total / (it_ms * 1e-3) / 1e6, "launch_ms": ms_total,
+            "keys_received": int(counts.sum().item())}
+
+
+def bench_halo(gpumpi, torch, w_kw):
+    """3D fp64 halo exchange on a 512^3 grid over 8x8x8 ranks (64^3 each), derived-datatype faces."""
+    import numpy as np
+    from gpumpi import apps
+    P, L, iters = 8, 64, 20
+    out = {"grid": "512^3 fp64", "ranks": P ** 3, "face_bytes_per_exchange": apps.halo_face_bytes(P, L)}
+    with gpumpi.World(P ** 3, **w_kw) as w:
+        for mode, name in ((0, "vector_hvector"), (1, "subarray")):
+            ns = np.zeros(iters, dtype=np.uint64)
+            rc, _ = apps.halo(w, P, L, iters=iters, mode=mode, iter_ns=ns)
+            if rc:
+                out[name] = {"error": f"rc={rc}: {w.last_error()}"}
+                continue
+            us = float(np.median(ns[2:])) / 1e3
+            out[name] = {"us_per_exchange_p50": us,
+                         "gbs": 2.0 * apps.halo_face_bytes(P, L) / (us * 1e-6) / 1e9}
+    return out
+
+
 def small_case(args, gpumpi, torch, local):
     """Allreduce fp32 SUM, 1024 ranks x 256 KiB (512 MiB of traffic per call): the profiled case."""
     n, count = 1024, 65536
@@ -372,7 +409,9 @@ def main():
     if not args.no_extra and rank == 0:
         for key, fn in (("alltoallv_bucket_sort", lambda: bench_alltoallv(gpumpi, torch, w_kw)),
                         ("alltoallv_1024ranks_1MiB", lambda: bench_alltoallv_1024(gpumpi, torch, w_kw, False)),
-                        ("alltoall_1024ranks_1MiB", lambda: bench_alltoallv_1024(gpumpi, torch, w_kw, True))):
+                        ("alltoall_1024ranks_1MiB", lambda: bench_alltoallv_1024(gpumpi, torch, w_kw, True)),
+                        ("bucket_sort_2e25_keys_256ranks", lambda: bench_bucket_sort(gpumpi, torch, w_kw)),
+                        ("halo_512cubed_512ranks", lambda: bench_halo(gpumpi, torch, w_kw))):
             try:
                 extra[key] = fn()
             except Exception as e:  # reported, not hidden

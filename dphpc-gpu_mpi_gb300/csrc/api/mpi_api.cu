@@ -1419,6 +1419,20 @@ extern "C" cudaError_t gpumpi_internal_install(Runtime* d_rt, MPI_Comm world, MP
     return cudaSuccess;
 }
 
+// The same from a device-resident array {Runtime*, world, group world, group empty}: device-to-device
+// copies only, so the sequence can be recorded in a CUDA graph and replayed later.
+extern "C" cudaError_t gpumpi_internal_install_dev(const void* const* d_vals, cudaStream_t stream) {
+    cudaError_t e;
+    if ((e = cudaMemcpyToSymbolAsync(g_rt, d_vals + 0, sizeof(void*), 0, cudaMemcpyDeviceToDevice, stream))) return e;
+    if ((e = cudaMemcpyToSymbolAsync(MPI_COMM_WORLD, d_vals + 1, sizeof(void*), 0, cudaMemcpyDeviceToDevice, stream)))
+        return e;
+    if ((e = cudaMemcpyToSymbolAsync(MPI_GROUP_WORLD, d_vals + 2, sizeof(void*), 0, cudaMemcpyDeviceToDevice, stream)))
+        return e;
+    if ((e = cudaMemcpyToSymbolAsync(MPI_GROUP_EMPTY, d_vals + 3, sizeof(void*), 0, cudaMemcpyDeviceToDevice, stream)))
+        return e;
+    return cudaSuccess;
+}
+
 __device__ MPI_Op gpumpi_predefined_op(int code) {
     return (code >= 0 && code < GPUMPI_NUM_PREDEFINED_OPS) ? &g_predef_ops[code] : nullptr;
 }

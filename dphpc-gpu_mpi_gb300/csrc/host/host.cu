@@ -29,6 +29,7 @@ extern const int g_num_app_programs;
 
 extern "C" cudaError_t gpumpi_internal_install(Runtime* d_rt, MPI_Comm world, MPI_Group gworld, MPI_Group gempty,
                                                 cudaStream_t stream);
+extern "C" cudaError_t gpumpi_internal_install_dev(const void* const* d_vals, cudaStream_t stream);
 
 namespace {
 
@@ -476,18 +477,14 @@ static int choose_geometry(gpumpi_world* w, const gpumpi_prog_entry* pe) {
     return GPUMPI_SUCCESS;
 }
 
-int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params, void* stream_v, int sync) {
-    if (!w || !params) return GPUMPI_ERR_ARG;
-    w->err.clear();
-    const gpumpi_prog_entry* pe = find_program(program);
-    if (!pe) {
-        w->err = "unknown program " + std::to_string(program);
-        return GPUMPI_ERR_ARG;
-    }
-    CK(cudaSetDevice(w->device));
+}  // extern "C"
+
+namespace {
+
+// Sets the runtime image for program pe (geometry and policy of the world as it is now).
+int prepare_runtime(gpumpi_world* w, const gpumpi_prog_entry* pe) {
     int rc = choose_geometry(w, pe);
     if (rc) return rc;
-    cudaStream_t s = stream_v ? (cudaStream_t)stream_v : w->stream;
     Runtime& r = w->h_rt;
     r.T = w->T;
     r.nengines = w->nengines;
@@ -498,6 +495,54 @@ int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params
     r.dyn_smem = (int)w->dyn_smem;
     r.tune_vec = w->tune_vec;
     r.tune_group = w->tune_group;
+    return GPUMPI_SUCCESS;
+}
+
+// Reads the device error records and exit codes after a finished launch.  Error records describe what
+// went wrong inside MPI calls; the calls also returned the codes to the program, so only a run that hit a
+// bounded-wait timeout fails here (other errors surface through the ranks' exit codes).
+int collect_results(gpumpi_world* w) {
+    const Runtime& r = w->h_rt;
+    const int nb = w->cfg.nranks + w->nengines;
+    CK(cudaMemcpy(w->h_err.data(), r.errors, sizeof(gpumpi::ErrorRecord) * nb, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(w->h_exit.data(), r.exit_codes, sizeof(int) * w->cfg.nranks, cudaMemcpyDeviceToHost));
+    int timeout = 0;
+    for (int b = 0; b < nb; b++) {
+        const gpumpi::ErrorRecord& e = w->h_err[b];
+        if (e.code) {
+            char buf[256];
+            snprintf(buf, sizeof buf, "rank %d: MPI error %d (detail %d) at runtime line %d, info %lld", e.rank,
+                     e.code, e.detail, e.line, e.info);
+            if (w->err.empty() || e.detail == GPUMPI_ERR_TIMEOUT) w->err = buf;
+            if (e.detail == GPUMPI_ERR_TIMEOUT) timeout = 1;
+        }
+    }
+    if (timeout) return GPUMPI_ERR_TIMEOUT;
+    for (int i = 0; i < w->cfg.nranks; i++)
+        if (w->h_exit[i] != 0) {
+            w->err = "rank " + std::to_string(i) + " returned " + std::to_string(w->h_exit[i]);
+            return w->h_exit[i];
+        }
+    return GPUMPI_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params, void* stream_v, int sync) {
+    if (!w || !params) return GPUMPI_ERR_ARG;
+    w->err.clear();
+    const gpumpi_prog_entry* pe = find_program(program);
+    if (!pe) {
+        w->err = "unknown program " + std::to_string(program);
+        return GPUMPI_ERR_ARG;
+    }
+    CK(cudaSetDevice(w->device));
+    int rc = prepare_runtime(w, pe);
+    if (rc) return rc;
+    cudaStream_t s = stream_v ? (cudaStream_t)stream_v : w->stream;
+    Runtime& r = w->h_rt;
     CK(cudaMemsetAsync(w->d_ctrl, 0, w->ctrl_bytes, s));
     CK(cudaMemcpyAsync(w->d_fixed, &w->h_fixed, sizeof(FixedImage), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(w->d_rt, &r, sizeof(Runtime), cudaMemcpyHostToDevice, s));
@@ -516,30 +561,101 @@ int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params
     float ms = 0;
     cudaEventElapsedTime(&ms, w->ev0, w->ev1);
     w->last_ms = ms;
-    // collect device-side error records
-    const int nb = w->cfg.nranks + w->nengines;
-    CK(cudaMemcpy(w->h_err.data(), r.errors, sizeof(gpumpi::ErrorRecord) * nb, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(w->h_exit.data(), r.exit_codes, sizeof(int) * w->cfg.nranks, cudaMemcpyDeviceToHost));
-    // Error records describe what went wrong inside MPI calls; the calls also returned the codes to the
-    // program, so only a run that hit a bounded-wait timeout fails here (other errors surface through
-    // the ranks' exit codes).
-    int timeout = 0;
-    for (int b = 0; b < nb; b++) {
-        const gpumpi::ErrorRecord& e = w->h_err[b];
-        if (e.code) {
-            char buf[256];
-            snprintf(buf, sizeof buf, "rank %d: MPI error %d (detail %d) at runtime line %d, info %lld", e.rank,
-                     e.code, e.detail, e.line, e.info);
-            if (w->err.empty() || e.detail == GPUMPI_ERR_TIMEOUT) w->err = buf;
-            if (e.detail == GPUMPI_ERR_TIMEOUT) timeout = 1;
-        }
+    return collect_results(w);
+}
+
+}  // extern "C"
+
+// A recorded launch: the per-launch reset, the runtime install and the cooperative kernel launch of one
+// program, captured once and replayed with cudaGraphLaunch.  The reset and install copy from device
+// images made at creation, so a replay reads no host memory.
+struct gpumpi_graph {
+    gpumpi_world* w = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    Runtime* d_rt_img = nullptr;
+    FixedImage* d_fixed_img = nullptr;
+    void** d_install = nullptr;
+};
+
+extern "C" {
+
+int gpumpi_graph_create(gpumpi_world* w, int program, const gpumpi_params* params, gpumpi_graph** out) {
+    if (!w || !params || !out) return GPUMPI_ERR_ARG;
+    *out = nullptr;
+    w->err.clear();
+    const gpumpi_prog_entry* pe = find_program(program);
+    if (!pe) {
+        w->err = "unknown program " + std::to_string(program);
+        return GPUMPI_ERR_ARG;
     }
-    if (timeout) return GPUMPI_ERR_TIMEOUT;
-    for (int i = 0; i < w->cfg.nranks; i++)
-        if (w->h_exit[i] != 0) {
-            w->err = "rank " + std::to_string(i) + " returned " + std::to_string(w->h_exit[i]);
-            return w->h_exit[i];
-        }
+    CK(cudaSetDevice(w->device));
+    int rc = prepare_runtime(w, pe);
+    if (rc) return rc;
+    gpumpi_graph* g = new gpumpi_graph();
+    g->w = w;
+    auto fail = [&](cudaError_t e, const char* what) {
+        w->err = std::string(what) + ": " + cudaGetErrorString(e);
+        cudaGetLastError();
+        gpumpi_graph_destroy(g);
+        return GPUMPI_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&g->d_rt_img, sizeof(Runtime)))) return fail(e, "cudaMalloc");
+    if ((e = cudaMalloc(&g->d_fixed_img, sizeof(FixedImage)))) return fail(e, "cudaMalloc");
+    if ((e = cudaMalloc(&g->d_install, 4 * sizeof(void*)))) return fail(e, "cudaMalloc");
+    void* vals[4] = {(void*)w->d_rt, (void*)&w->d_fixed->world, (void*)&w->d_fixed->gworld, (void*)&w->d_fixed->gempty};
+    if ((e = cudaMemcpy(g->d_rt_img, &w->h_rt, sizeof(Runtime), cudaMemcpyHostToDevice))) return fail(e, "image");
+    if ((e = cudaMemcpy(g->d_fixed_img, &w->h_fixed, sizeof(FixedImage), cudaMemcpyHostToDevice)))
+        return fail(e, "image");
+    if ((e = cudaMemcpy(g->d_install, vals, sizeof(vals), cudaMemcpyHostToDevice))) return fail(e, "image");
+    cudaStream_t cs = nullptr;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking))) return fail(e, "cudaStreamCreate");
+    if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal))) {
+        cudaStreamDestroy(cs);
+        return fail(e, "cudaStreamBeginCapture");
+    }
+    cudaError_t ce = cudaMemsetAsync(w->d_ctrl, 0, w->ctrl_bytes, cs);
+    if (!ce) ce = cudaMemcpyAsync(w->d_fixed, g->d_fixed_img, sizeof(FixedImage), cudaMemcpyDeviceToDevice, cs);
+    if (!ce) ce = cudaMemcpyAsync(w->d_rt, g->d_rt_img, sizeof(Runtime), cudaMemcpyDeviceToDevice, cs);
+    if (!ce) ce = gpumpi_internal_install_dev(g->d_install, cs);
+    if (!ce) ce = pe->launch(w->cfg.nranks + w->nengines, w->T, w->dyn_smem, cs, params);
+    e = cudaStreamEndCapture(cs, &g->graph);
+    cudaStreamDestroy(cs);
+    if (ce) return fail(ce, "capture");
+    if (e) return fail(e, "cudaStreamEndCapture");
+    if ((e = cudaGraphInstantiate(&g->exec, g->graph, 0))) return fail(e, "cudaGraphInstantiate");
+    *out = g;
+    return GPUMPI_SUCCESS;
+}
+
+int gpumpi_graph_launch(gpumpi_graph* g, void* stream_v, int sync) {
+    if (!g || !g->exec) return GPUMPI_ERR_ARG;
+    gpumpi_world* w = g->w;
+    w->err.clear();
+    CK(cudaSetDevice(w->device));
+    cudaStream_t s = stream_v ? (cudaStream_t)stream_v : w->stream;
+    CK(cudaEventRecord(w->ev0, s));
+    CK(cudaGraphLaunch(g->exec, s));
+    g_launches++;
+    CK(cudaEventRecord(w->ev1, s));
+    if (!sync) return GPUMPI_SUCCESS;
+    CK(cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+    w->last_ms = ms;
+    return collect_results(w);
+}
+
+int gpumpi_graph_destroy(gpumpi_graph* g) {
+    if (!g) return GPUMPI_SUCCESS;
+    if (g->w) cudaSetDevice(g->w->device);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    cudaFree(g->d_rt_img);
+    cudaFree(g->d_fixed_img);
+    cudaFree(g->d_install);
+    delete g;
     return GPUMPI_SUCCESS;
 }
 

@@ -1,5 +1,5 @@
-// prog_apps.cu — application programs on the MPI surface: the distributed bucket sort of integer keys
-// and the 3D halo exchange with derived-datatype faces.
+// prog_apps.cu — application programs on the MPI surface: the distributed bucket sort of integer keys,
+// the 3D halo exchange with derived-datatype faces, and a batch of communicators of uneven sizes.
 //
 // Scalar per-rank logic runs on each rank block's thread 0, like converted MPI code; the data-parallel
 // loops between MPI calls use the block's threads through gpumpi_block_parallel.
@@ -372,10 +372,71 @@ struct Halo {
     }
 };
 
+// ------------------------------------------------------------------------------------------------
+// Batched communicators: up to 64 communicators, each a contiguous range of world ranks made with
+// MPI_Comm_create, each running its own MPI_Allreduce every iteration in this one persistent launch.  A
+// rank in several communicators runs their collectives in communicator order (the same order on every
+// rank, so no cycle of waits can form); communicators on disjoint ranks progress at the same time and
+// each call's variant comes from the world's selection policy.  A world barrier ends each iteration, so
+// rank 0's time is the whole batch.
+//   i[0] communicators  i[1] iterations  i[2] datatype  i[3] op
+//   p[0] send base  p[1] recv base  p[2] int64 [comms][4] = {first world rank, size, count, element offset}
+//   p[6] int64 per-iteration ns (rank 0)  p[7] int rc [n]
+// Member i of communicator c sends from send + (offset_c + i * count_c) elements and receives likewise.
+// ------------------------------------------------------------------------------------------------
+constexpr int MAX_BATCH_COMMS = 64;
+
+struct Batch {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = -1, n = 0;
+        MPI_Comm_rank(MPI_COMM_WORLD, &rank);
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        const int ncomms = (int)p.i[0] < MAX_BATCH_COMMS ? (int)p.i[0] : MAX_BATCH_COMMS;
+        const int iters = (int)p.i[1];
+        const MPI_Datatype dt = (MPI_Datatype)p.i[2];
+        const MPI_Op op = gpumpi_predefined_op((int)p.i[3]);
+        const long long* tab = (const long long*)p.p[2];
+        int es = 0;
+        int rc = MPI_Type_size(dt, &es);
+        MPI_Group gw;
+        if (!rc) rc = MPI_Comm_group(MPI_COMM_WORLD, &gw);
+        MPI_Comm comms[MAX_BATCH_COMMS];
+        for (int c = 0; c < ncomms; c++) {
+            comms[c] = MPI_COMM_NULL;
+            if (rc) continue;
+            const int first = (int)tab[4 * c], size = (int)tab[4 * c + 1];
+            int range[1][3] = {{first, first + size - 1, 1}};
+            MPI_Group g;
+            rc = MPI_Group_range_incl(gw, 1, range, &g);
+            if (!rc) rc = MPI_Comm_create(MPI_COMM_WORLD, g, &comms[c]);
+            if (!rc) rc = MPI_Group_free(&g);
+        }
+        if (!rc) rc = MPI_Group_free(&gw);
+        long long* iter_ns = (long long*)p.p[6];
+        for (int it = 0; it < iters && rc == 0; it++) {
+            const unsigned long long t0 = gtime();
+            for (int c = 0; c < ncomms && rc == 0; c++) {
+                if (comms[c] == MPI_COMM_NULL) continue;
+                const long long count = tab[4 * c + 2];
+                const long long off = (tab[4 * c + 3] + (long long)(rank - (int)tab[4 * c]) * count) * es;
+                rc = MPI_Allreduce((const char*)p.p[0] + off, (char*)p.p[1] + off, (int)count, dt, op, comms[c]);
+            }
+            if (!rc) rc = MPI_Barrier(MPI_COMM_WORLD);
+            if (rank == 0 && iter_ns) iter_ns[it] = (long long)(gtime() - t0);
+        }
+        for (int c = 0; c < ncomms; c++)
+            if (comms[c] != MPI_COMM_NULL) MPI_Comm_free(&comms[c]);
+        if (p.p[7]) ((int*)p.p[7])[rank] = rc;
+        return rc ? rc : MPI_Finalize();
+    }
+};
+
 }  // namespace
 
 extern const gpumpi_prog_entry g_app_programs[] = {
     GPUMPI_PROGRAM(GPUMPI_P_BUCKET_SORT, "bucket_sort", BucketSort),
     GPUMPI_PROGRAM(GPUMPI_P_HALO, "halo", Halo),
+    GPUMPI_PROGRAM(GPUMPI_P_BATCH, "batch", Batch),
 };
 extern const int g_num_app_programs = sizeof(g_app_programs) / sizeof(g_app_programs[0]);

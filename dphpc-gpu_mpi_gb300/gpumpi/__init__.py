@@ -60,6 +60,7 @@ EXPORTS = [
     "gpumpi_kernel_launches", "gpumpi_test_run", "gpumpi_allreduce", "gpumpi_reduce", "gpumpi_bcast",
     "gpumpi_alltoall", "gpumpi_alltoallv", "gpumpi_allgather", "gpumpi_pingpong", "gpumpi_ring",
     "gpumpi_allreduce_noalloc", "gpumpi_mlp_forward", "gpumpi_mlp_loss_grad", "gpumpi_mlp_adam_step",
+    "gpumpi_graph_create", "gpumpi_graph_launch", "gpumpi_graph_destroy",
 ]
 
 
@@ -121,6 +122,9 @@ def lib():
         L.gpumpi_set_mlp.argtypes = [vp, vp, ctypes.c_size_t]
         L.gpumpi_read_trace.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         L.gpumpi_run_program.argtypes = [vp, i32, ctypes.POINTER(Params), vp, i32]
+        L.gpumpi_graph_create.argtypes = [vp, i32, ctypes.POINTER(Params), ctypes.POINTER(vp)]
+        L.gpumpi_graph_launch.argtypes = [vp, vp, i32]
+        L.gpumpi_graph_destroy.argtypes = [vp]
         L.gpumpi_last_kernel_ms.argtypes = [vp]
         L.gpumpi_last_kernel_ms.restype = ctypes.c_double
         L.gpumpi_kernel_launches.restype = ctypes.c_longlong
@@ -251,7 +255,8 @@ class World:
             self._check(rc, name)
         return rc, ok, oi, od
 
-    def run_program(self, program: int, i=(), p=(), d=(), stream=None, sync=True) -> int:
+    @staticmethod
+    def _params(i=(), p=(), d=()) -> Params:
         prm = Params()
         for k, v in enumerate(i):
             prm.i[k] = int(v)
@@ -259,7 +264,18 @@ class World:
             prm.d[k] = float(v)
         for k, v in enumerate(p):
             prm.p[k] = _ptr(v).value if v is not None else None
+        return prm
+
+    def run_program(self, program: int, i=(), p=(), d=(), stream=None, sync=True) -> int:
+        prm = self._params(i, p, d)
         return lib().gpumpi_run_program(self.h, program, ctypes.byref(prm), _stream(stream), int(sync))
+
+    def graph(self, program: int, i=(), p=(), d=()) -> "Graph":
+        """Records one launch of `program` into a CUDA graph (replay with Graph.launch)."""
+        prm = self._params(i, p, d)
+        h = ctypes.c_void_p()
+        self._check(lib().gpumpi_graph_create(self.h, program, ctypes.byref(prm), ctypes.byref(h)), "graph_create")
+        return Graph(self, h)
 
     # ---- hot path ----
     def _ns(self, iters, iter_ns):
@@ -306,6 +322,27 @@ class World:
         """Generic P_COLL launch on device (torch) buffers; returns the MPI code."""
         return self.run_program(P_COLL, i=(COLL[kind], count, dt, op, root, iters, send_stride, recv_stride),
                                 p=(send, recv, *mats, iter_ns, rcs), stream=stream, sync=sync)
+
+
+class Graph:
+    """A recorded launch of one program on one world."""
+
+    def __init__(self, world: World, h):
+        self.world, self.h = world, h
+
+    def launch(self, stream=None, sync=True) -> int:
+        return lib().gpumpi_graph_launch(self.h, _stream(stream), int(sync))
+
+    def close(self):
+        if self.h:
+            lib().gpumpi_graph_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def kernel_launches() -> int:

@@ -80,3 +80,47 @@ def halo(world: World, P: int, L: int, iters: int = 1, mode: int = 0, blocks=Non
 def halo_face_bytes(P: int, L: int) -> int:
     """Payload of one exchange: six faces of L*L doubles per rank."""
     return 6 * L * L * 8 * P ** 3
+
+
+def batch_layout(seed: int, nranks: int, ncomms: int = 64, min_size: int = 8, max_size: int = 512,
+                 min_bytes: int = 4, max_bytes: int = 1 << 16, esize: int = 4) -> np.ndarray:
+    """Seeded layout of a batch of communicators: sizes log-uniform in [min_size, max_size] (capped at the
+    world), each a contiguous range of world ranks at a random start, per-rank message bytes log-uniform
+    in [min_bytes, max_bytes].  Returns int64 [ncomms, 4] = {first rank, size, count, element offset}."""
+    rng = np.random.default_rng(seed)
+    hi = min(max_size, nranks)
+    tab = np.zeros((ncomms, 4), dtype=np.int64)
+    off = 0
+    for c in range(ncomms):
+        size = int(round(np.exp(rng.uniform(np.log(min_size), np.log(hi)))))
+        size = max(1, min(size, nranks))
+        first = int(rng.integers(0, nranks - size + 1))
+        count = max(1, int(np.exp(rng.uniform(np.log(min_bytes), np.log(max_bytes)))) // esize)
+        tab[c] = (first, size, count, off)
+        off += size * count
+    return tab
+
+
+def batch_elements(tab: np.ndarray) -> int:
+    return int((tab[:, 1] * tab[:, 2]).sum())
+
+
+def batch(world: World, tab: np.ndarray, send, recv, iters: int = 1, dt: int = 12, op: int = 2, iter_ns=None,
+          graph: bool = False):
+    """Runs the batch (every communicator's MPI_Allreduce, `iters` times) in one launch; with graph=True
+    returns a recorded Graph instead of running (replay with Graph.launch)."""
+    import torch
+    from . import P_BATCH
+    dev = torch.device("cuda", torch.cuda.current_device())
+    tab_d = torch.from_numpy(np.ascontiguousarray(tab, dtype=np.int64)).to(dev)
+    rcs = torch.zeros(world.nranks, dtype=torch.int32, device=dev)
+    ns = torch.zeros(max(1, iters), dtype=torch.int64, device=dev)
+    args = dict(i=(len(tab), iters, dt, op), p=(send, recv, tab_d, None, None, None, ns, rcs))
+    if graph:
+        g = world.graph(P_BATCH, **args)
+        g._keep = (tab_d, rcs, ns)  # device buffers the recorded launch reads and writes
+        return g
+    rc = world.run_program(P_BATCH, **args)
+    torch.cuda.synchronize()
+    _copy_ns(ns, iter_ns)
+    return _first_error(rc, rcs)

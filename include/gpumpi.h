@@ -105,7 +105,9 @@ enum gpumpi_program {
     GPUMPI_P_PI,               /* i[0]=seed i[1]=pairs per rank p[0]=int64 hits[nranks] p[1]=int64 total p[7]=rc */
     GPUMPI_P_BUCKET_SORT,      /* see bench / tests */
     GPUMPI_P_HALO,
-    GPUMPI_P_BATCH,
+    GPUMPI_P_BATCH,            /* i[0]=communicators (<= 64) i[1]=iters i[2]=datatype i[3]=op
+                                  p[0]=send base p[1]=recv base p[2]=int64 [comms][4] {first world rank,
+                                  size, count, element offset} p[6]=int64 ns per iteration p[7]=rc */
 };
 
 /* collective kinds for GPUMPI_P_COLL */
@@ -158,6 +160,15 @@ int gpumpi_read_trace(gpumpi_world* w, void* host_out, size_t cap, size_t* n);
 
 /* Runs built-in program `program` on all ranks; blocks until it finished when sync != 0. */
 int gpumpi_run_program(gpumpi_world* w, int program, const gpumpi_params* params, void* stream, int sync);
+/* Recorded launches (no counterpart in the reference, which launches once per process): the reset,
+ * runtime install and cooperative launch of `program` with `params`, captured into a CUDA graph once and
+ * replayed by gpumpi_graph_launch.  The graph keeps the world's geometry, policy and tuning as they were
+ * at creation; replays of one world must not overlap each other or other runs of that world. */
+typedef struct gpumpi_graph gpumpi_graph;
+int gpumpi_graph_create(gpumpi_world* w, int program, const gpumpi_params* params, gpumpi_graph** out);
+/* Replays on `stream` (the world's stream when NULL); with sync != 0 waits and returns like run_program. */
+int gpumpi_graph_launch(gpumpi_graph* g, void* stream, int sync);
+int gpumpi_graph_destroy(gpumpi_graph* g);
 /* Launch-time of the last run in milliseconds (CUDA events around the kernel). */
 double gpumpi_last_kernel_ms(gpumpi_world* w);
 /* How many kernels the library launched so far (all worlds). */
