@@ -13,7 +13,11 @@ Reported:
              inputs, the collective, device->host copy of all outputs, every step;
   roofline   against the measured HBM copy bandwidth (MEASURED_PEAKS.json, "of measured");
   cpu_baseline  the CPU oracle's multi-threaded allreduce on a bounded sample, on this host's cores;
-  extra      p50/p99 per-call latency, Alltoallv GB/s on the bucket-sort shape, per-variant GB/s.
+  extra      p50/p99 per-call latency; per-variant Allreduce GB/s; Alltoall(v) among 1024 ranks at 1 MiB
+             per rank (uniform and uneven counts) per piece order; the bucket sort (2^25 keys, 256
+             ranks), the 512^3 halo exchange and the batch of 64 communicators; the selector block:
+             plain / tuned / learned policies on the headline Allreduce and the uneven Alltoallv, and the
+             held-out regret of the packaged tuned table and network.
 
 --impl reference: the reference's algorithm for this path restated on the CPU (the oracle port:
 canonical-order fold, all host threads) on the same workload; the reference's own gpu_mpi runtime
@@ -310,6 +314,92 @@ def bench_halo(gpumpi, torch, w_kw):
     return out
 
 
+def bench_batch(gpumpi, torch, w_kw):
+    """64 communicators of uneven sizes (8..512 ranks, log-uniform, seeded) on 512 world ranks, each an
+    fp32 SUM Allreduce of 4 B .. 64 KiB per rank, in one persistent launch: as a plain launch and as a
+    replayed CUDA graph (one launch per batch)."""
+    import numpy as np
+    from gpumpi import apps
+    n = 512
+    tab = apps.batch_layout(7, n)
+    E = apps.batch_elements(tab)
+    send = (torch.rand(E, device="cuda") * 2 - 1).contiguous()
+    recv = torch.zeros_like(send)
+    payload = 4 * E
+    out = {"world_ranks": n, "communicators": len(tab), "sizes": [int(x) for x in tab[:, 1]],
+           "payload_bytes": payload}
+    with gpumpi.World(n, **w_kw) as w:
+        iters = 20
+        ns = np.zeros(iters, dtype=np.uint64)
+        rc = apps.batch(w, tab, send, recv, iters=iters, dt=gpumpi.FLOAT, op=gpumpi.OP_SUM, iter_ns=ns)
+        if rc:
+            return {"error": f"rc={rc}: {w.last_error()}"}
+        us = float(np.median(ns[2:])) / 1e3
+        out["in_launch_us_per_batch_p50"] = us
+        out["in_launch_gbs"] = 2.0 * payload / (us * 1e-6) / 1e9
+        with apps.batch(w, tab, send, recv, iters=1, dt=gpumpi.FLOAT, op=gpumpi.OP_SUM, graph=True) as g:
+            g.launch()
+            reps = 20
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                g.launch(sync=False)
+            torch.cuda.synchronize()
+            out["graph_replay_us_per_batch"] = (time.perf_counter() - t0) / reps * 1e6
+    return out
+
+
+def bench_selector(gpumpi, torch, w_kw):
+    """The three selection policies on the headline Allreduce (1024 ranks x 1 MiB fp32) and the uneven
+    Alltoallv (1024 ranks, 1 MiB per rank, int32), with the packaged tuned table and network; plus the
+    held-out regret summary recorded when they were trained."""
+    import numpy as np
+    from gpumpi import selector
+    out = {}
+    rep_path = selector.DATA / "selector_report.json"
+    if rep_path.exists():
+        rep = json.loads(rep_path.read_text())
+        out["heldout_stream"] = {k: rep[k] for k in ("all", "allreduce", "alltoallv") if k in rep}
+        out["training_timings"] = rep.get("train_records", 0) + rep.get("val_records", 0)
+        out["margin"] = rep.get("margin")
+    n, count = 1024, (1 << 20) // 4
+    send = (torch.rand((n, count), device="cuda") * 2 - 1).contiguous()
+    recv = torch.empty_like(send)
+    rng = np.random.default_rng(4242)
+    sc = rng.integers(0, 513, (n, n)).astype(np.int32)
+    rc_ = sc.T.copy()
+    sd, rd = (np.cumsum(sc, 1) - sc).astype(np.int32), (np.cumsum(rc_, 1) - rc_).astype(np.int32)
+    S, R = int(sc.sum(1).max()), int(rc_.sum(1).max())
+    a_send = torch.randint(-2**31, 2**31 - 1, (n, S), device="cuda", dtype=torch.int32)
+    a_recv = torch.zeros((n, R), dtype=torch.int32, device="cuda")
+    dev = [torch.from_numpy(a).cuda() for a in (sc, sd, rc_, rd)]
+    a_bytes = int(sc.sum()) * 4
+    with gpumpi.World(n, trace_capacity=64, **w_kw) as w:
+        for pol in ("plain", "tuned", "learned"):
+            try:
+                selector.apply_policy(w, pol)
+            except FileNotFoundError as e:
+                out[pol] = {"error": str(e)}
+                continue
+            iters = 20
+            ns = np.zeros(iters, dtype=np.uint64)
+            w.allreduce(send, recv, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=3)
+            w.allreduce(send, recv, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=iters, iter_ns=ns)
+            ar_ms = w.last_kernel_ms() / iters
+            ar_var = sorted(set(int(v) for v in w.read_trace()["variant"]))
+            ns2 = np.zeros(iters, dtype=np.uint64)
+            w.alltoallv(a_send, S * 4, *dev[:2], a_recv, R * 4, *dev[2:], gpumpi.INT, iters=3)
+            w.alltoallv(a_send, S * 4, *dev[:2], a_recv, R * 4, *dev[2:], gpumpi.INT, iters=iters, iter_ns=ns2)
+            a_ms = w.last_kernel_ms() / iters
+            a_var = sorted(set(int(v) for v in w.read_trace()["variant"]))
+            out[pol] = {"allreduce_gbs": 2.0 * n * count * 4 / (ar_ms * 1e-3) / 1e9,
+                        "allreduce_p50_us": float(pct(list(ns), 0.5)) / 1e3, "allreduce_variants": ar_var,
+                        "alltoallv_gbs": 2.0 * a_bytes / (a_ms * 1e-3) / 1e9,
+                        "alltoallv_p50_us": float(pct(list(ns2), 0.5)) / 1e3, "alltoallv_variants": a_var}
+        w.set_policy(-1, 3)
+    return out
+
+
 def small_case(args, gpumpi, torch, local):
     """Allreduce fp32 SUM, 1024 ranks x 256 KiB (512 MiB of traffic per call): the profiled case."""
     n, count = 1024, 65536
@@ -411,7 +501,9 @@ def main():
                         ("alltoallv_1024ranks_1MiB", lambda: bench_alltoallv_1024(gpumpi, torch, w_kw, False)),
                         ("alltoall_1024ranks_1MiB", lambda: bench_alltoallv_1024(gpumpi, torch, w_kw, True)),
                         ("bucket_sort_2e25_keys_256ranks", lambda: bench_bucket_sort(gpumpi, torch, w_kw)),
-                        ("halo_512cubed_512ranks", lambda: bench_halo(gpumpi, torch, w_kw))):
+                        ("halo_512cubed_512ranks", lambda: bench_halo(gpumpi, torch, w_kw)),
+                        ("batch_64_communicators", lambda: bench_batch(gpumpi, torch, w_kw)),
+                        ("selector", lambda: bench_selector(gpumpi, torch, w_kw))):
             try:
                 extra[key] = fn()
             except Exception as e:  # reported, not hidden

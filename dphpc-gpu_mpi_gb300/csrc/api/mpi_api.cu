@@ -441,6 +441,13 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     int best = 0;
     for (int v = 1; v < 4; v++)
         if (w->y[v] < w->y[best]) best = v;
+    // the tuned table is the fallback: its choice stands unless the network predicts a clear gain
+    const int row = kind == JOB_ALLREDUCE ? 0 : kind == JOB_REDUCE ? 1 : kind == JOB_ALLTOALLV ? 2 : -1;
+    if (row >= 0 && g_rt->tuned_table) {
+        const int b = clamp_i(ilog2_ll(bytes), 0, SEL_BYTES - 1), r = clamp_i(ilog2_ll(n), 0, SEL_RANKS - 1);
+        const int tv = g_rt->tuned_table[(row * SEL_BYTES + b) * SEL_RANKS + r];
+        if (tv >= 0 && tv < 4 && w->y[tv] <= w->y[best] + g_rt->mlp_margin) best = tv;
+    }
     R->sel_key_kind = kind;
     R->sel_key_bytes = bytes;
     R->sel_key_n = n;

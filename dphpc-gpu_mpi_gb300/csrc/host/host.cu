@@ -376,6 +376,7 @@ int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
     case GPUMPI_TUNE_ENGINES: w->cfg.engine_blocks = (int)value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_COPY_CHUNK: w->h_rt.copy_chunk_bytes = value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_ENGINE_MIN_BYTES: w->h_rt.engine_min_bytes = value; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_MLP_MARGIN: w->h_rt.mlp_margin = (float)value * 1e-3f; return GPUMPI_SUCCESS;
     default: return GPUMPI_ERR_ARG;
     }
 }

@@ -389,6 +389,9 @@ struct Runtime {
     // selector
     const signed char* tuned_table;   // [kind][log2 bytes][log2 ranks] -> variant (or nullptr)
     const float* mlp_params;          // learned selector weights (or nullptr)
+    float mlp_margin;                 // learned choice overrides the tuned table only if it predicts this
+                                      // much lower log-time
+
     TraceRec* trace;
     unsigned long long* trace_count;
     int clock_khz;

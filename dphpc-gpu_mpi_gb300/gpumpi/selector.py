@@ -1,4 +1,5 @@
-"""Autotuner and learned algorithm selector for the reduction variants (DIRECT, TREE, RING, STAGED).
+"""Autotuner and learned algorithm selector for the collective variants (DIRECT, TREE, RING, STAGED) of
+MPI_Allreduce/Reduce (fold orders, TMA staging) and MPI_Alltoall(v) (piece orders, TMA staging).
 
 No counterpart in the reference (one algorithm per collective there).  Pieces:
   * `features()` — the 12 call features; the same formula runs inside the kernel (mpi_api.cu,
@@ -130,32 +131,68 @@ RANKS = [16, 32, 64, 128, 256, 512, 1024, 2048]
 LOG2_BYTES = list(range(6, 26))          # 64 B .. 32 MiB per rank
 DTYPES = [gpumpi.FLOAT, gpumpi.INT, gpumpi.DOUBLE]
 BUDGET = 6 << 30                          # device bytes for send + recv buffers
+KINDS = (KIND_ALLREDUCE, KIND_ALLTOALLV)
+MARGIN = 0.05   # predicted log-time gain the network needs to override the tuned table (5%)
+TABLE_ROW = {KIND_ALLREDUCE: 0, KIND_REDUCE: 1, KIND_ALLTOALLV: 2}
+DATA = Path(__file__).resolve().parent / "data"
 
 
 def _buffers(torch, n, max_bytes):
-    send = torch.empty(n * max_bytes // 4, dtype=torch.int32, device="cuda")
+    send = torch.empty(2 * n * max_bytes // 4 + 2 * n * n, dtype=torch.int32, device="cuda")
     g = torch.Generator(device="cuda").manual_seed(n)
     send.copy_(torch.randint(-100000, 100000, send.shape, generator=g, device="cuda", dtype=torch.int32))
     recv = torch.empty_like(send)
     return send, recv
 
 
-def _measure(w, torch, send, recv, n, nbytes, dt, variant, iters):
-    """Per-call times (us) of `iters` calls, from the runtime's trace; plus device time per call."""
-    count = max(1, nbytes // DT_SIZE[dt])
-    stride = count * DT_SIZE[dt]
+class Exchange:
+    """Seeded uneven Alltoallv layout: every pair's count uniform in [0, 2m] int32, m = bytes / (4 n)."""
+
+    def __init__(self, torch, n, nbytes, seed):
+        rng = np.random.default_rng(seed)
+        m = nbytes / (4.0 * n)
+        sc = rng.integers(0, int(2 * m) + 1, (n, n)).astype(np.int32)
+        rc = sc.T.copy()
+        self.S, self.R = max(1, int(sc.sum(1).max())), max(1, int(rc.sum(1).max()))
+        sd, rd = (np.cumsum(sc, 1) - sc).astype(np.int32), (np.cumsum(rc, 1) - rc).astype(np.int32)
+        self.dev = [torch.from_numpy(a).cuda() for a in (sc, sd, rc, rd)]
+
+
+def _measure(w, torch, send, recv, n, nbytes, dt, kind, variant, iters, ex=None):
+    """Per-call records (log2 bytes seen by the kernel, us) of `iters` calls, from the runtime's trace."""
     w.set_policy(variant, 0)
-    rc = w.coll("allreduce", send, recv, count, dt, gpumpi.OP_SUM, iters=iters, send_stride=stride,
-                recv_stride=stride)
-    if rc:
-        raise gpumpi.GpumpiError(rc, w.last_error())
+    if kind == KIND_ALLTOALLV:
+        sc, sd, rc, rd = ex.dev
+        w.alltoallv(send, ex.S * 4, sc, sd, recv, ex.R * 4, rc, rd, gpumpi.INT, iters=iters)
+    else:
+        count = max(1, nbytes // DT_SIZE[dt])
+        stride = count * DT_SIZE[dt]
+        code = w.coll("allreduce", send, recv, count, dt, gpumpi.OP_SUM, iters=iters, send_stride=stride,
+                      recv_stride=stride)
+        if code:
+            raise gpumpi.GpumpiError(code, w.last_error())
     tr = w.read_trace()
-    return [float(r["us"]) for r in tr], w.last_kernel_ms() * 1e3 / iters
+    return [(float(r["log2_bytes"]), float(r["us"])) for r in tr]
+
+
+def _shapes_for(kind):
+    return DTYPES if kind == KIND_ALLREDUCE else [gpumpi.INT]
+
+
+def _sizes_for(lb):
+    """The power of two 2^lb and an off-grid size in the same octave that is 8 mod 16 bytes, so rank
+    buffers laid end to end lose 16-byte alignment (vector width and variant ranking change with it)."""
+    b = 1 << lb
+    off = int(round(b * 1.41 / 8)) * 8
+    if off % 16 == 0:
+        off += 8
+    return [b, off] if off < 2 * b else [b]
 
 
 def autotune(iters: int = 30, log=print):
-    """Sweep; returns (records, table, median grid, rank share per n).
-    records: list of (n, bytes, dt, variant, us)."""
+    """Sweep of Allreduce (SUM; fp32, int32, fp64) and uneven int32 Alltoallv over ranks x bytes per rank
+    x variant.  Returns (records, table, median grid, rank share per n); a record is
+    (kind, n, log2 bytes seen by the kernel, dt, variant, us)."""
     import torch
     records = []
     grid = {}
@@ -166,44 +203,46 @@ def autotune(iters: int = 30, log=print):
         send, recv = _buffers(torch, n, max_bytes)
         t0 = time.time()
         for lb in LOG2_BYTES:
-            nbytes = 1 << lb
-            if 2 * n * nbytes > BUDGET:
-                continue
-            for dt in DTYPES:
-                for v in range(NVAR):
-                    us, _ = _measure(w, torch, send, recv, n, nbytes, dt, v, iters)
-                    us = us[2:] if len(us) > 4 else us       # drop the first calls (cold)
-                    records += [(n, nbytes, dt, v, u) for u in us]
-                    grid[(n, lb, dt, v)] = float(np.median(us))
+            for nbytes in _sizes_for(lb):
+                if 2 * n * nbytes > BUDGET:
+                    continue
+                for kind in KINDS:
+                    ex = Exchange(torch, n, nbytes, seed=n * 100 + nbytes) if kind == KIND_ALLTOALLV else None
+                    for dt in _shapes_for(kind):
+                        for v in range(NVAR):
+                            recs = _measure(w, torch, send, recv, n, nbytes, dt, kind, v, iters, ex)
+                            recs = recs[2:] if len(recs) > 4 else recs    # drop the first calls (cold)
+                            records += [(kind, n, l2b, dt, v, u) for l2b, u in recs]
+                            # table cell: log2 bytes as the kernel sees them
+                            cell = int(math.floor(recs[0][0])) if recs and recs[0][0] > 0 else 0
+                            grid[(kind, n, nbytes, dt, v)] = (cell, float(np.median([u for _, u in recs])))
         info = w.info()
         shares[n] = n / (n + info["engine_blocks"])
         log(f"autotune: {n} ranks done in {time.time() - t0:.1f}s ({len(records)} records); world {info}")
         w.close()
         del send, recv
         torch.cuda.empty_cache()
-    table = np.full((2, 32, 16), -1, np.int8)
-    for n in RANKS:
-        for lb in LOG2_BYTES:
-            best, bt = None, None
-            for v in range(NVAR):
-                # score over datatypes: sum of medians
-                ts = [grid.get((n, lb, dt, v)) for dt in DTYPES]
-                if any(t is None for t in ts):
-                    continue
-                s = sum(ts)
-                if bt is None or s < bt:
-                    best, bt = v, s
-            if best is not None:
-                table[0, lb, int(math.log2(n))] = best
-                table[1, lb, int(math.log2(n))] = best
-    return records, table, grid, shares
+    # table: per (kind, cell of log2 bytes, log2 ranks) the variant with the least summed median time over
+    # every shape measured in the cell (both sizes, every datatype)
+    sums = {}
+    for (kind, n, nbytes, dt, v), (cell, t) in grid.items():
+        key = (kind, n, cell)
+        sums.setdefault(key, np.zeros(NVAR))[v] += t
+    table = np.full((3, 32, 16), -1, np.int8)
+    for (kind, n, cell), tv in sums.items():
+        best = int(np.argmin(tv))
+        table[TABLE_ROW[kind], min(31, cell), int(math.log2(n))] = best
+        if kind == KIND_ALLREDUCE:
+            table[TABLE_ROW[KIND_REDUCE], min(31, cell), int(math.log2(n))] = best
+    return records, table, {f"{k[0]}:{k[1]}:{k[2]}:{k[3]}:{k[4]}": t for k, (c, t) in grid.items()}, shares
 
 
 def dataset(records, rank_share_of):
-    X = np.stack([features(KIND_ALLREDUCE, b, n, dt, gpumpi.OP_SUM, rank_share_of[n]) for n, b, dt, v, u in records])
+    X = np.stack([features(k, 2.0 ** l2b, n, dt, gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1, rank_share_of[n])
+                  for k, n, l2b, dt, v, u in records])
     T = np.zeros((len(records), NVAR), np.float32)
     M = np.zeros((len(records), NVAR), np.float32)
-    for i, (n, b, dt, v, u) in enumerate(records):
+    for i, (k, n, l2b, dt, v, u) in enumerate(records):
         T[i, v] = math.log(max(u, 1e-3))
         M[i, v] = 1.0
     return X, T, M
@@ -211,71 +250,80 @@ def dataset(records, rank_share_of):
 
 def evaluate(mlp_params, table, calls: int = 10000, shapes_per_rank: int = 12, seed: int = 2026, iters: int = 12,
              log=print):
-    """Held-out stream: `calls` seeded Allreduce calls (sizes log-uniform 64 B .. 32 MiB, ranks 16 .. 2048,
-    fp32/int32/fp64) drawn from off-grid shapes; every variant of every shape is measured."""
+    """Held-out stream: `calls` seeded calls, half Allreduce (fp32/int32/fp64 SUM) and half uneven int32
+    Alltoallv, sizes log-uniform 64 B .. 32 MiB per rank, 16 .. 2048 ranks, drawn from off-grid shapes;
+    every variant of every shape is measured, so the exhaustive best is known."""
     import torch
     rng = np.random.default_rng(seed)
     shapes = []
     for n in RANKS:
-        for _ in range(shapes_per_rank):
+        for j in range(shapes_per_rank):
+            kind = KINDS[j % 2]
             while True:
                 b = int(2 ** rng.uniform(6, 25))
                 b -= b % 8
                 if b >= 64 and 2 * n * b <= BUDGET and (b & (b - 1)) != 0:
                     break
-            shapes.append((n, b, int(rng.choice(DTYPES))))
-    meas = {}
-    pick = {}
-    shares = {}
+            dt = int(rng.choice(DTYPES)) if kind == KIND_ALLREDUCE else gpumpi.INT
+            shapes.append((kind, n, b, dt))
+    meas, seen, shares = {}, {}, {}
     mlp = MLP(params=mlp_params)
     for n in RANKS:
-        sub = [s for s in shapes if s[0] == n]
-        max_bytes = max(b for _, b, _ in sub)
+        sub = [s for s in shapes if s[1] == n]
+        max_bytes = max(b for _, _, b, _ in sub)
         w = gpumpi.World(n, timeout_s=60.0, trace_capacity=4096)
         send, recv = _buffers(torch, n, max_bytes)
-        for (_, b, dt) in sub:
+        for k, (kind, _, b, dt) in enumerate(sub):
+            ex = Exchange(torch, n, b, seed=seed + 7 * k + n) if kind == KIND_ALLTOALLV else None
             times = []
             for v in range(NVAR):
-                us, _ = _measure(w, torch, send, recv, n, b, dt, v, iters)
-                us = us[2:] if len(us) > 4 else us
-                times.append(float(np.median(us)))
-            meas[(n, b, dt)] = times
+                recs = _measure(w, torch, send, recv, n, b, dt, kind, v, iters, ex)
+                recs = recs[2:] if len(recs) > 4 else recs
+                times.append(float(np.median([u for _, u in recs])))
+                seen[(kind, n, b, dt)] = recs[0][0]   # log2 bytes as the kernel saw it
+            meas[(kind, n, b, dt)] = times
         shares[n] = n / (n + w.info()["engine_blocks"])
         w.close()
         del send, recv
         torch.cuda.empty_cache()
     keys = list(meas)
-    # the learned choice uses the same features the kernel computes (rank share = ranks / launch blocks)
-    X = np.stack([features(KIND_ALLREDUCE, b, n, dt, gpumpi.OP_SUM, shares[n]) for (n, b, dt) in keys])
+    # the learned and tuned choices use what the kernel computes per call (bytes estimate, rank share)
+    X = np.stack([features(k, 2.0 ** seen[(k, n, b, dt)], n, dt, gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1,
+                           shares[n]) for (k, n, b, dt) in keys])
     pred = mlp.predict(X)
-    for i, k in enumerate(keys):
-        n, b, dt = k
-        pick[k] = {"learned": int(np.argmin(pred[i])),
-                   "tuned": int(table[0, min(31, int(math.log2(b))), int(math.log2(n))]),
-                   "plain": 0}
-        if pick[k]["tuned"] < 0:
-            pick[k]["tuned"] = 0
-    # stream of calls
+    pick = {}
+    for i, key in enumerate(keys):
+        kind, n, b, dt = key
+        tv = int(table[TABLE_ROW[kind], min(31, max(0, int(math.floor(seen[key])))), int(math.log2(n))])
+        pure = int(np.argmin(pred[i]))
+        learned = tv if (tv >= 0 and pred[i][tv] <= pred[i][pure] + MARGIN) else pure  # same rule as the kernel
+        pick[key] = {"learned": learned, "learned_pure": pure, "tuned": tv if tv >= 0 else 0, "plain": 0}
     idx = rng.integers(0, len(keys), calls)
-    tot = {"best": 0.0, "learned": 0.0, "tuned": 0.0, "plain": 0.0}
-    regrets = {"learned": [], "tuned": [], "plain": []}
-    for i in idx:
-        k = keys[i]
-        t = meas[k]
-        best = min(t)
-        tot["best"] += best
-        for pol in ("learned", "tuned", "plain"):
-            tp = t[pick[k][pol]]
-            tot[pol] += tp
-            regrets[pol].append(tp / best - 1.0)
-    rep = {"calls": calls, "shapes": len(keys),
-           "total_time_ms": {k: v / 1e3 for k, v in tot.items()},
-           "time_over_best": {p: tot[p] / tot["best"] - 1.0 for p in ("learned", "tuned", "plain")},
-           "mean_regret": {p: float(np.mean(regrets[p])) for p in regrets},
-           "p90_regret": {p: float(np.percentile(regrets[p], 90)) for p in regrets},
-           "learned_vs_tuned_time": tot["learned"] / tot["tuned"],
-           "choices": {f"{k[0]}x{k[1]}:{k[2]}": pick[k] for k in keys}}
-    log(json.dumps({k: v for k, v in rep.items() if k != "choices"}))
+    pols = ("learned", "learned_pure", "tuned", "plain")
+    rep = {"calls": calls, "shapes": len(keys)}
+    for label, kinds in (("all", KINDS), ("allreduce", (KIND_ALLREDUCE,)), ("alltoallv", (KIND_ALLTOALLV,))):
+        tot = {p: 0.0 for p in ("best",) + pols}
+        regrets = {p: [] for p in pols}
+        for i in idx:
+            key = keys[i]
+            if key[0] not in kinds:
+                continue
+            t = meas[key]
+            best = min(t)
+            tot["best"] += best
+            for pol in pols:
+                tp = t[pick[key][pol]]
+                tot[pol] += tp
+                regrets[pol].append(tp / best - 1.0)
+        rep[label] = {"calls": len(regrets["plain"]),
+                      "total_time_ms": {k: v / 1e3 for k, v in tot.items()},
+                      "time_over_best": {p: tot[p] / tot["best"] - 1.0 for p in pols},
+                      "mean_regret": {p: float(np.mean(regrets[p])) for p in pols},
+                      "p90_regret": {p: float(np.percentile(regrets[p], 90)) for p in pols},
+                      "learned_vs_tuned_time": tot["learned"] / tot["tuned"]}
+    rep["choices"] = {f"{k[0]}:{k[1]}x{k[2]}:{k[3]}": pick[k] for k in keys}
+    rep["measured_us"] = {f"{k[0]}:{k[1]}x{k[2]}:{k[3]}": meas[k] for k in keys}
+    log(json.dumps({k: rep[k] for k in ("all", "allreduce", "alltoallv")}))
     return rep
 
 
@@ -293,9 +341,10 @@ def run(out: Path, iters: int = 30):
     cut = int(0.8 * len(X))
     tr, va = perm[:cut], perm[cut:]
     mlp = MLP(seed=0)
-    hist = mlp.train(X[tr], T[tr], M[tr], epochs=40)
-    import torch as _t
-    xv = _t.from_numpy(X[va]).cuda(); tv = _t.from_numpy(T[va]).cuda(); mv = _t.from_numpy(M[va]).cuda()
+    hist = mlp.train(X[tr], T[tr], M[tr], epochs=60)
+    xv = torch.from_numpy(X[va]).cuda()
+    tv = torch.from_numpy(T[va]).cuda()
+    mv = torch.from_numpy(M[va]).cuda()
     vloss, _ = mlp.loss_grad(xv, tv, mv)
     params = mlp.params()
     np.save(out / "tuned_table.npy", table)
@@ -303,9 +352,43 @@ def run(out: Path, iters: int = 30):
     rep = evaluate(params, table)
     rep.update({"train_records": int(len(tr)), "val_records": int(len(va)), "train_loss": hist,
                 "val_loss": float(vloss.item()), "sweep_seconds": time.time() - t0,
-                "grid_median_us": {f"{n}:{lb}:{dt}:{v}": t for (n, lb, dt, v), t in grid.items()}})
+                "records_by_kind": {str(k): int(sum(1 for r in records if r[0] == k)) for k in KINDS},
+                "grid_median_us": grid})
+    rep["margin"] = MARGIN
     (out / "selector_report.json").write_text(json.dumps(rep, indent=1))
-    print(json.dumps({k: rep[k] for k in ("time_over_best", "mean_regret", "learned_vs_tuned_time", "val_loss")}))
+    print(json.dumps({k: rep[k] for k in ("all", "allreduce", "alltoallv", "val_loss", "train_records")}))
+
+
+def load_packaged():
+    """(tuned table, MLP parameters) shipped with the package, or (None, None)."""
+    t, p = DATA / "tuned_table.npy", DATA / "mlp_params.npy"
+    if not (t.exists() and p.exists()):
+        return None, None
+    return np.load(t), np.load(p)
+
+
+def apply_policy(world, policy: str):
+    """Sets a world's selection policy: "plain" (DIRECT), "tuned" (packaged table), "learned" (packaged
+    network, in-kernel inference per call), "heuristic" (the library default)."""
+    if policy == "plain":
+        world.set_policy(-1, 0)
+        return
+    if policy == "heuristic":
+        world.set_policy(-1, 3)
+        return
+    table, params = load_packaged()
+    if table is None:
+        raise FileNotFoundError(f"no trained selector in {DATA}")
+    if policy == "tuned":
+        world.set_tuned_table(table)
+        world.set_policy(-1, 1)
+    elif policy == "learned":
+        world.set_tuned_table(table)
+        world.set_mlp(params)
+        world.set_tuning(gpumpi.TUNE_MLP_MARGIN, int(round(MARGIN * 1000)))
+        world.set_policy(-1, 2)
+    else:
+        raise ValueError(policy)
 
 
 if __name__ == "__main__":

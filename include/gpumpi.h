@@ -148,6 +148,8 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
 #define GPUMPI_TUNE_ENGINES 3
 #define GPUMPI_TUNE_COPY_CHUNK 4
 #define GPUMPI_TUNE_ENGINE_MIN_BYTES 5
+/* Learned policy: predicted log-time gain (in 1/1000) the network needs to override the tuned table. */
+#define GPUMPI_TUNE_MLP_MARGIN 6
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Tuned table: int8 [3][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; log2 bytes per
  * rank; log2 ranks) -> variant or -1, host memory; a [2][32][16] table leaves Alltoall(v) untuned. */

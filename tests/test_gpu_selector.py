@@ -96,3 +96,33 @@ def test_learned_and_tuned_policies_drive_allreduce(gpulib, oracle):
         torch.cuda.synchronize()
         assert np.array_equal(r.cpu().numpy(), ref)
         assert set(w.read_trace()["variant"].tolist()) == {1}
+
+
+def test_packaged_policies_give_exact_integer_results(gpulib, oracle):
+    """The trained table and network shipped with the package drive real calls: every policy's choice
+    is exact on integer Allreduce and Alltoallv."""
+    from gpumpi import selector
+    table, params = selector.load_packaged()
+    assert table is not None and table.shape == (3, 32, 16) and params.shape == (gpulib.MLP_NPARAMS,)
+    n, count = 96, 3000
+    x = oracle.fill_i32(9, n * count).reshape(n, count) % 1000
+    ref = oracle.allreduce(x, 2, 2)
+    rng = np.random.default_rng(1)
+    sc = rng.integers(0, 60, (n, n)).astype(np.int32)
+    rc = sc.T.copy()
+    sd, rd = (np.cumsum(sc, 1) - sc).astype(np.int32), (np.cumsum(rc, 1) - rc).astype(np.int32)
+    S, R = int(sc.sum(1).max()), int(rc.sum(1).max())
+    y = oracle.fill_i32(10, n * S).reshape(n, S)
+    ref_a = oracle.alltoallv(y, sc, sd, R, rc, rd)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    with gpulib.World(n, timeout_s=20.0) as w:
+        for pol in ("plain", "tuned", "learned"):
+            selector.apply_policy(w, pol)
+            r = torch.zeros((n, count), dtype=torch.int32, device="cuda")
+            w.allreduce(dev(x), r, count, 2, 2)
+            torch.cuda.synchronize()
+            assert np.array_equal(r.cpu().numpy(), ref), pol
+            ra = torch.zeros((n, R), dtype=torch.int32, device="cuda")
+            w.alltoallv(dev(y), S * 4, dev(sc), dev(sd), ra, R * 4, dev(rc), dev(rd), 2)
+            torch.cuda.synchronize()
+            assert np.array_equal(ra.cpu().numpy(), ref_a), pol
