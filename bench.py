@@ -400,6 +400,57 @@ def bench_selector(gpumpi, torch, w_kw):
     return out
 
 
+def p2p_sweep(args, gpumpi, torch, local):
+    """Point-to-point sweep: ring (every rank sends to rank+1) and ping-pong (pairs 2k, 2k+1), blocking
+    MPI_Send/Recv and Isend/Irecv+Wait(all), 128..2048 ranks, 8 B .. 64 MiB in powers of two, fp32 payloads
+    uniform in [-1, 1) from a seed, 100 iterations per size.  Sizes are capped so send + receive buffers
+    stay within 24 GiB of device memory (2048 ranks: up to 4 MiB).  Received bytes are checked bit for bit;
+    per size: p50/p99 of rank 0's per-iteration time and GB/s = 2 x bytes sent per iteration / p50."""
+    import numpy as np
+    budget = 24 << 30
+    iters = 100
+    rows = []
+    for n in (128, 512, 1024, 2048):
+        with gpumpi.World(n, device=local, timeout_s=120.0) as w:
+            maxb = 1 << 26
+            while 2 * n * maxb > budget:
+                maxb //= 2
+            g = torch.Generator(device="cuda").manual_seed(n)
+            send = (torch.rand(n * maxb // 4, generator=g, device="cuda") * 2 - 1).view(torch.uint8)
+            recv = torch.empty_like(send)
+            b = 8
+            while b <= maxb:
+                s2 = send[: n * b].view(n, b)
+                r2 = recv[: n * b].view(n, b)
+                for pattern in ("ring", "pingpong"):
+                    for nb in (False, True):
+                        ns = np.zeros(iters, dtype=np.uint64)
+                        if pattern == "ring":
+                            r2.zero_()
+                            w.ring(s2, r2, b, iters=iters, nonblocking=nb, iter_ns=ns)
+                            expect = torch.roll(s2, 1, 0)
+                            moved = n * b
+                        else:
+                            r2.copy_(s2)
+                            w.pingpong(r2, b, n // 2, iters=iters, nonblocking=nb, iter_ns=ns)
+                            expect = s2.clone()
+                            expect[1::2] = s2[0::2]
+                            moved = 2 * (n // 2) * b
+                        bad = (r2 != expect).any(1).nonzero().flatten()
+                        p50, p99 = float(np.percentile(ns, 50)) / 1e3, float(np.percentile(ns, 99)) / 1e3
+                        row = {"pattern": pattern, "mode": "isend_irecv" if nb else "send_recv", "ranks": n,
+                               "bytes": b, "p50_us": p50, "p99_us": p99,
+                               "gbs": 2.0 * moved / (p50 * 1e-6) / 1e9, "bit_exact": bad.numel() == 0}
+                        if bad.numel():
+                            row["bad_ranks"] = bad[:8].tolist()
+                            row["bad_count"] = int(bad.numel())
+                        rows.append(row)
+                b *= 2
+            del send, recv
+            torch.cuda.empty_cache()
+    print(json.dumps({"case": "p2p_sweep", "iterations": iters, "rows": rows}), flush=True)
+
+
 def small_case(args, gpumpi, torch, local):
     """Allreduce fp32 SUM, 1024 ranks x 256 KiB (512 MiB of traffic per call): the profiled case."""
     n, count = 1024, 65536
@@ -423,7 +474,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extra", action="store_true")
-    ap.add_argument("--case", default="full", choices=["full", "small", "alltoallv_small"],
+    ap.add_argument("--case", default="full", choices=["full", "small", "alltoallv_small", "p2p_sweep"],
                     help="small: Allreduce 1024 ranks x 256 KiB; alltoallv_small: Alltoallv 1024 ranks x "
                          "256 KiB; device timing only (the ncu capture cases)")
     ap.add_argument("--variant", type=int, default=-1, help="variant override for the small cases")
@@ -444,6 +495,9 @@ def main():
         return
     if args.case == "alltoallv_small":
         small_alltoallv_case(args, gpumpi, torch, local)
+        return
+    if args.case == "p2p_sweep":
+        p2p_sweep(args, gpumpi, torch, local)
         return
     n, per = WORKLOAD["ranks"], WORKLOAD["bytes_per_rank"]
     count = per // 4

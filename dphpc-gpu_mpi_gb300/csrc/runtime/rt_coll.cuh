@@ -573,11 +573,26 @@ __device__ __noinline__ void copy_chunk(const JobParams* j, long long idx, int t
 __shared__ JobParams s_jp;
 
 __shared__ long long s_next_chunk;
+__shared__ int s_next_same_epoch;
 
-// Runs chunk idx of job jg, then keeps claiming and running chunks of the same job epoch until none is
-// left; thread 0 marks each chunk finished once every thread of the block is done with it (the barrier
-// orders the block's writes before thread 0's release).  One task per job and block keeps the call chain
-// (and its saved registers) out of the per-chunk path.
+// Claims one chunk like job_claim and also returns the epoch it belongs to.
+__device__ __forceinline__ long long job_claim_epoch(Job* j, unsigned* epoch) {
+    const unsigned long long t = atom_add_acqrel64(&j->next, 1ULL);
+    const unsigned e = (unsigned)(t >> 32);
+    const unsigned idx = (unsigned)t;
+    const unsigned long long lim = ld_acquire64(&j->limit);
+    if ((unsigned)(lim >> 32) != e || idx >= (unsigned)lim) return -1;
+    *epoch = e;
+    return idx;
+}
+
+// Runs chunk idx of job jg, then keeps claiming and running chunks until none is left; thread 0 marks
+// each chunk finished once every thread of the block is done with it (the barrier orders the block's
+// writes before thread 0's release).  One task per job and block keeps the call chain (and its saved
+// registers) out of the per-chunk path.  A job is reused: once its last chunk is finished its owner may
+// open the next epoch with new parameters, so a claim can return a chunk of a newer epoch than the
+// parameters in s_jp.  Such a chunk is not run here: the loop returns it in s_next_chunk and exec_chunk
+// reloads the parameters (stable while the chunk is unfinished) before running it.
 template <class F>
 __device__ __forceinline__ void chunk_loop(Job* jg, long long idx, int tid, int nt, F&& body) {
     for (;;) {
@@ -585,11 +600,13 @@ __device__ __forceinline__ void chunk_loop(Job* jg, long long idx, int tid, int 
         bar_sync(BAR_TASK, nt);
         if (tid == 0) {
             job_finish(jg);
-            s_next_chunk = job_claim(jg);
+            unsigned e = 0;
+            s_next_chunk = job_claim_epoch(jg, &e);
+            s_next_same_epoch = s_next_chunk >= 0 && e == s_jp.epoch;
         }
         bar_sync(BAR_TASK, nt);
         idx = s_next_chunk;
-        if (idx < 0) return;
+        if (idx < 0 || !s_next_same_epoch) return;
     }
 }
 
@@ -604,13 +621,20 @@ __device__ __noinline__ void copy_run(const JobParams* j, Job* jg, long long idx
 }
 
 __device__ __noinline__ void exec_chunk(Job* jg, long long idx, int tid, int nt) {
-    if (tid == 0) load_params(jg, s_jp);
-    bar_sync(BAR_TASK, nt);
-    const JobParams* j = &s_jp;
-    switch (j->kind) {
-    case JOB_COPY: copy_run(j, jg, idx, tid, nt); break;
-    case JOB_ALLREDUCE: case JOB_REDUCE: fold_run(j, jg, idx, tid, nt); break;
-    default: pull_run(j, jg, idx, tid, nt); break;
+    for (;;) {
+        // parameters of the epoch that chunk idx belongs to (the claim that returned it synchronised with
+        // the release that opened the epoch, and the epoch cannot end before this chunk is finished)
+        if (tid == 0) load_params(jg, s_jp);
+        bar_sync(BAR_TASK, nt);
+        const JobParams* j = &s_jp;
+        switch (j->kind) {
+        case JOB_COPY: copy_run(j, jg, idx, tid, nt); break;
+        case JOB_ALLREDUCE: case JOB_REDUCE: fold_run(j, jg, idx, tid, nt); break;
+        default: pull_run(j, jg, idx, tid, nt); break;
+        }
+        idx = s_next_chunk;  // -1, or a claimed chunk of a newer epoch
+        bar_sync(BAR_TASK, nt);  // every thread has read it before thread 0 reloads the parameters
+        if (idx < 0) return;
     }
 }
 

@@ -11,6 +11,7 @@ There is no CPU fallback: if libgpumpi.so is missing or no GPU is present, calls
 from __future__ import annotations
 
 import ctypes
+import sys
 import os
 from pathlib import Path
 
@@ -159,12 +160,21 @@ def _ptr(x):
     raise TypeError(f"unsupported buffer type {type(x)}")
 
 
+_CUDA_STREAM_LEGACY = 1   # cudaStreamLegacy: the default stream with its implicit synchronisation
+
+
 def _stream(s):
+    """The stream to launch on.  Default: torch's current stream when torch is in use, so a call is
+    ordered after the caller's earlier work on its tensors (the world's own stream is non-blocking and
+    would not be); torch's default stream (handle 0) is passed as the legacy default stream, because a
+    NULL stream means the world's own stream to the C ABI."""
     if s is None:
-        return None
-    if hasattr(s, "cuda_stream"):
-        return ctypes.c_void_p(s.cuda_stream)
-    return ctypes.c_void_p(int(s))
+        t = sys.modules.get("torch")
+        if t is None or not t.cuda.is_available() or not t.cuda.is_initialized():
+            return None
+        s = t.cuda.current_stream()
+    h = s.cuda_stream if hasattr(s, "cuda_stream") else int(s)
+    return ctypes.c_void_p(h if h else _CUDA_STREAM_LEGACY)
 
 
 class World:

@@ -2,7 +2,8 @@
  * gpumpi.h — host C ABI of the block-rank MPI runtime (libgpumpi.so).
  *
  * Plain C: opaque handles, plain pointers and sizes, no CUDA or torch types in the signatures
- * (streams are passed as void*, a cudaStream_t or NULL for the world's own stream).
+ * (streams are passed as void*, a cudaStream_t or NULL for the world's own stream; the world's stream is
+ * non-blocking, so a caller whose buffers were produced on another stream passes that stream).
  *
  * What each entry point replaces in the reference (lilyyangyn/dphpc-gpu_mpi):
  *   gpumpi_config_init / gpumpi_parse_args  <- parseGPUMPIArgs and its defaults,
