@@ -51,10 +51,12 @@ __device__ __noinline__ void copy_bytes(void* dst, const void* src, long long n,
     const char* s = (const char*)src;
     size_t mis = ((size_t)d ^ (size_t)s);
     int w = (mis & 15) == 0 ? 16 : (mis & 7) == 0 ? 8 : (mis & 3) == 0 ? 4 : 1;
-    if (w == 1 || n < 64) {
+    if (w == 1) {
         copy_bytes_slow(d, s, n, lane, nl);
         return;
     }
+    // (short copies take the same path: the byte loop's loads cannot move above its possibly aliasing
+    // stores, so a 16-byte eager payload would cost 16 dependent memory round trips instead of one)
     long long head = (long long)((w - ((size_t)s & (w - 1))) & (w - 1));
     if (head > n) head = n;
     long long body = (n - head) & ~(long long)(w - 1);
