@@ -32,7 +32,8 @@ VARIANT_AUTO, VARIANT_DIRECT, VARIANT_TREE, VARIANT_RING, VARIANT_STAGED = -1, 0
 VARIANT_NAMES = ["direct", "tree", "ring", "staged"]
 
 ERR_OTHER, ERR_TRUNCATE, ERR_TIMEOUT = 1, 12, 15
-TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES, TUNE_MLP_MARGIN = 1, 2, 3, 4, 5, 6
+TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES, TUNE_MLP_MARGIN, TUNE_DYN_SMEM = \
+    1, 2, 3, 4, 5, 6, 7
 
 TESTS = {
     "single_int": 1, "transfer_array": 2, "send_recv": 3, "repeat_send_recv": 4, "network_flood": 5,

@@ -151,6 +151,10 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
 #define GPUMPI_TUNE_ENGINE_MIN_BYTES 5
 /* Learned policy: predicted log-time gain (in 1/1000) the network needs to override the tuned table. */
 #define GPUMPI_TUNE_MLP_MARGIN 6
+/* Dynamic shared memory per rank block at most, in bytes (default 8192; -1 = all the SM leaves over).
+ * It holds the TMA stages of the STAGED variants and block-parallel user scratch; what it does not take
+ * stays L1 cache, which the executors' spilled registers and the ranks' private state use. */
+#define GPUMPI_TUNE_DYN_SMEM 7
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Tuned table: int8 [3][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; log2 bytes per
  * rank; log2 ranks) -> variant or -1, host memory; a [2][32][16] table leaves Alltoall(v) untuned. */

@@ -186,6 +186,7 @@ def test_alltoallv_piece_orders_and_shifts(gpulib, oracle, n, maxc, dt, npdt):
     x = oracle.fill_i32(n + 1, n * S).astype(npdt).reshape(n, S)
     ref = oracle.alltoallv(x, sc, sd, R, rc, rd)
     with gpulib.World(n, timeout_s=20.0, trace_capacity=64) as w:
+        w.set_tuning(gpulib.TUNE_DYN_SMEM, -1)   # room for the STAGED variant's shared-memory stages
         for v in range(4):
             w.set_policy(v, 0)
             s, r = dev(x), dev(np.zeros((n, R), npdt))
