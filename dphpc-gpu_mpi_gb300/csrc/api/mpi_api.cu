@@ -139,6 +139,7 @@ __device__ void engine_main() {
 }
 
 __device__ int is_rank_block() { return (int)blockIdx.x < g_rt->nranks; }
+__device__ void rank_begin() { p2p_rank_begin(); }
 
 }  // namespace gpumpi
 
@@ -621,7 +622,7 @@ __device__ int MPI_Irecv(void* buf, int count, MPI_Datatype datatype, int source
 }
 __device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int dest, int tag, MPI_Comm comm) {
     MPI_Request r = nullptr;
-    int rc = p2p_isend(buf, count, datatype, dest, tag, comm, &r, false);
+    int rc = p2p_isend(buf, count, datatype, dest, tag, comm, &r, false, /*blocking*/ true);
     int rw = r ? req_wait(&r, MPI_STATUS_IGNORE) : 0;
     return rc ? rc : rw;
 }
@@ -645,7 +646,7 @@ __device__ int MPI_Sendrecv(const void* sendbuf, int sendcount, MPI_Datatype sen
     // definition: a send and a receive executed concurrently
     MPI_Request rq[2] = {nullptr, nullptr};
     int rc = p2p_irecv(recvbuf, recvcount, recvtype, source, recvtag, comm, &rq[0]);
-    int rs = p2p_isend(sendbuf, sendcount, sendtype, dest, sendtag, comm, &rq[1], false);
+    int rs = p2p_isend(sendbuf, sendcount, sendtype, dest, sendtag, comm, &rq[1], false, /*blocking*/ true);
     int w0 = rq[0] ? req_wait(&rq[0], status) : 0;
     int w1 = rq[1] ? req_wait(&rq[1], MPI_STATUS_IGNORE) : 0;
     return rc ? rc : rs ? rs : w0 ? w0 : w1;
@@ -770,8 +771,9 @@ __device__ int MPI_Iprobe(int source, int tag, MPI_Comm comm, int* flag, MPI_Sta
     if (!c) return GPUMPI_ERR_COMM;
     progress();
     RankState* R = &g_rt->ranks[me()];
-    for (int i = 0; i < R->uq_count; i++) {
-        const Envelope& e = uq_at(i)->env;
+    for (int k = R->uq_head; k < R->uq_tail; k++) {
+        if (!uq_at(k)->live) continue;
+        const Envelope& e = uq_at(k)->env;
         if (e.ctx == c->ctx && (source == MPI_ANY_SOURCE || source == e.src) && (tag == MPI_ANY_TAG || tag == e.tag)) {
             *flag = 1;
             if (status) {
@@ -1222,10 +1224,10 @@ __device__ int new_type(const TypeDesc& d, MPI_Datatype* out) {
     TypeDesc* slot;
     int h = type_alloc(&slot);
     if (h < 0) return GPUMPI_ERR_NO_MEM;
-    int in_use = 1;
     *slot = d;
-    slot->in_use = in_use;
+    slot->in_use = 1;
     slot->committed = 0;
+    desc_prepare(slot);
     *out = (MPI_Datatype)h;
     return MPI_SUCCESS;
 }

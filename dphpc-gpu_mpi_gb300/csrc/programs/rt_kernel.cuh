@@ -15,6 +15,7 @@
 namespace gpumpi {
 __device__ void helper_loop();
 __device__ int is_rank_block();
+__device__ void rank_begin();
 __device__ void rank_finish(int rc);
 __device__ void engine_main();
 }  // namespace gpumpi
@@ -31,6 +32,7 @@ __global__ void __launch_bounds__(256, 4) gpumpi_rank_kernel(gpumpi_params prm) 
         return;
     }
     if (gpumpi::is_rank_block()) {
+        gpumpi::rank_begin();
         int rc = P::run(prm);
         gpumpi::rank_finish(rc);
     } else {

@@ -105,6 +105,11 @@ struct TypeDesc {
     long long stride[4];
     int committed;
     int in_use;
+    // set when the type is built (desc_prepare in rt_types.cuh):
+    unsigned fd_m[4];     // 32-bit division constants of size, block, cnt[0], cnt[1] (FastDiv)
+    unsigned fd_sh[4];    //   and their shifts, s1 | s2 << 8
+    int unit;             // largest power of two (<= 16) dividing block, size, extent, lb and the strides
+    int fd_ready;         // the 32-bit mapping applies: size < 2^31 and at most 3 levels
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -220,6 +225,7 @@ struct alignas(64) Envelope {
 struct UqEntry {
     Envelope env;
     int slot;              // payload slot index in the unexpected-payload pool (-1 if none)
+    int live;              // 0 once matched (the queue keeps arrival order without moving entries)
 };
 
 enum ReqKind { REQ_FREE = 0, REQ_SEND = 1, REQ_RECV = 2 };
@@ -271,8 +277,10 @@ struct alignas(128) RankState {
     unsigned long long mb_head;     // owner: advances with release; senders read for flow control
     char pad1[120];
     // owner-private below
-    int uq_count;
-    int nposted;
+    int uq_head;                    // unexpected queue: circular, entries [uq_head, uq_tail) in arrival
+    int uq_tail;                    // order, matched ones marked dead until the head passes them
+    int nposted;                    // posted receives: slots [posted_lo, nposted) of the rank's list in
+    int posted_lo;                  // posting order; matched slots hold -1 until trimmed
     int req_free_top;
     int ntypes;
     int initialized;

@@ -31,6 +31,47 @@ __device__ __forceinline__ int me() { return (int)blockIdx.x; }
 
 __device__ __forceinline__ bool block_addressable(const void* p) { return is_global_ptr(p) || is_shared_ptr(p); }
 
+// The rank's own copies of hot point-to-point state, in shared memory (thread 0 of the rank block is
+// their only user): the head of its envelope ring (the global copy is published for senders' flow
+// control) and a small cache of other rings' heads.  A cached head is a lower bound (heads only grow),
+// so a send re-reads the receiver's head only when the bound does not prove a free slot.
+constexpr int HEAD_CACHE = 16;
+struct RankFast {
+    unsigned long long mb_head;
+    unsigned long long hc_head[HEAD_CACHE];
+    int hc_rank[HEAD_CACHE];
+};
+__shared__ RankFast s_rf;
+
+// called by thread 0 of every rank block at the start of a launch (the ring heads are zero then)
+__device__ __forceinline__ void p2p_rank_begin() {
+    s_rf.mb_head = 0;
+    for (int i = 0; i < HEAD_CACHE; i++) {
+        s_rf.hc_rank[i] = -1;
+        s_rf.hc_head[i] = 0;
+    }
+}
+
+// Copy of n <= 128 bytes by the calling thread alone, with the widest accesses both addresses allow
+// (an out-of-line call would save and restore dozens of registers for a few bytes).  A global source
+// is read from L2 (another SM may have written it); local and shared sources with generic loads.
+template <class T>
+__device__ __forceinline__ void small_copy_t(char* d, const char* s, int n, bool g) {
+    if (g)
+        for (int i = 0; i < n; i += (int)sizeof(T)) *(T*)(d + i) = __ldcg((const T*)(s + i));
+    else
+        for (int i = 0; i < n; i += (int)sizeof(T)) *(T*)(d + i) = *(const T*)(s + i);
+}
+__device__ __forceinline__ void small_copy(void* dst, const void* src, int n) {
+    char* d = (char*)dst;
+    const char* s = (const char*)src;
+    const bool g = is_global_ptr(s);
+    const unsigned a = (unsigned)(size_t)d | (unsigned)(size_t)s | (unsigned)n;
+    if ((a & 7) == 0) small_copy_t<unsigned long long>(d, s, n, g);
+    else if ((a & 3) == 0) small_copy_t<unsigned>(d, s, n, g);
+    else small_copy_t<unsigned char>(d, s, n, g);
+}
+
 // Thread-0 entry to the copy engine: contiguous or typed copy of packed bytes [0, n).
 // Uses the whole block when both sides are addressable by it, a shared job for very large
 // contiguous global copies, and thread 0 alone for thread-local buffers.
@@ -101,14 +142,29 @@ __device__ void req_release(MPI_Request_impl* q) {
     g_rt->req_free[(size_t)me() * g_rt->pending + R->req_free_top++] = q->index;
 }
 
+// (the ring depth is a power of two, so the slot index is a mask, not a 64-bit division)
 __device__ __forceinline__ Envelope* ring_slot(int rank, unsigned long long t) {
-    return g_rt->ring + (size_t)rank * g_rt->mbox_depth + (t % (unsigned long long)g_rt->mbox_depth);
+    return g_rt->ring + (size_t)rank * g_rt->mbox_depth + (size_t)(t & (unsigned long long)(g_rt->mbox_depth - 1));
 }
 __device__ __forceinline__ unsigned char* ring_payload(int rank, unsigned long long t) {
-    return g_rt->ring_payload +
-           ((size_t)rank * g_rt->mbox_depth + (t % (unsigned long long)g_rt->mbox_depth)) * (size_t)g_rt->eager;
+    return g_rt->ring_payload + ((size_t)rank * g_rt->mbox_depth + (size_t)(t & (unsigned long long)(g_rt->mbox_depth - 1))) *
+                                    (size_t)g_rt->eager;
 }
-__device__ __forceinline__ UqEntry* uq_at(int i) { return g_rt->uq + (size_t)me() * g_rt->uq_depth + i; }
+// entry k (a monotonic position) of this rank's unexpected queue
+__device__ __forceinline__ UqEntry* uq_at(int k) { return g_rt->uq + (size_t)me() * g_rt->uq_depth + (k % g_rt->uq_depth); }
+
+// Makes room by moving the live entries of a full queue to its front, order kept (only when dead entries
+// are trapped behind a live one; removal never moves entries).
+__device__ __noinline__ void uq_compact(RankState* R) {
+    int w = R->uq_head;
+    for (int k = R->uq_head; k < R->uq_tail; k++) {
+        UqEntry* u = uq_at(k);
+        if (!u->live) continue;
+        if (w != k) *uq_at(w) = *u;
+        w++;
+    }
+    R->uq_tail = w;
+}
 __device__ __forceinline__ unsigned char* uq_payload(int slot) {
     return g_rt->uq_payload + ((size_t)me() * g_rt->uq_depth + slot) * (size_t)g_rt->eager;
 }
@@ -123,7 +179,8 @@ __device__ __noinline__ int complete_recv(MPI_Request_impl* q, const Envelope& e
     int err = e.bytes > q->bytes ? GPUMPI_ERR_TRUNCATE : 0;
     int rc = 0;
     if (e.flags & ENV_INLINE) {
-        rc = t0_copy(q->buf, q->desc, inl, nullptr, n);
+        if (!q->desc && n <= 128) small_copy(q->buf, inl, (int)n);
+        else rc = t0_copy(q->buf, q->desc, inl, nullptr, n);
     } else if (e.flags & ENV_HEAP) {
         rc = t0_copy(q->buf, q->desc, e.data, nullptr, n);
         free((void*)e.data);
@@ -140,9 +197,9 @@ __device__ __noinline__ int complete_recv(MPI_Request_impl* q, const Envelope& e
 }
 
 // Drains this rank's envelope ring: match posted receives in posting order, else queue as unexpected.
-__device__ __noinline__ int progress() {
+__device__ __noinline__ int progress_drain() {
     RankState* R = &g_rt->ranks[me()];
-    unsigned long long head = R->mb_head;
+    unsigned long long head = s_rf.mb_head;
     int* posted = g_rt->posted + (size_t)me() * g_rt->posted_cap;
     int rc = 0;
     for (;;) {
@@ -159,46 +216,74 @@ __device__ __noinline__ int progress() {
         e.count = __ldcg(&slot->count);
         e.flags = __ldcg(&slot->flags);
         e.world_src = __ldcg(&slot->world_src);
-        int match = -1;
-        for (int i = 0; i < R->nposted; i++) {
-            MPI_Request_impl* q = g_rt->reqs + (size_t)me() * g_rt->pending + posted[i];
-            if (env_matches(q, e.src, e.tag, e.ctx)) { match = i; break; }
+        int match = -1, qi = -1;
+        for (int i = R->posted_lo; i < R->nposted; i++) {
+            const int pi = posted[i];
+            if (pi < 0) continue;
+            MPI_Request_impl* q = g_rt->reqs + (size_t)me() * g_rt->pending + pi;
+            if (env_matches(q, e.src, e.tag, e.ctx)) {
+                match = i;
+                qi = pi;
+                break;
+            }
         }
         if (match >= 0) {
-            MPI_Request_impl* q = g_rt->reqs + (size_t)me() * g_rt->pending + posted[match];
-            for (int i = match; i + 1 < R->nposted; i++) posted[i] = posted[i + 1];
-            R->nposted--;
+            MPI_Request_impl* q = g_rt->reqs + (size_t)me() * g_rt->pending + qi;
+            // remove without moving the others: a hole, then trim holes at both ends
+            posted[match] = -1;
+            while (R->posted_lo < R->nposted && posted[R->posted_lo] < 0) R->posted_lo++;
+            while (R->nposted > R->posted_lo && posted[R->nposted - 1] < 0) R->nposted--;
+            if (R->posted_lo == R->nposted) R->posted_lo = R->nposted = 0;
             int r = complete_recv(q, e, ring_payload(me(), head));
             if (r) rc = r;
             if (q->freed) req_release(q);
         } else {
-            if (R->uq_count >= g_rt->uq_depth) break;  // unexpected queue full: leave it in the ring
-            UqEntry* u = uq_at(R->uq_count);
+            if (R->uq_tail - R->uq_head >= g_rt->uq_depth) {
+                uq_compact(R);
+                if (R->uq_tail - R->uq_head >= g_rt->uq_depth) break;  // full: leave it in the ring
+            }
+            UqEntry* u = uq_at(R->uq_tail);
             u->env = e;
             u->slot = -1;
+            u->live = 1;
             if ((e.flags & ENV_INLINE) && e.bytes > 0) {
                 int* fl = g_rt->uq_free + (size_t)me() * g_rt->uq_depth;
                 int s = R->uq_free_top > 0 ? fl[--R->uq_free_top] : R->uq_hwm++;
                 u->slot = s;
-                t0_copy(uq_payload(s), nullptr, ring_payload(me(), head), nullptr, e.bytes);
+                if (e.bytes <= 128) small_copy(uq_payload(s), ring_payload(me(), head), (int)e.bytes);
+                else t0_copy(uq_payload(s), nullptr, ring_payload(me(), head), nullptr, e.bytes);
             }
-            R->uq_count++;
+            R->uq_tail++;
         }
         head++;
+        s_rf.mb_head = head;
         st_release64(&R->mb_head, head);
     }
     return rc;
 }
 
-__device__ __forceinline__ void uq_remove(int i) {
+// Nothing to do unless the next envelope of this rank's ring has been published (one acquire load).
+__device__ __forceinline__ int progress() {
+    const unsigned long long h = s_rf.mb_head;
+    if (ld_acquire(&ring_slot(me(), h)->seq) != (unsigned)(h + 1)) return 0;
+    return progress_drain();
+}
+
+// Removes the entry at position k: it is marked dead, and the head moves past dead entries at the front.
+__device__ __forceinline__ void uq_remove(int k) {
     RankState* R = &g_rt->ranks[me()];
-    UqEntry* u = uq_at(i);
+    UqEntry* u = uq_at(k);
     if (u->slot >= 0) {
         int* fl = g_rt->uq_free + (size_t)me() * g_rt->uq_depth;
         fl[R->uq_free_top++] = u->slot;
     }
-    for (int k = i; k + 1 < R->uq_count; k++) *uq_at(k) = *uq_at(k + 1);
-    R->uq_count--;
+    u->live = 0;
+    if (k == R->uq_head) {
+        int h = k + 1;
+        while (h < R->uq_tail && !uq_at(h)->live) h++;
+        R->uq_head = h;
+        if (h == R->uq_tail) R->uq_head = R->uq_tail = 0;  // empty: positions restart (no overflow)
+    }
 }
 
 __device__ __forceinline__ MPI_Comm_impl* check_comm(MPI_Comm c) {
@@ -206,64 +291,85 @@ __device__ __forceinline__ MPI_Comm_impl* check_comm(MPI_Comm c) {
     return c;
 }
 
+// blocking: the caller waits for completion right away (MPI_Send); an eager send is complete when this
+// returns, so it needs no request and *out is set to MPI_REQUEST_NULL.
 __device__ __noinline__ int p2p_isend(const void* buf, long long count, int dt, int dest, int tag, MPI_Comm c,
-                         MPI_Request* out, bool sync) {
+                         MPI_Request* out, bool sync, bool blocking = false) {
+    if (out) *out = nullptr;
     if (!check_comm(c)) return GPUMPI_ERR_COMM;
     if (count < 0) return GPUMPI_ERR_COUNT;
     if (tag < 0) return GPUMPI_ERR_TAG;
-    MPI_Request_impl* q = req_alloc();
-    if (!q) {
-        record_error(GPUMPI_ERR_REQUEST, 0, __LINE__, g_rt->pending);
-        return GPUMPI_ERR_REQUEST;
+    const TypeDesc* d = (dest >= 0 && dest < c->size) ? resolve_type(dt) : nullptr;
+    const long long bytes = d ? count * d->size : 0;
+    const bool eager = d && bytes <= g_rt->eager && !sync;
+    MPI_Request_impl* q = nullptr;
+    if (!(eager && blocking)) {
+        q = req_alloc();
+        if (!q) {
+            record_error(GPUMPI_ERR_REQUEST, 0, __LINE__, g_rt->pending);
+            return GPUMPI_ERR_REQUEST;
+        }
+        q->kind = REQ_SEND;
+        q->comm = c;
+        q->tag = tag;
+        q->ctx = c->ctx;
+        if (out) *out = q;
     }
-    q->kind = REQ_SEND;
-    q->comm = c;
-    q->tag = tag;
-    q->ctx = c->ctx;
-    if (out) *out = q;
     if (dest == MPI_PROC_NULL) {
-        q->state = RS_DONE;
-        q->st_source = MPI_PROC_NULL;
+        if (q) {
+            q->state = RS_DONE;
+            q->st_source = MPI_PROC_NULL;
+        }
         return 0;
     }
     if (dest < 0 || dest >= c->size) {
-        q->state = RS_DONE;
+        if (q) q->state = RS_DONE;
         return GPUMPI_ERR_RANK;
     }
-    const TypeDesc* d = resolve_type(dt);
     if (!d) {
-        q->state = RS_DONE;
+        if (q) q->state = RS_DONE;
         return GPUMPI_ERR_TYPE;
     }
     const TypeDesc* sdesc = desc_contiguous(d) ? nullptr : d;
-    long long bytes = count * d->size;
     int dw = c->is_world ? dest : c->members[dest];
     int mycr = comm_rank_of(c, me());
-    q->peer = dw;
-    q->buf = (void*)buf;
-    q->bytes = bytes;
+    if (q) {
+        q->peer = dw;
+        q->buf = (void*)buf;
+        q->bytes = bytes;
+    }
     RankState* RD = &g_rt->ranks[dw];
     unsigned long long t = atomicAdd(&RD->mb_tail, 1ULL);
-    // flow control: wait for a free slot in the receiver's ring, draining our own meanwhile
-    if (t - ld_acquire64(&RD->mb_head) >= (unsigned long long)g_rt->mbox_depth) {
-        Deadline dl = make_deadline();
-        while (t - ld_acquire64(&RD->mb_head) >= (unsigned long long)g_rt->mbox_depth) {
-            progress();
-            if (int e = wait_tick(dl, __LINE__)) {
-                q->state = RS_DONE;
-                return e;
+    // flow control: the receiver's ring must have a free slot for ticket t; a cached head (a lower
+    // bound) usually proves it without reading the receiver's head
+    const unsigned long long depth = (unsigned long long)g_rt->mbox_depth;
+    const int hc = dw & (HEAD_CACHE - 1);
+    unsigned long long known = s_rf.hc_rank[hc] == dw ? s_rf.hc_head[hc] : 0;
+    if (t - known >= depth) {
+        known = ld_acquire64(&RD->mb_head);
+        if (t - known >= depth) {
+            Deadline dl = make_deadline();
+            while (t - (known = ld_acquire64(&RD->mb_head)) >= depth) {
+                progress();
+                if (int e = wait_tick(dl, __LINE__)) {
+                    if (q) q->state = RS_DONE;
+                    return e;
+                }
             }
         }
+        s_rf.hc_rank[hc] = dw;
+        s_rf.hc_head[hc] = known;
     }
     Envelope* slot = ring_slot(dw, t);
     int flags = 0;
     const void* data = nullptr;
     unsigned* flag = nullptr;
     const TypeDesc* edesc = nullptr;
-    if (bytes <= g_rt->eager && !sync) {
-        t0_copy(ring_payload(dw, t), nullptr, buf, sdesc, bytes);
+    if (eager) {
+        if (!sdesc && bytes <= 128) small_copy(ring_payload(dw, t), buf, (int)bytes);
+        else t0_copy(ring_payload(dw, t), nullptr, buf, sdesc, bytes);
         flags = ENV_INLINE;
-        q->state = RS_DONE;
+        if (q) q->state = RS_DONE;
     } else if (!is_global_ptr(buf)) {
         void* h = malloc(bytes > 0 ? bytes : 1);
         if (!h) {
@@ -337,14 +443,23 @@ __device__ __noinline__ int p2p_irecv(void* buf, long long count, int dt, int sr
     q->state = RS_ACTIVE;
     RankState* R = &g_rt->ranks[me()];
     // earliest matching unexpected message first
-    for (int i = 0; i < R->uq_count; i++) {
-        UqEntry* u = uq_at(i);
+    for (int k = R->uq_head; k < R->uq_tail; k++) {
+        UqEntry* u = uq_at(k);
+        if (!u->live) continue;
         if (env_matches(q, u->env.src, u->env.tag, u->env.ctx)) {
             Envelope e = u->env;
             int rc = complete_recv(q, e, u->slot >= 0 ? uq_payload(u->slot) : nullptr);
-            uq_remove(i);
+            uq_remove(k);
             return rc;
         }
+    }
+    if (R->nposted >= g_rt->posted_cap) {  // full: move the live entries to the front, order kept
+        int* posted = g_rt->posted + (size_t)me() * g_rt->posted_cap;
+        int w = 0;
+        for (int i = R->posted_lo; i < R->nposted; i++)
+            if (posted[i] >= 0) posted[w++] = posted[i];
+        R->posted_lo = 0;
+        R->nposted = w;
     }
     if (R->nposted >= g_rt->posted_cap) {
         record_error(GPUMPI_ERR_REQUEST, 1, __LINE__, g_rt->posted_cap);

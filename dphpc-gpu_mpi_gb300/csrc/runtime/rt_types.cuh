@@ -70,10 +70,45 @@ __device__ __forceinline__ long long desc_map(const TypeDesc* t, long long off) 
     return addr;
 }
 
+// Unsigned 32-bit division by a divisor fixed for the life of a datatype, as a multiply-high and two
+// shifts (division by invariant integers, Granlund & Montgomery 1994): with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0), t = mulhi(m, n),
+// exact for every 32-bit n.
+struct FastDiv {
+    unsigned m, s1, s2;
+    __device__ __forceinline__ void init(unsigned d) {
+        if (d == 0) d = 1;
+        const unsigned l = d > 1 ? 32u - (unsigned)__clz((int)(d - 1)) : 0u;
+        m = (unsigned)((((unsigned long long)1 << 32) * (((unsigned long long)1 << l) - d)) / d + 1);
+        s1 = l < 1 ? l : 1;
+        s2 = l > 1 ? l - 1 : 0;
+    }
+};
+
 __device__ __forceinline__ long long pow2_div(long long v) {  // largest power of two dividing v (<= 16)
     if (v == 0) return 16;
     long long a = v & -v;
     return a > 16 ? 16 : a;
+}
+
+// Completes a descriptor once its shape is final: the copy unit it allows and the division constants
+// of its 32-bit mapping, so that no copy divides by a variable.
+__device__ __forceinline__ void desc_prepare(TypeDesc* t) {
+    long long u = 16;
+    u = min(u, pow2_div(t->block));
+    u = min(u, pow2_div(t->size));
+    u = min(u, pow2_div(t->extent));
+    u = min(u, pow2_div(t->lb));
+    for (int l = 0; l < t->nlev; l++) u = min(u, pow2_div(t->stride[l]));
+    t->unit = (int)u;
+    const long long v[4] = {t->size, t->block, t->cnt[0], t->cnt[1]};
+    for (int k = 0; k < 4; k++) {
+        FastDiv f;
+        f.init(v[k] > 0 && v[k] <= 0x7fffffffLL ? (unsigned)v[k] : 1u);
+        t->fd_m[k] = f.m;
+        t->fd_sh[k] = f.s1 | (f.s2 << 8);
+    }
+    t->fd_ready = t->size >= 0 && t->size <= 0x7fffffffLL && t->nlev <= 3;
 }
 
 // Unit (1..16 bytes) that divides every block, stride, extent, offset and base address involved.
@@ -83,6 +118,10 @@ __device__ __forceinline__ int typed_unit(const TypeDesc* s, const void* sb, con
     for (int k = 0; k < 2; k++) {
         const TypeDesc* t = ts[k];
         if (!t) continue;
+        if (t->fd_ready) {
+            u = min(u, (long long)t->unit);
+            continue;
+        }
         u = min(u, pow2_div(t->block));
         u = min(u, pow2_div(t->size));
         u = min(u, pow2_div(t->extent));
@@ -94,60 +133,187 @@ __device__ __forceinline__ int typed_unit(const TypeDesc* s, const void* sb, con
     return (int)u;
 }
 
+template <int U> struct UnitType;
+template <> struct UnitType<16> { using T = uint4; };
+template <> struct UnitType<8> { using T = unsigned long long; };
+template <> struct UnitType<4> { using T = unsigned; };
+template <> struct UnitType<2> { using T = unsigned short; };
+template <> struct UnitType<1> { using T = unsigned char; };
+
 template <int U, bool CG>
-__device__ __forceinline__ void copy_unit(char* d, const char* s) {
-    if constexpr (U == 16) {
-        if constexpr (CG) __stcg((uint4*)d, __ldcg((const uint4*)s));
-        else *(uint4*)d = *(const uint4*)s;
-    } else if constexpr (U == 8) {
-        if constexpr (CG) __stcg((unsigned long long*)d, __ldcg((const unsigned long long*)s));
-        else *(unsigned long long*)d = *(const unsigned long long*)s;
-    } else if constexpr (U == 4) {
-        if constexpr (CG) __stcg((unsigned*)d, __ldcg((const unsigned*)s));
-        else *(unsigned*)d = *(const unsigned*)s;
-    } else if constexpr (U == 2) {
-        *(unsigned short*)d = *(const volatile unsigned short*)s;
+__device__ __forceinline__ typename UnitType<U>::T load_unit(const char* s) {
+    using T = typename UnitType<U>::T;
+    if constexpr (U >= 4) {
+        if constexpr (CG) return __ldcg((const T*)s);
+        else return *(const T*)s;
     } else {
-        *d = *(const volatile char*)s;
+        return *(const volatile T*)s;
     }
 }
 
+template <int U, bool CG>
+__device__ __forceinline__ void store_unit(char* d, typename UnitType<U>::T v) {
+    using T = typename UnitType<U>::T;
+    if constexpr (U >= 4 && CG) __stcg((T*)d, v);
+    else *(T*)d = v;
+}
+
+// ---- 32-bit mapping through a per-warp copy of the descriptor in shared memory ----
+// A copy group is one thread or whole warps, so each warp owns one slot pair.  Reading the fields from
+// shared memory at every use (volatile) keeps the loop's registers for the data in flight: with both
+// descriptors in registers the loop spills, and a spilled load serialises the memory round trips.
+struct DescS {
+    unsigned d[4], m[4], sh[4];  // size, block, cnt[0], cnt[1]: divisor, magic number, shifts
+    int nlev;
+    int same;                    // (destination slot) both sides have the same shape, lb aside
+    long long lb, extent, st[3];
+    long long shift;             // (destination slot) destination lb - source lb, when same
+};
+constexpr int kMaxWarps = 8;
+__shared__ DescS s_tdesc[kMaxWarps][2];
+
+__device__ __forceinline__ void descs_fill(DescS* o, const TypeDesc* t) {
+    const long long v[4] = {t->size, t->block, t->cnt[0], t->cnt[1]};
+    for (int k = 0; k < 4; k++) {
+        o->d[k] = v[k] > 0 && v[k] <= 0x7fffffffLL ? (unsigned)v[k] : 1u;
+        o->m[k] = t->fd_m[k];
+        o->sh[k] = t->fd_sh[k];
+    }
+    o->nlev = t->nlev;
+    o->lb = t->lb;
+    o->extent = t->extent;
+    for (int l = 0; l < 3; l++) o->st[l] = t->stride[l];
+}
+
+__device__ __forceinline__ bool same_shape(const TypeDesc* a, const TypeDesc* b) {
+    if (a->size != b->size || a->block != b->block || a->nlev != b->nlev || a->extent != b->extent) return false;
+    for (int l = 0; l < a->nlev; l++)
+        if (a->cnt[l] != b->cnt[l] || a->stride[l] != b->stride[l]) return false;
+    return true;
+}
+
+__device__ __forceinline__ unsigned fdiv_s(const volatile DescS* t, int k, unsigned n) {
+    const unsigned th = __umulhi(t->m[k], n);
+    const unsigned sh = t->sh[k];
+    return (th + ((n - th) >> (sh & 255u))) >> (sh >> 8);
+}
+
+// Byte address of packed offset off.  q < size = block * cnt[0] * ... * cnt[nlev-1], so the outermost
+// level's index is the last quotient and needs no division.
+__device__ __forceinline__ long long map_s(const volatile DescS* t, unsigned off) {
+    const unsigned e = fdiv_s(t, 0, off);
+    const unsigned q = off - e * t->d[0];
+    const unsigned blk = fdiv_s(t, 1, q);
+    long long a = t->lb + (long long)e * t->extent + (q - blk * t->d[1]);
+    const int nl = t->nlev;
+    if (nl == 1) {
+        a += (long long)blk * t->st[0];
+    } else if (nl == 2) {
+        const unsigned b1 = fdiv_s(t, 2, blk);
+        a += (long long)(blk - b1 * t->d[2]) * t->st[0] + (long long)b1 * t->st[1];
+    } else if (nl == 3) {
+        const unsigned b1 = fdiv_s(t, 2, blk);
+        const unsigned b2 = fdiv_s(t, 3, b1);
+        a += (long long)(blk - b1 * t->d[2]) * t->st[0] + (long long)(b1 - b2 * t->d[3]) * t->st[1] +
+             (long long)b2 * t->st[2];
+    }
+    return a;
+}
+
 // CG selects L2-only accesses; legal only when both buffers are in global memory.
+template <int U, bool CG>
+__device__ __noinline__ void typed_copy_fast(char* db, bool dmap, const char* sb, bool smap, unsigned b0, unsigned b1,
+                                             int lane, int nl) {
+    const volatile DescS* ss = &s_tdesc[threadIdx.x >> 5][0];
+    const volatile DescS* ds = &s_tdesc[threadIdx.x >> 5][1];
+    const bool same = smap && dmap && ds->same;
+    if (same) db += ds->shift;
+    const unsigned step = (unsigned)nl * U;
+    unsigned off = b0 + (unsigned)lane * U;
+    // K loads issued before the K stores: a strided unit is its own memory round trip, and a store
+    // followed by the next load would serialise them (the compiler cannot move a load above a store it
+    // cannot prove disjoint).
+    constexpr int K = 4;
+    using T = typename UnitType<U>::T;
+    for (; (unsigned long long)off + (K - 1) * (unsigned long long)step < b1; off += K * step) {
+        T v[K];
+        long long sa[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const unsigned o = off + k * step;
+            sa[k] = smap ? map_s(ss, o) : (long long)o;
+            v[k] = load_unit<U, CG>(sb + sa[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const unsigned o = off + k * step;
+            const long long da = same ? sa[k] : (dmap ? map_s(ds, o) : (long long)o);
+            store_unit<U, CG>(db + da, v[k]);
+        }
+    }
+    for (; off < b1; off += step) {
+        const long long sa = smap ? map_s(ss, off) : (long long)off;
+        const long long da = same ? sa : (dmap ? map_s(ds, off) : (long long)off);
+        store_unit<U, CG>(db + da, load_unit<U, CG>(sb + sa));
+    }
+}
+
+// The general form: 64-bit offsets, up to 4 levels, descriptors read through the pointers.
 template <int U, bool CG>
 __device__ __noinline__ void typed_copy_u(char* db, const TypeDesc* dt_, const char* sb, const TypeDesc* st_,
                                           long long b0, long long b1, int lane, int nl) {
     for (long long off = b0 + (long long)lane * U; off < b1; off += (long long)nl * U) {
         long long sa = st_ ? desc_map(st_, off) : off;
         long long da = dt_ ? desc_map(dt_, off) : off;
-        copy_unit<U, CG>(db + da, sb + sa);
+        store_unit<U, CG>(db + da, load_unit<U, CG>(sb + sa));
     }
 }
 
+#define GPUMPI_TYPED_SWITCH(F, CG, ...)                  \
+    switch (u) {                                         \
+    case 16: F<16, CG>(__VA_ARGS__); break;              \
+    case 8: F<8, CG>(__VA_ARGS__); break;                \
+    case 4: F<4, CG>(__VA_ARGS__); break;                \
+    case 2: F<2, CG>(__VA_ARGS__); break;                \
+    default: F<1, CG>(__VA_ARGS__); break;               \
+    }
+
 // Copy packed-stream bytes [b0, b1) from (sb, st) to (db, dt); a null descriptor means contiguous.
-// Executed by nl cooperating threads, this one being `lane`.
+// Executed by nl cooperating threads, this one being `lane`: one thread, or whole warps.
 __device__ __noinline__ void typed_copy(void* db, const TypeDesc* dt_, const void* sb, const TypeDesc* st_,
-                                           long long b0, long long b1, int lane, int nl) {
+                                        long long b0, long long b1, int lane, int nl) {
     int u = typed_unit(st_, sb, dt_, db);
     u = min(u, (int)pow2_div(b0));
     u = min(u, (int)pow2_div(b1));
     char* d = (char*)db;
     const char* s = (const char*)sb;
-    if (is_global_ptr(db) && is_global_ptr(sb)) {
-        switch (u) {
-        case 16: typed_copy_u<16, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
-        case 8: typed_copy_u<8, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
-        case 4: typed_copy_u<4, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
-        case 2: typed_copy_u<2, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
-        default: typed_copy_u<1, true>(d, dt_, s, st_, b0, b1, lane, nl); break;
+    const bool cg = is_global_ptr(db) && is_global_ptr(sb);
+    const bool fast = b1 <= 0x7fffffffLL && b0 >= 0 && (!st_ || st_->fd_ready) && (!dt_ || dt_->fd_ready) &&
+                      (nl == 1 || (nl & 31) == 0) && (threadIdx.x >> 5) < kMaxWarps;
+    if (fast) {
+        DescS* slot = s_tdesc[threadIdx.x >> 5];
+        if (nl > 1) __syncwarp();
+        if (nl == 1 || (threadIdx.x & 31) == 0) {
+            if (st_) descs_fill(&slot[0], st_);
+            if (dt_) descs_fill(&slot[1], dt_);
+            slot[1].same = st_ && dt_ && same_shape(st_, dt_);
+            slot[1].shift = slot[1].same ? dt_->lb - st_->lb : 0;
         }
+        if (nl > 1) __syncwarp();
+        const unsigned c0 = (unsigned)b0, c1 = (unsigned)b1;
+        if (cg) {
+            GPUMPI_TYPED_SWITCH(typed_copy_fast, true, d, dt_ != nullptr, s, st_ != nullptr, c0, c1, lane, nl)
+        } else {
+            GPUMPI_TYPED_SWITCH(typed_copy_fast, false, d, dt_ != nullptr, s, st_ != nullptr, c0, c1, lane, nl)
+        }
+        return;
+    }
+    if (cg) {
+        GPUMPI_TYPED_SWITCH(typed_copy_u, true, d, dt_, s, st_, b0, b1, lane, nl)
     } else {
-        switch (u) {
-        case 16: typed_copy_u<16, false>(d, dt_, s, st_, b0, b1, lane, nl); break;
-        case 8: typed_copy_u<8, false>(d, dt_, s, st_, b0, b1, lane, nl); break;
-        case 4: typed_copy_u<4, false>(d, dt_, s, st_, b0, b1, lane, nl); break;
-        default: typed_copy_u<1, false>(d, dt_, s, st_, b0, b1, lane, nl); break;
-        }
+        GPUMPI_TYPED_SWITCH(typed_copy_u, false, d, dt_, s, st_, b0, b1, lane, nl)
     }
 }
+#undef GPUMPI_TYPED_SWITCH
 
 }  // namespace gpumpi
