@@ -21,7 +21,7 @@ using namespace gpumpi;
 // globals of the MPI surface
 // ------------------------------------------------------------------------------------------------
 namespace gpumpi {
-__device__ Runtime* g_rt = nullptr;
+__constant__ Runtime c_rt;
 
 #define GPUMPI_PT(sz, dt) {sz, sz, 0, sz, 0, dt, {0, 0, 0, 0}, {0, 0, 0, 0}, 1, 1}
 __device__ TypeDesc g_predef_types[GPUMPI_NUM_PREDEFINED_TYPES] = {
@@ -68,7 +68,7 @@ namespace gpumpi {
 __shared__ Task s_task;
 
 __device__ void record_error(int code, int detail, int line, long long info) {
-    ErrorRecord* e = &g_rt->errors[blockIdx.x];
+    ErrorRecord* e = &c_rt.errors[blockIdx.x];
     if (e->code == 0) {
         e->code = code;
         e->detail = detail;
@@ -76,12 +76,12 @@ __device__ void record_error(int code, int detail, int line, long long info) {
         e->rank = (int)blockIdx.x;
         e->info = info;
     }
-    if (detail == GPUMPI_ERR_TIMEOUT || code == GPUMPI_ERR_INTERN) atomicExch(g_rt->abort_flag, 1u);
+    if (detail == GPUMPI_ERR_TIMEOUT || code == GPUMPI_ERR_INTERN) atomicExch(c_rt.abort_flag, 1u);
 }
 
-__device__ __noinline__ void execute_task(const Task& t, int tid, int nt) {
+__device__ __forceinline__ void execute_task(const Task& t, int tid, int nt) {
     switch (t.kind) {
-    case TASK_COPY: copy_bytes(t.p1, t.p0, t.n0, tid, nt); break;
+    case TASK_COPY: copy_bytes_inl(t.p1, t.p0, t.n0, tid, nt); break;
     case TASK_CHUNK: exec_chunk((Job*)t.p0, t.n0, tid, nt); break;
     case TASK_TYPED_COPY:
         typed_copy(t.p1, (const TypeDesc*)t.p4, t.p0, (const TypeDesc*)t.p2, t.n0, t.n1, tid, nt);
@@ -91,17 +91,23 @@ __device__ __noinline__ void execute_task(const Task& t, int tid, int nt) {
     }
 }
 
+__device__ __noinline__ void execute_task_call(const Task& t, int tid, int nt) { execute_task(t, tid, nt); }
+
+// Contiguous copies are latency-bound messages on the rank's critical path: in blocks of two or more
+// warps they run on warps 1.. only, so thread 0 waits at the barrier instead of entering the copy (whose
+// register saves and restores cost it about as much as a 1 KiB copy).  Typed copies, bound by their
+// address arithmetic, keep every warp.
+__device__ __forceinline__ bool copy_on_helpers(int kind, int nt) { return nt >= 64 && kind == TASK_COPY; }
+
 // Thread 0: run task t on the whole block and return when every thread has finished it.
 __device__ void dispatch(const Task& t) {
     const int nt = nthreads();
-    if (nt == 1) {
-        execute_task(t, 0, 1);
-        return;
+    if (nt > 1) {
+        s_task = t;
+        bar_sync(BAR_CMD, nt);
     }
-    s_task = t;
-    bar_sync(BAR_CMD, nt);
-    execute_task(t, 0, nt);
-    bar_sync(BAR_DONE, nt);
+    if (!copy_on_helpers(t.kind, nt)) execute_task_call(t, 0, nt);
+    if (nt > 1) bar_sync(BAR_DONE, nt);
 }
 
 // Threads 1..T-1: sleep on the command barrier, execute, report, until EXIT.
@@ -110,9 +116,13 @@ __device__ void helper_loop() {
     const int tid = (int)threadIdx.x;
     for (;;) {
         bar_sync(BAR_CMD, nt);
-        Task t = s_task;
-        if (t.kind == TASK_EXIT) return;
-        execute_task(t, tid, nt);
+        const int kind = s_task.kind;
+        if (kind == TASK_EXIT) return;
+        if (copy_on_helpers(kind, nt)) {
+            if (tid >= 32) execute_task(s_task, tid - 32, nt - 32);
+        } else {
+            execute_task(s_task, tid, nt);
+        }
         bar_sync(BAR_DONE, nt);
     }
 }
@@ -126,10 +136,10 @@ __device__ void release_helpers() {
 // Thread 0 of a rank block after the user program returned.
 __device__ void rank_finish(int rc) {
     release_helpers();
-    g_rt->exit_codes[blockIdx.x] = rc;
-    g_rt->ranks[blockIdx.x].exited = 1;
+    c_rt.exit_codes[blockIdx.x] = rc;
+    c_rt.ranks[blockIdx.x].exited = 1;
     __threadfence();
-    atomicAdd(g_rt->ranks_done, 1u);
+    atomicAdd(c_rt.ranks_done, 1u);
 }
 
 // Thread 0 of a copy-engine block.
@@ -138,7 +148,7 @@ __device__ void engine_main() {
     release_helpers();
 }
 
-__device__ int is_rank_block() { return (int)blockIdx.x < g_rt->nranks; }
+__device__ int is_rank_block() { return (int)blockIdx.x < c_rt.nranks; }
 __device__ void rank_begin() { p2p_rank_begin(); }
 
 }  // namespace gpumpi
@@ -194,8 +204,8 @@ __device__ int pick_vec(long long count, int T, int es, long long target, int al
         const int need = v * es >= 16 ? 16 : v * es;
         if (v > 1 && aligned < need) continue;
         if (stage_room < 2 * T * v * es) continue;
-        if (g_rt->tune_vec > 0) {
-            if (v == g_rt->tune_vec) return v;
+        if (c_rt.tune_vec > 0) {
+            if (v == c_rt.tune_vec) return v;
             continue;
         }
         const long long nch = (count + (long long)T * v - 1) / ((long long)T * v);
@@ -223,8 +233,8 @@ __device__ int pick_vec(long long count, int T, int es, long long target, int al
         const int need = v * es >= 16 ? 16 : v * es;
         if (v > 1 && aligned < need) continue;
         if (stage_room < 2 * T * v * es) continue;
-        if (g_rt->tune_vec > 0) {
-            if (v == g_rt->tune_vec) return v;
+        if (c_rt.tune_vec > 0) {
+            if (v == c_rt.tune_vec) return v;
             continue;
         }
         const long long nch = (count + (long long)T * v - 1) / ((long long)T * v);
@@ -259,26 +269,26 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
     const int n = c->size;
     int nchunks = 0;
     long long bytes = 0;
-    bool may_post = g_rt->nengines > 0;
+    bool may_post = c_rt.nengines > 0;
     if (a.kind == JOB_ALLREDUCE || a.kind == JOB_REDUCE) {
         j->count = a.count;
         bytes = a.count * a.esize * (long long)n;
         int variant = select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, a.variant);
-        may_post = may_post && bytes >= g_rt->engine_min_bytes;
-        long long target = n + (may_post ? g_rt->nengines : 0);
+        may_post = may_post && bytes >= c_rt.engine_min_bytes;
+        long long target = n + (may_post ? c_rt.nengines : 0);
         int vec = 1;
         j->tile = 0;
         if (variant == GPUMPI_VARIANT_STAGED) {
             // canonical order through shared-memory stages: needs 16-byte aligned buffers and room for
             // two stages of at least one rank
             const int es = a.esize;
-            const int stage_room = g_rt->dyn_smem - 128;
+            const int stage_room = c_rt.dyn_smem - 128;
             if (!fold_has_staged(a.dt, a.op, a.ufn) || j->aligned16 < 16 || stage_room < 2 * T * es) {
                 variant = GPUMPI_VARIANT_DIRECT;
             } else {
                 vec = pick_vec(a.count, T, es, target, 16, stage_room);
                 int G = stage_room / (2 * T * vec * es);
-                if (g_rt->tune_group > 0 && g_rt->tune_group < G) G = g_rt->tune_group;
+                if (c_rt.tune_group > 0 && c_rt.tune_group < G) G = c_rt.tune_group;
                 j->tile = G < 1 ? 1 : G > 64 ? 64 : G;
             }
         }
@@ -287,15 +297,15 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             // so that chunks x groups covers the blocks; partials and flags must fit the tree scratch
             const int es = a.esize;
             int v = (j->aligned16 >= 16) ? 16 / es : 1;
-            if (g_rt->tune_vec > 0) v = g_rt->tune_vec == 16 / es ? v : 1;
+            if (c_rt.tune_vec > 0) v = c_rt.tune_vec == 16 / es ? v : 1;
             const long long E = (long long)T * v;
             const long long C = (a.count + E - 1) / E;
             int R = 2;
             while (R < 16 && R * 2 <= n / 8 && C * R < target) R *= 2;
-            if (g_rt->tune_group > 0) R = g_rt->tune_group;
+            if (c_rt.tune_group > 0) R = c_rt.tune_group;
             const bool ok = fold_has_tree(a.dt, a.op, a.ufn) && c->is_world && n >= 16 && R >= 2 && R <= n &&
-                            (long long)R * a.count * es <= g_rt->tree_scratch_bytes && C * R <= g_rt->tree_flags_cap &&
-                            g_rt->tree_scratch && g_rt->tree_flags;
+                            (long long)R * a.count * es <= c_rt.tree_scratch_bytes && C * R <= c_rt.tree_flags_cap &&
+                            c_rt.tree_scratch && c_rt.tree_flags;
             if (ok) {
                 vec = v;
                 j->tile = R;
@@ -328,8 +338,8 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             variant = GPUMPI_VARIANT_DIRECT;
         j->variant = variant;
         bytes = a.est_piece * P;
-        may_post = may_post && bytes >= g_rt->engine_min_bytes;
-        long long target = n + (may_post ? g_rt->nengines : 0);
+        may_post = may_post && bytes >= c_rt.engine_min_bytes;
+        long long target = n + (may_post ? c_rt.nengines : 0);
         if (a.est_piece >= 65536) {
             int parts = (int)((a.est_piece + 65535) / 65536);
             j->vec = parts;
@@ -355,15 +365,15 @@ __device__ __noinline__ int coll_run(MPI_Comm_impl* c, const CollSlot& mine, con
     const unsigned e_next = c->job.epoch + 1;
     unsigned mis = (unsigned)((size_t)mine.sbuf | (size_t)mine.rbuf) & 15u;
     if (mis) atomicOr(&c->misalign[e_next & 1], mis);
-    RankState* R = &g_rt->ranks[me()];
+    RankState* R = &c_rt.ranks[me()];
     R->coll_calls++;
-    unsigned long long t0 = g_rt->trace_enabled ? now_ns() : 0;
+    unsigned long long t0 = c_rt.trace_enabled ? now_ns() : 0;
     int rc = comm_barrier(c, [&]() { coll_setup(c, a, e_next); }, line);
     if (rc) return rc;
     if (a.kind == JOB_BARRIER) return 0;
     rc = job_run_and_wait(&c->job, line);
     if (rc) return rc;
-    if (g_rt->trace_enabled && cr == 0) trace_record(c, a.kind, c->job.variant, a.dt, a.op,
+    if (c_rt.trace_enabled && cr == 0) trace_record(c, a.kind, c->job.variant, a.dt, a.op,
                                                     a.kind == JOB_ALLREDUCE || a.kind == JOB_REDUCE
                                                         ? a.count * a.esize : a.est_piece * c->size,
                                                     now_ns() - t0);
@@ -393,7 +403,7 @@ __shared__ MlpWork s_mlp;
 
 __device__ void mlp_infer_task(void* arg, int tid, int nt) {
     MlpWork* w = (MlpWork*)arg;
-    const float* p = g_rt->mlp_params;
+    const float* p = c_rt.mlp_params;
     constexpr int W1 = 0, B1 = 64 * 12, W2 = B1 + 64, B2 = W2 + 64 * 64, W3 = B2 + 64, B3 = W3 + 4 * 64;
     if (tid < 64) {
         float z = __ldcg(p + B1 + tid);
@@ -417,7 +427,7 @@ __device__ void mlp_infer_task(void* arg, int tid, int nt) {
 // Variant with the smallest predicted time; every member computes it from the same inputs with the
 // same operation order, so all members agree.  Cached per rank for repeated calls of one shape.
 __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, int dt, int op) {
-    RankState* R = &g_rt->ranks[me()];
+    RankState* R = &c_rt.ranks[me()];
     if (R->sel_key_kind == kind && R->sel_key_bytes == bytes && R->sel_key_n == n && R->sel_key_dt == dt &&
         R->sel_key_op == op)
         return R->sel_variant;
@@ -432,7 +442,7 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
         const int oslot = op == GPUMPI_OP_SUM ? 6 : op == GPUMPI_OP_MAX ? 7 : op == GPUMPI_OP_MIN ? 8 : 9;
         w->f[oslot] = 1.f;
     }
-    w->f[10] = (float)n / (float)(g_rt->nranks + g_rt->nengines);
+    w->f[10] = (float)n / (float)(c_rt.nranks + c_rt.nengines);
     w->f[11] = kind == JOB_REDUCE ? 1.f : kind == JOB_ALLTOALLV ? -1.f : 0.f;
     Task t;
     t.kind = TASK_USER;
@@ -444,10 +454,10 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
         if (w->y[v] < w->y[best]) best = v;
     // the tuned table is the fallback: its choice stands unless the network predicts a clear gain
     const int row = kind == JOB_ALLREDUCE ? 0 : kind == JOB_REDUCE ? 1 : kind == JOB_ALLTOALLV ? 2 : -1;
-    if (row >= 0 && g_rt->tuned_table) {
+    if (row >= 0 && c_rt.tuned_table) {
         const int b = clamp_i(ilog2_ll(bytes), 0, SEL_BYTES - 1), r = clamp_i(ilog2_ll(n), 0, SEL_RANKS - 1);
-        const int tv = g_rt->tuned_table[(row * SEL_BYTES + b) * SEL_RANKS + r];
-        if (tv >= 0 && tv < 4 && w->y[tv] <= w->y[best] + g_rt->mlp_margin) best = tv;
+        const int tv = c_rt.tuned_table[(row * SEL_BYTES + b) * SEL_RANKS + r];
+        if (tv >= 0 && tv < 4 && w->y[tv] <= w->y[best] + c_rt.mlp_margin) best = tv;
     }
     R->sel_key_kind = kind;
     R->sel_key_bytes = bytes;
@@ -499,8 +509,8 @@ __device__ __noinline__ int fold_collective(int kind, const void* sendbuf, void*
     a.esize = es;
     a.ufn = ufn;
     a.est_piece = 0;
-    a.variant = g_rt->variant_override;
-    if (a.variant < 0 && g_rt->selector_mode == 2 && g_rt->mlp_params)
+    a.variant = c_rt.variant_override;
+    if (a.variant < 0 && c_rt.selector_mode == 2 && c_rt.mlp_params)
         a.variant = learned_variant(kind, bytes, c->size, dt, opc);
     int rc = coll_run(c, my, a, __LINE__);
     stage_out(ss, false);
@@ -531,8 +541,8 @@ __device__ __noinline__ int pull_collective(int kind, MPI_Comm_impl* c, CollSlot
     a.esize = 0;
     a.ufn = nullptr;
     a.est_piece = est_piece;
-    a.variant = g_rt->variant_override;
-    if (a.variant < 0 && kind == JOB_ALLTOALLV && g_rt->selector_mode == 2 && g_rt->mlp_params)
+    a.variant = c_rt.variant_override;
+    if (a.variant < 0 && kind == JOB_ALLTOALLV && c_rt.selector_mode == 2 && c_rt.mlp_params)
         a.variant = learned_variant(kind, est_piece * c->size, c->size, my.stype, -1);
     int rc = coll_run(c, my, a, __LINE__);
     stage_out(ss, false);
@@ -556,7 +566,7 @@ __device__ long long sample_counts(const int* counts, int n) {
 __device__ int MPI_Init(int* argc, char*** argv) {
     (void)argc;
     (void)argv;
-    g_rt->ranks[me()].initialized = 1;
+    c_rt.ranks[me()].initialized = 1;
     return MPI_SUCCESS;
 }
 __device__ int MPI_Init_thread(int* argc, char*** argv, int required, int* provided) {
@@ -565,21 +575,21 @@ __device__ int MPI_Init_thread(int* argc, char*** argv, int required, int* provi
     return MPI_Init(argc, argv);
 }
 __device__ int MPI_Initialized(int* flag) {
-    *flag = g_rt->ranks[me()].initialized;
+    *flag = c_rt.ranks[me()].initialized;
     return MPI_SUCCESS;
 }
 __device__ int MPI_Finalize(void) {
-    g_rt->ranks[me()].finalized = 1;
+    c_rt.ranks[me()].finalized = 1;
     return MPI_Barrier(MPI_COMM_WORLD);
 }
 __device__ int MPI_Finalized(int* flag) {
-    *flag = g_rt->ranks[me()].finalized;
+    *flag = c_rt.ranks[me()].finalized;
     return MPI_SUCCESS;
 }
 __device__ int MPI_Abort(MPI_Comm comm, int errorcode) {
     (void)comm;
     record_error(GPUMPI_ERR_OTHER, errorcode, __LINE__, errorcode);
-    atomicExch(g_rt->abort_flag, 1u);
+    atomicExch(c_rt.abort_flag, 1u);
     return MPI_SUCCESS;
 }
 __device__ int MPI_Get_processor_name(char* name, int* resultlen) {
@@ -601,8 +611,8 @@ __device__ int gpumpi_block_parallel(void (*fn)(void*, int, int), void* arg) {
 }
 __device__ void gpumpi_block_sync(int nthreads) { bar_sync(BAR_TASK, nthreads); }
 __device__ void* gpumpi_block_scratch(size_t* bytes) {
-    if (bytes) *bytes = (size_t)g_rt->dyn_smem;
-    return g_rt->dyn_smem > 0 ? (void*)g_dyn_smem : nullptr;
+    if (bytes) *bytes = (size_t)c_rt.dyn_smem;
+    return c_rt.dyn_smem > 0 ? (void*)g_dyn_smem : nullptr;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -770,7 +780,7 @@ __device__ int MPI_Iprobe(int source, int tag, MPI_Comm comm, int* flag, MPI_Sta
     MPI_Comm_impl* c = check_comm(comm);
     if (!c) return GPUMPI_ERR_COMM;
     progress();
-    RankState* R = &g_rt->ranks[me()];
+    RankState* R = &c_rt.ranks[me()];
     for (int k = R->uq_head; k < R->uq_tail; k++) {
         if (!uq_at(k)->live) continue;
         const Envelope& e = uq_at(k)->env;
@@ -1421,18 +1431,19 @@ __device__ int MPI_Group_translate_ranks(MPI_Group g1, int n, const int ranks1[]
 extern "C" cudaError_t gpumpi_internal_install(Runtime* d_rt, MPI_Comm world, MPI_Group gworld, MPI_Group gempty,
                                                 cudaStream_t stream) {
     cudaError_t e;
-    if ((e = cudaMemcpyToSymbolAsync(g_rt, &d_rt, sizeof(d_rt), 0, cudaMemcpyHostToDevice, stream))) return e;
+    if ((e = cudaMemcpyToSymbolAsync(c_rt, d_rt, sizeof(Runtime), 0, cudaMemcpyDeviceToDevice, stream))) return e;
     if ((e = cudaMemcpyToSymbolAsync(MPI_COMM_WORLD, &world, sizeof(world), 0, cudaMemcpyHostToDevice, stream))) return e;
     if ((e = cudaMemcpyToSymbolAsync(MPI_GROUP_WORLD, &gworld, sizeof(gworld), 0, cudaMemcpyHostToDevice, stream))) return e;
     if ((e = cudaMemcpyToSymbolAsync(MPI_GROUP_EMPTY, &gempty, sizeof(gempty), 0, cudaMemcpyHostToDevice, stream))) return e;
     return cudaSuccess;
 }
 
-// The same from a device-resident array {Runtime*, world, group world, group empty}: device-to-device
-// copies only, so the sequence can be recorded in a CUDA graph and replayed later.
-extern "C" cudaError_t gpumpi_internal_install_dev(const void* const* d_vals, cudaStream_t stream) {
+// The same from device-resident sources (the runtime image and the array {world, group world, group
+// empty} at d_vals + 1): device-to-device copies only, so the sequence can be recorded in a CUDA graph
+// and replayed later.
+extern "C" cudaError_t gpumpi_internal_install_dev(const Runtime* d_rt, const void* const* d_vals, cudaStream_t stream) {
     cudaError_t e;
-    if ((e = cudaMemcpyToSymbolAsync(g_rt, d_vals + 0, sizeof(void*), 0, cudaMemcpyDeviceToDevice, stream))) return e;
+    if ((e = cudaMemcpyToSymbolAsync(c_rt, d_rt, sizeof(Runtime), 0, cudaMemcpyDeviceToDevice, stream))) return e;
     if ((e = cudaMemcpyToSymbolAsync(MPI_COMM_WORLD, d_vals + 1, sizeof(void*), 0, cudaMemcpyDeviceToDevice, stream)))
         return e;
     if ((e = cudaMemcpyToSymbolAsync(MPI_GROUP_WORLD, d_vals + 2, sizeof(void*), 0, cudaMemcpyDeviceToDevice, stream)))

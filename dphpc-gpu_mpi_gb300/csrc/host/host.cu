@@ -29,7 +29,7 @@ extern const int g_num_app_programs;
 
 extern "C" cudaError_t gpumpi_internal_install(Runtime* d_rt, MPI_Comm world, MPI_Group gworld, MPI_Group gempty,
                                                 cudaStream_t stream);
-extern "C" cudaError_t gpumpi_internal_install_dev(const void* const* d_vals, cudaStream_t stream);
+extern "C" cudaError_t gpumpi_internal_install_dev(const Runtime* d_rt, const void* const* d_vals, cudaStream_t stream);
 
 namespace {
 
@@ -626,7 +626,7 @@ int gpumpi_graph_create(gpumpi_world* w, int program, const gpumpi_params* param
     cudaError_t ce = cudaMemsetAsync(w->d_ctrl, 0, w->ctrl_bytes, cs);
     if (!ce) ce = cudaMemcpyAsync(w->d_fixed, g->d_fixed_img, sizeof(FixedImage), cudaMemcpyDeviceToDevice, cs);
     if (!ce) ce = cudaMemcpyAsync(w->d_rt, g->d_rt_img, sizeof(Runtime), cudaMemcpyDeviceToDevice, cs);
-    if (!ce) ce = gpumpi_internal_install_dev(g->d_install, cs);
+    if (!ce) ce = gpumpi_internal_install_dev(w->d_rt, g->d_install, cs);
     if (!ce) ce = pe->launch(w->cfg.nranks + w->nengines, w->T, w->dyn_smem, cs, params);
     e = cudaStreamEndCapture(cs, &g->graph);
     cudaStreamDestroy(cs);

@@ -76,8 +76,8 @@ __device__ __forceinline__ void job_finish(Job* j) { atom_add_acqrel64(&j->done,
 
 // Posts job j (epoch e) on the board so copy-engine blocks help with it.
 __device__ __forceinline__ void board_post(Job* j, unsigned e) {
-    Board* b = g_rt->board;
-    if (!b || g_rt->nengines <= 0) return;
+    Board* b = c_rt.board;
+    if (!b || c_rt.nengines <= 0) return;
     unsigned long long i = atomicAdd(&b->reserve, 1ULL);
     BoardEntry* en = &b->ring[i % (unsigned long long)b->cap];
     en->job = j;
@@ -99,9 +99,10 @@ __device__ __noinline__ int job_run_and_wait(Job* j, int line) {
     const unsigned long long target = ld_acquire64(&j->limit);  // (epoch << 32) | nchunks
     if (ld_acquire64(&j->done) == target) return 0;
     Deadline d = make_deadline();
-    while (ld_acquire64(&j->done) != target) {
+    while (ld_relaxed64(&j->done) != target) {
         if (int e = wait_tick(d, line, 128)) return e;
     }
+    fence_acqrel();
     return 0;
 }
 
@@ -119,9 +120,10 @@ __device__ int comm_barrier(MPI_Comm_impl* c, F&& setup, int line) {
         return 0;
     }
     Deadline d = make_deadline();
-    while (ld_acquire(&c->bar_gen) == g) {
+    while (ld_relaxed(&c->bar_gen) == g) {
         if (int e = wait_tick(d, line, 64)) return e;
     }
+    fence_acqrel();
     return 0;
 }
 
@@ -642,20 +644,21 @@ __device__ __noinline__ void exec_chunk(Job* jg, long long idx, int tid, int nt)
 // copy-engine loop (blocks >= nranks): claim chunks of any job posted on the board
 // ------------------------------------------------------------------------------------------------
 __device__ void engine_loop() {
-    Board* b = g_rt->board;
+    Board* b = c_rt.board;
     const unsigned long long cap = (unsigned long long)b->cap;
     unsigned long long cursor = 0;
     unsigned ns = 32;
     for (;;) {
         bool worked = false;
-        unsigned long long res = ld_acquire64(&b->reserve);
+        unsigned long long res = ld_relaxed64(&b->reserve);
         if (res > cap && res - cap > cursor) cursor = res - cap;
         for (unsigned long long i = cursor; i < res; i++) {
             BoardEntry* en = &b->ring[i % cap];
-            unsigned seq = ld_acquire(&en->seq);
+            unsigned seq = ld_relaxed(&en->seq);
             int diff = (int)(seq - (unsigned)(i + 1));
             if (diff < 0) break;             // not written yet
             if (diff == 0) {
+                fence_acqrel();
                 Job* j = (Job*)__ldcg((const unsigned long long*)&en->job);
                 const long long idx = job_claim(j);
                 if (idx >= 0) {  // the task claims the job's remaining chunks itself
@@ -669,7 +672,7 @@ __device__ void engine_loop() {
             }
             if (i == cursor) cursor++;
         }
-        if (ld_relaxed(g_rt->ranks_done) >= (unsigned)g_rt->nranks || ld_relaxed(g_rt->abort_flag)) return;
+        if (ld_relaxed(c_rt.ranks_done) >= (unsigned)c_rt.nranks || ld_relaxed(c_rt.abort_flag)) return;
         if (!worked) {
             __nanosleep(ns);
             ns = ns * 2 > 1024 ? 1024 : ns * 2;

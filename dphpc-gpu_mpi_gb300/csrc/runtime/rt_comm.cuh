@@ -18,9 +18,9 @@ namespace gpumpi {
 
 __device__ void* arena_alloc(unsigned long long bytes) {
     bytes = (bytes + 127) & ~127ULL;
-    unsigned long long off = atomicAdd(g_rt->arena_top, bytes);
-    if (off + bytes > g_rt->arena_bytes) return nullptr;
-    return g_rt->arena + off;
+    unsigned long long off = atomicAdd(c_rt.arena_top, bytes);
+    if (off + bytes > c_rt.arena_bytes) return nullptr;
+    return c_rt.arena + off;
 }
 
 struct SplitScan {
@@ -105,22 +105,22 @@ __device__ __noinline__ int comm_split_impl(MPI_Comm parent, int color, int key,
         if (newrank == 0) {
             obj = (MPI_Comm_impl*)arena_alloc(sizeof(MPI_Comm_impl));
             int* members = (int*)arena_alloc(sizeof(int) * (unsigned long long)newsize);
-            int* rank_of = (int*)arena_alloc(sizeof(int) * (unsigned long long)g_rt->nranks);
+            int* rank_of = (int*)arena_alloc(sizeof(int) * (unsigned long long)c_rt.nranks);
             CollSlot* slots = (CollSlot*)arena_alloc(sizeof(CollSlot) * (unsigned long long)newsize);
             if (!obj || !members || !rank_of || !slots) {
-                record_error(GPUMPI_ERR_NO_MEM, 0, __LINE__, (long long)g_rt->arena_bytes);
+                record_error(GPUMPI_ERR_NO_MEM, 0, __LINE__, (long long)c_rt.arena_bytes);
                 obj = nullptr;
             } else {
                 memset(obj, 0, sizeof(MPI_Comm_impl));
                 obj->size = newsize;
-                obj->ctx = (int)atomicAdd(g_rt->ctx_counter, 1u);
+                obj->ctx = (int)atomicAdd(c_rt.ctx_counter, 1u);
                 obj->is_world = 0;
                 obj->members = members;
                 obj->rank_of = rank_of;
                 obj->slots = slots;
                 obj->magic = COMM_MAGIC;
                 s_split.fill = rank_of;
-                s_split.fill_n = g_rt->nranks;
+                s_split.fill_n = c_rt.nranks;
                 dispatch(t);
             }
             __threadfence();
@@ -160,13 +160,13 @@ __device__ MPI_Group group_new(int n) {
 
 // ---- derived datatypes (per-rank table; handle encodes owner rank and slot) ----
 __device__ int type_alloc(TypeDesc** out) {
-    TypeDesc* tab = g_rt->types + (size_t)me() * g_rt->max_types;
-    for (int i = 0; i < g_rt->max_types; i++) {
+    TypeDesc* tab = c_rt.types + (size_t)me() * c_rt.max_types;
+    for (int i = 0; i < c_rt.max_types; i++) {
         if (!tab[i].in_use) {
             tab[i].in_use = 1;
             tab[i].committed = 0;
             *out = &tab[i];
-            return GPUMPI_DERIVED_BASE + me() * g_rt->max_types + i;
+            return GPUMPI_DERIVED_BASE + me() * c_rt.max_types + i;
         }
     }
     return -1;

@@ -45,7 +45,9 @@ __device__ __forceinline__ void copy_bytes_slow(char* d, const char* s, long lon
 }
 
 // Cooperative contiguous copy of n bytes; works for global and (same-block) shared addresses.
-__device__ __noinline__ void copy_bytes(void* dst, const void* src, long long n, int lane, int nl) {
+// Inlined into the block-task loop (an out-of-line call there costs its register saves and restores
+// in every helper thread, about as much as a 1 KiB copy); copy_bytes is the out-of-line form.
+__device__ __forceinline__ void copy_bytes_inl(void* dst, const void* src, long long n, int lane, int nl) {
     if (n <= 0) return;
     char* d = (char*)dst;
     const char* s = (const char*)src;
@@ -73,6 +75,10 @@ __device__ __noinline__ void copy_bytes(void* dst, const void* src, long long n,
         else copy_vec_body<unsigned, false>((unsigned*)(d + head), (const unsigned*)(s + head), body / 4, lane, nl);
     }
     for (long long i = lane; i < tail; i += nl) d[head + body + i] = s[head + body + i];
+}
+
+__device__ __noinline__ void copy_bytes(void* dst, const void* src, long long n, int lane, int nl) {
+    copy_bytes_inl(dst, src, n, lane, nl);
 }
 
 }  // namespace gpumpi

@@ -67,6 +67,16 @@ __device__ __forceinline__ unsigned long long atom_exch_release64(unsigned long 
 }
 __device__ __forceinline__ void fence_acqrel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
+// Spin-waits poll with relaxed loads and order what follows with one fence once the awaited value is
+// seen.  An acquire load or fence makes the SM drop its L1 contents, so acquire-polling from any block
+// (idle copy engines, a rank waiting for a message) would turn every cached read of the other blocks on
+// that SM (runtime tables, descriptors, spilled registers' lines) into an L2 round trip.
+__device__ __forceinline__ bool seen_u32(const unsigned* p, unsigned v) {
+    if (ld_relaxed(p) != v) return false;
+    fence_acqrel();
+    return true;
+}
+
 __device__ __forceinline__ unsigned long long now_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -405,8 +415,10 @@ struct Runtime {
     int clock_khz;
 };
 
-// The one runtime the current launch works on (set by the host before each launch).
-extern __device__ Runtime* g_rt;
+// The one runtime the current launch works on, copied by the host into constant memory before each
+// launch (read-only on the device: its fields are sizes and pointers to the state arrays).  Constant
+// memory keeps these reads out of L1, which every acquire on the SM invalidates.
+extern __constant__ Runtime c_rt;
 
 __device__ __forceinline__ int my_block() { return (int)blockIdx.x; }
 __device__ __forceinline__ int nthreads() { return (int)blockDim.x; }
@@ -423,7 +435,7 @@ struct Deadline {
 };
 __device__ __forceinline__ Deadline make_deadline() {
     Deadline d;
-    d.end = now_ns() + (unsigned long long)g_rt->timeout_ns;
+    d.end = now_ns() + (unsigned long long)c_rt.timeout_ns;
     d.spins = 0;
     d.ns = 0;
     return d;
@@ -432,7 +444,7 @@ __device__ __forceinline__ Deadline make_deadline() {
 // Backs off with nanosleep so idle waiters leave issue slots to working blocks.
 __device__ __forceinline__ int wait_tick(Deadline& d, int line, unsigned max_ns = 256) {
     if ((++d.spins & 31u) == 0) {
-        if (ld_relaxed(g_rt->abort_flag)) return GPUMPI_ERR_OTHER;
+        if (ld_relaxed(c_rt.abort_flag)) return GPUMPI_ERR_OTHER;
         if (now_ns() > d.end) {
             record_error(GPUMPI_ERR_OTHER, GPUMPI_ERR_TIMEOUT, line, 0);
             return GPUMPI_ERR_OTHER;

@@ -83,14 +83,14 @@ __device__ __noinline__ int t0_copy(void* dst, const TypeDesc* dd, const void* s
         else typed_copy(dst, dd, src, sd, 0, n, 0, 1);
         return 0;
     }
-    if (!dd && !sd && is_global_ptr(dst) && is_global_ptr(src) && g_rt->nengines > 0 &&
-        n >= g_rt->engine_min_bytes) {
-        Job* j = &g_rt->ranks[me()].p2p_job;
+    if (!dd && !sd && is_global_ptr(dst) && is_global_ptr(src) && c_rt.nengines > 0 &&
+        n >= c_rt.engine_min_bytes) {
+        Job* j = &c_rt.ranks[me()].p2p_job;
         j->kind = JOB_COPY;
         j->src = src;
         j->dst = dst;
         j->count = n;
-        j->chunk = g_rt->copy_chunk_bytes;
+        j->chunk = c_rt.copy_chunk_bytes;
         int nch = (int)((n + j->chunk - 1) / j->chunk);
         unsigned e = job_open(j, nch);
         if (nch > 1) board_post(j, e);
@@ -117,13 +117,13 @@ __device__ __noinline__ int t0_copy(void* dst, const TypeDesc* dd, const void* s
 
 // ---- request pool ----
 __device__ __noinline__ MPI_Request_impl* req_alloc() {
-    RankState* R = &g_rt->ranks[me()];
-    int* fl = g_rt->req_free + (size_t)me() * g_rt->pending;
+    RankState* R = &c_rt.ranks[me()];
+    int* fl = c_rt.req_free + (size_t)me() * c_rt.pending;
     int idx;
     if (R->req_free_top > 0) idx = fl[--R->req_free_top];
-    else if (R->req_hwm < g_rt->pending) idx = R->req_hwm++;
+    else if (R->req_hwm < c_rt.pending) idx = R->req_hwm++;
     else return nullptr;
-    MPI_Request_impl* q = g_rt->reqs + (size_t)me() * g_rt->pending + idx;
+    MPI_Request_impl* q = c_rt.reqs + (size_t)me() * c_rt.pending + idx;
     q->index = idx;
     q->done_flag = 0;
     q->freed = 0;
@@ -136,22 +136,22 @@ __device__ __noinline__ MPI_Request_impl* req_alloc() {
 }
 
 __device__ void req_release(MPI_Request_impl* q) {
-    RankState* R = &g_rt->ranks[me()];
+    RankState* R = &c_rt.ranks[me()];
     q->kind = REQ_FREE;
     q->state = RS_IDLE;
-    g_rt->req_free[(size_t)me() * g_rt->pending + R->req_free_top++] = q->index;
+    c_rt.req_free[(size_t)me() * c_rt.pending + R->req_free_top++] = q->index;
 }
 
 // (the ring depth is a power of two, so the slot index is a mask, not a 64-bit division)
 __device__ __forceinline__ Envelope* ring_slot(int rank, unsigned long long t) {
-    return g_rt->ring + (size_t)rank * g_rt->mbox_depth + (size_t)(t & (unsigned long long)(g_rt->mbox_depth - 1));
+    return c_rt.ring + (size_t)rank * c_rt.mbox_depth + (size_t)(t & (unsigned long long)(c_rt.mbox_depth - 1));
 }
 __device__ __forceinline__ unsigned char* ring_payload(int rank, unsigned long long t) {
-    return g_rt->ring_payload + ((size_t)rank * g_rt->mbox_depth + (size_t)(t & (unsigned long long)(g_rt->mbox_depth - 1))) *
-                                    (size_t)g_rt->eager;
+    return c_rt.ring_payload + ((size_t)rank * c_rt.mbox_depth + (size_t)(t & (unsigned long long)(c_rt.mbox_depth - 1))) *
+                                    (size_t)c_rt.eager;
 }
 // entry k (a monotonic position) of this rank's unexpected queue
-__device__ __forceinline__ UqEntry* uq_at(int k) { return g_rt->uq + (size_t)me() * g_rt->uq_depth + (k % g_rt->uq_depth); }
+__device__ __forceinline__ UqEntry* uq_at(int k) { return c_rt.uq + (size_t)me() * c_rt.uq_depth + (k % c_rt.uq_depth); }
 
 // Makes room by moving the live entries of a full queue to its front, order kept (only when dead entries
 // are trapped behind a live one; removal never moves entries).
@@ -166,7 +166,7 @@ __device__ __noinline__ void uq_compact(RankState* R) {
     R->uq_tail = w;
 }
 __device__ __forceinline__ unsigned char* uq_payload(int slot) {
-    return g_rt->uq_payload + ((size_t)me() * g_rt->uq_depth + slot) * (size_t)g_rt->eager;
+    return c_rt.uq_payload + ((size_t)me() * c_rt.uq_depth + slot) * (size_t)c_rt.eager;
 }
 
 __device__ __forceinline__ bool env_matches(const MPI_Request_impl* q, int src, int tag, int ctx) {
@@ -198,9 +198,9 @@ __device__ __noinline__ int complete_recv(MPI_Request_impl* q, const Envelope& e
 
 // Drains this rank's envelope ring: match posted receives in posting order, else queue as unexpected.
 __device__ __noinline__ int progress_drain() {
-    RankState* R = &g_rt->ranks[me()];
+    RankState* R = &c_rt.ranks[me()];
     unsigned long long head = s_rf.mb_head;
-    int* posted = g_rt->posted + (size_t)me() * g_rt->posted_cap;
+    int* posted = c_rt.posted + (size_t)me() * c_rt.posted_cap;
     int rc = 0;
     for (;;) {
         Envelope* slot = ring_slot(me(), head);
@@ -220,7 +220,7 @@ __device__ __noinline__ int progress_drain() {
         for (int i = R->posted_lo; i < R->nposted; i++) {
             const int pi = posted[i];
             if (pi < 0) continue;
-            MPI_Request_impl* q = g_rt->reqs + (size_t)me() * g_rt->pending + pi;
+            MPI_Request_impl* q = c_rt.reqs + (size_t)me() * c_rt.pending + pi;
             if (env_matches(q, e.src, e.tag, e.ctx)) {
                 match = i;
                 qi = pi;
@@ -228,7 +228,7 @@ __device__ __noinline__ int progress_drain() {
             }
         }
         if (match >= 0) {
-            MPI_Request_impl* q = g_rt->reqs + (size_t)me() * g_rt->pending + qi;
+            MPI_Request_impl* q = c_rt.reqs + (size_t)me() * c_rt.pending + qi;
             // remove without moving the others: a hole, then trim holes at both ends
             posted[match] = -1;
             while (R->posted_lo < R->nposted && posted[R->posted_lo] < 0) R->posted_lo++;
@@ -238,16 +238,16 @@ __device__ __noinline__ int progress_drain() {
             if (r) rc = r;
             if (q->freed) req_release(q);
         } else {
-            if (R->uq_tail - R->uq_head >= g_rt->uq_depth) {
+            if (R->uq_tail - R->uq_head >= c_rt.uq_depth) {
                 uq_compact(R);
-                if (R->uq_tail - R->uq_head >= g_rt->uq_depth) break;  // full: leave it in the ring
+                if (R->uq_tail - R->uq_head >= c_rt.uq_depth) break;  // full: leave it in the ring
             }
             UqEntry* u = uq_at(R->uq_tail);
             u->env = e;
             u->slot = -1;
             u->live = 1;
             if ((e.flags & ENV_INLINE) && e.bytes > 0) {
-                int* fl = g_rt->uq_free + (size_t)me() * g_rt->uq_depth;
+                int* fl = c_rt.uq_free + (size_t)me() * c_rt.uq_depth;
                 int s = R->uq_free_top > 0 ? fl[--R->uq_free_top] : R->uq_hwm++;
                 u->slot = s;
                 if (e.bytes <= 128) small_copy(uq_payload(s), ring_payload(me(), head), (int)e.bytes);
@@ -265,16 +265,16 @@ __device__ __noinline__ int progress_drain() {
 // Nothing to do unless the next envelope of this rank's ring has been published (one acquire load).
 __device__ __forceinline__ int progress() {
     const unsigned long long h = s_rf.mb_head;
-    if (ld_acquire(&ring_slot(me(), h)->seq) != (unsigned)(h + 1)) return 0;
+    if (ld_relaxed(&ring_slot(me(), h)->seq) != (unsigned)(h + 1)) return 0;
     return progress_drain();
 }
 
 // Removes the entry at position k: it is marked dead, and the head moves past dead entries at the front.
 __device__ __forceinline__ void uq_remove(int k) {
-    RankState* R = &g_rt->ranks[me()];
+    RankState* R = &c_rt.ranks[me()];
     UqEntry* u = uq_at(k);
     if (u->slot >= 0) {
-        int* fl = g_rt->uq_free + (size_t)me() * g_rt->uq_depth;
+        int* fl = c_rt.uq_free + (size_t)me() * c_rt.uq_depth;
         fl[R->uq_free_top++] = u->slot;
     }
     u->live = 0;
@@ -301,12 +301,12 @@ __device__ __noinline__ int p2p_isend(const void* buf, long long count, int dt, 
     if (tag < 0) return GPUMPI_ERR_TAG;
     const TypeDesc* d = (dest >= 0 && dest < c->size) ? resolve_type(dt) : nullptr;
     const long long bytes = d ? count * d->size : 0;
-    const bool eager = d && bytes <= g_rt->eager && !sync;
+    const bool eager = d && bytes <= c_rt.eager && !sync;
     MPI_Request_impl* q = nullptr;
     if (!(eager && blocking)) {
         q = req_alloc();
         if (!q) {
-            record_error(GPUMPI_ERR_REQUEST, 0, __LINE__, g_rt->pending);
+            record_error(GPUMPI_ERR_REQUEST, 0, __LINE__, c_rt.pending);
             return GPUMPI_ERR_REQUEST;
         }
         q->kind = REQ_SEND;
@@ -338,11 +338,11 @@ __device__ __noinline__ int p2p_isend(const void* buf, long long count, int dt, 
         q->buf = (void*)buf;
         q->bytes = bytes;
     }
-    RankState* RD = &g_rt->ranks[dw];
+    RankState* RD = &c_rt.ranks[dw];
     unsigned long long t = atomicAdd(&RD->mb_tail, 1ULL);
     // flow control: the receiver's ring must have a free slot for ticket t; a cached head (a lower
     // bound) usually proves it without reading the receiver's head
-    const unsigned long long depth = (unsigned long long)g_rt->mbox_depth;
+    const unsigned long long depth = (unsigned long long)c_rt.mbox_depth;
     const int hc = dw & (HEAD_CACHE - 1);
     unsigned long long known = s_rf.hc_rank[hc] == dw ? s_rf.hc_head[hc] : 0;
     if (t - known >= depth) {
@@ -412,7 +412,7 @@ __device__ __noinline__ int p2p_irecv(void* buf, long long count, int dt, int sr
     if (count < 0) return GPUMPI_ERR_COUNT;
     MPI_Request_impl* q = req_alloc();
     if (!q) {
-        record_error(GPUMPI_ERR_REQUEST, 0, __LINE__, g_rt->pending);
+        record_error(GPUMPI_ERR_REQUEST, 0, __LINE__, c_rt.pending);
         return GPUMPI_ERR_REQUEST;
     }
     q->kind = REQ_RECV;
@@ -441,7 +441,7 @@ __device__ __noinline__ int p2p_irecv(void* buf, long long count, int dt, int sr
     q->bytes = count * d->size;
     q->count = count;
     q->state = RS_ACTIVE;
-    RankState* R = &g_rt->ranks[me()];
+    RankState* R = &c_rt.ranks[me()];
     // earliest matching unexpected message first
     for (int k = R->uq_head; k < R->uq_tail; k++) {
         UqEntry* u = uq_at(k);
@@ -453,27 +453,28 @@ __device__ __noinline__ int p2p_irecv(void* buf, long long count, int dt, int sr
             return rc;
         }
     }
-    if (R->nposted >= g_rt->posted_cap) {  // full: move the live entries to the front, order kept
-        int* posted = g_rt->posted + (size_t)me() * g_rt->posted_cap;
+    if (R->nposted >= c_rt.posted_cap) {  // full: move the live entries to the front, order kept
+        int* posted = c_rt.posted + (size_t)me() * c_rt.posted_cap;
         int w = 0;
         for (int i = R->posted_lo; i < R->nposted; i++)
             if (posted[i] >= 0) posted[w++] = posted[i];
         R->posted_lo = 0;
         R->nposted = w;
     }
-    if (R->nposted >= g_rt->posted_cap) {
-        record_error(GPUMPI_ERR_REQUEST, 1, __LINE__, g_rt->posted_cap);
+    if (R->nposted >= c_rt.posted_cap) {
+        record_error(GPUMPI_ERR_REQUEST, 1, __LINE__, c_rt.posted_cap);
         q->state = RS_DONE;
         return GPUMPI_ERR_REQUEST;
     }
-    g_rt->posted[(size_t)me() * g_rt->posted_cap + R->nposted++] = q->index;
+    c_rt.posted[(size_t)me() * c_rt.posted_cap + R->nposted++] = q->index;
     return progress();
 }
 
 // Non-blocking completion check; returns true when q is complete.
 __device__ __forceinline__ bool req_poll(MPI_Request_impl* q) {
     if (q->state == RS_DONE) return true;
-    if (q->kind == REQ_SEND && ld_acquire(&q->done_flag)) {
+    if (q->kind == REQ_SEND && ld_relaxed(&q->done_flag)) {
+        fence_acqrel();
         q->state = RS_DONE;
         return true;
     }
@@ -499,7 +500,7 @@ __device__ __noinline__ int req_wait(MPI_Request* rp, MPI_Status* st) {
         Deadline dl = make_deadline();
         while (!req_poll(q)) {
             progress();
-            if (int e = wait_tick(dl, __LINE__)) return e;
+            if (int e = wait_tick(dl, __LINE__, 32)) return e;
         }
     }
     int err = q->st_error;

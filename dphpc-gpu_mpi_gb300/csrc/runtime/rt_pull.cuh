@@ -229,7 +229,7 @@ struct SegRec {
 constexpr int SP_HDR = 128 + 2 * 32 * (int)sizeof(SegRec);  // 2 mbarriers (padded) + 2 segment tables
 
 __device__ __forceinline__ int staged_pull_stage_bytes(int nt) {
-    const int q = (g_rt->dyn_smem / (nt >> 5)) & ~127;
+    const int q = (c_rt.dyn_smem / (nt >> 5)) & ~127;
     const int h = ((q - SP_HDR) / 2) & ~127;
     return h;
 }
@@ -237,7 +237,7 @@ __device__ __forceinline__ int staged_pull_stage_bytes(int nt) {
 // `warp` selects this warp's shared-memory region; the warp moves share wi of nwk of [u0, u1)
 __device__ __noinline__ bool staged_copy(PTab t, long long u0, long long u1, int lane, int warp, int nw, int wi,
                                          int nwk) {
-    const int q = (g_rt->dyn_smem / nw) & ~127;
+    const int q = (c_rt.dyn_smem / nw) & ~127;
     const int H = ((q - SP_HDR) / 2) & ~127;
     const long long per = (u1 - u0 + nwk - 1) / nwk;
     const long long wb = min(u1, u0 + per * wi), we = min(u1, wb + per);

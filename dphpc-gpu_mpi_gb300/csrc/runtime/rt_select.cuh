@@ -21,22 +21,22 @@ __device__ int select_variant(int kind, long long bytes_per_rank, int n, int dt,
     if (override_v >= 0 && override_v < GPUMPI_NUM_VARIANTS) return override_v;
     const int k = kind == JOB_ALLREDUCE ? 0 : kind == JOB_REDUCE ? 1 : kind == JOB_ALLTOALLV ? 2 : -1;
     if (k < 0) return GPUMPI_VARIANT_DIRECT;
-    if (g_rt->selector_mode == 1 && g_rt->tuned_table) {
+    if (c_rt.selector_mode == 1 && c_rt.tuned_table) {
         int b = clamp_i(ilog2_ll(bytes_per_rank), 0, SEL_BYTES - 1);
         int r = clamp_i(ilog2_ll(n), 0, SEL_RANKS - 1);
-        int v = g_rt->tuned_table[(k * SEL_BYTES + b) * SEL_RANKS + r];
+        int v = c_rt.tuned_table[(k * SEL_BYTES + b) * SEL_RANKS + r];
         if (v >= 0 && v < GPUMPI_NUM_VARIANTS) return v;
     }
-    if (g_rt->selector_mode == 2 && g_rt->mlp_params) return mlp_select(kind, bytes_per_rank, n, dt, op);
+    if (c_rt.selector_mode == 2 && c_rt.mlp_params) return mlp_select(kind, bytes_per_rank, n, dt, op);
     return GPUMPI_VARIANT_DIRECT;
 }
 
 __device__ __forceinline__ void trace_record(const MPI_Comm_impl* c, int kind, int variant, int dt, int op,
                                              long long bytes, unsigned long long ns) {
-    if (!g_rt->trace || !g_rt->trace_count) return;
-    unsigned long long i = atomicAdd(g_rt->trace_count, 1ULL);
-    if (i >= (unsigned long long)g_rt->trace_cap) return;
-    TraceRec* r = &g_rt->trace[i];
+    if (!c_rt.trace || !c_rt.trace_count) return;
+    unsigned long long i = atomicAdd(c_rt.trace_count, 1ULL);
+    if (i >= (unsigned long long)c_rt.trace_cap) return;
+    TraceRec* r = &c_rt.trace[i];
     r->log2_bytes = bytes > 0 ? log2f((float)bytes) : 0.f;
     r->log2_ranks = log2f((float)c->size);
     r->kind = kind;

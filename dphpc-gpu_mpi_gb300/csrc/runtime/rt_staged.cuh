@@ -28,7 +28,7 @@ __device__ __forceinline__ void stage_issue(unsigned long long* bar, T* sdst, lo
         const T* src = (const T*)s_chunk.f.ptile[k0 + k] + e0;
         const unsigned long long s_off = (unsigned long long)((const unsigned char*)(sdst + (long long)k * E) - g_dyn_smem);
         const bool ok = (((unsigned long long)(size_t)src | s_off) & 15ull) == 0 && CB > 0 && (CB & 15u) == 0 &&
-                        s_off + CB <= (unsigned long long)g_rt->dyn_smem && is_global_ptr(src);
+                        s_off + CB <= (unsigned long long)c_rt.dyn_smem && is_global_ptr(src);
         if (!ok) {
             record_error(GPUMPI_ERR_INTERN, 2, __LINE__, (long long)s_off);
             s_stage_abort = 1;

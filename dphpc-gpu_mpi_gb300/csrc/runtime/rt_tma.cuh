@@ -9,7 +9,7 @@
 
 namespace gpumpi {
 
-// Dynamic shared memory of the rank kernel (size chosen per launch by the host; g_rt->dyn_smem).
+// Dynamic shared memory of the rank kernel (size chosen per launch by the host; c_rt.dyn_smem).
 extern __shared__ __align__(128) unsigned char g_dyn_smem[];
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -53,7 +53,7 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
 // Waits for the phase of parity `parity` to complete; false if it did not within the runtime timeout.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
     if (mbar_try_wait(bar, parity)) return true;
-    const unsigned long long end = now_ns() + (unsigned long long)g_rt->timeout_ns;
+    const unsigned long long end = now_ns() + (unsigned long long)c_rt.timeout_ns;
     for (unsigned i = 1;; i++) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((i & 63u) == 0 && now_ns() > end) return false;

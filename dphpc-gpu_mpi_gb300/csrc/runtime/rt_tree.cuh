@@ -59,8 +59,8 @@ __device__ __noinline__ void fold_tree(const JobParams* j, long long idx, int ti
     const long long count = j->count;
     const long long C = (count + E - 1) / E;
     const bool vec = j->aligned16 >= (int)(V * sizeof(T) >= 16 ? 16 : V * sizeof(T));
-    T* partial = (T*)g_rt->tree_scratch;
-    unsigned* flags = g_rt->tree_flags;
+    T* partial = (T*)c_rt.tree_scratch;
+    unsigned* flags = c_rt.tree_flags;
     T acc[V];
 #pragma unroll
     for (int q = 0; q < V; q++) acc[q] = T();
@@ -88,7 +88,7 @@ __device__ __noinline__ void fold_tree(const JobParams* j, long long idx, int ti
         s_tree_ok = 1;
         Deadline d = make_deadline();
         for (int g = 0; g < R; g++) {
-            while (ld_acquire(&flags[cc * R + g]) != j->epoch) {
+            while (ld_relaxed(&flags[cc * R + g]) != j->epoch) {
                 if (wait_tick(d, __LINE__, 256)) {
                     s_tree_ok = 0;
                     break;
@@ -96,6 +96,7 @@ __device__ __noinline__ void fold_tree(const JobParams* j, long long idx, int ti
             }
             if (!s_tree_ok) break;
         }
+        fence_acqrel();
     }
     bar_sync(BAR_TASK, nt);
     if (!s_tree_ok) return;

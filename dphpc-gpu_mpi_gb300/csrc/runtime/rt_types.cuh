@@ -41,9 +41,9 @@ __device__ __forceinline__ const TypeDesc* resolve_type(int dt) {
     if (dt >= 0 && dt < GPUMPI_NUM_PREDEFINED_TYPES) return &g_predef_types[dt];
     if (is_derived(dt)) {
         long long idx = (long long)dt - GPUMPI_DERIVED_BASE;
-        long long total = (long long)g_rt->nranks * g_rt->max_types;
+        long long total = (long long)c_rt.nranks * c_rt.max_types;
         if (idx < total) {
-            const TypeDesc* t = &g_rt->types[idx];
+            const TypeDesc* t = &c_rt.types[idx];
             if (t->in_use) return t;
         }
     }
@@ -222,7 +222,7 @@ __device__ __forceinline__ long long map_s(const volatile DescS* t, unsigned off
 
 // CG selects L2-only accesses; legal only when both buffers are in global memory.
 template <int U, bool CG>
-__device__ __noinline__ void typed_copy_fast(char* db, bool dmap, const char* sb, bool smap, unsigned b0, unsigned b1,
+__device__ __forceinline__ void typed_copy_fast(char* db, bool dmap, const char* sb, bool smap, unsigned b0, unsigned b1,
                                              int lane, int nl) {
     const volatile DescS* ss = &s_tdesc[threadIdx.x >> 5][0];
     const volatile DescS* ds = &s_tdesc[threadIdx.x >> 5][1];
