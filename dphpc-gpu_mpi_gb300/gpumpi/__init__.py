@@ -32,8 +32,8 @@ VARIANT_AUTO, VARIANT_DIRECT, VARIANT_TREE, VARIANT_RING, VARIANT_STAGED = -1, 0
 VARIANT_NAMES = ["direct", "tree", "ring", "staged"]
 
 ERR_OTHER, ERR_TRUNCATE, ERR_TIMEOUT = 1, 12, 15
-TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES, TUNE_MLP_MARGIN, TUNE_DYN_SMEM = \
-    1, 2, 3, 4, 5, 6, 7
+(TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES, TUNE_MLP_MARGIN, TUNE_DYN_SMEM,
+ TUNE_HOST_DIRECT) = 1, 2, 3, 4, 5, 6, 7, 8
 
 TESTS = {
     "single_int": 1, "transfer_array": 2, "send_recv": 3, "repeat_send_recv": 4, "network_flood": 5,
@@ -232,7 +232,8 @@ class World:
         self._check(lib().gpumpi_set_policy(self.h, variant, mode), "set_policy")
 
     def set_tuning(self, key: int, value: int):
-        """Autotuner knobs (TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES)."""
+        """Autotuner knobs (TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES,
+        TUNE_MLP_MARGIN, TUNE_DYN_SMEM) and TUNE_HOST_DIRECT (page-locked host buffers in place or staged)."""
         self._check(lib().gpumpi_set_tuning(self.h, key, value), "set_tuning")
 
     def set_tuned_table(self, table: np.ndarray):

@@ -21,8 +21,9 @@
  *                                               mpi_communication.c:10-55 (point-to-point benchmark)
  *   gpumpi_last_error                       <- CudaMPI::printLastError, gpu_libs/gpu_libc/assert.cu:58-71
  *
- * Buffers: every data pointer may be device memory or host memory (pageable or pinned); host memory
- * is staged through device memory inside the call (the host<->device copies are part of the call).
+ * Buffers: every data pointer may be device memory or host memory (pageable or pinned); pageable host
+ * memory is staged through device memory inside the call (the host<->device copies are part of the
+ * call), page-locked host memory is read and written in place by the kernel (GPUMPI_TUNE_HOST_DIRECT).
  * Rank-major layout: rank r's buffer starts at base + r * stride_bytes.
  * Return value: GPUMPI_SUCCESS (0) or an error code from gpumpi_abi.h; never aborts the process.
  */
@@ -155,6 +156,10 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
  * It holds the TMA stages of the STAGED variants and block-parallel user scratch; what it does not take
  * stays L1 cache, which the executors' spilled registers and the ranks' private state use. */
 #define GPUMPI_TUNE_DYN_SMEM 7
+/* GPUMPI_TUNE_HOST_DIRECT: 1 (default) = page-locked host buffers are read and written in place by the
+ * kernel through their device alias (every byte crosses the host link once, both directions at once;
+ * the STAGED variants then run as DIRECT); 0 = staged through device memory around the kernel. */
+#define GPUMPI_TUNE_HOST_DIRECT 8
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Tuned table: int8 [3][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; log2 bytes per
  * rank; log2 ranks) -> variant or -1, host memory; a [2][32][16] table leaves Alltoall(v) untuned. */

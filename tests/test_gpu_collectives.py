@@ -73,6 +73,33 @@ def test_allreduce_host_buffers_and_in_place(gpulib, oracle):
         assert np.array_equal(host(buf), ref)
 
 
+def test_pinned_host_buffers_in_place_and_staged(gpulib, oracle):
+    """Page-locked host buffers are read and written in place by the kernel (TUNE_HOST_DIRECT 1, the
+    default) or staged through device memory (0): both bit-exact, for a fold and for a pull, with every
+    variant requested (STAGED runs as DIRECT on host memory: no bulk copies from the host)."""
+    n, count = 64, 3000
+    x = make_input(oracle, n, count, np.int32, 11)   # integers: every variant's order gives the same sum
+    ref = oracle.allreduce(x, 2, 2)
+    rng = np.random.default_rng(3)
+    sc, sd, rc, rd, S, R = uneven_exchange(rng, n, 90, 0.2, min_c=0)
+    y = oracle.fill_i32(n + 2, n * S).reshape(n, S)
+    ref_v = oracle.alltoallv(y, sc, sd, R, rc, rd)
+    hx = torch.from_numpy(x).pin_memory()
+    hy = torch.from_numpy(y).pin_memory()
+    with gpulib.World(n, timeout_s=10.0) as w:
+        w.set_tuning(gpulib.TUNE_DYN_SMEM, -1)
+        for direct in (1, 0):
+            w.set_tuning(gpulib.TUNE_HOST_DIRECT, direct)
+            for v in range(4):
+                w.set_policy(v, 0)
+                out = torch.zeros(n, count, dtype=torch.int32).pin_memory()
+                w.allreduce(hx.numpy(), out.numpy(), count, 2, 2)
+                assert np.array_equal(out.numpy(), ref), (direct, v)
+                outv = torch.zeros(n, R, dtype=torch.int32).pin_memory()
+                w.alltoallv(hy.numpy(), S * 4, sc, sd, outv.numpy(), R * 4, rc, rd, 2)
+                assert np.array_equal(outv.numpy(), ref_v), (direct, v)
+
+
 def test_allreduce_variants_agree(gpulib, oracle):
     n, count = 64, 1 << 14
     x = make_input(oracle, n, count, np.float32, 9)
