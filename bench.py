@@ -331,9 +331,12 @@ def bench_batch(gpumpi, torch, w_kw):
     with gpumpi.World(n, **w_kw) as w:
         iters = 20
         ns = np.zeros(iters, dtype=np.uint64)
-        rc = apps.batch(w, tab, send, recv, iters=iters, dt=gpumpi.FLOAT, op=gpumpi.OP_SUM, iter_ns=ns)
+        setup = np.zeros(2, dtype=np.int64)
+        rc = apps.batch(w, tab, send, recv, iters=iters, dt=gpumpi.FLOAT, op=gpumpi.OP_SUM, iter_ns=ns,
+                        setup_ns=setup)
         if rc:
             return {"error": f"rc={rc}: {w.last_error()}"}
+        out["setup_us"] = {"group_calls": float(setup[0]) / 1e3, "comm_create": float(setup[1]) / 1e3}
         us = float(np.median(ns[2:])) / 1e3
         out["in_launch_us_per_batch_p50"] = us
         out["in_launch_gbs"] = 2.0 * payload / (us * 1e-6) / 1e9

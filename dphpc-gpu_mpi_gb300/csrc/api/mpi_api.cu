@@ -1352,7 +1352,7 @@ __device__ int MPI_Group_incl(MPI_Group group, int n, const int ranks[], MPI_Gro
     if (!g) return GPUMPI_ERR_NO_MEM;
     for (int i = 0; i < n; i++) {
         if (ranks[i] < 0 || ranks[i] >= group->size) {
-            free(g);
+            group_delete(g);
             return GPUMPI_ERR_RANK;
         }
         g->ranks[i] = group->ranks[ranks[i]];
@@ -1377,7 +1377,7 @@ __device__ int MPI_Group_range_incl(MPI_Group group, int n, int ranges[][3], MPI
         int first = ranges[i][0], last = ranges[i][1], stride = ranges[i][2];
         for (int r = first; stride > 0 ? r <= last : r >= last; r += stride) {
             if (r < 0 || r >= group->size) {
-                free(g);
+                group_delete(g);
                 return GPUMPI_ERR_RANK;
             }
             g->ranks[k++] = group->ranks[r];
@@ -1388,7 +1388,7 @@ __device__ int MPI_Group_range_incl(MPI_Group group, int n, int ranges[][3], MPI
 }
 __device__ int MPI_Group_free(MPI_Group* group) {
     if (group && *group && !(*group)->is_static) {
-        if (--(*group)->refcount <= 0) free(*group);
+        if (--(*group)->refcount <= 0) group_delete(*group);
     }
     if (group) *group = MPI_GROUP_NULL;
     return MPI_SUCCESS;

@@ -402,17 +402,29 @@ struct Batch {
         MPI_Group gw;
         if (!rc) rc = MPI_Comm_group(MPI_COMM_WORLD, &gw);
         MPI_Comm comms[MAX_BATCH_COMMS];
+        // setup_ns (optional): rank 0's time in the group calls and in MPI_Comm_create, summed
+        long long* setup_ns = (long long*)p.p[5];
+        long long t_group = 0, t_create = 0;
         for (int c = 0; c < ncomms; c++) {
             comms[c] = MPI_COMM_NULL;
             if (rc) continue;
             const int first = (int)tab[4 * c], size = (int)tab[4 * c + 1];
             int range[1][3] = {{first, first + size - 1, 1}};
             MPI_Group g;
+            const unsigned long long ta = gtime();
             rc = MPI_Group_range_incl(gw, 1, range, &g);
+            const unsigned long long tb = gtime();
             if (!rc) rc = MPI_Comm_create(MPI_COMM_WORLD, g, &comms[c]);
+            const unsigned long long tc = gtime();
             if (!rc) rc = MPI_Group_free(&g);
+            t_group += (long long)(tb - ta + gtime() - tc);
+            t_create += (long long)(tc - tb);
         }
         if (!rc) rc = MPI_Group_free(&gw);
+        if (rank == 0 && setup_ns) {
+            setup_ns[0] = t_group;
+            setup_ns[1] = t_create;
+        }
         long long* iter_ns = (long long*)p.p[6];
         for (int it = 0; it < iters && rc == 0; it++) {
             const unsigned long long t0 = gtime();

@@ -147,15 +147,57 @@ __device__ __noinline__ int comm_split_impl(MPI_Comm parent, int color, int key,
     return 0;
 }
 
-// ---- groups (rank-local objects on the device heap) ----
+// ---- groups: rank-local objects, from the rank's group pool (a stack: a freed block is reclaimed once
+// every block above it is freed too, which is the order MPI codes create and free groups in) or, when the
+// pool is full, from the device heap.  The heap allocator serialises concurrent callers: 512 ranks each
+// building a group per communicator spent about 1 ms per communicator in malloc and free. ----
+struct GroupBlock {
+    int prev1;   // 1 + offset of the block below (0: none)
+    int freed;
+    int pad[2];
+};
+
 __device__ MPI_Group group_new(int n) {
-    MPI_Group g = (MPI_Group)malloc(sizeof(MPI_Group_impl) + sizeof(int) * (n > 0 ? n : 1));
-    if (!g) return nullptr;
+    const unsigned long long body = sizeof(MPI_Group_impl) + sizeof(int) * (unsigned long long)(n > 0 ? n : 1);
+    const long long need = (long long)((sizeof(GroupBlock) + body + 15) & ~15ULL);
+    RankState* R = &c_rt.ranks[me()];
+    MPI_Group g = nullptr;
+    if (c_rt.group_pool && R->grp_top + need <= c_rt.group_pool_bytes) {
+        GroupBlock* b = (GroupBlock*)(c_rt.group_pool + (long long)me() * c_rt.group_pool_bytes + R->grp_top);
+        b->prev1 = R->grp_last1;
+        b->freed = 0;
+        R->grp_last1 = R->grp_top + 1;
+        R->grp_top += (int)need;
+        g = (MPI_Group)(b + 1);
+        g->pooled = 1;
+    } else {
+        g = (MPI_Group)malloc(body);
+        if (!g) return nullptr;
+        g->pooled = 0;
+    }
     g->size = n;
     g->ranks = (int*)(g + 1);
     g->refcount = 1;
     g->is_static = 0;
     return g;
+}
+
+// Releases a group object made by group_new.
+__device__ void group_delete(MPI_Group g) {
+    if (!g || g->is_static) return;
+    if (!g->pooled) {
+        free(g);
+        return;
+    }
+    ((GroupBlock*)g - 1)->freed = 1;
+    RankState* R = &c_rt.ranks[me()];
+    unsigned char* base = c_rt.group_pool + (long long)me() * c_rt.group_pool_bytes;
+    while (R->grp_last1 > 0) {
+        GroupBlock* top = (GroupBlock*)(base + (R->grp_last1 - 1));
+        if (!top->freed) break;
+        R->grp_top = R->grp_last1 - 1;
+        R->grp_last1 = top->prev1;
+    }
 }
 
 // ---- derived datatypes (per-rank table; handle encodes owner rank and slot) ----

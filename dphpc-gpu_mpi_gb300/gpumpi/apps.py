@@ -106,21 +106,25 @@ def batch_elements(tab: np.ndarray) -> int:
 
 
 def batch(world: World, tab: np.ndarray, send, recv, iters: int = 1, dt: int = 12, op: int = 2, iter_ns=None,
-          graph: bool = False):
+          graph: bool = False, setup_ns=None):
     """Runs the batch (every communicator's MPI_Allreduce, `iters` times) in one launch; with graph=True
-    returns a recorded Graph instead of running (replay with Graph.launch)."""
+    returns a recorded Graph instead of running (replay with Graph.launch).  setup_ns (2 int64, host)
+    receives rank 0's time in the group calls and in MPI_Comm_create, summed over the communicators."""
     import torch
     from . import P_BATCH
     dev = torch.device("cuda", torch.cuda.current_device())
     tab_d = torch.from_numpy(np.ascontiguousarray(tab, dtype=np.int64)).to(dev)
     rcs = torch.zeros(world.nranks, dtype=torch.int32, device=dev)
     ns = torch.zeros(max(1, iters), dtype=torch.int64, device=dev)
-    args = dict(i=(len(tab), iters, dt, op), p=(send, recv, tab_d, None, None, None, ns, rcs))
+    st = torch.zeros(2, dtype=torch.int64, device=dev)
+    args = dict(i=(len(tab), iters, dt, op), p=(send, recv, tab_d, None, None, st, ns, rcs))
     if graph:
         g = world.graph(P_BATCH, **args)
-        g._keep = (tab_d, rcs, ns)  # device buffers the recorded launch reads and writes
+        g._keep = (tab_d, rcs, ns, st)  # device buffers the recorded launch reads and writes
         return g
     rc = world.run_program(P_BATCH, **args)
     torch.cuda.synchronize()
     _copy_ns(ns, iter_ns)
+    if setup_ns is not None:
+        setup_ns[:2] = st.cpu().numpy()
     return _first_error(rc, rcs)

@@ -109,7 +109,8 @@ enum gpumpi_program {
     GPUMPI_P_HALO,
     GPUMPI_P_BATCH,            /* i[0]=communicators (<= 64) i[1]=iters i[2]=datatype i[3]=op
                                   p[0]=send base p[1]=recv base p[2]=int64 [comms][4] {first world rank,
-                                  size, count, element offset} p[6]=int64 ns per iteration p[7]=rc */
+                                  size, count, element offset} p[5]=int64[2] rank 0's setup ns (group
+                                  calls, MPI_Comm_create; may be NULL) p[6]=int64 ns per iteration p[7]=rc */
 };
 
 /* collective kinds for GPUMPI_P_COLL */
