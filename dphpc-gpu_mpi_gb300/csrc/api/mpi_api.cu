@@ -160,7 +160,8 @@ namespace {
 
 __device__ __forceinline__ const TypeDesc* tdesc(int dt) { return resolve_type(dt); }
 
-// Stages a buffer other ranks cannot address (thread 0's stack) into the device heap.
+// Stages a buffer other ranks cannot address (thread 0's stack) into the rank's scratch pool (the device
+// heap when it is full).
 struct Stage {
     void* heap = nullptr;
     void* user = nullptr;
@@ -168,7 +169,7 @@ struct Stage {
 };
 __device__ __noinline__ void* stage_in(Stage& s, const void* p, long long bytes, bool copy_in) {
     if (p == nullptr || p == MPI_IN_PLACE || is_global_ptr(p) || bytes <= 0) return (void*)p;
-    s.heap = malloc(bytes);
+    s.heap = scratch_alloc((unsigned long long)bytes);
     s.user = (void*)p;
     s.bytes = bytes;
     if (!s.heap) return nullptr;
@@ -178,7 +179,7 @@ __device__ __noinline__ void* stage_in(Stage& s, const void* p, long long bytes,
 __device__ __noinline__ void stage_out(Stage& s, bool copy_out) {
     if (!s.heap) return;
     if (copy_out) t0_copy(s.user, nullptr, s.heap, nullptr, s.bytes);
-    free(s.heap);
+    scratch_free(s.heap);
     s.heap = nullptr;
 }
 
@@ -939,7 +940,7 @@ __device__ int MPI_Alltoall(const void* sendbuf, int sendcount, MPI_Datatype sen
         sendtype = recvtype;
         st = rt;
         long long span = rt->lb + (long long)n * recvcount * rt->extent;
-        tmp.heap = malloc(span > 0 ? span : 1);
+        tmp.heap = scratch_alloc((unsigned long long)(span > 0 ? span : 1));
         if (!tmp.heap) return GPUMPI_ERR_NO_MEM;
         t0_copy(tmp.heap, nullptr, recvbuf, nullptr, span);
         sb = tmp.heap;
@@ -956,7 +957,7 @@ __device__ int MPI_Alltoall(const void* sendbuf, int sendcount, MPI_Datatype sen
     long long sspan = st->lb + (long long)n * sendcount * st->extent;
     long long rspan = rt->lb + (long long)n * recvcount * rt->extent;
     int rc = pull_collective(JOB_ALLTOALLV, c, my, sspan, rspan, (long long)sendcount * st->size, 0);
-    if (tmp.heap) free(tmp.heap);
+    scratch_free(tmp.heap);
     return rc;
 }
 

@@ -147,34 +147,67 @@ __device__ __noinline__ int comm_split_impl(MPI_Comm parent, int color, int key,
     return 0;
 }
 
-// ---- groups: rank-local objects, from the rank's group pool (a stack: a freed block is reclaimed once
-// every block above it is freed too, which is the order MPI codes create and free groups in) or, when the
-// pool is full, from the device heap.  The heap allocator serialises concurrent callers: 512 ranks each
-// building a group per communicator spent about 1 ms per communicator in malloc and free. ----
-struct GroupBlock {
+// ---- the rank's scratch pool: a stack in device memory (a freed block is reclaimed once every block above
+// it is freed too, the order in which MPI codes free groups and the library releases staging buffers).
+// Group objects and staged copies of thread-local buffers come from it; when it is full, from the device
+// heap, whose allocator serialises concurrent callers: 512 ranks each building a group per communicator
+// spent about 1 ms per communicator in malloc and free. ----
+struct PoolBlock {
     int prev1;   // 1 + offset of the block below (0: none)
     int freed;
     int pad[2];
 };
 
+__device__ __forceinline__ unsigned char* pool_base() {
+    return c_rt.group_pool + (long long)me() * c_rt.group_pool_bytes;
+}
+
+// 16-byte aligned scratch of `bytes` from this rank's pool, or nullptr when it does not fit.
+__device__ void* pool_alloc(unsigned long long bytes) {
+    const long long need = (long long)((sizeof(PoolBlock) + bytes + 15) & ~15ULL);
+    RankState* R = &c_rt.ranks[me()];
+    if (!c_rt.group_pool || R->grp_top + need > c_rt.group_pool_bytes) return nullptr;
+    PoolBlock* b = (PoolBlock*)(pool_base() + R->grp_top);
+    b->prev1 = R->grp_last1;
+    b->freed = 0;
+    R->grp_last1 = R->grp_top + 1;
+    R->grp_top += (int)need;
+    return b + 1;
+}
+
+__device__ __forceinline__ bool pool_owns(const void* p) {
+    const unsigned char* b = pool_base();
+    return c_rt.group_pool && (const unsigned char*)p >= b && (const unsigned char*)p < b + c_rt.group_pool_bytes;
+}
+
+__device__ void pool_free(void* p) {
+    ((PoolBlock*)p - 1)->freed = 1;
+    RankState* R = &c_rt.ranks[me()];
+    unsigned char* base = pool_base();
+    while (R->grp_last1 > 0) {
+        PoolBlock* top = (PoolBlock*)(base + (R->grp_last1 - 1));
+        if (!top->freed) break;
+        R->grp_top = R->grp_last1 - 1;
+        R->grp_last1 = top->prev1;
+    }
+}
+
+// Scratch from the pool, else the device heap; release with scratch_free.
+__device__ void* scratch_alloc(unsigned long long bytes) {
+    void* p = pool_alloc(bytes);
+    return p ? p : malloc(bytes ? bytes : 1);
+}
+__device__ void scratch_free(void* p) {
+    if (!p) return;
+    if (pool_owns(p)) pool_free(p);
+    else free(p);
+}
+
+// ---- groups (rank-local objects) ----
 __device__ MPI_Group group_new(int n) {
     const unsigned long long body = sizeof(MPI_Group_impl) + sizeof(int) * (unsigned long long)(n > 0 ? n : 1);
-    const long long need = (long long)((sizeof(GroupBlock) + body + 15) & ~15ULL);
-    RankState* R = &c_rt.ranks[me()];
-    MPI_Group g = nullptr;
-    if (c_rt.group_pool && R->grp_top + need <= c_rt.group_pool_bytes) {
-        GroupBlock* b = (GroupBlock*)(c_rt.group_pool + (long long)me() * c_rt.group_pool_bytes + R->grp_top);
-        b->prev1 = R->grp_last1;
-        b->freed = 0;
-        R->grp_last1 = R->grp_top + 1;
-        R->grp_top += (int)need;
-        g = (MPI_Group)(b + 1);
-        g->pooled = 1;
-    } else {
-        g = (MPI_Group)malloc(body);
-        if (!g) return nullptr;
-        g->pooled = 0;
-    }
+    MPI_Group g = (MPI_Group)scratch_alloc(body);
+    if (!g) return nullptr;
     g->size = n;
     g->ranks = (int*)(g + 1);
     g->refcount = 1;
@@ -184,20 +217,7 @@ __device__ MPI_Group group_new(int n) {
 
 // Releases a group object made by group_new.
 __device__ void group_delete(MPI_Group g) {
-    if (!g || g->is_static) return;
-    if (!g->pooled) {
-        free(g);
-        return;
-    }
-    ((GroupBlock*)g - 1)->freed = 1;
-    RankState* R = &c_rt.ranks[me()];
-    unsigned char* base = c_rt.group_pool + (long long)me() * c_rt.group_pool_bytes;
-    while (R->grp_last1 > 0) {
-        GroupBlock* top = (GroupBlock*)(base + (R->grp_last1 - 1));
-        if (!top->freed) break;
-        R->grp_top = R->grp_last1 - 1;
-        R->grp_last1 = top->prev1;
-    }
+    if (g && !g->is_static) scratch_free(g);
 }
 
 // ---- derived datatypes (per-rank table; handle encodes owner rank and slot) ----

@@ -274,7 +274,6 @@ struct MPI_Group_impl {
     int* ranks;                // group rank -> world rank
     int refcount;
     int is_static;
-    int pooled;                // allocated from the rank's group pool (else the device heap)
 };
 
 namespace gpumpi {
@@ -293,7 +292,7 @@ struct alignas(128) RankState {
     int nposted;                    // posted receives: slots [posted_lo, nposted) of the rank's list in
     int posted_lo;                  // posting order; matched slots hold -1 until trimmed
     int req_free_top;
-    int grp_top;                    // group pool: bytes in use, and 1 + offset of the last block
+    int grp_top;                    // scratch pool: bytes in use, and 1 + offset of the last block
     int grp_last1;                  //   (0: none); blocks are released from the top down
     int ntypes;
     int initialized;
@@ -400,7 +399,8 @@ struct Runtime {
     int* world_members;
     CollSlot* world_slots;
     Board* board;
-    unsigned char* group_pool;        // nranks * group_pool_bytes: each rank's MPI_Group objects
+    unsigned char* group_pool;        // nranks * group_pool_bytes: each rank's scratch pool (MPI_Group
+                                      // objects, staged copies of thread-local buffers)
     long long group_pool_bytes;
     unsigned char* arena;             // communicator objects created at run time
     unsigned long long arena_bytes;
