@@ -399,6 +399,21 @@ int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
     }
 }
 
+int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value) {
+    if (!w || !value) return GPUMPI_ERR_ARG;
+    switch (key) {
+    case GPUMPI_TUNE_VEC: *value = w->tune_vec; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_DYN_SMEM: *value = w->dyn_smem_cap; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_HOST_DIRECT: *value = w->host_direct; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_STAGE_GROUP: *value = w->tune_group; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_ENGINES: *value = w->cfg.engine_blocks; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_COPY_CHUNK: *value = w->h_rt.copy_chunk_bytes; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_ENGINE_MIN_BYTES: *value = w->h_rt.engine_min_bytes; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_MLP_MARGIN: *value = (long long)(w->h_rt.mlp_margin * 1e3f + 0.5f); return GPUMPI_SUCCESS;
+    default: return GPUMPI_ERR_ARG;
+    }
+}
+
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes) {
     // [kinds][32][16]: kinds 0 Allreduce, 1 Reduce, 2 Alltoall(v); a two-kind table leaves kind 2 unset
     if (!w || !table || (bytes != 2 * 32 * 16 && bytes != 3 * 32 * 16)) return GPUMPI_ERR_ARG;

@@ -112,6 +112,22 @@ __device__ void sort_gen_task(void* arg, int tid, int nt) {
     }
 }
 
+// Calls f(i, key) for this thread's keys i = tid, tid + nt, ... < count, loading KB keys before handling
+// any: the handler's atomics and stores may alias the keys as far as the compiler knows, so one key at a
+// time would cost a full memory round trip per key.
+template <int KB, class F>
+__device__ __forceinline__ void for_keys(const int* keys, long long count, int tid, int nt, F&& f) {
+    long long i = tid;
+    for (; i + (long long)(KB - 1) * nt < count; i += (long long)KB * nt) {
+        int k[KB];
+#pragma unroll
+        for (int j = 0; j < KB; j++) k[j] = __ldcg(keys + i + (long long)j * nt);
+#pragma unroll
+        for (int j = 0; j < KB; j++) f(i + (long long)j * nt, k[j]);
+    }
+    for (; i < count; i += nt) f(i, __ldcg(keys + i));
+}
+
 // bucket counts, send displacements and the packed send buffer (keys grouped by destination rank)
 __device__ void sort_pack_task(void* arg, int tid, int nt) {
     SortWork* w = (SortWork*)arg;
@@ -122,7 +138,8 @@ __device__ void sort_pack_task(void* arg, int tid, int nt) {
     if (!in_smem) bins = w->sc;
     for (int d = tid; d < n; d += nt) bins[d] = 0;
     gpumpi_block_sync(nt);
-    for (long long i = tid; i < w->kpr; i += nt) atomicAdd(&bins[((long long)w->keys[i] * n) >> KEY_BITS], 1);
+    for_keys<8>(w->keys, w->kpr, tid, nt,
+                 [&](long long, int k) { atomicAdd(&bins[((long long)k * n) >> KEY_BITS], 1); });
     gpumpi_block_sync(nt);
     int* sd = w->sc + n;
     for (int d = tid; d < n; d += nt) {
@@ -136,11 +153,11 @@ __device__ void sort_pack_task(void* arg, int tid, int nt) {
     int* cur = in_smem ? bins : w->sc + 3 * n;  // spare n ints of the scratch row when not in shared memory
     for (int d = tid; d < n; d += nt) cur[d] = sd[d];
     gpumpi_block_sync(nt);
-    for (long long i = tid; i < w->kpr; i += nt) {
-        const int k = w->keys[i];
+    int* send = w->send;
+    for_keys<8>(w->keys, w->kpr, tid, nt, [&](long long, int k) {
         const int pos = atomicAdd(&cur[((long long)k * n) >> KEY_BITS], 1);
-        w->send[pos] = k;
-    }
+        send[pos] = k;
+    });
 }
 
 __device__ void sort_rdispl_task(void* arg, int tid, int nt) {
@@ -162,11 +179,14 @@ __device__ void sort_local_task(void* arg, int tid, int nt) {
     if (!hist || sbytes < (size_t)w->range * sizeof(int)) hist = w->hist_global;
     for (int k = tid; k < w->range; k += nt) hist[k] = 0;
     gpumpi_block_sync(nt);
-    for (long long i = tid; i < w->nrecv; i += nt) {
-        const int k = w->recv[i] - w->lo;
-        if (k >= 0 && k < w->range) atomicAdd(&hist[k], 1);
-        else w->err = 1;
-    }
+    const int lo = w->lo, range = w->range;
+    bool bad = false;
+    for_keys<8>(w->recv, w->nrecv, tid, nt, [&](long long, int key) {
+        const int k = key - lo;
+        if (k >= 0 && k < range) atomicAdd(&hist[k], 1);
+        else bad = true;
+    });
+    if (bad) w->err = 1;
     gpumpi_block_sync(nt);
     // positions: exclusive prefix of the histogram by segments, then each thread writes its values' runs
     const int seg = (w->range + nt - 1) / nt;

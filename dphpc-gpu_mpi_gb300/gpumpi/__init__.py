@@ -57,7 +57,7 @@ MLP_NPARAMS = 64 * 12 + 64 + 64 * 64 + 64 + 4 * 64 + 4
 # symbols include/gpumpi.h declares (checked by the CPU test suite)
 EXPORTS = [
     "gpumpi_config_init", "gpumpi_parse_args", "gpumpi_world_create", "gpumpi_world_destroy",
-    "gpumpi_world_get_info", "gpumpi_last_error", "gpumpi_set_policy", "gpumpi_set_tuning", "gpumpi_set_tuned_table",
+    "gpumpi_world_get_info", "gpumpi_last_error", "gpumpi_set_policy", "gpumpi_set_tuning", "gpumpi_get_tuning", "gpumpi_set_tuned_table",
     "gpumpi_set_mlp", "gpumpi_read_trace", "gpumpi_run_program", "gpumpi_last_kernel_ms",
     "gpumpi_kernel_launches", "gpumpi_test_run", "gpumpi_allreduce", "gpumpi_reduce", "gpumpi_bcast",
     "gpumpi_alltoall", "gpumpi_alltoallv", "gpumpi_allgather", "gpumpi_pingpong", "gpumpi_ring",
@@ -120,6 +120,7 @@ def lib():
         L.gpumpi_last_error.restype = ctypes.c_char_p
         L.gpumpi_set_policy.argtypes = [vp, i32, i32]
         L.gpumpi_set_tuning.argtypes = [vp, i32, i64]
+        L.gpumpi_get_tuning.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_longlong)]
         L.gpumpi_set_tuned_table.argtypes = [vp, vp, ctypes.c_size_t]
         L.gpumpi_set_mlp.argtypes = [vp, vp, ctypes.c_size_t]
         L.gpumpi_read_trace.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
@@ -235,6 +236,11 @@ class World:
         """Autotuner knobs (TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES,
         TUNE_MLP_MARGIN, TUNE_DYN_SMEM) and TUNE_HOST_DIRECT (page-locked host buffers in place or staged)."""
         self._check(lib().gpumpi_set_tuning(self.h, key, value), "set_tuning")
+
+    def get_tuning(self, key: int) -> int:
+        v = ctypes.c_longlong(0)
+        self._check(lib().gpumpi_get_tuning(self.h, key, ctypes.byref(v)), "get_tuning")
+        return int(v.value)
 
     def set_tuned_table(self, table: np.ndarray):
         t = np.ascontiguousarray(table, dtype=np.int8)

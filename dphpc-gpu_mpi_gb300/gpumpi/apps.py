@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import P_BUCKET_SORT, P_HALO, World
+from . import P_BUCKET_SORT, P_HALO, TUNE_DYN_SMEM, World
 
 KEY_RANGE = 1 << 21
 
@@ -51,8 +51,17 @@ def bucket_sort(world: World, seed: int, total_keys: int, iters: int = 10, keys=
     hist = torch.empty((n, hstride), dtype=i32, device=dev)
     rcs = torch.zeros(n, dtype=i32, device=dev)
     ns = torch.zeros(max(1, iters), dtype=torch.int64, device=dev)
-    rc = world.run_program(P_BUCKET_SORT, i=(seed, kpr, iters, cap, int(gen), hstride),
-                           p=(keys, send, recv, out, counts, scratch, hist, rcs, ns))
+    # the local counting sort keeps its histogram (hstride ints) in the block's shared memory when the
+    # launch gives it that much: raise the world's cap for this launch
+    cap0 = world.get_tuning(TUNE_DYN_SMEM)
+    want = 4 * hstride + 1024
+    if 0 <= cap0 < want:
+        world.set_tuning(TUNE_DYN_SMEM, want)
+    try:
+        rc = world.run_program(P_BUCKET_SORT, i=(seed, kpr, iters, cap, int(gen), hstride),
+                               p=(keys, send, recv, out, counts, scratch, hist, rcs, ns))
+    finally:
+        world.set_tuning(TUNE_DYN_SMEM, cap0)
     torch.cuda.synchronize()
     _copy_ns(ns, iter_ns)
     return _first_error(rc, rcs), keys, out, counts

@@ -162,6 +162,8 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
  * the STAGED variants then run as DIRECT); 0 = staged through device memory around the kernel. */
 #define GPUMPI_TUNE_HOST_DIRECT 8
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
+/* The current value of a GPUMPI_TUNE_* knob. */
+int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value);
 /* Tuned table: int8 [3][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; log2 bytes per
  * rank; log2 ranks) -> variant or -1, host memory; a [2][32][16] table leaves Alltoall(v) untuned. */
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes);
