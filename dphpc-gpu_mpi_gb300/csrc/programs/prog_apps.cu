@@ -154,10 +154,24 @@ __device__ void sort_pack_task(void* arg, int tid, int nt) {
     for (int d = tid; d < n; d += nt) cur[d] = sd[d];
     gpumpi_block_sync(nt);
     int* send = w->send;
-    for_keys<8>(w->keys, w->kpr, tid, nt, [&](long long, int k) {
-        const int pos = atomicAdd(&cur[((long long)k * n) >> KEY_BITS], 1);
-        send[pos] = k;
-    });
+    // eight keys at a time: their loads, then their cursor atomics, then their stores (a store between two
+    // atomics would keep the second from issuing before the first returned)
+    const int* keys = w->keys;
+    const long long kpr = w->kpr;
+    long long i = tid;
+    for (; i + 7LL * nt < kpr; i += 8LL * nt) {
+        int k[8], pos[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) k[j] = __ldcg(keys + i + (long long)j * nt);
+#pragma unroll
+        for (int j = 0; j < 8; j++) pos[j] = atomicAdd(&cur[((long long)k[j] * n) >> KEY_BITS], 1);
+#pragma unroll
+        for (int j = 0; j < 8; j++) send[pos[j]] = k[j];
+    }
+    for (; i < kpr; i += nt) {
+        const int k = __ldcg(keys + i);
+        send[atomicAdd(&cur[((long long)k * n) >> KEY_BITS], 1)] = k;
+    }
 }
 
 __device__ void sort_rdispl_task(void* arg, int tid, int nt) {
