@@ -1317,10 +1317,34 @@ __device__ int MPI_Comm_rank(MPI_Comm comm, int* rank) {
 __device__ int MPI_Comm_split(MPI_Comm comm, int color, int key, MPI_Comm* newcomm) {
     return comm_split_impl(comm, color, key, newcomm);
 }
+namespace {
+// Member 0 of the new communicator o sets its topology, then every member waits for it (a barrier on o).
+__device__ int set_topology(MPI_Comm_impl* o, int kind, int ndims, const int* dims, const int* periods) {
+    if (comm_rank_of(o, me()) == 0) {
+        o->topo_kind = kind;
+        o->topo_ndims = ndims;
+        for (int i = 0; i < ndims; i++) {
+            o->topo_dims[i] = dims[i];
+            o->topo_periods[i] = periods[i] ? 1 : 0;
+        }
+        __threadfence();
+    }
+    return comm_barrier(o, []() {}, __LINE__);
+}
+}  // namespace
+
 __device__ int MPI_Comm_dup(MPI_Comm comm, MPI_Comm* newcomm) {
     MPI_Comm_impl* c = check_comm(comm);
     if (!c) return GPUMPI_FAILURE;  // reference returns MPI_FAILURE for MPI_COMM_NULL (communicator.cu:118-121)
-    return comm_split_impl(comm, 0, comm_rank_of(c, me()), newcomm);
+    int rc = comm_split_impl(comm, 0, comm_rank_of(c, me()), newcomm);
+    if (rc || !c->topo_kind || *newcomm == MPI_COMM_NULL) return rc;
+    // a duplicate keeps the topology
+    int dims[MPI_MAX_DIMS], periods[MPI_MAX_DIMS];
+    for (int i = 0; i < c->topo_ndims; i++) {
+        dims[i] = c->topo_dims[i];
+        periods[i] = c->topo_periods[i];
+    }
+    return set_topology(*newcomm, c->topo_kind, c->topo_ndims, dims, periods);
 }
 __device__ int MPI_Comm_create(MPI_Comm comm, MPI_Group group, MPI_Comm* newcomm) {
     MPI_Comm_impl* c = check_comm(comm);
@@ -1329,6 +1353,182 @@ __device__ int MPI_Comm_create(MPI_Comm comm, MPI_Group group, MPI_Comm* newcomm
     if (group) MPI_Group_rank(group, &grank);
     return comm_split_impl(comm, grank == MPI_UNDEFINED ? GPUMPI_UNDEFINED : 0, grank, newcomm);
 }
+// ---- Cartesian topologies: a Cartesian communicator is a communicator of the first prod(dims) ranks of
+// the old one, in their order, that also records the grid; coordinates are row-major (the last
+// dimension varies fastest), as the MPI standard specifies. ----
+__device__ int MPI_Dims_create(int nnodes, int ndims, int dims[]) {
+    if (nnodes < 1 || ndims < 1 || ndims > MPI_MAX_DIMS || !dims) return GPUMPI_ERR_ARG;
+    long long fixed = 1;
+    int nfree = 0;
+    for (int i = 0; i < ndims; i++) {
+        if (dims[i] < 0) return GPUMPI_ERR_ARG;
+        if (dims[i] > 0) fixed *= dims[i];
+        else nfree++;
+    }
+    if (fixed > nnodes || nnodes % fixed) return GPUMPI_ERR_ARG;
+    int rem = (int)(nnodes / fixed);
+    if (nfree == 0) return rem == 1 ? MPI_SUCCESS : GPUMPI_ERR_ARG;
+    // prime factors of the remainder, each given (largest first) to the smallest free dimension so far,
+    // then the free dimensions in non-increasing order
+    int primes[32], np = 0;
+    for (int p = 2; (long long)p * p <= rem; p++)
+        while (rem % p == 0) {
+            primes[np++] = p;
+            rem /= p;
+        }
+    if (rem > 1) primes[np++] = rem;
+    int f[MPI_MAX_DIMS];
+    for (int k = 0; k < nfree; k++) f[k] = 1;
+    for (int k = np - 1; k >= 0; k--) {
+        int m = 0;
+        for (int q = 1; q < nfree; q++)
+            if (f[q] < f[m]) m = q;
+        f[m] *= primes[k];
+    }
+    for (int a = 0; a < nfree; a++)  // descending order (at most 8 entries)
+        for (int b = a + 1; b < nfree; b++)
+            if (f[b] > f[a]) {
+                const int t = f[a];
+                f[a] = f[b];
+                f[b] = t;
+            }
+    for (int i = 0, k = 0; i < ndims; i++)
+        if (dims[i] == 0) dims[i] = f[k++];
+    return MPI_SUCCESS;
+}
+
+__device__ int MPI_Cart_create(MPI_Comm comm_old, int ndims, const int dims[], const int periods[], int reorder,
+                               MPI_Comm* comm_cart) {
+    (void)reorder;
+    MPI_Comm_impl* c = check_comm(comm_old);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (ndims < 0 || ndims > MPI_MAX_DIMS || (ndims > 0 && (!dims || !periods)) || !comm_cart) return GPUMPI_ERR_ARG;
+    long long prod = 1;
+    for (int i = 0; i < ndims; i++) {
+        if (dims[i] <= 0) return GPUMPI_ERR_ARG;
+        prod *= dims[i];
+    }
+    if (prod > c->size) return GPUMPI_ERR_ARG;
+    const int cr = comm_rank_of(c, me());
+    int rc = comm_split_impl(comm_old, cr < prod ? 0 : GPUMPI_UNDEFINED, cr, comm_cart);
+    if (rc || *comm_cart == MPI_COMM_NULL) return rc;
+    return set_topology(*comm_cart, MPI_CART, ndims, dims, periods);
+}
+
+namespace {
+__device__ __forceinline__ MPI_Comm_impl* cart_of(MPI_Comm comm) {
+    MPI_Comm_impl* c = check_comm(comm);
+    return c && c->topo_kind == MPI_CART ? c : nullptr;
+}
+__device__ void cart_coords_of(const MPI_Comm_impl* c, int rank, int* coords) {
+    for (int i = c->topo_ndims - 1; i >= 0; i--) {
+        coords[i] = rank % c->topo_dims[i];
+        rank /= c->topo_dims[i];
+    }
+}
+// Rank of coords (periodic dimensions wrap); -1 when a non-periodic coordinate is outside the grid.
+__device__ int cart_rank_of(const MPI_Comm_impl* c, const int* coords) {
+    int r = 0;
+    for (int i = 0; i < c->topo_ndims; i++) {
+        const int d = c->topo_dims[i];
+        int x = coords[i];
+        if (x < 0 || x >= d) {
+            if (!c->topo_periods[i]) return -1;
+            x = ((x % d) + d) % d;
+        }
+        r = r * d + x;
+    }
+    return r;
+}
+}  // namespace
+
+__device__ int MPI_Cart_coords(MPI_Comm comm, int rank, int maxdims, int coords[]) {
+    MPI_Comm_impl* c = cart_of(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (rank < 0 || rank >= c->size) return GPUMPI_ERR_RANK;
+    if (maxdims < c->topo_ndims || (c->topo_ndims > 0 && !coords)) return GPUMPI_ERR_ARG;
+    cart_coords_of(c, rank, coords);
+    return MPI_SUCCESS;
+}
+
+__device__ int MPI_Cart_rank(MPI_Comm comm, const int coords[], int* rank) {
+    MPI_Comm_impl* c = cart_of(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (!rank || (c->topo_ndims > 0 && !coords)) return GPUMPI_ERR_ARG;
+    const int r = cart_rank_of(c, coords);
+    if (r < 0) return GPUMPI_ERR_RANK;
+    *rank = r;
+    return MPI_SUCCESS;
+}
+
+__device__ int MPI_Cart_shift(MPI_Comm comm, int direction, int disp, int* rank_source, int* rank_dest) {
+    MPI_Comm_impl* c = cart_of(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (direction < 0 || direction >= c->topo_ndims || !rank_source || !rank_dest) return GPUMPI_ERR_ARG;
+    int coords[MPI_MAX_DIMS];
+    cart_coords_of(c, comm_rank_of(c, me()), coords);
+    const int x = coords[direction];
+    coords[direction] = x + disp;
+    int r = cart_rank_of(c, coords);
+    *rank_dest = r < 0 ? MPI_PROC_NULL : r;
+    coords[direction] = x - disp;
+    r = cart_rank_of(c, coords);
+    *rank_source = r < 0 ? MPI_PROC_NULL : r;
+    return MPI_SUCCESS;
+}
+
+__device__ int MPI_Cart_get(MPI_Comm comm, int maxdims, int dims[], int periods[], int coords[]) {
+    MPI_Comm_impl* c = cart_of(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (maxdims < c->topo_ndims) return GPUMPI_ERR_ARG;
+    if (c->topo_ndims > 0 && (!dims || !periods || !coords)) return GPUMPI_ERR_ARG;
+    for (int i = 0; i < c->topo_ndims; i++) {
+        dims[i] = c->topo_dims[i];
+        periods[i] = c->topo_periods[i];
+    }
+    cart_coords_of(c, comm_rank_of(c, me()), coords);
+    return MPI_SUCCESS;
+}
+
+__device__ int MPI_Cartdim_get(MPI_Comm comm, int* ndims) {
+    MPI_Comm_impl* c = cart_of(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (!ndims) return GPUMPI_ERR_ARG;
+    *ndims = c->topo_ndims;
+    return MPI_SUCCESS;
+}
+
+__device__ int MPI_Cart_sub(MPI_Comm comm, const int remain_dims[], MPI_Comm* newcomm) {
+    MPI_Comm_impl* c = cart_of(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (!newcomm || (c->topo_ndims > 0 && !remain_dims)) return GPUMPI_ERR_ARG;
+    int coords[MPI_MAX_DIMS], dims[MPI_MAX_DIMS], periods[MPI_MAX_DIMS];
+    cart_coords_of(c, comm_rank_of(c, me()), coords);
+    // colour: position in the dropped dimensions; key: position in the kept ones (row-major both)
+    int color = 0, key = 0, nd = 0;
+    for (int i = 0; i < c->topo_ndims; i++) {
+        if (remain_dims[i]) {
+            key = key * c->topo_dims[i] + coords[i];
+            dims[nd] = c->topo_dims[i];
+            periods[nd] = c->topo_periods[i];
+            nd++;
+        } else {
+            color = color * c->topo_dims[i] + coords[i];
+        }
+    }
+    int rc = comm_split_impl(comm, color, key, newcomm);
+    if (rc || *newcomm == MPI_COMM_NULL) return rc;
+    return set_topology(*newcomm, MPI_CART, nd, dims, periods);
+}
+
+__device__ int MPI_Topo_test(MPI_Comm comm, int* status) {
+    MPI_Comm_impl* c = check_comm(comm);
+    if (!c) return GPUMPI_ERR_COMM;
+    if (!status) return GPUMPI_ERR_ARG;
+    *status = c->topo_kind == MPI_CART ? MPI_CART : MPI_UNDEFINED;
+    return MPI_SUCCESS;
+}
+
 __device__ int MPI_Comm_free(MPI_Comm* comm) {
     // communicator objects live in the run's arena and are reclaimed when the launch ends
     if (comm) *comm = MPI_COMM_NULL;

@@ -644,6 +644,80 @@ struct Errors {
     }
 };
 
+// Cartesian topologies: MPI_Dims_create on fixed cases (rank 0), a periodic/non-periodic 3D grid over
+// the world, coordinates, ranks, shifts, MPI_Cart_sub and a neighbour exchange along each dimension.
+// Values go to outi for the host to check against the restatement of the same rules.
+//   outi[0..2] dims of the world grid   [3..5] coords   [6] Cart_rank(coords)   [7..12] shift (src, dst)
+//   for dims 0..2 with disp 1   [13..14] Cart_sub({1,0,1}) size, rank   [15] Cartdim_get   [16] Topo_test
+//   cart   [17] Topo_test world   [18..20] value received along dims 0..2 (-7 from MPI_PROC_NULL)
+//   [21] Cart_rank of out-of-grid coords on the non-periodic dimension (error code)
+//   rank 0 only: [24..] Dims_create cases, 4 entries each
+struct Cart {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        long long* o = outi(p, rank);
+        bool ok = true;
+        int dims[3] = {0, 0, 0};
+        ok = ok && MPI_Dims_create(n, 3, dims) == MPI_SUCCESS;
+        const int periods[3] = {1, 0, 1};
+        MPI_Comm cart = MPI_COMM_NULL;
+        ok = ok && MPI_Cart_create(MPI_COMM_WORLD, 3, dims, periods, 1, &cart) == MPI_SUCCESS;
+        int crank = -1;
+        MPI_Comm_rank(cart, &crank);
+        int coords[3] = {-1, -1, -1}, back = -1;
+        ok = ok && MPI_Cart_coords(cart, crank, 3, coords) == MPI_SUCCESS;
+        ok = ok && MPI_Cart_rank(cart, coords, &back) == MPI_SUCCESS;
+        for (int i = 0; i < 3; i++) {
+            o[i] = dims[i];
+            o[3 + i] = coords[i];
+        }
+        o[6] = back;
+        int src[3], dst[3];
+        for (int d = 0; d < 3; d++) {
+            ok = ok && MPI_Cart_shift(cart, d, 1, &src[d], &dst[d]) == MPI_SUCCESS;
+            o[7 + 2 * d] = src[d];
+            o[8 + 2 * d] = dst[d];
+        }
+        MPI_Comm sub = MPI_COMM_NULL;
+        const int remain[3] = {1, 0, 1};
+        ok = ok && MPI_Cart_sub(cart, remain, &sub) == MPI_SUCCESS;
+        int ssize = -1, srank = -1;
+        MPI_Comm_size(sub, &ssize);
+        MPI_Comm_rank(sub, &srank);
+        o[13] = ssize;
+        o[14] = srank;
+        int nd = -1, tc = -1, tw = -1;
+        MPI_Cartdim_get(cart, &nd);
+        MPI_Topo_test(cart, &tc);
+        MPI_Topo_test(MPI_COMM_WORLD, &tw);
+        o[15] = nd;
+        o[16] = tc;
+        o[17] = tw;
+        for (int d = 0; d < 3; d++) {  // send my rank up dimension d, receive from below
+            int got = -7;
+            ok = ok && MPI_Sendrecv(&crank, 1, MPI_INT, dst[d], 30 + d, &got, 1, MPI_INT, src[d], 30 + d, cart,
+                                    MPI_STATUS_IGNORE) == MPI_SUCCESS;
+            o[18 + d] = got;
+        }
+        int far[3] = {coords[0], dims[1], coords[2]}, r2 = -1;
+        o[21] = MPI_Cart_rank(cart, far, &r2);
+        if (rank == 0) {
+            const int cases[6][4] = {{12, 2, 0, 0}, {30, 3, 0, 0}, {16, 4, 0, 0}, {7, 2, 0, 0}, {24, 3, 3, 0}, {360, 3, 0, 0}};
+            for (int k = 0; k < 6; k++) {
+                int dd[4] = {0, 0, 0, 0};
+                dd[1] = cases[k][2];  // a fixed second dimension where given
+                const int rc = MPI_Dims_create(cases[k][0], cases[k][1], dd);
+                o[24 + 4 * k] = rc;
+                for (int i = 0; i < 3; i++) o[25 + 4 * k + i] = i < cases[k][1] ? dd[i] : 0;
+            }
+        }
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
 }  // namespace
 
 extern const gpumpi_prog_entry g_test_programs[] = {
@@ -667,5 +741,6 @@ extern const gpumpi_prog_entry g_test_programs[] = {
     GPUMPI_PROGRAM(GPUMPI_T_DATATYPES, "datatypes", Datatypes),
     GPUMPI_PROGRAM(GPUMPI_T_SUBCOMM_COLL, "subcomm_coll", SubcommColl),
     GPUMPI_PROGRAM(GPUMPI_T_ERRORS, "errors", Errors),
+    GPUMPI_PROGRAM(GPUMPI_T_CART, "cart", Cart),
 };
 extern const int g_num_test_programs = sizeof(g_test_programs) / sizeof(g_test_programs[0]);

@@ -208,6 +208,11 @@ struct alignas(128) MPI_Comm_impl {
     unsigned misalign[2];               // OR of members' buffer addresses (low bits), per epoch parity
     unsigned long long creation_token;  // comm-creation handshake
     MPI_Comm_impl* created;            // result published by the creating member
+    // Cartesian topology (MPI_Cart_create / MPI_Cart_sub); topo_kind 0 = none, 1 = Cartesian
+    int topo_kind;
+    int topo_ndims;
+    int topo_dims[8];
+    int topo_periods[8];
 };
 namespace gpumpi {
 constexpr int COMM_MAGIC = 0x434f4d4d;

@@ -39,6 +39,8 @@
 #define MPI_ERR_NO_MEM GPUMPI_ERR_NO_MEM
 #define MPI_ERR_INTERN GPUMPI_ERR_INTERN
 #define MPI_UNDEFINED -1
+#define MPI_CART 1
+#define MPI_MAX_DIMS 8
 #define MPI_THREAD_SINGLE 1
 #define MPI_THREAD_FUNNELED 2
 #define MPI_THREAD_SERIALIZED 3
@@ -229,6 +231,19 @@ __device__ int MPI_Group_free(MPI_Group* group);
 __device__ int MPI_Group_size(MPI_Group group, int* size);
 __device__ int MPI_Group_rank(MPI_Group group, int* rank);
 __device__ int MPI_Group_translate_ranks(MPI_Group group1, int n, const int ranks1[], MPI_Group group2, int ranks2[]);
+
+// ---- Cartesian topologies (MPI-3.1 section 7.5; not in the reference) ----
+// Ranks keep their order (reorder is accepted and ignored); at most MPI_MAX_DIMS dimensions.
+__device__ int MPI_Dims_create(int nnodes, int ndims, int dims[]);
+__device__ int MPI_Cart_create(MPI_Comm comm_old, int ndims, const int dims[], const int periods[], int reorder,
+                               MPI_Comm* comm_cart);
+__device__ int MPI_Cart_coords(MPI_Comm comm, int rank, int maxdims, int coords[]);
+__device__ int MPI_Cart_rank(MPI_Comm comm, const int coords[], int* rank);
+__device__ int MPI_Cart_shift(MPI_Comm comm, int direction, int disp, int* rank_source, int* rank_dest);
+__device__ int MPI_Cart_get(MPI_Comm comm, int maxdims, int dims[], int periods[], int coords[]);
+__device__ int MPI_Cartdim_get(MPI_Comm comm, int* ndims);
+__device__ int MPI_Cart_sub(MPI_Comm comm, const int remain_dims[], MPI_Comm* newcomm);
+__device__ int MPI_Topo_test(MPI_Comm comm, int* status);
 
 // ---- block-rank extensions (no counterpart in the reference) ----
 // Rank of the calling block in MPI_COMM_WORLD, usable anywhere in the rank's block.

@@ -273,5 +273,76 @@ def unpack(t: TypeMap, count: int, packed: np.ndarray, dst: np.ndarray) -> np.nd
     return dst
 
 
+# ---- Cartesian topologies (MPI-3.1 section 7.5; the reference has no topology functions) ----
+PROC_NULL = -2
+
+
+def dims_create(nnodes: int, dims):
+    """MPI_Dims_create: the zero entries of dims filled so that the product is nnodes, as balanced as the
+    greedy rule makes them (prime factors of the remainder, largest first, each to the smallest free
+    dimension so far; the free dimensions then in non-increasing order).  Returns None when impossible."""
+    dims = list(dims)
+    fixed = 1
+    for d in dims:
+        if d < 0:
+            return None
+        if d > 0:
+            fixed *= d
+    nfree = dims.count(0)
+    if fixed > nnodes or nnodes % fixed:
+        return None
+    rem = nnodes // fixed
+    if nfree == 0:
+        return dims if rem == 1 else None
+    primes, r, q = [], rem, 2
+    while q * q <= r:
+        while r % q == 0:
+            primes.append(q)
+            r //= q
+        q += 1
+    if r > 1:
+        primes.append(r)
+    f = [1] * nfree
+    for pr in reversed(primes):
+        m = min(range(nfree), key=lambda k: (f[k], k))
+        f[m] *= pr
+    f.sort(reverse=True)
+    it = iter(f)
+    return [d if d > 0 else next(it) for d in dims]
+
+
+def cart_coords(dims, rank: int):
+    """Row-major coordinates (the last dimension varies fastest)."""
+    c = [0] * len(dims)
+    for i in range(len(dims) - 1, -1, -1):
+        c[i] = rank % dims[i]
+        rank //= dims[i]
+    return c
+
+
+def cart_rank(dims, periods, coords):
+    """Rank of coords; periodic dimensions wrap, None outside a non-periodic one."""
+    r = 0
+    for d, p, x in zip(dims, periods, coords):
+        if not 0 <= x < d:
+            if not p:
+                return None
+            x %= d
+        r = r * d + x
+    return r
+
+
+def cart_shift(dims, periods, rank: int, direction: int, disp: int):
+    """(source, dest) of MPI_Cart_shift; PROC_NULL off a non-periodic edge."""
+    c = cart_coords(dims, rank)
+    out = []
+    for s in (-disp, disp):
+        cc = list(c)
+        cc[direction] += s
+        r = cart_rank(dims, periods, cc)
+        out.append(PROC_NULL if r is None else r)
+    return out[0], out[1]
+
+
 if __name__ == "__main__":
     print(build(force=bool(os.environ.get("FORCE"))))

@@ -179,3 +179,28 @@ def test_mlp_gradient_matches_finite_differences(oracle):
         lp, _ = oracle.mlp_loss_grad(p + e, x, t, m)
         lm, _ = oracle.mlp_loss_grad(p - e, x, t, m)
         assert abs((lp - lm) / 2e-6 - g[k]) < 1e-5 * max(1.0, abs(g[k]))
+
+
+def test_dims_create_matches_the_standards_examples(oracle):
+    # the MPI standard's MPI_Dims_create examples (MPI-3.1 section 7.5.2): (6, 2) -> 3x2, (7, 2) -> 7x1,
+    # (6, {0,3,0}) -> 2x3x1, (7, {0,3,0}) -> erroneous
+    assert oracle.dims_create(6, [0, 0]) == [3, 2]
+    assert oracle.dims_create(7, [0, 0]) == [7, 1]
+    assert oracle.dims_create(6, [0, 3, 0]) == [2, 3, 1]
+    assert oracle.dims_create(7, [0, 3, 0]) is None
+    # properties: product, non-increasing free entries, fixed entries kept
+    for n in range(1, 200):
+        for nd in (1, 2, 3, 4):
+            d = oracle.dims_create(n, [0] * nd)
+            assert int(np.prod(d)) == n and d == sorted(d, reverse=True)
+
+
+def test_cart_rules(oracle):
+    dims, periods = [3, 4, 2], [1, 0, 1]
+    for r in range(24):
+        c = oracle.cart_coords(dims, r)
+        assert oracle.cart_rank(dims, periods, c) == r
+    assert oracle.cart_rank(dims, periods, [-1, 0, 0]) == oracle.cart_rank(dims, periods, [2, 0, 0])
+    assert oracle.cart_rank(dims, periods, [0, 4, 0]) is None
+    assert oracle.cart_shift(dims, periods, 0, 1, 1) == (oracle.PROC_NULL, 2)   # non-periodic edge
+    assert oracle.cart_shift(dims, periods, 0, 0, 1) == (16, 8)                 # periodic wrap
