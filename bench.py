@@ -12,7 +12,8 @@ Reported:
   e2e        the same metric through the C ABI with pinned HOST buffers: host->device copy of the
              inputs, the collective, device->host copy of all outputs, every step;
   roofline   against the measured HBM copy bandwidth (MEASURED_PEAKS.json, "of measured");
-  cpu_baseline  the CPU oracle's multi-threaded allreduce on a bounded sample, on this host's cores;
+  cpu_baseline  the CPU oracle's multi-threaded allreduce on the same workload (bounded number of calls),
+             on this host's cores;
   extra      p50/p99 per-call latency; per-variant Allreduce GB/s; Alltoall(v) among 1024 ranks at 1 MiB
              per rank (uniform and uneven counts) per piece order; the bucket sort (2^25 keys, 256
              ranks), the 512^3 halo exchange and the batch of 64 communicators; the selector block:
@@ -133,47 +134,45 @@ def traffic_from_profile():
     return None
 
 
-def cpu_baseline(threads: int):
+def oracle_allreduce_timing(threads: int, warmup: int, max_steps: int, budget_s: float):
+    """The oracle's multi-threaded canonical-order Allreduce on the full headline workload (1024 ranks x
+    1 MiB fp32): `warmup` untimed calls, then timed calls until `max_steps` or `budget_s` is reached."""
     from oracle import oracle
-    import numpy as np
-    n, count = 1024, 16384  # 64 KiB per rank: same rank count, bounded sample
-    x = oracle.fill_f32(7, n * count).reshape(n, count)
-    oracle.allreduce(x, 12, 2, threads=threads)
-    t0 = time.perf_counter()
-    reps = 0
-    while True:
+    n, count = WORKLOAD["ranks"], WORKLOAD["bytes_per_rank"] // 4
+    x = oracle.fill_f32(1, n * count).reshape(n, count)
+    for _ in range(warmup):
         oracle.allreduce(x, 12, 2, threads=threads)
-        reps += 1
-        if time.perf_counter() - t0 > 4.0 or reps >= 200:
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        oracle.allreduce(x, 12, 2, threads=threads)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
             break
-    dt = (time.perf_counter() - t0) / reps
-    gbs = 2.0 * n * count * 4 / dt / 1e9
+    dt = (time.perf_counter() - t0) / steps
+    return 2.0 * n * count * 4 / dt / 1e9, dt, steps
+
+
+def cpu_baseline(threads: int):
+    gbs, _, steps = oracle_allreduce_timing(threads, 3, 200, 3.0)
     return {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
-            "sample": f"oracle allreduce fp32 SUM, 1024 ranks x 64 KiB, {reps} reps, {threads} threads"}
+            "sample": f"oracle allreduce fp32 SUM, full workload (1024 ranks x 1 MiB), {steps} calls after 3 "
+                      f"warm-up calls, {threads} threads"}
 
 
 def run_reference(args, dist, rank, ws):
     """The reference's CPU restatement (oracle port) on the same workload, all host threads."""
     if rank != 0:
         return
-    from oracle import oracle
     threads = os.cpu_count() or 1
-    n, count = WORKLOAD["ranks"], WORKLOAD["bytes_per_rank"] // 4
-    x = oracle.fill_f32(1, n * count).reshape(n, count)
-    for _ in range(max(0, min(args.warmup, 1))):
-        oracle.allreduce(x, 12, 2, threads=threads)
-    steps = max(1, min(args.steps, 5))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        oracle.allreduce(x, 12, 2, threads=threads)
-    dt = (time.perf_counter() - t0) / steps
-    gbs = 2.0 * n * count * 4 / dt / 1e9
+    warmup = max(0, min(args.warmup, 10))
+    gbs, dt, steps = oracle_allreduce_timing(threads, warmup, max(1, min(args.steps, 200)), 20.0)
     line = {"impl": "reference", "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": ws, "steps": steps,
-            "warmup": min(args.warmup, 1), "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "warmup": warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (LCG)",
             "config": dict(WORKLOAD),
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
-                             "sample": f"full workload, {steps} steps (bounded), {threads} threads"},
+                             "sample": f"full workload, {steps} steps (bounded by 200 steps / 20 s), {threads} threads"},
             "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
