@@ -87,5 +87,38 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
+def build_program(sources: list, out: Path, extra_flags: list | None = None) -> Path:
+    """Builds an executable from a converted MPI program (the reference's gpumpicc step): the user's
+    sources define `__device__ int __gpu_main(int, char**)` and include <mpi.h.cuh>; they are compiled with
+    the runtime's flags and device-linked with the runtime's objects and csrc/host/user_main.cu (main() ->
+    gpumpi_main).  Run it as `out [program args] ---gpumpi -n RANKS [...]`."""
+    build()
+    nv = nvcc()
+    flags = common_flags() + list(extra_flags or [])
+    udir = BUILD / "user"
+    udir.mkdir(parents=True, exist_ok=True)
+    objs = []
+    for k, src in enumerate([Path(x) for x in sources] + [CSRC / "host" / "user_main.cu"]):
+        obj = udir / f"{k}_{src.stem}.o"
+        r = subprocess.run([nv, *flags, "-c", str(src), "-o", str(obj)], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr[-8000:]}")
+        objs.append(obj)
+    runtime = [BUILD / (src.stem + ".o") for src in SOURCES]
+    out = Path(out)
+    r = subprocess.run([nv, *ARCH, "-rdc=true", *map(str, runtime + objs), "-o", str(out)], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr[-8000:]}")
+    return out
+
+
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    if "--program" in sys.argv:
+        # build.py --program a.cu [b.cu ...] -o OUT
+        args = sys.argv[sys.argv.index("--program") + 1:]
+        out = args[args.index("-o") + 1] if "-o" in args else "a.out"
+        srcs = [a for i, a in enumerate(args) if a != "-o" and (i == 0 or args[i - 1] != "-o")]
+        print(build_program(srcs, Path(out)))
+    else:
+        print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

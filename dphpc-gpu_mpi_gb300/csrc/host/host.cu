@@ -26,6 +26,9 @@ extern const gpumpi_prog_entry g_hot_programs[];
 extern const int g_num_hot_programs;
 extern const gpumpi_prog_entry g_app_programs[];
 extern const int g_num_app_programs;
+// a converted program's table (csrc/host/user_main.cu), present only in executables built around one
+extern const gpumpi_prog_entry g_user_programs[] __attribute__((weak));
+extern const int g_num_user_programs __attribute__((weak));
 
 extern "C" cudaError_t gpumpi_internal_install(Runtime* d_rt, MPI_Comm world, MPI_Group gworld, MPI_Group gempty,
                                                 cudaStream_t stream);
@@ -45,6 +48,9 @@ const gpumpi_prog_entry* find_program(int id) {
         if (g_hot_programs[i].id == id) return &g_hot_programs[i];
     for (int i = 0; i < g_num_app_programs; i++)
         if (g_app_programs[i].id == id) return &g_app_programs[i];
+    if (&g_num_user_programs != nullptr && g_user_programs != nullptr)
+        for (int i = 0; i < g_num_user_programs; i++)
+            if (g_user_programs[i].id == id) return &g_user_programs[i];
     return nullptr;
 }
 
@@ -938,3 +944,51 @@ int gpumpi_ring(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long b
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// The launcher of a converted program (replaces gpu_libs/gpu_main/main.cu:133-320): the arguments
+// before `---gpumpi` are the program's, the ones after configure the run (gpumpi_parse_args); every
+// rank runs the program with a device copy of its arguments; the exit status is 1 when the run failed
+// or any rank returned non-zero (main.cu:126-129,320), with the reason on stderr.
+// ------------------------------------------------------------------------------------------------
+extern "C" int gpumpi_main(int argc, char** argv, int program) {
+    gpumpi_config cfg;
+    gpumpi_config_init(&cfg);
+    const int pos = gpumpi_parse_args(argc, argv, &cfg);
+    const int pargc = pos < 0 ? argc : pos;
+    gpumpi_world* w = nullptr;
+    int rc = gpumpi_world_create(&cfg, &w);
+    if (rc) {
+        fprintf(stderr, "gpumpi: %s\n", gpumpi_last_error(nullptr));
+        return 1;
+    }
+    // argv on the device: pointer table, then the strings
+    size_t bytes = sizeof(char*) * (size_t)(pargc + 1);
+    for (int i = 0; i < pargc; i++) bytes += strlen(argv[i]) + 1;
+    std::vector<char> img(bytes, 0);
+    char* d_img = nullptr;
+    if (cudaMalloc(&d_img, bytes) != cudaSuccess) {
+        fprintf(stderr, "gpumpi: cudaMalloc of %zu bytes for the arguments failed\n", bytes);
+        gpumpi_world_destroy(w);
+        return 1;
+    }
+    char** tab = (char**)img.data();
+    size_t off = sizeof(char*) * (size_t)(pargc + 1);
+    for (int i = 0; i < pargc; i++) {
+        const size_t len = strlen(argv[i]) + 1;
+        memcpy(img.data() + off, argv[i], len);
+        tab[i] = d_img + off;
+        off += len;
+    }
+    tab[pargc] = nullptr;
+    gpumpi_params prm;
+    memset(&prm, 0, sizeof(prm));
+    prm.i[0] = pargc;
+    prm.p[0] = d_img;
+    if (cudaMemcpy(d_img, img.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = GPUMPI_ERR_CUDA;
+    else rc = gpumpi_run_program(w, program, &prm, nullptr, 1);
+    if (rc) fprintf(stderr, "gpumpi: %s\n", gpumpi_last_error(w));
+    cudaFree(d_img);
+    gpumpi_world_destroy(w);
+    return rc ? 1 : 0;
+}

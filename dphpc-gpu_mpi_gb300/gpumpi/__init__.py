@@ -63,7 +63,7 @@ EXPORTS = [
     "gpumpi_kernel_launches", "gpumpi_test_run", "gpumpi_allreduce", "gpumpi_reduce", "gpumpi_bcast",
     "gpumpi_alltoall", "gpumpi_alltoallv", "gpumpi_allgather", "gpumpi_pingpong", "gpumpi_ring",
     "gpumpi_allreduce_noalloc", "gpumpi_mlp_forward", "gpumpi_mlp_loss_grad", "gpumpi_mlp_adam_step",
-    "gpumpi_graph_create", "gpumpi_graph_launch", "gpumpi_graph_destroy",
+    "gpumpi_graph_create", "gpumpi_graph_launch", "gpumpi_graph_destroy", "gpumpi_main",
 ]
 
 

@@ -163,6 +163,13 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
  * the STAGED variants then run as DIRECT); 0 = staged through device memory around the kernel. */
 #define GPUMPI_TUNE_HOST_DIRECT 8
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
+/* Launcher of a converted program (the reference's gpu_main): argv holds the program's arguments, then
+ * optionally `---gpumpi` and the run's options (gpumpi_parse_args); creates the world, runs `program` on
+ * every rank with the program's arguments copied to the device, and returns the process exit status:
+ * 1 when the run failed or any rank returned non-zero (the reason on stderr), else 0. */
+int gpumpi_main(int argc, char** argv, int program);
+/* Program id of a converted program linked by the program builder (csrc/host/user_main.cu). */
+#define GPUMPI_P_USER 200
 /* The current value of a GPUMPI_TUNE_* knob. */
 int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value);
 /* Tuned table: int8 [3][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; log2 bytes per

@@ -1,0 +1,56 @@
+"""GPU: a converted MPI program (main renamed __gpu_main, the reference's converter contract) built into an
+executable by the program builder and run through the launcher, `prog [args] ---gpumpi -n RANKS`, as the
+reference's gpumpicc output runs (gpu_libs/gpu_main/main.cu)."""
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT / "dphpc-gpu_mpi_gb300"))
+
+
+@pytest.fixture(scope="module")
+def pi_exe(tmp_path_factory):
+    import build
+    out = tmp_path_factory.mktemp("prog") / "mpi_pi"
+    return build.build_program([ROOT / "tests" / "programs" / "mpi_pi_integrate.cu"], out)
+
+
+def expected_pi(n: int, ranks: int) -> float:
+    h = 1.0 / n
+    total = 0.0
+    for r in range(ranks):   # canonical rank order, as MPI_Reduce folds here
+        s = 0.0
+        for i in range(r, n, ranks):
+            x = h * (i + 0.5)
+            s += 4.0 / (1.0 + x * x)
+        total += h * s
+    return total
+
+
+@pytest.mark.parametrize("ranks,n", [(1, 1000), (64, 200000), (300, 30000)])
+def test_converted_program_runs(pi_exe, ranks, n):
+    r = subprocess.run([str(pi_exe), str(n), "---gpumpi", "-n", str(ranks)], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    line = [l for l in r.stdout.splitlines() if l.startswith("pi ")][-1].split()
+    assert int(line[3]) == ranks and int(line[5]) == n
+    # fused multiply-adds on the device may round the terms differently: a relative tolerance
+    assert abs(float(line[1]) - expected_pi(n, ranks)) <= 1e-12 * 3.2
+
+
+def test_failing_rank_gives_exit_status_1(pi_exe):
+    # a rank returning non-zero makes the launcher exit with 1 and name the rank (main.cu:126-129,320)
+    r = subprocess.run([str(pi_exe), "1000", "5", "---gpumpi", "-n", "8"], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 1 and "rank 5 returned 3" in r.stderr, (r.returncode, r.stderr)
+
+
+def test_bad_options_fail_cleanly(pi_exe):
+    r = subprocess.run([str(pi_exe), "1000", "---gpumpi", "-n", "8", "-b", "48"], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 1 and "threads_per_block" in r.stderr
