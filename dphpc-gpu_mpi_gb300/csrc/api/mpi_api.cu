@@ -196,9 +196,34 @@ struct CollArgs {
 // 8 bytes (4-byte types), one element.  Score = blocks busy per wave x bytes in flight per thread
 // (the rank-unrolled loads of fold_fast keep ~128 bytes in flight, at most 16 loads): the canonical
 // order makes every element a sequential chain over all ranks, so memory parallelism comes only from
-// elements in flight.  A tuning override (gpumpi_set_tuning) takes precedence when it is legal.
-__device__ int pick_vec(long long count, int T, int es, long long target, int aligned, int stage_room) {
+// elements in flight.  When every candidate fits in one wave of blocks the call is latency-bound: the
+// time is one thread's chain of ceil(n / U) batches of loads (U ranks per batch, U = min(16, 128 / (v
+// es))), so the candidate with the shortest chain wins (measured at 512 ranks x 256 B: one element per
+// thread 33 µs, one 16-byte vector 119 µs).  A tuning override (gpumpi_set_tuning) takes precedence
+// when it is legal.
+__device__ int pick_vec(long long count, int T, int es, long long target, int aligned, int stage_room, int n) {
     int cands[3] = {16 / es, es == 4 ? 2 : 1, 1};
+    if (c_rt.tune_vec <= 0) {
+        bool one_wave = true;
+        int pick = -1;
+        long long pick_chain = 0, pick_nch = 0;
+        for (int k = 2; k >= 0; k--) {  // narrowest first: on equal chains, more threads keep loads in flight
+            const int v = cands[k];
+            const int need = v * es >= 16 ? 16 : v * es;
+            if ((v > 1 && aligned < need) || stage_room < 2 * T * v * es) continue;
+            const long long nch = (count + (long long)T * v - 1) / ((long long)T * v);
+            if (nch > target) one_wave = false;
+            int u = 128 / (v * es);
+            u = u < 1 ? 1 : u > 16 ? 16 : u;
+            const long long chain = (n + u - 1) / u;
+            if (pick < 0 || chain < pick_chain || (chain == pick_chain && nch > pick_nch)) {
+                pick = k;
+                pick_chain = chain;
+                pick_nch = nch;
+            }
+        }
+        if (one_wave && pick >= 0) return cands[pick];
+    }
     double score_of[3] = {-1.0, -1.0, -1.0}, busy_of[3] = {0, 0, 0};
     for (int k = 0; k < 3; k++) {
         const int v = cands[k];
@@ -287,7 +312,7 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             if (!fold_has_staged(a.dt, a.op, a.ufn) || j->aligned16 < 16 || stage_room < 2 * T * es) {
                 variant = GPUMPI_VARIANT_DIRECT;
             } else {
-                vec = pick_vec(a.count, T, es, target, 16, stage_room);
+                vec = pick_vec(a.count, T, es, target, 16, stage_room, n);
                 int G = stage_room / (2 * T * vec * es);
                 if (c_rt.tune_group > 0 && c_rt.tune_group < G) G = c_rt.tune_group;
                 j->tile = G < 1 ? 1 : G > 64 ? 64 : G;
@@ -317,7 +342,7 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         j->variant = variant;
         if (variant == GPUMPI_VARIANT_DIRECT && fold_has_fast(a.dt, a.op, a.ufn)) {
             int es = a.esize;
-            vec = pick_vec(a.count, T, es, target, j->aligned16, 1 << 30);
+            vec = pick_vec(a.count, T, es, target, j->aligned16, 1 << 30, n);
         }
         j->vec = vec;
         j->chunk = (long long)T * vec;
@@ -469,6 +494,106 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     return best;
 }
 
+// ---- tiny reductions (at most TINY_BYTES per rank): one barrier, no job ----
+// Each member writes its operand into its inline slot of the parity of the barrier it is about to enter,
+// enters the barrier, and the members that need the result fold all n operands themselves, in rank order
+// (the canonical order: bit-identical to the job path).  The next collective on the communicator writes
+// the other parity, and the one after it can only start once every member has passed the barrier in
+// between, that is, has finished reading; so no second barrier is needed.  A job would take a barrier,
+// a chunk claim and dispatch, completion counting and a wait for the last chunk: about 10 µs more.
+struct TinyFold {
+    const unsigned char* tiny;
+    int n, parity, count, es, dt, op;
+    unsigned char out[TINY_BYTES];  // the result, also the accumulators (element e at e * es)
+};
+__shared__ TinyFold s_tiny_fold;
+
+// fold of a staged tile of m ranks (the first at r0) into the accumulators, element tid; typed for the
+// common (type, op) pairs (the same op_apply as the job path's fast fold), generic otherwise
+template <class T, int OP>
+__device__ __forceinline__ void tiny_fold_typed(TinyFold* w, const unsigned char* buf, int m, int r0, int tid) {
+    T* acc = (T*)w->out + tid;
+    T a = r0 == 0 ? ((const T*)buf)[tid] : *acc;
+    for (int i = r0 == 0 ? 1 : 0; i < m; i++) a = op_apply<OP, T>(((const T*)(buf + (size_t)i * TINY_BYTES))[tid], a);
+    *acc = a;
+}
+
+template <class T>
+__device__ __forceinline__ bool tiny_fold_arith(TinyFold* w, const unsigned char* buf, int m, int r0, int tid) {
+    switch (w->op) {
+    case GPUMPI_OP_SUM: tiny_fold_typed<T, GPUMPI_OP_SUM>(w, buf, m, r0, tid); return true;
+    case GPUMPI_OP_MAX: tiny_fold_typed<T, GPUMPI_OP_MAX>(w, buf, m, r0, tid); return true;
+    case GPUMPI_OP_MIN: tiny_fold_typed<T, GPUMPI_OP_MIN>(w, buf, m, r0, tid); return true;
+    case GPUMPI_OP_PROD: tiny_fold_typed<T, GPUMPI_OP_PROD>(w, buf, m, r0, tid); return true;
+    default: return false;
+    }
+}
+
+__device__ __forceinline__ bool tiny_fold_fast(TinyFold* w, const unsigned char* buf, int m, int r0, int tid) {
+    switch (w->dt) {
+    case GPUMPI_FLOAT: return tiny_fold_arith<float>(w, buf, m, r0, tid);
+    case GPUMPI_DOUBLE: case GPUMPI_LONG_DOUBLE: return tiny_fold_arith<double>(w, buf, m, r0, tid);
+    case GPUMPI_INT: case GPUMPI_INT32_T: return tiny_fold_arith<int>(w, buf, m, r0, tid);
+    case GPUMPI_LONG: case GPUMPI_LONG_LONG_INT: case GPUMPI_LONG_LONG: case GPUMPI_INT64_T:
+        return tiny_fold_arith<long long>(w, buf, m, r0, tid);
+    default: return false;
+    }
+}
+
+__device__ void tiny_fold_task(void* arg, int tid, int nt) {
+    TinyFold* w = (TinyFold*)arg;
+    unsigned char* buf = (unsigned char*)g_dyn_smem;  // staged operands, TINY_BYTES per rank
+    const int tile = c_rt.dyn_smem / TINY_BYTES;
+    const int vecs = (w->count * w->es + 15) / 16;
+    unsigned char* acc = w->out + tid * w->es;
+    for (int r0 = 0; r0 < w->n; r0 += tile) {
+        const int m = min(tile, w->n - r0);
+        for (int x = tid; x < m * vecs; x += nt) {
+            const int i = x / vecs, k = x % vecs;
+            const uint4* src = (const uint4*)(w->tiny + ((size_t)(r0 + i) * 2 + w->parity) * TINY_BYTES) + k;
+            ((uint4*)(buf + (size_t)i * TINY_BYTES))[k] = __ldcg(src);
+        }
+        bar_sync(BAR_TASK, nt);
+        if (tid < w->count && !tiny_fold_fast(w, buf, m, r0, tid)) {
+            for (int i = 0; i < m; i++) {
+                const unsigned char* src = buf + (size_t)i * TINY_BYTES + tid * w->es;
+                if (r0 + i == 0) {
+                    for (int b = 0; b < w->es; b++) acc[b] = src[b];
+                } else {
+                    apply_elem(w->op, w->dt, src, acc);
+                }
+            }
+        }
+        bar_sync(BAR_TASK, nt);
+    }
+}
+
+__device__ __noinline__ int tiny_fold(MPI_Comm_impl* c, int kind, const void* sb, void* recvbuf, int count, int dt,
+                                      int op, int root, int es) {
+    const int cr = comm_rank_of(c, me());
+    const int bytes = count * es;
+    const unsigned g = ld_acquire(&c->bar_gen);
+    unsigned char* mine = c->tiny + ((size_t)cr * 2 + (g & 1)) * TINY_BYTES;
+    small_copy(mine, sb, bytes);
+    int rc = comm_barrier_from(c, g, []() {}, __LINE__);
+    if (rc || !(kind == JOB_ALLREDUCE || cr == root)) return rc;
+    TinyFold* w = &s_tiny_fold;
+    w->tiny = c->tiny;
+    w->n = c->size;
+    w->parity = (int)(g & 1);
+    w->count = count;
+    w->es = es;
+    w->dt = dt;
+    w->op = op;
+    Task t;
+    t.kind = TASK_USER;
+    t.p0 = (const void*)&tiny_fold_task;
+    t.p1 = w;
+    dispatch(t);
+    small_copy(recvbuf, w->out, bytes);
+    return 0;
+}
+
 __device__ __noinline__ int fold_collective(int kind, const void* sendbuf, void* recvbuf, int count, MPI_Datatype dt, MPI_Op op,
                                int root, MPI_Comm comm) {
     MPI_Comm_impl* c = check_comm(comm);
@@ -489,6 +614,10 @@ __device__ __noinline__ int fold_collective(int kind, const void* sendbuf, void*
     const int cr = comm_rank_of(c, me());
     const bool has_out = kind == JOB_ALLREDUCE || cr == root;
     const void* sb = sendbuf == MPI_IN_PLACE ? recvbuf : sendbuf;
+    // (a forced variant, as the autotuner and the variant tests set, always takes the job path)
+    if (opc != GPUMPI_OP_USER && bytes <= TINY_BYTES && c->tiny && c_rt.variant_override < 0 &&
+        c_rt.dyn_smem >= 32 * TINY_BYTES && nthreads() >= count && sb && (!has_out || recvbuf))
+        return tiny_fold(c, kind, sb, recvbuf, count, dt, opc, root, es);
     Stage ss, rs;
     const void* gsb = stage_in(ss, sb, bytes, true);
     void* grb = has_out ? stage_in(rs, recvbuf, bytes, sendbuf == MPI_IN_PLACE) : nullptr;
@@ -850,6 +979,15 @@ __device__ int MPI_Bcast(void* buffer, int count, MPI_Datatype datatype, int roo
     long long bytes = (long long)count * t->size;
     long long span = t->lb + (long long)count * t->extent;
     const int cr = comm_rank_of(c, me());
+    if (bytes <= TINY_BYTES && t->nlev == 0 && t->lb == 0 && t->size == t->extent && c->tiny) {
+        // tiny contiguous broadcast: the root's bytes travel in its inline slot, one barrier (the
+        // parity argument of the tiny reductions)
+        const unsigned g = ld_acquire(&c->bar_gen);
+        if (cr == root) small_copy(c->tiny + ((size_t)cr * 2 + (g & 1)) * TINY_BYTES, buffer, (int)bytes);
+        int rc = comm_barrier_from(c, g, []() {}, __LINE__);
+        if (!rc && cr != root) small_copy(buffer, c->tiny + ((size_t)root * 2 + (g & 1)) * TINY_BYTES, (int)bytes);
+        return rc;
+    }
     Stage st;
     void* gb = buffer;
     if (!is_global_ptr(buffer)) {

@@ -254,6 +254,7 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     size_t o_tasks = dc.take<gpumpi::Task>(nb);
     size_t o_wmembers = dc.take<int>(n);
     size_t o_wslots = dc.take<gpumpi::CollSlot>(n);
+    size_t o_wtiny = dc.take<unsigned char>(2 * (size_t)gpumpi::TINY_BYTES * n);
     size_t o_board_ring = dc.take<gpumpi::BoardEntry>(4096);
     size_t o_trace = dc.take<gpumpi::TraceRec>(cfg.trace_capacity > 0 ? cfg.trace_capacity : 1);
     size_t o_arena = dc.take<unsigned char>(cfg.arena_bytes);
@@ -336,6 +337,7 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     f.world.members = r.world_members;
     f.world.rank_of = nullptr;
     f.world.slots = r.world_slots;
+    f.world.tiny = (unsigned char*)(w->d_data + o_wtiny);
     f.board.ring = (gpumpi::BoardEntry*)(w->d_data + o_board_ring);
     f.board.cap = 4096;
     f.gworld.size = n;

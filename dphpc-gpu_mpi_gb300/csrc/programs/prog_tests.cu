@@ -718,6 +718,50 @@ struct Cart {
     }
 };
 
+// Back-to-back tiny collectives (one-barrier path, inline operands alternating between two slots by
+// barrier parity) with per-iteration values and deliberately skewed ranks: every result is checked, so a
+// slot overwritten while a slower rank still reads it would show.  Also on a split communicator.
+//   outi[0] = first failing iteration (-1 if none)
+struct TinyStress {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        MPI_Comm half;
+        MPI_Comm_split(MPI_COMM_WORLD, rank & 1, rank, &half);
+        int hn = 0, hr = 0;
+        MPI_Comm_size(half, &hn);
+        MPI_Comm_rank(half, &hr);
+        long long bad = -1;
+        for (int it = 0; it < 200 && bad < 0; it++) {
+            if ((rank + it) % 7 == 0) {  // skew: some ranks arrive late
+                const long long t0 = clock64();
+                while (clock64() - t0 < 20000) {
+                }
+            }
+            long long v[3] = {rank * 1000LL + it, -rank - it, (long long)it * rank}, s[3] = {0, 0, 0};
+            MPI_Allreduce(v, s, 3, MPI_LONG_LONG, MPI_SUM, MPI_COMM_WORLD);
+            const long long tri = (long long)n * (n - 1) / 2;
+            if (s[0] != tri * 1000 + (long long)n * it || s[1] != -tri - (long long)n * it || s[2] != (long long)it * tri)
+                bad = it;
+            double d = rank + 0.25 * it, mx = 0;
+            MPI_Allreduce(&d, &mx, 1, MPI_DOUBLE, MPI_MAX, half);
+            const int top = (rank & 1) + 2 * (hn - 1);  // the half's highest world rank
+            if (mx != top + 0.25 * it) bad = it;
+            int root = it % n, b = rank == root ? it * 7 + root : -1;
+            MPI_Bcast(&b, 1, MPI_INT, root, MPI_COMM_WORLD);
+            if (b != it * 7 + root) bad = it;
+            int mine = rank + it, red = -1;
+            MPI_Reduce(&mine, &red, 1, MPI_INT, MPI_SUM, root, MPI_COMM_WORLD);
+            if (rank == root && red != (int)(tri + (long long)n * it)) bad = it;
+        }
+        outi(p, rank)[0] = bad;
+        okp(p)[rank] = bad < 0;
+        (void)hr;
+        return MPI_Finalize();
+    }
+};
+
 }  // namespace
 
 extern const gpumpi_prog_entry g_test_programs[] = {
@@ -742,5 +786,6 @@ extern const gpumpi_prog_entry g_test_programs[] = {
     GPUMPI_PROGRAM(GPUMPI_T_SUBCOMM_COLL, "subcomm_coll", SubcommColl),
     GPUMPI_PROGRAM(GPUMPI_T_ERRORS, "errors", Errors),
     GPUMPI_PROGRAM(GPUMPI_T_CART, "cart", Cart),
+    GPUMPI_PROGRAM(GPUMPI_T_TINY_STRESS, "tiny_stress", TinyStress),
 };
 extern const int g_num_test_programs = sizeof(g_test_programs) / sizeof(g_test_programs[0]);

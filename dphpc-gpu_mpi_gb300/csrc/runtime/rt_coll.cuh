@@ -109,9 +109,9 @@ __device__ __noinline__ int job_run_and_wait(Job* j, int line) {
 // ------------------------------------------------------------------------------------------------
 // communicator barrier: generation counter; the last arriver runs `setup` before releasing
 // ------------------------------------------------------------------------------------------------
+// The barrier whose generation word the caller read as g (it cannot change before the caller arrives).
 template <class F>
-__device__ int comm_barrier(MPI_Comm_impl* c, F&& setup, int line) {
-    unsigned g = ld_acquire(&c->bar_gen);
+__device__ int comm_barrier_from(MPI_Comm_impl* c, unsigned g, F&& setup, int line) {
     unsigned a = atom_add_acqrel(&c->bar_count, 1u);
     if (a == (unsigned)c->size - 1) {
         c->bar_count = 0;
@@ -125,6 +125,11 @@ __device__ int comm_barrier(MPI_Comm_impl* c, F&& setup, int line) {
     }
     fence_acqrel();
     return 0;
+}
+
+template <class F>
+__device__ int comm_barrier(MPI_Comm_impl* c, F&& setup, int line) {
+    return comm_barrier_from(c, ld_acquire(&c->bar_gen), setup, line);
 }
 
 // Parameters of the job epoch being executed, read once per chunk with L2-only loads (the Job

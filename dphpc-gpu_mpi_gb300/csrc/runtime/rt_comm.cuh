@@ -107,7 +107,8 @@ __device__ __noinline__ int comm_split_impl(MPI_Comm parent, int color, int key,
             int* members = (int*)arena_alloc(sizeof(int) * (unsigned long long)newsize);
             int* rank_of = (int*)arena_alloc(sizeof(int) * (unsigned long long)c_rt.nranks);
             CollSlot* slots = (CollSlot*)arena_alloc(sizeof(CollSlot) * (unsigned long long)newsize);
-            if (!obj || !members || !rank_of || !slots) {
+            unsigned char* tiny = (unsigned char*)arena_alloc(2ULL * TINY_BYTES * (unsigned long long)newsize);
+            if (!obj || !members || !rank_of || !slots || !tiny) {
                 record_error(GPUMPI_ERR_NO_MEM, 0, __LINE__, (long long)c_rt.arena_bytes);
                 obj = nullptr;
             } else {
@@ -118,6 +119,7 @@ __device__ __noinline__ int comm_split_impl(MPI_Comm parent, int color, int key,
                 obj->members = members;
                 obj->rank_of = rank_of;
                 obj->slots = slots;
+                obj->tiny = tiny;
                 obj->magic = COMM_MAGIC;
                 s_split.fill = rank_of;
                 s_split.fill_n = c_rt.nranks;

@@ -174,6 +174,8 @@ struct alignas(128) Job {
 // translates nothing, gpu_libs/gpu_mpi/communicator.cu:16-30; here the comm rank <-> world rank map
 // is explicit and used by point-to-point too).
 // ------------------------------------------------------------------------------------------------
+constexpr int TINY_BYTES = 64;  // reductions of at most this many bytes per rank take the one-barrier path
+
 struct CollSlot {            // what each member publishes when it enters a collective
     const void* sbuf;
     void* rbuf;
@@ -205,6 +207,7 @@ struct alignas(128) MPI_Comm_impl {
     int* members;      // comm rank -> world rank
     int* rank_of;      // world rank -> comm rank (-1 if absent); nullptr for the world
     gpumpi::CollSlot* slots;   // size entries
+    unsigned char* tiny;       // size x 2 x TINY_BYTES: inline operands of tiny reductions, by barrier parity
     unsigned misalign[2];               // OR of members' buffer addresses (low bits), per epoch parity
     unsigned long long creation_token;  // comm-creation handshake
     MPI_Comm_impl* created;            // result published by the creating member

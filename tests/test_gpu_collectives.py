@@ -286,3 +286,35 @@ def test_timeout_returns_error_not_hang(gpulib):
         # the world is still usable afterwards
         rc2, ok2, _, _ = w.run_test("sample")
         assert rc2 == 0 and ok2.all()
+
+
+@pytest.mark.parametrize("n", [2, 33, 300, 1024])
+def test_tiny_reductions_all_types_bit_exact(gpulib, oracle, n):
+    """Reductions of at most 64 bytes per rank take the one-barrier path (operands inline, folded by each
+    member in rank order): bit-exact with the oracle for every legal (type, op) pair tried, in place too."""
+    cases = [(12, 2, np.float32, 16), (13, 2, np.float64, 8), (2, 3, np.int32, 5), (20, 0, np.int64, 3),
+             (12, 1, np.float32, 1), (18, 2, np.int16, 32), (16, 8, np.uint8, 64), (2, 9, np.int32, 7)]
+    with gpulib.World(n, timeout_s=10.0) as w:
+        for k, (dt, op, npdt, count) in enumerate(cases):
+            x = make_input(oracle, n, count, npdt, 300 + k)
+            ref = oracle.allreduce(x, dt, op)
+            s, r = dev(x), dev(np.zeros_like(x))
+            w.allreduce(s, r, count, dt, op)
+            assert np.array_equal(host(r).view(np.uint8), ref.view(np.uint8)), (dt, op, count)
+        x = make_input(oracle, n, 7, np.float64, 77)
+        ref = oracle.allreduce(x, 13, 2)
+        buf = dev(x)
+        rc = w.coll("allreduce", 1, buf, 7, 13, 2, send_stride=0, recv_stride=7 * 8)  # MPI_IN_PLACE
+        assert rc == 0 and np.array_equal(host(buf), ref)
+        x = make_input(oracle, n, 9, np.int32, 78)
+        refr = oracle.reduce(x, 2, 2)
+        s, r = dev(x), dev(np.zeros_like(x))
+        w.reduce(s, r, 9, 2, 2, n - 1)
+        assert np.array_equal(host(r)[n - 1], refr)
+
+
+@pytest.mark.parametrize("n", [3, 64, 512])
+def test_tiny_collectives_back_to_back(gpulib, n):
+    with gpulib.World(n, timeout_s=20.0) as w:
+        rc, ok, oi, _ = w.run_test("tiny_stress")
+    assert rc == 0 and ok.all(), oi[:, 0][oi[:, 0] >= 0][:10]

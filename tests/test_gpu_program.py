@@ -38,7 +38,7 @@ def test_converted_program_runs(pi_exe, ranks, n):
                        timeout=120)
     assert r.returncode == 0, r.stderr
     line = [l for l in r.stdout.splitlines() if l.startswith("pi ")][-1].split()
-    assert int(line[3]) == ranks and int(line[5]) == n
+    assert int(line[3]) == ranks and int(line[5]) == n and int(line[7]) == n   # per-rank globals summed
     # fused multiply-adds on the device may round the terms differently: a relative tolerance
     assert abs(float(line[1]) - expected_pi(n, ranks)) <= 1e-12 * 3.2
 
