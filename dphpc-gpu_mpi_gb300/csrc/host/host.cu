@@ -258,9 +258,9 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     size_t o_board_ring = dc.take<gpumpi::BoardEntry>(4096);
     size_t o_trace = dc.take<gpumpi::TraceRec>(cfg.trace_capacity > 0 ? cfg.trace_capacity : 1);
     size_t o_arena = dc.take<unsigned char>(cfg.arena_bytes);
-    // each rank's group pool: room for four groups of the whole world
-    const size_t group_pool_bytes = align_up(std::max<size_t>(4096, 4 * (sizeof(int) * (size_t)n + 128)), 256);
-    size_t o_groups = dc.take<unsigned char>(group_pool_bytes * (size_t)n);
+    // each rank's scratch pool (groups, staged thread-local buffers): room for four groups of the whole world
+    const size_t scratch_pool_bytes = align_up(std::max<size_t>(4096, 4 * (sizeof(int) * (size_t)n + 128)), 256);
+    size_t o_pool = dc.take<unsigned char>(scratch_pool_bytes * (size_t)n);
     const size_t tree_bytes = 64ull << 20;
     size_t o_tree = dc.take<unsigned char>(tree_bytes);
     w->data_bytes = align_up(dc.off, 256);
@@ -305,8 +305,8 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     r.ranks_done = (unsigned*)(w->d_ctrl + o_done);
     r.abort_flag = (unsigned*)(w->d_ctrl + o_abort);
     r.trace_count = (unsigned long long*)(w->d_ctrl + o_trace_count);
-    r.group_pool = (unsigned char*)(w->d_data + o_groups);
-    r.group_pool_bytes = (long long)group_pool_bytes;
+    r.scratch_pool = (unsigned char*)(w->d_data + o_pool);
+    r.scratch_pool_bytes = (long long)scratch_pool_bytes;
     r.ring_payload = (unsigned char*)(w->d_data + o_ring_pl);
     r.uq = (gpumpi::UqEntry*)(w->d_data + o_uq);
     r.uq_payload = (unsigned char*)(w->d_data + o_uq_pl);

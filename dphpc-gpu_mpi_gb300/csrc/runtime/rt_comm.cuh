@@ -161,36 +161,36 @@ struct PoolBlock {
 };
 
 __device__ __forceinline__ unsigned char* pool_base() {
-    return c_rt.group_pool + (long long)me() * c_rt.group_pool_bytes;
+    return c_rt.scratch_pool + (long long)me() * c_rt.scratch_pool_bytes;
 }
 
 // 16-byte aligned scratch of `bytes` from this rank's pool, or nullptr when it does not fit.
 __device__ void* pool_alloc(unsigned long long bytes) {
     const long long need = (long long)((sizeof(PoolBlock) + bytes + 15) & ~15ULL);
     RankState* R = &c_rt.ranks[me()];
-    if (!c_rt.group_pool || R->grp_top + need > c_rt.group_pool_bytes) return nullptr;
-    PoolBlock* b = (PoolBlock*)(pool_base() + R->grp_top);
-    b->prev1 = R->grp_last1;
+    if (!c_rt.scratch_pool || R->pool_top + need > c_rt.scratch_pool_bytes) return nullptr;
+    PoolBlock* b = (PoolBlock*)(pool_base() + R->pool_top);
+    b->prev1 = R->pool_last1;
     b->freed = 0;
-    R->grp_last1 = R->grp_top + 1;
-    R->grp_top += (int)need;
+    R->pool_last1 = R->pool_top + 1;
+    R->pool_top += (int)need;
     return b + 1;
 }
 
 __device__ __forceinline__ bool pool_owns(const void* p) {
     const unsigned char* b = pool_base();
-    return c_rt.group_pool && (const unsigned char*)p >= b && (const unsigned char*)p < b + c_rt.group_pool_bytes;
+    return c_rt.scratch_pool && (const unsigned char*)p >= b && (const unsigned char*)p < b + c_rt.scratch_pool_bytes;
 }
 
 __device__ void pool_free(void* p) {
     ((PoolBlock*)p - 1)->freed = 1;
     RankState* R = &c_rt.ranks[me()];
     unsigned char* base = pool_base();
-    while (R->grp_last1 > 0) {
-        PoolBlock* top = (PoolBlock*)(base + (R->grp_last1 - 1));
+    while (R->pool_last1 > 0) {
+        PoolBlock* top = (PoolBlock*)(base + (R->pool_last1 - 1));
         if (!top->freed) break;
-        R->grp_top = R->grp_last1 - 1;
-        R->grp_last1 = top->prev1;
+        R->pool_top = R->pool_last1 - 1;
+        R->pool_last1 = top->prev1;
     }
 }
 

@@ -300,8 +300,8 @@ struct alignas(128) RankState {
     int nposted;                    // posted receives: slots [posted_lo, nposted) of the rank's list in
     int posted_lo;                  // posting order; matched slots hold -1 until trimmed
     int req_free_top;
-    int grp_top;                    // scratch pool: bytes in use, and 1 + offset of the last block
-    int grp_last1;                  //   (0: none); blocks are released from the top down
+    int pool_top;                   // scratch pool: bytes in use, and 1 + offset of the last block
+    int pool_last1;                 //   (0: none); blocks are released from the top down
     int ntypes;
     int initialized;
     int finalized;
@@ -407,9 +407,9 @@ struct Runtime {
     int* world_members;
     CollSlot* world_slots;
     Board* board;
-    unsigned char* group_pool;        // nranks * group_pool_bytes: each rank's scratch pool (MPI_Group
+    unsigned char* scratch_pool;      // nranks * scratch_pool_bytes: each rank's scratch pool (MPI_Group
                                       // objects, staged copies of thread-local buffers)
-    long long group_pool_bytes;
+    long long scratch_pool_bytes;
     unsigned char* arena;             // communicator objects created at run time
     unsigned long long arena_bytes;
     unsigned long long* arena_top;
