@@ -1099,6 +1099,21 @@ __device__ int MPI_Alltoall(const void* sendbuf, int sendcount, MPI_Datatype sen
     return rc;
 }
 
+namespace {
+// Tiny allgather: member q's contribution, from its inline slot of parity p, to recvbuf + q * bytes.
+struct TinyGather {
+    const unsigned char* tiny;
+    unsigned char* dst;
+    int n, parity, bytes;
+};
+__shared__ TinyGather s_tiny_gather;
+__device__ void tiny_gather_task(void* arg, int tid, int nt) {
+    const TinyGather* w = (const TinyGather*)arg;
+    for (int q = tid; q < w->n; q += nt)
+        small_copy(w->dst + (size_t)q * w->bytes, w->tiny + ((size_t)q * 2 + w->parity) * TINY_BYTES, w->bytes);
+}
+}  // namespace
+
 __device__ int MPI_Allgather(const void* sendbuf, int sendcount, MPI_Datatype sendtype, void* recvbuf, int recvcount,
                              MPI_Datatype recvtype, MPI_Comm comm) {
     MPI_Comm_impl* c = check_comm(comm);
@@ -1108,6 +1123,29 @@ __device__ int MPI_Allgather(const void* sendbuf, int sendcount, MPI_Datatype se
     if (!rt || (sendbuf != MPI_IN_PLACE && !st)) return GPUMPI_ERR_TYPE;
     const int n = c->size;
     const int cr = comm_rank_of(c, me());
+    if (sendbuf != MPI_IN_PLACE && c->tiny && sendcount >= 0 && recvcount >= 0 && desc_contiguous(st) &&
+        desc_contiguous(rt) && (long long)sendcount * st->size <= TINY_BYTES &&
+        (long long)sendcount * st->size == (long long)recvcount * rt->size && is_global_ptr(recvbuf)) {
+        // tiny contiguous contributions: through the inline slots, one barrier (the parity argument of
+        // the tiny reductions), then the block copies the n contributions out
+        const int bytes = (int)((long long)sendcount * st->size);
+        const unsigned g = ld_acquire(&c->bar_gen);
+        small_copy(c->tiny + ((size_t)cr * 2 + (g & 1)) * TINY_BYTES, sendbuf, bytes);
+        const int rc = comm_barrier_from(c, g, []() {}, __LINE__);
+        if (rc || bytes == 0) return rc;
+        TinyGather* w = &s_tiny_gather;
+        w->tiny = c->tiny;
+        w->dst = (unsigned char*)recvbuf;
+        w->n = n;
+        w->parity = (int)(g & 1);
+        w->bytes = bytes;
+        Task t;
+        t.kind = TASK_USER;
+        t.p0 = (const void*)&tiny_gather_task;
+        t.p1 = w;
+        dispatch(t);
+        return MPI_SUCCESS;
+    }
     CollSlot my{};
     my.rbuf = recvbuf;
     my.rcount = recvcount;

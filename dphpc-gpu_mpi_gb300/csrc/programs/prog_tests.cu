@@ -733,6 +733,7 @@ struct TinyStress {
         MPI_Comm_size(half, &hn);
         MPI_Comm_rank(half, &hr);
         long long bad = -1;
+        int* all = (int*)p.p[3];  // optional int[n][n]: allgather rows
         for (int it = 0; it < 200 && bad < 0; it++) {
             if ((rank + it) % 7 == 0) {  // skew: some ranks arrive late
                 const long long t0 = clock64();
@@ -754,6 +755,12 @@ struct TinyStress {
             int mine = rank + it, red = -1;
             MPI_Reduce(&mine, &red, 1, MPI_INT, MPI_SUM, root, MPI_COMM_WORLD);
             if (rank == root && red != (int)(tri + (long long)n * it)) bad = it;
+            if (all) {  // tiny allgather into a global buffer
+                int* row = all + (size_t)rank * n;
+                MPI_Allgather(&mine, 1, MPI_INT, row, 1, MPI_INT, MPI_COMM_WORLD);
+                for (int q = 0; q < n; q++)
+                    if (row[q] != q + it) bad = it;
+            }
         }
         outi(p, rank)[0] = bad;
         okp(p)[rank] = bad < 0;
