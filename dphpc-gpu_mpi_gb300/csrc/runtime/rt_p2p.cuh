@@ -67,7 +67,8 @@ __device__ __forceinline__ void small_copy(void* dst, const void* src, int n) {
     const char* s = (const char*)src;
     const bool g = is_global_ptr(s);
     const unsigned a = (unsigned)(size_t)d | (unsigned)(size_t)s | (unsigned)n;
-    if ((a & 7) == 0) small_copy_t<unsigned long long>(d, s, n, g);
+    if ((a & 15) == 0) small_copy_t<uint4>(d, s, n, g);
+    else if ((a & 7) == 0) small_copy_t<unsigned long long>(d, s, n, g);
     else if ((a & 3) == 0) small_copy_t<unsigned>(d, s, n, g);
     else small_copy_t<unsigned char>(d, s, n, g);
 }
