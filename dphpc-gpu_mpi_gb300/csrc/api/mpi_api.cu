@@ -979,13 +979,15 @@ __device__ int MPI_Bcast(void* buffer, int count, MPI_Datatype datatype, int roo
     long long bytes = (long long)count * t->size;
     long long span = t->lb + (long long)count * t->extent;
     const int cr = comm_rank_of(c, me());
-    if (bytes <= TINY_BYTES && t->nlev == 0 && t->lb == 0 && t->size == t->extent && c->tiny) {
-        // tiny contiguous broadcast: the root's bytes travel in its inline slot, one barrier (the
-        // parity argument of the tiny reductions)
+    if (bytes <= TINY_BYTES && c->tiny) {
+        // tiny broadcast: the root's packed bytes travel in its inline slot, one barrier (the parity
+        // argument of the tiny reductions).  The choice depends on the message size only, which every
+        // member shares; each member packs or unpacks its own datatype and buffer.
+        const TypeDesc* d = desc_contiguous(t) ? nullptr : t;
         const unsigned g = ld_acquire(&c->bar_gen);
-        if (cr == root) small_copy(c->tiny + ((size_t)cr * 2 + (g & 1)) * TINY_BYTES, buffer, (int)bytes);
+        if (cr == root) t0_copy(c->tiny + ((size_t)cr * 2 + (g & 1)) * TINY_BYTES, nullptr, buffer, d, bytes);
         int rc = comm_barrier_from(c, g, []() {}, __LINE__);
-        if (!rc && cr != root) small_copy(buffer, c->tiny + ((size_t)root * 2 + (g & 1)) * TINY_BYTES, (int)bytes);
+        if (!rc && cr != root) t0_copy(buffer, d, c->tiny + ((size_t)root * 2 + (g & 1)) * TINY_BYTES, nullptr, bytes);
         return rc;
     }
     Stage st;
@@ -1121,9 +1123,10 @@ __device__ void piece_gather_task(void* arg, int tid, int nt) {
     const int parts = (w->bytes + 15) / 16;
     for (int x = tid; x < w->n * parts; x += nt) {
         const int q = x / parts, k = x % parts;
-        const unsigned char* src =
-            w->tiny ? w->tiny + ((size_t)q * 2 + w->parity) * TINY_BYTES
-                    : (const unsigned char*)slot_in(&w->slots[q]) + (size_t)w->cr * w->bytes;
+        const unsigned char* base =
+            w->tiny ? w->tiny + ((size_t)q * 2 + w->parity) * TINY_BYTES : (const unsigned char*)slot_in(&w->slots[q]);
+        if (!base) continue;  // a member that could not stage its buffer published none
+        const unsigned char* src = w->tiny ? base : base + (size_t)w->cr * w->bytes;
         const int len = min(16, w->bytes - 16 * k);
         small_copy(w->dst + (size_t)q * w->bytes + 16 * k, src + 16 * k, len);
     }
@@ -1137,18 +1140,33 @@ __device__ __forceinline__ void piece_gather(const unsigned char* tiny, const Co
 // n^2 pieces (1024 ranks x 4 bytes: about 90 us as a job).  Returns -1 when the call does not qualify.
 __device__ int small_alltoall(MPI_Comm_impl* c, const void* sendbuf, int sendcount, const TypeDesc* st, void* recvbuf,
                               int recvcount, const TypeDesc* rt) {
-    if (sendbuf == MPI_IN_PLACE || !desc_contiguous(st) || !desc_contiguous(rt) || sendcount < 0 ||
-        (long long)sendcount * st->size != (long long)recvcount * rt->size || (long long)sendcount * st->size > 256 ||
-        (long long)sendcount * st->size * c->size > 65536 || !is_global_ptr(sendbuf) || !is_global_ptr(recvbuf) ||
-        c_rt.variant_override >= 0)
+    // the choice depends only on what every member shares (sizes, the policy); a member whose buffers
+    // are thread-local or whose types are not contiguous packs and unpacks through its scratch pool
+    const long long pb = (long long)sendcount * st->size;
+    if (sendbuf == MPI_IN_PLACE || sendcount < 0 || pb != (long long)recvcount * rt->size || pb > 256 ||
+        pb * c->size > 65536 || c_rt.variant_override >= 0)
         return -1;
-    const int bytes = (int)((long long)sendcount * st->size);
+    const int bytes = (int)pb, n = c->size;
     const int cr = comm_rank_of(c, me());
-    c->slots[cr].sbuf = sendbuf;
-    int rc = comm_barrier(c, []() {}, __LINE__);
-    if (rc) return rc;
-    if (bytes > 0) piece_gather(nullptr, c->slots, recvbuf, c->size, 0, bytes, cr);
-    return comm_barrier(c, []() {}, __LINE__);
+    const long long all = (long long)n * bytes;
+    const bool direct_send = desc_contiguous(st) && is_global_ptr(sendbuf);
+    const bool direct_recv = desc_contiguous(rt) && is_global_ptr(recvbuf);
+    void* sstage = direct_send || all == 0 ? nullptr : scratch_alloc((unsigned long long)all);
+    void* rstage = direct_recv || all == 0 ? nullptr : scratch_alloc((unsigned long long)all);
+    int rc = 0;
+    if ((!direct_send && all && !sstage) || (!direct_recv && all && !rstage)) rc = GPUMPI_ERR_NO_MEM;
+    if (sstage) t0_copy(sstage, nullptr, sendbuf, desc_contiguous(st) ? nullptr : st, all);
+    c->slots[cr].sbuf = direct_send ? sendbuf : sstage;  // nullptr when staging failed: the others skip it
+    // (a member that could not stage still takes part in both barriers, so the others do not wait)
+    const int rb = comm_barrier(c, []() {}, __LINE__);
+    if (!rc) rc = rb;
+    if (!rc && bytes > 0) piece_gather(nullptr, c->slots, rstage ? rstage : recvbuf, n, 0, bytes, cr);
+    const int rb2 = comm_barrier(c, []() {}, __LINE__);
+    if (!rc) rc = rb2;
+    if (!rc && rstage) t0_copy(recvbuf, desc_contiguous(rt) ? nullptr : rt, rstage, nullptr, all);
+    scratch_free(rstage);
+    scratch_free(sstage);
+    return rc;
 }
 
 __device__ __forceinline__ void piece_gather(const unsigned char* tiny, const CollSlot* slots, void* dst, int n,
@@ -1178,17 +1196,25 @@ __device__ int MPI_Allgather(const void* sendbuf, int sendcount, MPI_Datatype se
     if (!rt || (sendbuf != MPI_IN_PLACE && !st)) return GPUMPI_ERR_TYPE;
     const int n = c->size;
     const int cr = comm_rank_of(c, me());
-    if (sendbuf != MPI_IN_PLACE && c->tiny && sendcount >= 0 && recvcount >= 0 && desc_contiguous(st) &&
-        desc_contiguous(rt) && (long long)sendcount * st->size <= TINY_BYTES &&
-        (long long)sendcount * st->size == (long long)recvcount * rt->size && is_global_ptr(recvbuf)) {
-        // tiny contiguous contributions: through the inline slots, one barrier (the parity argument of
-        // the tiny reductions), then the block copies the n contributions out
+    if (sendbuf != MPI_IN_PLACE && c->tiny && sendcount >= 0 && recvcount >= 0 &&
+        (long long)sendcount * st->size <= TINY_BYTES &&
+        (long long)sendcount * st->size == (long long)recvcount * rt->size) {
+        // tiny contributions (the choice depends on the contribution size only, which every member
+        // shares): packed into the inline slots, one barrier (the parity argument of the tiny
+        // reductions), then each member unpacks the n contributions
         const int bytes = (int)((long long)sendcount * st->size);
         const unsigned g = ld_acquire(&c->bar_gen);
-        small_copy(c->tiny + ((size_t)cr * 2 + (g & 1)) * TINY_BYTES, sendbuf, bytes);
+        t0_copy(c->tiny + ((size_t)cr * 2 + (g & 1)) * TINY_BYTES, nullptr, sendbuf, desc_contiguous(st) ? nullptr : st,
+                bytes);
         const int rc = comm_barrier_from(c, g, []() {}, __LINE__);
         if (rc || bytes == 0) return rc;
-        piece_gather(c->tiny, nullptr, recvbuf, n, (int)(g & 1), bytes, cr);
+        if (desc_contiguous(rt) && is_global_ptr(recvbuf)) {
+            piece_gather(c->tiny, nullptr, recvbuf, n, (int)(g & 1), bytes, cr);
+        } else {
+            for (int q = 0; q < n; q++)
+                t0_copy((char*)recvbuf + (long long)q * recvcount * rt->extent, desc_contiguous(rt) ? nullptr : rt,
+                        c->tiny + ((size_t)q * 2 + (g & 1)) * TINY_BYTES, nullptr, bytes);
+        }
         return MPI_SUCCESS;
     }
     CollSlot my{};

@@ -769,6 +769,60 @@ struct TinyStress {
     }
 };
 
+// The small-message paths choose by message size only, so members may mix thread-local and global
+// buffers and different (same-signature) datatypes: odd ranks use stack arrays and a strided type, even
+// ranks global memory and contiguous types.  Ranks: 2..64.  p[3]: int scratch [n][288] (global): bcast
+// [0, 4), allgather row [8, 138), alltoall send [140, 204), receive [208, 272).
+struct TinyMixed {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        int rank = wrank(), n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        if (n > 64) {  // the local arrays hold 64 ranks (every member returns here alike)
+            okp(p)[rank] = 0;
+            return MPI_Finalize();
+        }
+        bool ok = true;
+        int* g = (int*)p.p[3] + (size_t)rank * 288;
+        const bool odd = rank & 1;
+        MPI_Datatype vec;
+        MPI_Type_vector(4, 1, 2, MPI_INT, &vec);
+        MPI_Type_commit(&vec);
+        int loc[8];
+        for (int i = 0; i < 8; i++) loc[i] = -1;
+        int vals[4] = {11, 22, 33, 44};
+        // broadcast of 16 bytes: root contiguous, odd ranks into a strided local array
+        if (rank == 0) MPI_Bcast(vals, 4, MPI_INT, 0, MPI_COMM_WORLD);
+        else if (odd) MPI_Bcast(loc, 1, vec, 0, MPI_COMM_WORLD);
+        else MPI_Bcast(g, 4, MPI_INT, 0, MPI_COMM_WORLD);
+        for (int i = 0; i < 4 && rank != 0; i++) ok = ok && (odd ? loc[2 * i] == vals[i] && loc[2 * i + 1] == -1 : g[i] == vals[i]);
+        // allgather of 2 ints per member
+        int mine[2] = {rank, rank * 3}, lrow[128];
+        int* grow = g + 8;
+        if (odd) MPI_Allgather(mine, 2, MPI_INT, lrow, 2, MPI_INT, MPI_COMM_WORLD);
+        else {
+            grow[0] = mine[0];
+            grow[1] = mine[1];
+            MPI_Allgather(grow, 2, MPI_INT, grow + 2, 2, MPI_INT, MPI_COMM_WORLD);
+        }
+        for (int q = 0; q < n && ok; q++) {
+            const int* r = odd ? lrow : grow + 2;
+            ok = r[2 * q] == q && r[2 * q + 1] == 3 * q;
+        }
+        // alltoall of one int per pair: send q gets rank * 100 + q
+        int ls[64], lr[64];
+        int* gs = g + 140;
+        int* gr = g + 208;
+        for (int q = 0; q < n && q < 64; q++) (odd ? ls : gs)[q] = rank * 100 + q;
+        if (odd) MPI_Alltoall(ls, 1, MPI_INT, lr, 1, MPI_INT, MPI_COMM_WORLD);
+        else MPI_Alltoall(gs, 1, MPI_INT, gr, 1, MPI_INT, MPI_COMM_WORLD);
+        for (int q = 0; q < n && ok; q++) ok = (odd ? lr : gr)[q] == q * 100 + rank;
+        MPI_Type_free(&vec);
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
 }  // namespace
 
 extern const gpumpi_prog_entry g_test_programs[] = {
@@ -794,5 +848,6 @@ extern const gpumpi_prog_entry g_test_programs[] = {
     GPUMPI_PROGRAM(GPUMPI_T_ERRORS, "errors", Errors),
     GPUMPI_PROGRAM(GPUMPI_T_CART, "cart", Cart),
     GPUMPI_PROGRAM(GPUMPI_T_TINY_STRESS, "tiny_stress", TinyStress),
+    GPUMPI_PROGRAM(GPUMPI_T_TINY_MIXED, "tiny_mixed", TinyMixed),
 };
 extern const int g_num_test_programs = sizeof(g_test_programs) / sizeof(g_test_programs[0]);

@@ -40,7 +40,7 @@ TESTS = {
     "single_int": 1, "transfer_array": 2, "send_recv": 3, "repeat_send_recv": 4, "network_flood": 5,
     "all_to_all": 6, "reduce_int16_prod": 7, "allreduce_f64_sum": 8, "allgather_int": 9, "scatter_int": 10,
     "scatterv_int": 11, "comm_rank": 12, "comm_dup_isolation": 13, "comm_split": 14, "sample": 15,
-    "p2p_matching": 16, "timeout": 17, "datatypes": 18, "subcomm_coll": 19, "errors": 20, "cart": 21, "tiny_stress": 22,
+    "p2p_matching": 16, "timeout": 17, "datatypes": 18, "subcomm_coll": 19, "errors": 20, "cart": 21, "tiny_stress": 22, "tiny_mixed": 23,
 }
 P_COLL, P_PINGPONG, P_RING, P_PI, P_BUCKET_SORT, P_HALO, P_BATCH = 100, 101, 102, 103, 104, 105, 106
 COLL = {"allreduce": 0, "reduce": 1, "bcast": 2, "alltoall": 3, "alltoallv": 4, "allgather": 5, "gather": 6,

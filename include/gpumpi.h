@@ -99,6 +99,7 @@ enum gpumpi_program {
     GPUMPI_T_ERRORS,           /* argument errors return codes, never trap */
     GPUMPI_T_CART,             /* Cartesian topologies: dims, coords, shifts, sub-grids, exchange */
     GPUMPI_T_TINY_STRESS,      /* back-to-back tiny collectives with skewed ranks, every result checked */
+    GPUMPI_T_TINY_MIXED,       /* small collectives mixing thread-local/global buffers and datatypes */
     /* hot-path programs */
     GPUMPI_P_COLL = 100,       /* i[0]=kind i[1]=count i[2]=dt i[3]=op i[4]=root i[5]=iters i[6]=send stride
                                   i[7]=recv stride i[8]=variant p[0]=send p[1]=recv p[2..5]=count/displ matrices

@@ -324,3 +324,16 @@ def test_tiny_collectives_back_to_back(gpulib, n):
         rc = w.run_program(gpulib.TESTS["tiny_stress"], p=(ok, oi, od, rows))
     bad = host(oi)[:, 0]
     assert rc == 0 and host(ok).all(), bad[bad >= 0][:10]
+
+
+@pytest.mark.parametrize("n", [2, 5, 33, 64])
+def test_small_paths_mixed_buffers_and_types(gpulib, n):
+    # members choose the small paths by size alone, so stack and global buffers and strided and
+    # contiguous same-signature datatypes can meet in one call
+    ok = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    oi = torch.zeros((n, 64), dtype=torch.int64, device="cuda")
+    od = torch.zeros((n, 64), dtype=torch.float64, device="cuda")
+    scratch = torch.zeros((n, 288), dtype=torch.int32, device="cuda")
+    with gpulib.World(n, timeout_s=20.0) as w:
+        rc = w.run_program(gpulib.TESTS["tiny_mixed"], p=(ok, oi, od, scratch))
+    assert rc == 0 and host(ok).all(), host(ok)
