@@ -190,6 +190,8 @@ struct CollArgs {
     MPI_User_function* ufn;
     long long est_piece;   // pulls: estimated bytes per piece
     int variant;
+    bool learned = false;  // `variant` is the network's choice; pred = its predicted log-times
+    float pred[4] = {0.f, 0.f, 0.f, 0.f};
 };
 
 // Elements per thread for a fold chunk (chunk = T * v elements).  Candidates: one 16-byte vector,
@@ -299,7 +301,8 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
     if (a.kind == JOB_ALLREDUCE || a.kind == JOB_REDUCE) {
         j->count = a.count;
         bytes = a.count * a.esize * (long long)n;
-        int variant = select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, a.variant);
+        int variant = select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, a.variant, j->aligned16,
+                                     a.learned ? a.pred : nullptr);
         may_post = may_post && bytes >= c_rt.engine_min_bytes;
         long long target = n + (may_post ? c_rt.nengines : 0);
         int vec = 1;
@@ -356,7 +359,8 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         j->count = P;
         // piece order (DIRECT / TREE / RING, see piece_of) or bulk-copy staging (STAGED)
         int variant = a.kind == JOB_ALLTOALLV
-                          ? select_variant(a.kind, a.est_piece * n, n, a.dt, -1, a.variant)
+                          ? select_variant(a.kind, a.est_piece * n, n, a.dt, -1, a.variant, j->aligned16,
+                                           a.learned ? a.pred : nullptr)
                           : (matrix && a.variant >= 0 && a.variant < GPUMPI_NUM_VARIANTS ? a.variant
                                                                                           : GPUMPI_VARIANT_DIRECT);
         // STAGED needs shared memory for two bulk-copy stages of at least 512 bytes per warp
@@ -450,13 +454,17 @@ __device__ void mlp_infer_task(void* arg, int tid, int nt) {
     }
 }
 
-// Variant with the smallest predicted time; every member computes it from the same inputs with the
-// same operation order, so all members agree.  Cached per rank for repeated calls of one shape.
-__device__ __noinline__ int learned_variant(int kind, long long bytes, int n, int dt, int op) {
+// Variant with the smallest predicted time, and the predicted log-times in pred[4] (the setup weighs the
+// tuned table's choice against them once the buffers' alignment is known); every member computes it from
+// the same inputs with the same operation order, so all members agree.  Cached per rank for repeated
+// calls of one shape.
+__device__ __noinline__ int learned_variant(int kind, long long bytes, int n, int dt, int op, float* pred) {
     RankState* R = &c_rt.ranks[me()];
     if (R->sel_key_kind == kind && R->sel_key_bytes == bytes && R->sel_key_n == n && R->sel_key_dt == dt &&
-        R->sel_key_op == op)
+        R->sel_key_op == op) {
+        for (int v = 0; v < 4; v++) pred[v] = R->sel_y[v];
         return R->sel_variant;
+    }
     MlpWork* w = &s_mlp;
     for (int i = 0; i < 12; i++) w->f[i] = 0.f;
     w->f[0] = (log2f((float)(bytes > 0 ? bytes : 1)) - 16.f) / 8.f;
@@ -478,13 +486,7 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     int best = 0;
     for (int v = 1; v < 4; v++)
         if (w->y[v] < w->y[best]) best = v;
-    // the tuned table is the fallback: its choice stands unless the network predicts a clear gain
-    const int row = kind == JOB_ALLREDUCE ? 0 : kind == JOB_REDUCE ? 1 : kind == JOB_ALLTOALLV ? 2 : -1;
-    if (row >= 0 && c_rt.tuned_table) {
-        const int b = clamp_i(ilog2_ll(bytes), 0, SEL_BYTES - 1), r = clamp_i(ilog2_ll(n), 0, SEL_RANKS - 1);
-        const int tv = c_rt.tuned_table[(row * SEL_BYTES + b) * SEL_RANKS + r];
-        if (tv >= 0 && tv < 4 && w->y[tv] <= w->y[best] + c_rt.mlp_margin) best = tv;
-    }
+    for (int v = 0; v < 4; v++) R->sel_y[v] = pred[v] = w->y[v];
     R->sel_key_kind = kind;
     R->sel_key_bytes = bytes;
     R->sel_key_n = n;
@@ -640,8 +642,11 @@ __device__ __noinline__ int fold_collective(int kind, const void* sendbuf, void*
     a.ufn = ufn;
     a.est_piece = 0;
     a.variant = c_rt.variant_override;
-    if (a.variant < 0 && c_rt.selector_mode == 2 && c_rt.mlp_params)
-        a.variant = learned_variant(kind, bytes, c->size, dt, opc);
+    a.learned = false;
+    if (a.variant < 0 && c_rt.selector_mode == 2 && c_rt.mlp_params) {
+        a.variant = learned_variant(kind, bytes, c->size, dt, opc, a.pred);
+        a.learned = true;
+    }
     int rc = coll_run(c, my, a, __LINE__);
     stage_out(ss, false);
     stage_out(rs, has_out);
@@ -672,8 +677,11 @@ __device__ __noinline__ int pull_collective(int kind, MPI_Comm_impl* c, CollSlot
     a.ufn = nullptr;
     a.est_piece = est_piece;
     a.variant = c_rt.variant_override;
-    if (a.variant < 0 && kind == JOB_ALLTOALLV && c_rt.selector_mode == 2 && c_rt.mlp_params)
-        a.variant = learned_variant(kind, est_piece * c->size, c->size, my.stype, -1);
+    a.learned = false;
+    if (a.variant < 0 && kind == JOB_ALLTOALLV && c_rt.selector_mode == 2 && c_rt.mlp_params) {
+        a.variant = learned_variant(kind, est_piece * c->size, c->size, my.stype, -1, a.pred);
+        a.learned = true;
+    }
     int rc = coll_run(c, my, a, __LINE__);
     stage_out(ss, false);
     stage_out(rs, true);
@@ -1905,9 +1913,3 @@ __device__ MPI_Op gpumpi_predefined_op(int code) {
     return (code >= 0 && code < GPUMPI_NUM_PREDEFINED_OPS) ? &g_predef_ops[code] : nullptr;
 }
 
-namespace gpumpi {
-__device__ int mlp_select(int kind, long long bytes, int n, int dt, int op) {
-    (void)kind; (void)bytes; (void)n; (void)dt; (void)op;
-    return GPUMPI_VARIANT_DIRECT;
-}
-}  // namespace gpumpi

@@ -423,12 +423,21 @@ int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value) {
 }
 
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes) {
-    // [kinds][32][16]: kinds 0 Allreduce, 1 Reduce, 2 Alltoall(v); a two-kind table leaves kind 2 unset
-    if (!w || !table || (bytes != 2 * 32 * 16 && bytes != 3 * 32 * 16)) return GPUMPI_ERR_ARG;
+    // device layout [3 kinds][2 alignment classes][32][16]; kinds 0 Allreduce, 1 Reduce, 2 Alltoall(v);
+    // class 0: every member's buffers 16-byte aligned, 1: not.  A table without classes ([2 or 3][32][16])
+    // serves both classes; a two-kind table leaves kind 2 unset.
+    constexpr size_t cell = 32 * 16;
+    if (!w || !table || (bytes != 2 * cell && bytes != 3 * cell && bytes != 6 * cell)) return GPUMPI_ERR_ARG;
+    std::vector<int8_t> img(6 * cell, (int8_t)-1);
+    if (bytes == 6 * cell) {
+        memcpy(img.data(), table, bytes);
+    } else {
+        for (size_t k = 0; k < bytes / cell; k++)
+            for (int c = 0; c < 2; c++) memcpy(img.data() + (k * 2 + c) * cell, table + k * cell, cell);
+    }
     cudaSetDevice(w->device);
-    if (!w->d_table) CK(cudaMalloc(&w->d_table, 3 * 32 * 16));
-    CK(cudaMemset(w->d_table, 0xff, 3 * 32 * 16));
-    CK(cudaMemcpy(w->d_table, table, bytes, cudaMemcpyHostToDevice));
+    if (!w->d_table) CK(cudaMalloc(&w->d_table, 6 * cell));
+    CK(cudaMemcpy(w->d_table, img.data(), 6 * cell, cudaMemcpyHostToDevice));
     return GPUMPI_SUCCESS;
 }
 

@@ -315,6 +315,7 @@ struct alignas(128) RankState {
     int sel_key_dt;
     int sel_key_op;
     int sel_variant;
+    float sel_y[4];                 // the network's predicted log-times of the cached shape
     unsigned long long coll_calls;
     Job p2p_job;
 };
@@ -369,7 +370,7 @@ struct TraceRec {
     int dt;
     int op;
     float us;
-    int pad;
+    int aligned;   // the call's buffer alignment (16, 8, 4 or 0 bytes): its tuned-table class
 };
 
 struct Runtime {
@@ -418,7 +419,7 @@ struct Runtime {
     unsigned* abort_flag;
     int* exit_codes;                  // nranks
     // selector
-    const signed char* tuned_table;   // [kind][log2 bytes][log2 ranks] -> variant (or nullptr)
+    const signed char* tuned_table;   // [kind][alignment class][log2 bytes][log2 ranks] -> variant (or nullptr)
     const float* mlp_params;          // learned selector weights (or nullptr)
     float mlp_margin;                 // learned choice overrides the tuned table only if it predicts this
                                       // much lower log-time

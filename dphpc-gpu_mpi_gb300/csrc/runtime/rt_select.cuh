@@ -12,22 +12,39 @@ namespace gpumpi {
 __device__ __forceinline__ int clamp_i(int v, int lo, int hi) { return v < lo ? lo : v > hi ? hi : v; }
 __device__ __forceinline__ int ilog2_ll(long long v) { return v <= 1 ? 0 : 63 - __clzll(v); }
 
-// tuned table layout: [kind 0..1][log2 bytes-per-rank 0..31][log2 ranks 0..15] -> variant
-constexpr int SEL_KINDS = 3, SEL_BYTES = 32, SEL_RANKS = 16;
+// tuned table layout: [kind 0..2][alignment class 0..1][log2 bytes-per-rank 0..31][log2 ranks 0..15] ->
+// variant; class 0 when every member's buffers are 16-byte aligned (aligned16 >= 16), else 1.  The
+// alignment changes the winner (at 1024 ranks x 1 MiB fp32, 16-byte aligned: DIRECT 366 us, RING 401;
+// 8-byte aligned 1.41 MiB: DIRECT 766, RING 721), and only the setup knows it: it ORs every member's
+// buffer addresses.
+constexpr int SEL_KINDS = 3, SEL_CLASSES = 2, SEL_BYTES = 32, SEL_RANKS = 16;
 
-__device__ int mlp_select(int kind, long long bytes, int n, int dt, int op);
-
-__device__ int select_variant(int kind, long long bytes_per_rank, int n, int dt, int op, int override_v) {
-    if (override_v >= 0 && override_v < GPUMPI_NUM_VARIANTS) return override_v;
+__device__ __forceinline__ int tuned_cell(int kind, long long bytes_per_rank, int n, int aligned16) {
     const int k = kind == JOB_ALLREDUCE ? 0 : kind == JOB_REDUCE ? 1 : kind == JOB_ALLTOALLV ? 2 : -1;
-    if (k < 0) return GPUMPI_VARIANT_DIRECT;
-    if (c_rt.selector_mode == 1 && c_rt.tuned_table) {
-        int b = clamp_i(ilog2_ll(bytes_per_rank), 0, SEL_BYTES - 1);
-        int r = clamp_i(ilog2_ll(n), 0, SEL_RANKS - 1);
-        int v = c_rt.tuned_table[(k * SEL_BYTES + b) * SEL_RANKS + r];
-        if (v >= 0 && v < GPUMPI_NUM_VARIANTS) return v;
+    if (k < 0 || !c_rt.tuned_table) return -1;
+    const int cls = aligned16 >= 16 ? 0 : 1;
+    const int b = clamp_i(ilog2_ll(bytes_per_rank), 0, SEL_BYTES - 1);
+    const int r = clamp_i(ilog2_ll(n), 0, SEL_RANKS - 1);
+    const int v = c_rt.tuned_table[((k * SEL_CLASSES + cls) * SEL_BYTES + b) * SEL_RANKS + r];
+    return v >= 0 && v < GPUMPI_NUM_VARIANTS ? v : -1;
+}
+
+// The setup's choice.  override_v: an explicit variant, or the learned policy's network choice (then
+// `pred` holds the network's predicted log-times and the tuned table, now that the alignment is known,
+// is the fallback: its choice stands unless the network predicts at least the margin lower time).
+__device__ int select_variant(int kind, long long bytes_per_rank, int n, int dt, int op, int override_v,
+                              int aligned16, const float* pred) {
+    if (override_v >= 0 && override_v < GPUMPI_NUM_VARIANTS) {
+        if (pred) {
+            const int tv = tuned_cell(kind, bytes_per_rank, n, aligned16);
+            if (tv >= 0 && pred[tv] <= pred[override_v] + c_rt.mlp_margin) return tv;
+        }
+        return override_v;
     }
-    if (c_rt.selector_mode == 2 && c_rt.mlp_params) return mlp_select(kind, bytes_per_rank, n, dt, op);
+    if (c_rt.selector_mode == 1) {
+        const int tv = tuned_cell(kind, bytes_per_rank, n, aligned16);
+        if (tv >= 0) return tv;
+    }
     return GPUMPI_VARIANT_DIRECT;
 }
 
@@ -44,7 +61,7 @@ __device__ __forceinline__ void trace_record(const MPI_Comm_impl* c, int kind, i
     r->dt = dt;
     r->op = op;
     r->us = (float)ns * 1e-3f;
-    r->pad = 0;
+    r->aligned = c->job.aligned16;
 }
 
 }  // namespace gpumpi

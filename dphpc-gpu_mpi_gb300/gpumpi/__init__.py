@@ -254,7 +254,7 @@ class World:
     def read_trace(self, cap: int = 1 << 20) -> np.ndarray:
         dt = np.dtype([("log2_bytes", np.float32), ("log2_ranks", np.float32), ("kind", np.int32),
                        ("variant", np.int32), ("dt", np.int32), ("op", np.int32), ("us", np.float32),
-                       ("pad", np.int32)])
+                       ("aligned", np.int32)])
         out = np.zeros(cap, dtype=dt)
         n = ctypes.c_size_t()
         self._check(lib().gpumpi_read_trace(self.h, _ptr(out), cap, ctypes.byref(n)), "read_trace")

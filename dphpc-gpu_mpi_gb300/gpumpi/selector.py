@@ -132,7 +132,7 @@ LOG2_BYTES = list(range(6, 26))          # 64 B .. 32 MiB per rank
 DTYPES = [gpumpi.FLOAT, gpumpi.INT, gpumpi.DOUBLE]
 BUDGET = 6 << 30                          # device bytes for send + recv buffers
 KINDS = (KIND_ALLREDUCE, KIND_ALLTOALLV)
-MARGIN = 0.05   # predicted log-time gain the network needs to override the tuned table (5%)
+MARGIN = 0.05   # default predicted log-time gain the network needs to override the tuned table (5%)
 TABLE_ROW = {KIND_ALLREDUCE: 0, KIND_REDUCE: 1, KIND_ALLTOALLV: 2}
 DATA = Path(__file__).resolve().parent / "data"
 
@@ -159,7 +159,8 @@ class Exchange:
 
 
 def _measure(w, torch, send, recv, n, nbytes, dt, kind, variant, iters, ex=None):
-    """Per-call records (log2 bytes seen by the kernel, us) of `iters` calls, from the runtime's trace."""
+    """Per-call records (log2 bytes seen by the kernel, us, buffer alignment) of `iters` calls, from the
+    runtime's trace."""
     w.set_policy(variant, 0)
     if kind == KIND_ALLTOALLV:
         sc, sd, rc, rd = ex.dev
@@ -172,7 +173,7 @@ def _measure(w, torch, send, recv, n, nbytes, dt, kind, variant, iters, ex=None)
         if code:
             raise gpumpi.GpumpiError(code, w.last_error())
     tr = w.read_trace()
-    return [(float(r["log2_bytes"]), float(r["us"])) for r in tr]
+    return [(float(r["log2_bytes"]), float(r["us"]), int(r["aligned"])) for r in tr]
 
 
 def _shapes_for(kind):
@@ -212,29 +213,65 @@ def autotune(iters: int = 30, log=print):
                         for v in range(NVAR):
                             recs = _measure(w, torch, send, recv, n, nbytes, dt, kind, v, iters, ex)
                             recs = recs[2:] if len(recs) > 4 else recs    # drop the first calls (cold)
-                            records += [(kind, n, l2b, dt, v, u) for l2b, u in recs]
-                            # table cell: log2 bytes as the kernel sees them
+                            records += [(kind, n, l2b, dt, v, u) for l2b, u, _ in recs]
+                            # table cell: log2 bytes as the kernel sees them, alignment class
                             cell = int(math.floor(recs[0][0])) if recs and recs[0][0] > 0 else 0
-                            grid[(kind, n, nbytes, dt, v)] = (cell, float(np.median([u for _, u in recs])))
+                            cls = 0 if recs and recs[0][2] >= 16 else 1
+                            grid[(kind, n, nbytes, dt, v)] = (cell, cls, float(np.median([u for _, u, _ in recs])),
+                                                              recs[0][0] if recs else 0.0)
         info = w.info()
         shares[n] = n / (n + info["engine_blocks"])
         log(f"autotune: {n} ranks done in {time.time() - t0:.1f}s ({len(records)} records); world {info}")
         w.close()
         del send, recv
         torch.cuda.empty_cache()
-    # table: per (kind, cell of log2 bytes, log2 ranks) the variant with the least summed median time over
-    # every shape measured in the cell (both sizes, every datatype)
+    # table: per (kind, alignment class, cell of log2 bytes, log2 ranks) the variant with the least summed
+    # median time over every shape measured in the cell (every datatype); class 0 = 16-byte aligned buffers
+    # (the power-of-two sizes), 1 = not (the off-grid sizes, 8 mod 16 bytes); a class the sweep did not
+    # reach in a cell takes the other class's choice
     sums = {}
-    for (kind, n, nbytes, dt, v), (cell, t) in grid.items():
-        key = (kind, n, cell)
+    for (kind, n, nbytes, dt, v), (cell, cls, t, _) in grid.items():
+        key = (kind, n, cell, cls)
         sums.setdefault(key, np.zeros(NVAR))[v] += t
-    table = np.full((3, 32, 16), -1, np.int8)
-    for (kind, n, cell), tv in sums.items():
+    table = np.full((3, 2, 32, 16), -1, np.int8)
+    for (kind, n, cell, cls), tv in sums.items():
         best = int(np.argmin(tv))
-        table[TABLE_ROW[kind], min(31, cell), int(math.log2(n))] = best
+        table[TABLE_ROW[kind], cls, min(31, cell), int(math.log2(n))] = best
         if kind == KIND_ALLREDUCE:
-            table[TABLE_ROW[KIND_REDUCE], min(31, cell), int(math.log2(n))] = best
-    return records, table, {f"{k[0]}:{k[1]}:{k[2]}:{k[3]}:{k[4]}": t for k, (c, t) in grid.items()}, shares
+            table[TABLE_ROW[KIND_REDUCE], cls, min(31, cell), int(math.log2(n))] = best
+    for cls in (0, 1):
+        other = table[:, 1 - cls]
+        mine = table[:, cls]
+        mine[mine < 0] = other[mine < 0]
+    return records, table, grid, shares
+
+
+def choose_margin(mlp, table, grid, shares, candidates=(0.05, 0.1, 0.2, 0.3, 0.5, 1.0, 2.0)):
+    """The override margin of the learned policy, chosen on the sweep's own shapes (never on the held-out
+    stream): the one with the least total time of "the table's choice unless the network predicts at least
+    the margin lower log-time" (ties go to the larger margin)."""
+    shapes = {}
+    for (kind, n, nbytes, dt, v), (cell, cls, t, l2b) in grid.items():
+        s = shapes.setdefault((kind, n, nbytes, dt), {"t": [np.inf] * NVAR, "cell": cell, "cls": cls, "l2b": l2b})
+        s["t"][v] = t
+    keys = [k for k in shapes if all(np.isfinite(shapes[k]["t"]))]
+    if not keys:
+        return MARGIN
+    X = np.stack([features(k, 2.0 ** shapes[(k, n, b, dt)]["l2b"], n, dt,
+                           gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1, shares[n]) for (k, n, b, dt) in keys])
+    pred = mlp.predict(X)
+    best_m, best_t = MARGIN, None
+    for m in candidates:
+        tot = 0.0
+        for i, key in enumerate(keys):
+            s = shapes[key]
+            tv = int(table[TABLE_ROW[key[0]], s["cls"], min(31, s["cell"]), int(math.log2(key[1]))])
+            pure = int(np.argmin(pred[i]))
+            pick = tv if (tv >= 0 and pred[i][tv] <= pred[i][pure] + m) else pure
+            tot += s["t"][pick]
+        if best_t is None or tot <= best_t:
+            best_m, best_t = m, tot
+    return best_m
 
 
 def dataset(records, rank_share_of):
@@ -249,11 +286,12 @@ def dataset(records, rank_share_of):
 
 
 def evaluate(mlp_params, table, calls: int = 10000, shapes_per_rank: int = 12, seed: int = 2026, iters: int = 12,
-             log=print):
+             log=print, margin: float = None):
     """Held-out stream: `calls` seeded calls, half Allreduce (fp32/int32/fp64 SUM) and half uneven int32
     Alltoallv, sizes log-uniform 64 B .. 32 MiB per rank, 16 .. 2048 ranks, drawn from off-grid shapes;
     every variant of every shape is measured, so the exhaustive best is known."""
     import torch
+    margin = MARGIN if margin is None else margin
     rng = np.random.default_rng(seed)
     shapes = []
     for n in RANKS:
@@ -279,8 +317,8 @@ def evaluate(mlp_params, table, calls: int = 10000, shapes_per_rank: int = 12, s
             for v in range(NVAR):
                 recs = _measure(w, torch, send, recv, n, b, dt, kind, v, iters, ex)
                 recs = recs[2:] if len(recs) > 4 else recs
-                times.append(float(np.median([u for _, u in recs])))
-                seen[(kind, n, b, dt)] = recs[0][0]   # log2 bytes as the kernel saw it
+                times.append(float(np.median([u for _, u, _ in recs])))
+                seen[(kind, n, b, dt)] = (recs[0][0], recs[0][2])   # log2 bytes and alignment the kernel saw
             meas[(kind, n, b, dt)] = times
         shares[n] = n / (n + w.info()["engine_blocks"])
         w.close()
@@ -288,15 +326,16 @@ def evaluate(mlp_params, table, calls: int = 10000, shapes_per_rank: int = 12, s
         torch.cuda.empty_cache()
     keys = list(meas)
     # the learned and tuned choices use what the kernel computes per call (bytes estimate, rank share)
-    X = np.stack([features(k, 2.0 ** seen[(k, n, b, dt)], n, dt, gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1,
+    X = np.stack([features(k, 2.0 ** seen[(k, n, b, dt)][0], n, dt, gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1,
                            shares[n]) for (k, n, b, dt) in keys])
     pred = mlp.predict(X)
     pick = {}
     for i, key in enumerate(keys):
         kind, n, b, dt = key
-        tv = int(table[TABLE_ROW[kind], min(31, max(0, int(math.floor(seen[key])))), int(math.log2(n))])
+        l2b, al = seen[key]
+        tv = int(table[TABLE_ROW[kind], 0 if al >= 16 else 1, min(31, max(0, int(math.floor(l2b)))), int(math.log2(n))])
         pure = int(np.argmin(pred[i]))
-        learned = tv if (tv >= 0 and pred[i][tv] <= pred[i][pure] + MARGIN) else pure  # same rule as the kernel
+        learned = tv if (tv >= 0 and pred[i][tv] <= pred[i][pure] + margin) else pure  # same rule as the kernel
         pick[key] = {"learned": learned, "learned_pure": pure, "tuned": tv if tv >= 0 else 0, "plain": 0}
     idx = rng.integers(0, len(keys), calls)
     pols = ("learned", "learned_pure", "tuned", "plain")
@@ -347,14 +386,16 @@ def run(out: Path, iters: int = 30):
     mv = torch.from_numpy(M[va]).cuda()
     vloss, _ = mlp.loss_grad(xv, tv, mv)
     params = mlp.params()
+    margin = choose_margin(mlp, table, grid, shares)
+    print(f"override margin chosen on the sweep shapes: {margin}", flush=True)
     np.save(out / "tuned_table.npy", table)
     np.save(out / "mlp_params.npy", params)
-    rep = evaluate(params, table)
+    rep = evaluate(params, table, margin=margin)
     rep.update({"train_records": int(len(tr)), "val_records": int(len(va)), "train_loss": hist,
                 "val_loss": float(vloss.item()), "sweep_seconds": time.time() - t0,
                 "records_by_kind": {str(k): int(sum(1 for r in records if r[0] == k)) for k in KINDS},
-                "grid_median_us": grid})
-    rep["margin"] = MARGIN
+                "grid_median_us": {f"{k[0]}:{k[1]}:{k[2]}:{k[3]}:{k[4]}": g[2] for k, g in grid.items()}})
+    rep["margin"] = margin
     (out / "selector_report.json").write_text(json.dumps(rep, indent=1))
     print(json.dumps({k: rep[k] for k in ("all", "allreduce", "alltoallv", "val_loss", "train_records")}))
 
@@ -365,6 +406,14 @@ def load_packaged():
     if not (t.exists() and p.exists()):
         return None, None
     return np.load(t), np.load(p)
+
+
+def packaged_margin() -> float:
+    """The override margin the packaged network was evaluated with (chosen on its sweep), else MARGIN."""
+    rep = DATA / "selector_report.json"
+    if rep.exists():
+        return float(json.loads(rep.read_text()).get("margin", MARGIN))
+    return MARGIN
 
 
 def apply_policy(world, policy: str):
@@ -385,7 +434,7 @@ def apply_policy(world, policy: str):
     elif policy == "learned":
         world.set_tuned_table(table)
         world.set_mlp(params)
-        world.set_tuning(gpumpi.TUNE_MLP_MARGIN, int(round(MARGIN * 1000)))
+        world.set_tuning(gpumpi.TUNE_MLP_MARGIN, int(round(packaged_margin() * 1000)))
         world.set_policy(-1, 2)
     else:
         raise ValueError(policy)

@@ -174,12 +174,14 @@ int gpumpi_main(int argc, char** argv, int program);
 #define GPUMPI_P_USER 200
 /* The current value of a GPUMPI_TUNE_* knob. */
 int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value);
-/* Tuned table: int8 [3][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; log2 bytes per
- * rank; log2 ranks) -> variant or -1, host memory; a [2][32][16] table leaves Alltoall(v) untuned. */
+/* Tuned table: int8 [3][2][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; alignment class:
+ * 0 when every member's buffers are 16-byte aligned, else 1; log2 bytes per rank; log2 ranks) -> variant
+ * or -1, host memory.  A [3][32][16] table serves both classes; a [2][32][16] one leaves Alltoall(v)
+ * untuned. */
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes);
 /* Learned selector weights: float[GPUMPI_MLP_NPARAMS] in the layout of the training kernels. */
 int gpumpi_set_mlp(gpumpi_world* w, const float* params, size_t count);
-/* Timing trace: copies up to `cap` records {log2 bytes, log2 ranks, kind, variant, dt, op, us, pad}
+/* Timing trace: copies up to `cap` records {log2 bytes, log2 ranks, kind, variant, dt, op, us, aligned}
  * (32 bytes each) into host memory; returns the number of records written in *n. */
 int gpumpi_read_trace(gpumpi_world* w, void* host_out, size_t cap, size_t* n);
 

@@ -103,7 +103,7 @@ def test_packaged_policies_give_exact_integer_results(gpulib, oracle):
     is exact on integer Allreduce and Alltoallv."""
     from gpumpi import selector
     table, params = selector.load_packaged()
-    assert table is not None and table.shape == (3, 32, 16) and params.shape == (gpulib.MLP_NPARAMS,)
+    assert table is not None and table.shape == (3, 2, 32, 16) and params.shape == (gpulib.MLP_NPARAMS,)
     n, count = 96, 3000
     x = oracle.fill_i32(9, n * count).reshape(n, count) % 1000
     ref = oracle.allreduce(x, 2, 2)
