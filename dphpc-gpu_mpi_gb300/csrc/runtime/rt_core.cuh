@@ -104,6 +104,18 @@ __device__ __forceinline__ bool is_shared_ptr(const void* p) {
 // ------------------------------------------------------------------------------------------------
 // datatype descriptors (predefined and derived)
 // ------------------------------------------------------------------------------------------------
+// What a typed copy reads of a datatype, laid out for six 16-byte loads (filled by desc_prepare in
+// rt_types.cuh): the 32-bit mapping of a packed offset to a byte address.
+struct alignas(16) TypeImg {
+    unsigned d[4];        // divisors: size, block, cnt[0], cnt[1] (1 where unused)
+    unsigned m[4];        // their FastDiv multipliers
+    unsigned sh[4];       //   and shifts, s1 | s2 << 8
+    long long lb, extent;
+    long long st[3];      // strides of levels 0..2
+    int nlev;
+    int fast_unit;        // copy unit when the 32-bit mapping applies (size < 2^31, <= 3 levels), else 0
+};
+
 struct TypeDesc {
     long long size;       // bytes of data in one element
     long long extent;     // lb..ub span
@@ -116,10 +128,9 @@ struct TypeDesc {
     int committed;
     int in_use;
     // set when the type is built (desc_prepare in rt_types.cuh):
-    unsigned fd_m[4];     // 32-bit division constants of size, block, cnt[0], cnt[1] (FastDiv)
-    unsigned fd_sh[4];    //   and their shifts, s1 | s2 << 8
     int unit;             // largest power of two (<= 16) dividing block, size, extent, lb and the strides
     int fd_ready;         // the 32-bit mapping applies: size < 2^31 and at most 3 levels
+    TypeImg img;          // the mapping image (all zero, i.e. not ready, for the predefined types)
 };
 
 // ------------------------------------------------------------------------------------------------

@@ -91,8 +91,9 @@ __device__ __forceinline__ long long pow2_div(long long v) {  // largest power o
     return a > 16 ? 16 : a;
 }
 
-// Completes a descriptor once its shape is final: the copy unit it allows and the division constants
-// of its 32-bit mapping, so that no copy divides by a variable.
+// Completes a descriptor once its shape is final: the copy unit it allows and the image of its 32-bit
+// mapping with the division constants, so that no copy divides by a variable and a copying warp reads the
+// whole mapping with one 16-byte load per lane.
 __device__ __forceinline__ void desc_prepare(TypeDesc* t) {
     long long u = 16;
     u = min(u, pow2_div(t->block));
@@ -101,14 +102,22 @@ __device__ __forceinline__ void desc_prepare(TypeDesc* t) {
     u = min(u, pow2_div(t->lb));
     for (int l = 0; l < t->nlev; l++) u = min(u, pow2_div(t->stride[l]));
     t->unit = (int)u;
+    TypeImg& g = t->img;
     const long long v[4] = {t->size, t->block, t->cnt[0], t->cnt[1]};
     for (int k = 0; k < 4; k++) {
+        const unsigned dv = v[k] > 0 && v[k] <= 0x7fffffffLL ? (unsigned)v[k] : 1u;
         FastDiv f;
-        f.init(v[k] > 0 && v[k] <= 0x7fffffffLL ? (unsigned)v[k] : 1u);
-        t->fd_m[k] = f.m;
-        t->fd_sh[k] = f.s1 | (f.s2 << 8);
+        f.init(dv);
+        g.d[k] = dv;
+        g.m[k] = f.m;
+        g.sh[k] = f.s1 | (f.s2 << 8);
     }
+    g.lb = t->lb;
+    g.extent = t->extent;
+    for (int l = 0; l < 3; l++) g.st[l] = t->stride[l];
+    g.nlev = t->nlev;
     t->fd_ready = t->size >= 0 && t->size <= 0x7fffffffLL && t->nlev <= 3;
+    g.fast_unit = t->fd_ready ? t->unit : 0;
 }
 
 // Unit (1..16 bytes) that divides every block, stride, extent, offset and base address involved.
@@ -163,36 +172,34 @@ __device__ __forceinline__ void store_unit(char* d, typename UnitType<U>::T v) {
 // shared memory at every use (volatile) keeps the loop's registers for the data in flight: with both
 // descriptors in registers the loop spills, and a spilled load serialises the memory round trips.
 struct DescS {
-    unsigned d[4], m[4], sh[4];  // size, block, cnt[0], cnt[1]: divisor, magic number, shifts
-    int nlev;
-    int same;                    // (destination slot) both sides have the same shape, lb aside
-    long long lb, extent, st[3];
+    TypeImg t;
+    int same;                    // (destination slot) both sides have the same mapping, lb aside
+    int pad;
     long long shift;             // (destination slot) destination lb - source lb, when same
 };
 constexpr int kMaxWarps = 8;
+constexpr int kImgVecs = (int)(sizeof(TypeImg) / 16);
+static_assert(sizeof(TypeImg) % 16 == 0 && kImgVecs <= 8, "a mapping image is at most eight 16-byte vectors");
 __shared__ DescS s_tdesc[kMaxWarps][2];
 
-__device__ __forceinline__ void descs_fill(DescS* o, const TypeDesc* t) {
-    const long long v[4] = {t->size, t->block, t->cnt[0], t->cnt[1]};
-    for (int k = 0; k < 4; k++) {
-        o->d[k] = v[k] > 0 && v[k] <= 0x7fffffffLL ? (unsigned)v[k] : 1u;
-        o->m[k] = t->fd_m[k];
-        o->sh[k] = t->fd_sh[k];
-    }
-    o->nlev = t->nlev;
-    o->lb = t->lb;
-    o->extent = t->extent;
-    for (int l = 0; l < 3; l++) o->st[l] = t->stride[l];
+// Lane l < kImgVecs copies vector l of the source image, lane 8 + l that of the destination image
+// (a null descriptor's slot is left alone): the whole mapping in one memory round trip per warp.
+__device__ __forceinline__ void img_load_lane(DescS* slot, const TypeDesc* st_, const TypeDesc* dt_, int l32) {
+    const int k = l32 & 7;
+    const TypeDesc* t = l32 < 8 ? st_ : l32 < 16 ? dt_ : nullptr;
+    if (t && k < kImgVecs) ((uint4*)&slot[l32 >> 3].t)[k] = ((const uint4*)&t->img)[k];
 }
 
-__device__ __forceinline__ bool same_shape(const TypeDesc* a, const TypeDesc* b) {
-    if (a->size != b->size || a->block != b->block || a->nlev != b->nlev || a->extent != b->extent) return false;
-    for (int l = 0; l < a->nlev; l++)
-        if (a->cnt[l] != b->cnt[l] || a->stride[l] != b->stride[l]) return false;
-    return true;
+// Both images map every packed offset to the same address up to lb: equal divisors, levels, extent and
+// the strides of the levels in use (the multipliers follow from the divisors).
+__device__ __forceinline__ bool same_mapping(const volatile TypeImg* a, const volatile TypeImg* b) {
+    bool eq = a->nlev == b->nlev && a->extent == b->extent;
+    for (int k = 0; k < 4; k++) eq = eq && a->d[k] == b->d[k];
+    for (int l = 0; l < 3; l++) eq = eq && (l >= a->nlev || a->st[l] == b->st[l]);
+    return eq;
 }
 
-__device__ __forceinline__ unsigned fdiv_s(const volatile DescS* t, int k, unsigned n) {
+__device__ __forceinline__ unsigned fdiv_s(const volatile TypeImg* t, int k, unsigned n) {
     const unsigned th = __umulhi(t->m[k], n);
     const unsigned sh = t->sh[k];
     return (th + ((n - th) >> (sh & 255u))) >> (sh >> 8);
@@ -200,7 +207,7 @@ __device__ __forceinline__ unsigned fdiv_s(const volatile DescS* t, int k, unsig
 
 // Byte address of packed offset off.  q < size = block * cnt[0] * ... * cnt[nlev-1], so the outermost
 // level's index is the last quotient and needs no division.
-__device__ __forceinline__ long long map_s(const volatile DescS* t, unsigned off) {
+__device__ __forceinline__ long long map_s(const volatile TypeImg* t, unsigned off) {
     const unsigned e = fdiv_s(t, 0, off);
     const unsigned q = off - e * t->d[0];
     const unsigned blk = fdiv_s(t, 1, q);
@@ -224,10 +231,12 @@ __device__ __forceinline__ long long map_s(const volatile DescS* t, unsigned off
 template <int U, bool CG>
 __device__ __forceinline__ void typed_copy_fast(char* db, bool dmap, const char* sb, bool smap, unsigned b0, unsigned b1,
                                              int lane, int nl) {
-    const volatile DescS* ss = &s_tdesc[threadIdx.x >> 5][0];
-    const volatile DescS* ds = &s_tdesc[threadIdx.x >> 5][1];
-    const bool same = smap && dmap && ds->same;
-    if (same) db += ds->shift;
+    const volatile DescS* ss_ = &s_tdesc[threadIdx.x >> 5][0];
+    const volatile DescS* ds_ = &s_tdesc[threadIdx.x >> 5][1];
+    const volatile TypeImg* ss = &ss_->t;
+    const volatile TypeImg* ds = &ds_->t;
+    const bool same = smap && dmap && ds_->same;
+    if (same) db += ds_->shift;
     const unsigned step = (unsigned)nl * U;
     unsigned off = b0 + (unsigned)lane * U;
     // K loads issued before the K stores: a strided unit is its own memory round trip, and a store
@@ -282,32 +291,47 @@ __device__ __noinline__ void typed_copy_u(char* db, const TypeDesc* dt_, const c
 // Executed by nl cooperating threads, this one being `lane`: one thread, or whole warps.
 __device__ __noinline__ void typed_copy(void* db, const TypeDesc* dt_, const void* sb, const TypeDesc* st_,
                                         long long b0, long long b1, int lane, int nl) {
-    int u = typed_unit(st_, sb, dt_, db);
-    u = min(u, (int)pow2_div(b0));
-    u = min(u, (int)pow2_div(b1));
     char* d = (char*)db;
     const char* s = (const char*)sb;
     const bool cg = is_global_ptr(db) && is_global_ptr(sb);
-    const bool fast = b1 <= 0x7fffffffLL && b0 >= 0 && (!st_ || st_->fd_ready) && (!dt_ || dt_->fd_ready) &&
-                      (nl == 1 || (nl & 31) == 0) && (threadIdx.x >> 5) < kMaxWarps;
-    if (fast) {
+    int u;
+    if (b1 <= 0x7fffffffLL && b0 >= 0 && (nl == 1 || (nl & 31) == 0) && (threadIdx.x >> 5) < kMaxWarps) {
+        // the mapping images into this warp's slots (one round trip), then every decision from shared memory
         DescS* slot = s_tdesc[threadIdx.x >> 5];
-        if (nl > 1) __syncwarp();
-        if (nl == 1 || (threadIdx.x & 31) == 0) {
-            if (st_) descs_fill(&slot[0], st_);
-            if (dt_) descs_fill(&slot[1], dt_);
-            slot[1].same = st_ && dt_ && same_shape(st_, dt_);
-            slot[1].shift = slot[1].same ? dt_->lb - st_->lb : 0;
-        }
-        if (nl > 1) __syncwarp();
-        const unsigned c0 = (unsigned)b0, c1 = (unsigned)b1;
-        if (cg) {
-            GPUMPI_TYPED_SWITCH(typed_copy_fast, true, d, dt_ != nullptr, s, st_ != nullptr, c0, c1, lane, nl)
+        if (nl > 1) {
+            __syncwarp();
+            img_load_lane(slot, st_, dt_, (int)(threadIdx.x & 31));
+            __syncwarp();
         } else {
-            GPUMPI_TYPED_SWITCH(typed_copy_fast, false, d, dt_ != nullptr, s, st_ != nullptr, c0, c1, lane, nl)
+#pragma unroll
+            for (int l = 0; l < 16; l++) img_load_lane(slot, st_, dt_, l);
         }
-        return;
+        const volatile DescS* vs = slot;
+        const int us = st_ ? vs[0].t.fast_unit : 16, ud = dt_ ? vs[1].t.fast_unit : 16;
+        if (us && ud) {
+            if (nl == 1 || (threadIdx.x & 31) == 0) {
+                const bool same = st_ && dt_ && same_mapping(&vs[0].t, &vs[1].t);
+                slot[1].same = same;
+                slot[1].shift = same ? vs[1].t.lb - vs[0].t.lb : 0;
+            }
+            if (nl > 1) __syncwarp();
+            u = min(us, ud);
+            u = min(u, (int)pow2_div((long long)(size_t)sb));
+            u = min(u, (int)pow2_div((long long)(size_t)db));
+            u = min(u, (int)pow2_div(b0));
+            u = min(u, (int)pow2_div(b1));
+            const unsigned c0 = (unsigned)b0, c1 = (unsigned)b1;
+            if (cg) {
+                GPUMPI_TYPED_SWITCH(typed_copy_fast, true, d, dt_ != nullptr, s, st_ != nullptr, c0, c1, lane, nl)
+            } else {
+                GPUMPI_TYPED_SWITCH(typed_copy_fast, false, d, dt_ != nullptr, s, st_ != nullptr, c0, c1, lane, nl)
+            }
+            return;
+        }
     }
+    u = typed_unit(st_, sb, dt_, db);
+    u = min(u, (int)pow2_div(b0));
+    u = min(u, (int)pow2_div(b1));
     if (cg) {
         GPUMPI_TYPED_SWITCH(typed_copy_u, true, d, dt_, s, st_, b0, b1, lane, nl)
     } else {
