@@ -453,6 +453,71 @@ def p2p_sweep(args, gpumpi, torch, local):
     print(json.dumps({"case": "p2p_sweep", "iterations": iters, "rows": rows}), flush=True)
 
 
+def coll_sweep(args, gpumpi, torch, local):
+    """Collectives sweep: MPI_Bcast (root 0), MPI_Allreduce SUM on int32, fp32 and fp64, and MPI_Alltoall,
+    32..2048 ranks, 4 B .. 16 MiB per rank, default (heuristic) variant choice.  Inputs: int32 uniform in
+    [0, 1000] from a seed (read as fp32 / fp64 bit patterns, small finite values, for the floating-point
+    Allreduces).  Per
+    shape: p50/p99 of rank 0's per-iteration time over 10 calls after 3 warm-up calls, and GB/s of the
+    algorithmic bytes (Allreduce 2 n b, Bcast b + n b, Alltoall 2 n b with b = bytes a rank sends).  The
+    int32 Allreduce, the Bcast and the Alltoall are checked bit for bit on sampled ranks."""
+    import numpy as np
+    iters, warm = 10, 3
+    rows = []
+    sizes = [4, 64, 1 << 10, 1 << 14, 1 << 18, 1 << 22, 1 << 24]
+    rng = np.random.default_rng(11)
+
+    def timed(fn):
+        fn(warm, None)
+        ns = np.zeros(iters, dtype=np.uint64)
+        fn(iters, ns)
+        return float(np.percentile(ns, 50)) / 1e3, float(np.percentile(ns, 99)) / 1e3
+
+    for n in (32, 128, 512, 1024, 2048):
+        with gpumpi.World(n, device=local, timeout_s=120.0) as w:
+            maxb = max(sizes)
+            g = torch.Generator(device="cuda").manual_seed(n)
+            send = torch.randint(0, 1001, (n * maxb // 4,), generator=g, device="cuda", dtype=torch.int32)
+            recv = torch.empty_like(send)
+            for b in sizes:
+                cnt = b // 4
+                s2, r2 = send[: n * cnt].view(n, cnt), recv[: n * cnt].view(n, cnt)
+                sample = sorted({0, n - 1, int(rng.integers(0, n))})
+                for name, dt, view in (("allreduce_int32", gpumpi.INT, None),
+                                       ("allreduce_fp32", gpumpi.FLOAT, torch.float32),
+                                       ("allreduce_fp64", gpumpi.DOUBLE, torch.float64)):
+                    if dt == gpumpi.DOUBLE and b < 8:
+                        continue
+                    s_, r_ = (s2, r2) if view is None else (s2.view(view), r2.view(view))
+                    c_ = s_.shape[1]
+                    p50, p99 = timed(lambda k, ns: w.allreduce(s_, r_, c_, dt, gpumpi.OP_SUM, iters=k, iter_ns=ns))
+                    row = {"coll": name, "ranks": n, "bytes_per_rank": b, "p50_us": p50, "p99_us": p99,
+                           "gbs": 2.0 * n * b / (p50 * 1e-6) / 1e9}
+                    if view is None:
+                        ref = torch.zeros(cnt, dtype=torch.int64, device="cuda")
+                        for i in range(0, n, 64):
+                            ref += s2[i:i + 64].sum(0, dtype=torch.int64)
+                        ref = ref.to(torch.int32)
+                        row["bit_exact"] = all(bool(torch.equal(r2[q], ref)) for q in sample)
+                    rows.append(row)
+                r2.copy_(s2)
+                p50, p99 = timed(lambda k, ns: w.bcast(r2, cnt, gpumpi.INT, 0, iters=k, iter_ns=ns))
+                rows.append({"coll": "bcast", "ranks": n, "bytes_per_rank": b, "p50_us": p50, "p99_us": p99,
+                             "gbs": (b + n * b) / (p50 * 1e-6) / 1e9,
+                             "bit_exact": all(bool(torch.equal(r2[q], s2[0])) for q in sample)})
+                c = max(1, cnt // n)                       # int32 per pair
+                s3, r3 = send[: n * n * c].view(n, n * c), recv[: n * n * c].view(n, n * c)
+                r3.zero_()
+                p50, p99 = timed(lambda k, ns: w.alltoall(s3, r3, c, gpumpi.INT, iters=k, iter_ns=ns))
+                ok = all(bool(torch.equal(r3[q, t * c:(t + 1) * c], s3[t, q * c:(q + 1) * c]))
+                         for q in sample for t in sample)
+                rows.append({"coll": "alltoall", "ranks": n, "bytes_per_rank": n * c * 4, "p50_us": p50,
+                             "p99_us": p99, "gbs": 2.0 * n * n * c * 4 / (p50 * 1e-6) / 1e9, "bit_exact": ok})
+            del send, recv
+            torch.cuda.empty_cache()
+    print(json.dumps({"case": "coll_sweep", "iterations": iters, "warmup": warm, "rows": rows}), flush=True)
+
+
 def small_case(args, gpumpi, torch, local):
     """Allreduce fp32 SUM, 1024 ranks x 256 KiB (512 MiB of traffic per call): the profiled case."""
     n, count = 1024, 65536
@@ -476,9 +541,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extra", action="store_true")
-    ap.add_argument("--case", default="full", choices=["full", "small", "alltoallv_small", "p2p_sweep"],
+    ap.add_argument("--case", default="full",
+                    choices=["full", "small", "alltoallv_small", "p2p_sweep", "coll_sweep"],
                     help="small: Allreduce 1024 ranks x 256 KiB; alltoallv_small: Alltoallv 1024 ranks x "
-                         "256 KiB; device timing only (the ncu capture cases)")
+                         "256 KiB; device timing only (the ncu capture cases); p2p_sweep / coll_sweep: the "
+                         "point-to-point and collectives sweeps")
     ap.add_argument("--variant", type=int, default=-1, help="variant override for the small cases")
     args = ap.parse_args()
     dist, rank, ws = dist_setup()
@@ -500,6 +567,9 @@ def main():
         return
     if args.case == "p2p_sweep":
         p2p_sweep(args, gpumpi, torch, local)
+        return
+    if args.case == "coll_sweep":
+        coll_sweep(args, gpumpi, torch, local)
         return
     n, per = WORKLOAD["ranks"], WORKLOAD["bytes_per_rank"]
     count = per // 4
