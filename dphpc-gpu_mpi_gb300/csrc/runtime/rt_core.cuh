@@ -65,17 +65,11 @@ __device__ __forceinline__ unsigned long long atom_exch_release64(unsigned long 
     asm volatile("atom.release.gpu.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
     return old;
 }
-__device__ __forceinline__ void fence_acqrel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
-
-// Spin-waits poll with relaxed loads and order what follows with one fence once the awaited value is
+// Spin-waits poll with relaxed loads and order what follows with this one fence once the awaited value is
 // seen.  An acquire load or fence makes the SM drop its L1 contents, so acquire-polling from any block
 // (idle copy engines, a rank waiting for a message) would turn every cached read of the other blocks on
 // that SM (runtime tables, descriptors, spilled registers' lines) into an L2 round trip.
-__device__ __forceinline__ bool seen_u32(const unsigned* p, unsigned v) {
-    if (ld_relaxed(p) != v) return false;
-    fence_acqrel();
-    return true;
-}
+__device__ __forceinline__ void fence_acqrel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
 __device__ __forceinline__ unsigned long long now_ns() {
     unsigned long long t;
@@ -445,7 +439,6 @@ struct Runtime {
 // memory keeps these reads out of L1, which every acquire on the SM invalidates.
 extern __constant__ Runtime c_rt;
 
-__device__ __forceinline__ int my_block() { return (int)blockIdx.x; }
 __device__ __forceinline__ int nthreads() { return (int)blockDim.x; }
 
 // ------------------------------------------------------------------------------------------------
