@@ -12,7 +12,6 @@ from __future__ import annotations
 
 import ctypes
 import sys
-import os
 from pathlib import Path
 
 import numpy as np

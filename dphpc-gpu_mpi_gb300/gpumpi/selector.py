@@ -19,7 +19,6 @@ writes tuned_table.npy, mlp_params.npy, selector_report.json into <dir>.
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
 import math
 import sys

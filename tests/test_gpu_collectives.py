@@ -67,7 +67,6 @@ def test_allreduce_host_buffers_and_in_place(gpulib, oracle):
         w.allreduce(x, out, count, 12, 2)          # host (numpy) buffers, staged by the library
         assert np.array_equal(out, ref)
         buf = dev(x)
-        import ctypes
         rc = w.coll("allreduce", 1, buf, count, 12, 2, send_stride=0, recv_stride=count * 4)  # MPI_IN_PLACE
         assert rc == 0, w.last_error()
         assert np.array_equal(host(buf), ref)

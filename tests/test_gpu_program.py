@@ -14,7 +14,7 @@ sys.path.insert(0, str(ROOT / "dphpc-gpu_mpi_gb300"))
 
 
 @pytest.fixture(scope="module")
-def pi_exe(tmp_path_factory):
+def pi_exe(tmp_path_factory, gpulib):   # gpulib: skips without a GPU
     import build
     out = tmp_path_factory.mktemp("prog") / "mpi_pi"
     return build.build_program([ROOT / "tests" / "programs" / "mpi_pi_integrate.cu"], out)

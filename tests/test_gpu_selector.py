@@ -1,7 +1,6 @@
 """GPU: the learned selector's network trained by the library's own kernels — forward and gradients
 against the CPU oracle's fp64 restatement, training, what the trained network gains over the plain
 policy, and the tuned-table / learned policies driving real collectives."""
-import math
 
 import numpy as np
 import pytest
