@@ -20,9 +20,12 @@ Reported:
              plain / tuned / learned policies on the headline Allreduce and the uneven Alltoallv, and the
              held-out regret of the packaged tuned table and network.
 
+  parity     the headline result of every rank compared bit for bit with the CPU oracle's canonical
+             rank-order fold of the same inputs (outside the timed region); a mismatch fails the run.
+
 --impl reference: the reference's algorithm for this path restated on the CPU (the oracle port:
-canonical-order fold, all host threads) on the same workload; the reference's own gpu_mpi runtime
-cannot run on the GPU machine.
+canonical-order fold, all host threads) on the same workload.  The reference has no CPU
+implementation of its own: its runtime is GPU code.
 """
 import argparse
 import json
@@ -120,6 +123,10 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of the 1024 ranks x 256 KiB "
+                  "capture (profiles/allreduce_fold_1024ranks.md), scaled x4 to 1 MiB per rank")
+
+
 def traffic_from_profile():
     """DRAM bytes per step of the allreduce from the committed ncu summary (scaled to the bench size)."""
     p = ROOT / "profiles" / "allreduce_fold_1024ranks.md"
@@ -158,6 +165,21 @@ def cpu_baseline(threads: int):
     return {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": f"oracle allreduce fp32 SUM, full workload (1024 ranks x 1 MiB), {steps} calls after 3 "
                       f"warm-up calls, {threads} threads"}
+
+
+def parity_vs_oracle(send, recv, torch):
+    """Every rank's headline result against the oracle's canonical rank-order fold of the same inputs,
+    bit for bit (fails the run on a mismatch).  Outside the timed region."""
+    import numpy as np
+    from oracle import oracle
+    torch.cuda.synchronize()
+    ref = oracle.reduce(send.cpu().numpy(), 12, 2)
+    ref_d = torch.from_numpy(np.ascontiguousarray(ref)).cuda()
+    bad = (~(recv.view(torch.int32) == ref_d.view(torch.int32).unsqueeze(0)).all(1)).nonzero().flatten()
+    if bad.numel():
+        raise SystemExit(f"parity failure: {bad.numel()} of {recv.shape[0]} ranks differ from the oracle "
+                         f"(first {bad[:8].tolist()})")
+    return f"bit-exact vs oracle (all {recv.shape[0]} ranks)"
 
 
 def run_reference(args, dist, rank, ws):
@@ -231,9 +253,12 @@ def bench_alltoallv_1024(gpumpi, torch, w_kw, uniform: bool):
     dsc, dsd, drc, drd = (torch.from_numpy(a).cuda() for a in (sc, sd, rc, rd))
     total = int(sc.sum()) * 4
     out = {"ranks": n, "bytes_moved_per_call": total, "counts": "uniform 256" if uniform else "uniform [0,512]"}
+    from oracle import oracle
+    ref = oracle.alltoallv(send.cpu().numpy(), sc, sd, R, rc, rd, threads=os.cpu_count() or 1)
+    exact = []
     with gpumpi.World(n, **w_kw) as w:
-        for v, name in ((0, "direct"), (1, "tree"), (2, "ring"), (3, "staged")):
-            w.set_policy(v, 0)
+        for v, name in ((-1, "default"), (0, "direct"), (1, "tree"), (2, "ring"), (3, "staged")):
+            w.set_policy(v, 0 if v >= 0 else 3)
             w.alltoallv(send, S * 4, dsc, dsd, recv, R * 4, drc, drd, gpumpi.INT, iters=3)
             iters = 20
             ns = np.zeros(iters, dtype=np.uint64)
@@ -241,10 +266,10 @@ def bench_alltoallv_1024(gpumpi, torch, w_kw, uniform: bool):
             ms = w.last_kernel_ms() / iters
             out[name] = {"gbs": 2.0 * total / (ms * 1e-3) / 1e9, "ms_per_call": ms,
                          "p50_us": float(pct(list(ns), 0.5)) / 1e3}
-    # spot check: receiver 5's block from sender 7 equals sender 7's block for receiver 5
-    r5 = recv[5, int(rd[5, 7]):int(rd[5, 7]) + int(rc[5, 7])]
-    s7 = send[7, int(sd[7, 5]):int(sd[7, 5]) + int(sc[7, 5])]
-    assert torch.equal(r5, s7), "alltoallv placement"
+            torch.cuda.synchronize()
+            exact.append(bool(np.array_equal(recv.cpu().numpy(), ref)))
+            recv.zero_()   # the oracle's output starts at zero too (bytes no piece covers)
+    out["parity"] = "bit-exact vs oracle, every variant" if all(exact) else f"MISMATCH {exact}"
     return out
 
 
@@ -581,8 +606,7 @@ def main():
     world = gpumpi.World(n, **w_kw)
     world.allreduce(send, recv, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=W)
     torch.cuda.synchronize()
-    # canonical-order result is identical on every rank
-    assert torch.equal(recv[0], recv[n - 1]), "allreduce results differ between ranks"
+    parity = parity_vs_oracle(send, recv, torch)
 
     ns = np.zeros(K, dtype=np.uint64)
     clocks = ClockSampler(local)
@@ -619,6 +643,7 @@ def main():
     achieved = algo_bytes / (ms_total / K * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"hbm_gbs of {peak_kind}", "traffic": traffic_from_profile(),
+                "traffic_source": TRAFFIC_SOURCE,
                 "algorithmic_bytes_per_step": algo_bytes, "kernel": "gpumpi_rank_kernel<Coll> (fold_fast<float,SUM>)"}
 
     extra = {"p50_us": p50, "p99_us": p99, "world": world.info()}
@@ -647,7 +672,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": ws, "steps": K, "warmup": W,
                 "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic (torch.rand uniform [-1,1), seeded)",
-                "config": dict(WORKLOAD, parallelism=f"replicas x{ws}"),
+                "config": dict(WORKLOAD), "replicas": ws, "parity": parity,
                 "roofline": roofline, "e2e": e2e,
                 "cpu_baseline": cpu_baseline(os.cpu_count() or 1),
                 "clocks": clk, "gpu_launches": launches, "extra": extra}

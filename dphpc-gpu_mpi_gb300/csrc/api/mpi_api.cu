@@ -136,6 +136,10 @@ __device__ void release_helpers() {
 // Thread 0 of a rank block after the user program returned.
 __device__ void rank_finish(int rc) {
     release_helpers();
+    if (c_rt.ranks[blockIdx.x].attrs) {
+        free(c_rt.ranks[blockIdx.x].attrs);
+        c_rt.ranks[blockIdx.x].attrs = nullptr;
+    }
     c_rt.exit_codes[blockIdx.x] = rc;
     c_rt.ranks[blockIdx.x].exited = 1;
     __threadfence();
@@ -736,8 +740,31 @@ __device__ int MPI_Get_processor_name(char* name, int* resultlen) {
     *resultlen = (int)sizeof(n) - 1;
     return MPI_SUCCESS;
 }
+// Wall-clock time from the GPU's global nanosecond timer (%globaltimer), which every SM reads alike, so
+// times taken by different ranks compare directly (the reference scales clock64 by the peak SM clock,
+// mpi.cu:142-146, 271-274, which counts per-SM cycles).
 __device__ double MPI_Wtime(void) { return (double)now_ns() * 1e-9; }
-__device__ double MPI_Wtick(void) { return 1e-9; }
+
+namespace {
+__device__ unsigned long long g_wtick_ns = 0;
+}
+// The timer's resolution as observed: the shortest step between consecutive distinct readings, over three
+// steps (the first change only ends a partial interval); measured once per process and cached.
+__device__ double MPI_Wtick(void) {
+    unsigned long long tick = *(volatile unsigned long long*)&g_wtick_ns;
+    if (tick) return (double)tick * 1e-9;
+    unsigned long long best = ~0ULL, prev = now_ns();
+    for (int k = 0; k < 4; k++) {
+        unsigned long long t = prev;
+        for (int spin = 0; spin < (1 << 20) && t == prev; spin++) t = now_ns();
+        if (t == prev) break;  // the timer did not move within the spin bound
+        if (k > 0 && t - prev < best) best = t - prev;
+        prev = t;
+    }
+    tick = best == ~0ULL ? 1 : best;
+    *(volatile unsigned long long*)&g_wtick_ns = tick;
+    return (double)tick * 1e-9;
+}
 __device__ int gpumpi_world_rank(void) { return (int)blockIdx.x; }
 __device__ int gpumpi_block_parallel(void (*fn)(void*, int, int), void* arg) {
     Task t;
@@ -1588,11 +1615,170 @@ __device__ int set_topology(MPI_Comm_impl* o, int kind, int ndims, const int* di
 }
 }  // namespace
 
+// ---- attribute caching (MPI-1.3 section 5.7).  The reference declares the keyval functions and traps
+// in each (mpi.cu:519-536).  A rank's keyvals and attributes live in one table on the device heap, made
+// on first use and released when the rank's program returns; keyval k is slot k - 1. ----
+namespace {
+struct KeyvalRec {
+    MPI_Copy_function* copy;
+    MPI_Delete_function* del;
+    void* extra;
+    int used;
+};
+struct AttrRec {
+    MPI_Comm comm;  // nullptr: free slot
+    int keyval;
+    void* val;
+};
+struct AttrState {
+    KeyvalRec kv[GPUMPI_MAX_KEYVALS];
+    AttrRec at[GPUMPI_MAX_ATTRS];
+};
+__device__ int g_tag_ub_value = MPI_TAG_UB;
+
+__device__ AttrState* attr_state(bool create) {
+    RankState* R = &c_rt.ranks[me()];
+    if (!R->attrs && create) {
+        AttrState* a = (AttrState*)malloc(sizeof(AttrState));
+        if (!a) return nullptr;
+        memset(a, 0, sizeof(AttrState));
+        R->attrs = a;
+    }
+    return (AttrState*)R->attrs;
+}
+__device__ KeyvalRec* keyval_rec(AttrState* a, int keyval) {
+    if (!a || keyval < 1 || keyval > GPUMPI_MAX_KEYVALS || !a->kv[keyval - 1].used) return nullptr;
+    return &a->kv[keyval - 1];
+}
+__device__ AttrRec* attr_find(AttrState* a, MPI_Comm comm, int keyval) {
+    if (!a) return nullptr;
+    for (int i = 0; i < GPUMPI_MAX_ATTRS; i++)
+        if (a->at[i].comm == comm && a->at[i].keyval == keyval) return &a->at[i];
+    return nullptr;
+}
+__device__ int attr_set(AttrState* a, MPI_Comm comm, int keyval, void* val) {
+    AttrRec* r = attr_find(a, comm, keyval);
+    if (!r) r = attr_find(a, nullptr, 0);
+    if (!r) return GPUMPI_ERR_NO_MEM;
+    r->comm = comm;
+    r->keyval = keyval;
+    r->val = val;
+    return MPI_SUCCESS;
+}
+// Calls the delete function of the attribute in r and frees the slot.
+__device__ int attr_drop(AttrState* a, AttrRec* r) {
+    const KeyvalRec* k = keyval_rec(a, r->keyval);
+    int rc = MPI_SUCCESS;
+    if (k && k->del) rc = k->del(r->comm, r->keyval, r->val, k->extra);
+    if (rc == MPI_SUCCESS) {
+        r->comm = nullptr;
+        r->keyval = 0;
+        r->val = nullptr;
+    }
+    return rc;
+}
+// MPI_Comm_dup: every attribute of oldc whose copy function sets *flag is cached on newc.
+__device__ int attr_copy_all(MPI_Comm oldc, MPI_Comm newc) {
+    AttrState* a = attr_state(false);
+    if (!a) return MPI_SUCCESS;
+    for (int i = 0; i < GPUMPI_MAX_ATTRS; i++) {
+        if (a->at[i].comm != oldc) continue;
+        const int kv = a->at[i].keyval;
+        const KeyvalRec* k = keyval_rec(a, kv);
+        if (!k || !k->copy) continue;
+        void* out = nullptr;
+        int flag = 0;
+        const int rc = k->copy(oldc, kv, k->extra, a->at[i].val, &out, &flag);
+        if (rc != MPI_SUCCESS) return rc;
+        if (flag) {
+            const int rs = attr_set(a, newc, kv, out);
+            if (rs != MPI_SUCCESS) return rs;
+        }
+    }
+    return MPI_SUCCESS;
+}
+}  // namespace
+
+__device__ int MPI_NULL_COPY_FN(MPI_Comm, int, void*, void*, void*, int* flag) {
+    if (flag) *flag = 0;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_DUP_FN(MPI_Comm, int, void*, void* attribute_val_in, void* attribute_val_out, int* flag) {
+    if (attribute_val_out) *(void**)attribute_val_out = attribute_val_in;
+    if (flag) *flag = 1;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_NULL_DELETE_FN(MPI_Comm, int, void*, void*) { return MPI_SUCCESS; }
+
+__device__ int MPI_Keyval_create(MPI_Copy_function* copy_fn, MPI_Delete_function* delete_fn, int* keyval,
+                                 void* extra_state) {
+    if (!keyval) return GPUMPI_ERR_ARG;
+    AttrState* a = attr_state(true);
+    if (!a) return GPUMPI_ERR_NO_MEM;
+    for (int i = 0; i < GPUMPI_MAX_KEYVALS; i++) {
+        if (a->kv[i].used) continue;
+        a->kv[i].copy = copy_fn;
+        a->kv[i].del = delete_fn;
+        a->kv[i].extra = extra_state;
+        a->kv[i].used = 1;
+        *keyval = i + 1;
+        return MPI_SUCCESS;
+    }
+    return GPUMPI_ERR_NO_MEM;
+}
+__device__ int MPI_Keyval_free(int* keyval) {
+    if (!keyval) return GPUMPI_ERR_ARG;
+    AttrState* a = attr_state(false);
+    KeyvalRec* k = keyval_rec(a, *keyval);
+    if (!k) return GPUMPI_ERR_ARG;
+    // attributes still cached under the keyval keep their delete function until they are deleted
+    bool in_use = false;
+    for (int i = 0; i < GPUMPI_MAX_ATTRS; i++) in_use = in_use || (a->at[i].comm && a->at[i].keyval == *keyval);
+    if (!in_use) k->used = 0;
+    *keyval = MPI_KEYVAL_INVALID;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Attr_put(MPI_Comm comm, int keyval, void* attribute_val) {
+    if (!check_comm(comm)) return GPUMPI_ERR_COMM;
+    AttrState* a = attr_state(false);
+    if (!keyval_rec(a, keyval)) return GPUMPI_ERR_ARG;
+    AttrRec* old = attr_find(a, comm, keyval);
+    if (old) {
+        const int rc = attr_drop(a, old);  // the standard deletes the old value first
+        if (rc != MPI_SUCCESS) return rc;
+    }
+    return attr_set(a, comm, keyval, attribute_val);
+}
+__device__ int MPI_Attr_get(MPI_Comm comm, int keyval, void* attribute_val, int* flag) {
+    if (!check_comm(comm)) return GPUMPI_ERR_COMM;
+    if (!attribute_val || !flag) return GPUMPI_ERR_ARG;
+    if (keyval == MPI_TAG_UB) {
+        *(void**)attribute_val = &g_tag_ub_value;
+        *flag = 1;
+        return MPI_SUCCESS;
+    }
+    AttrState* a = attr_state(false);
+    if (!keyval_rec(a, keyval)) return GPUMPI_ERR_ARG;
+    const AttrRec* r = attr_find(a, comm, keyval);
+    *flag = r != nullptr;
+    if (r) *(void**)attribute_val = r->val;
+    return MPI_SUCCESS;
+}
+__device__ int MPI_Attr_delete(MPI_Comm comm, int keyval) {
+    if (!check_comm(comm)) return GPUMPI_ERR_COMM;
+    AttrState* a = attr_state(false);
+    if (!keyval_rec(a, keyval)) return GPUMPI_ERR_ARG;
+    AttrRec* r = attr_find(a, comm, keyval);
+    return r ? attr_drop(a, r) : GPUMPI_ERR_ARG;
+}
+
 __device__ int MPI_Comm_dup(MPI_Comm comm, MPI_Comm* newcomm) {
     MPI_Comm_impl* c = check_comm(comm);
     if (!c) return GPUMPI_FAILURE;  // reference returns MPI_FAILURE for MPI_COMM_NULL (communicator.cu:118-121)
     int rc = comm_split_impl(comm, 0, comm_rank_of(c, me()), newcomm);
-    if (rc || !c->topo_kind || *newcomm == MPI_COMM_NULL) return rc;
+    if (rc || *newcomm == MPI_COMM_NULL) return rc;
+    rc = attr_copy_all(comm, *newcomm);
+    if (rc || !c->topo_kind) return rc;
     // a duplicate keeps the topology
     int dims[MPI_MAX_DIMS], periods[MPI_MAX_DIMS];
     for (int i = 0; i < c->topo_ndims; i++) {
@@ -1785,8 +1971,19 @@ __device__ int MPI_Topo_test(MPI_Comm comm, int* status) {
 }
 
 __device__ int MPI_Comm_free(MPI_Comm* comm) {
-    // communicator objects live in the run's arena and are reclaimed when the launch ends
-    if (comm) *comm = MPI_COMM_NULL;
+    // communicator objects live in the run's arena and are reclaimed when the launch ends; the
+    // attributes the rank cached on the communicator are deleted (their delete functions run)
+    if (!comm) return GPUMPI_ERR_ARG;
+    if (*comm != MPI_COMM_NULL) {
+        AttrState* a = attr_state(false);
+        if (a)
+            for (int i = 0; i < GPUMPI_MAX_ATTRS; i++)
+                if (a->at[i].comm == *comm) {
+                    const int rc = attr_drop(a, &a->at[i]);
+                    if (rc != MPI_SUCCESS) return rc;
+                }
+    }
+    *comm = MPI_COMM_NULL;
     return MPI_SUCCESS;
 }
 __device__ int MPI_Comm_group(MPI_Comm comm, MPI_Group* group) {

@@ -1,10 +1,11 @@
 // noalloc.cu — MPI_Allreduce among block-ranks without any allocation by the library.
 //
 // Some callers of this library cannot allocate device memory at the moment they need a reduction:
-// code running while a CUDA stream is being captured into a graph (cudaMalloc is not capturable),
-// code inside allocators, schedulers or memory-pool callbacks that must not re-enter the allocator, and
-// processes that budget every device byte up front.  gpumpi_allreduce needs a world (cudaMalloc'd
-// runtime state, device-heap staging); this entry point needs nothing but the caller's device buffers.
+// code inside an allocator, a scheduler or a memory-pool callback that must not re-enter the allocator,
+// processes that reserve every device byte up front and may not grow past that budget, and loops that
+// cannot afford cudaMalloc's implicit device-wide synchronisation.  gpumpi_allreduce needs a world
+// (cudaMalloc'd runtime state, device-heap staging); this entry point needs nothing but the caller's
+// device buffers.
 //
 // Its scratch memory — the table where every rank publishes its buffer addresses, the grid-barrier
 // words and the chunk counter — lives in the file-scope array below, of a fixed maximum size that every
@@ -14,11 +15,15 @@
 //     different threads) race and produce wrong results — serialise them;
 //   * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with that
 //     device current; make that first call before any stream capture begins;
-//   * buffers must be device memory (staging host buffers would allocate).
+//   * buffers must be device memory of the current device (staging host buffers would allocate);
+//   * the grid barrier inside the kernel is bounded: if it runs out, the kernel writes nothing, records
+//     the failure in the array's error word and returns; gpumpi_allreduce_noalloc_status reports it
+//     once the caller has synchronised the call's stream.
 // The reduction is the same canonical rank-order fold as the runtime's DIRECT variant, so results are
 // bit-identical to gpumpi_allreduce.
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstdio>
 #include <mutex>
 
@@ -69,7 +74,7 @@ struct NoallocArgs {
     long long stride;           // bytes per rank
     long long count;            // elements per rank
     int nranks;
-    int vec;                    // elements per thread of a chunk
+    int missing;                // arrivals the barrier waits for beyond the launched blocks (test hook)
     int aligned;                // 16 / 8 / 0: alignment of every rank's buffers
     unsigned long long timeout_ns;
 };
@@ -164,7 +169,7 @@ __global__ void __launch_bounds__(256) noalloc_allreduce_kernel(NoallocArgs a) {
         const unsigned g = ld_acq(&t->h.gen);
         __threadfence();
         const unsigned arrived = atomicAdd(&t->h.arrive, 1u);
-        if (arrived == gridDim.x - 1) {
+        if (arrived + 1u == gridDim.x + (unsigned)a.missing) {
             t->h.arrive = 0;
             st_rel(&t->h.gen, g + 1);
         } else {
@@ -237,6 +242,10 @@ int elem_size(int dt) {
 
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[64] = {};
+// test hook: bounded-wait limit and arrivals the barrier pretends are missing (0 / 0 = defaults)
+unsigned long long g_noalloc_timeout_ns = 0;
+int g_noalloc_missing = 0;
+constexpr unsigned long long NOALLOC_DEFAULT_TIMEOUT_NS = 20ull * 1000000000ull;
 
 }  // namespace
 
@@ -254,14 +263,17 @@ extern "C" int gpumpi_allreduce_noalloc(const void* sendbuf, void* recvbuf, long
         return GPUMPI_ERR_TYPE;
     }
     if (count == 0) return GPUMPI_SUCCESS;
-    cudaPointerAttributes pa;
-    if (cudaPointerGetAttributes(&pa, sendbuf) != cudaSuccess || pa.type != cudaMemoryTypeDevice ||
-        cudaPointerGetAttributes(&pa, recvbuf) != cudaSuccess || pa.type != cudaMemoryTypeDevice) {
-        cudaGetLastError();
-        return GPUMPI_ERR_BUFFER;  // host buffers would need a device staging copy (an allocation)
-    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return GPUMPI_ERR_CUDA;
+    // host buffers would need a device staging copy (an allocation); a buffer on another GPU would be
+    // read through peer access while the kernel and the scratch live on this one
+    for (const void* b : {sendbuf, (const void*)recvbuf}) {
+        cudaPointerAttributes pa;
+        if (cudaPointerGetAttributes(&pa, b) != cudaSuccess || pa.type != cudaMemoryTypeDevice || pa.device != dev) {
+            cudaGetLastError();
+            return GPUMPI_ERR_BUFFER;
+        }
+    }
     void* scratch = nullptr;
     {
         // set-up, once per device, with that device current: the array's device address
@@ -336,14 +348,36 @@ extern "C" int gpumpi_allreduce_noalloc(const void* sendbuf, void* recvbuf, long
     a.stride = stride;
     a.count = count;
     a.nranks = nranks;
-    a.vec = vbest;
     a.aligned = aligned;
-    a.timeout_ns = 20ull * 1000000000ull;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        a.missing = g_noalloc_missing;
+        a.timeout_ns = g_noalloc_timeout_ns ? g_noalloc_timeout_ns : NOALLOC_DEFAULT_TIMEOUT_NS;
+    }
     void* args[] = {&a};
     cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3((unsigned)blocks), dim3(T), args, 0, s);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return GPUMPI_ERR_LAUNCH;
     }
+    return GPUMPI_SUCCESS;
+}
+
+extern "C" int gpumpi_allreduce_noalloc_status(void) {
+    // the error word of the most recent call on the current device; the caller synchronised its stream
+    unsigned err = 0;
+    if (cudaMemcpyFromSymbol(&err, g_noalloc_scratch, sizeof(err), offsetof(NoallocHeader, error),
+                             cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return GPUMPI_ERR_CUDA;
+    }
+    return err ? GPUMPI_ERR_TIMEOUT : GPUMPI_SUCCESS;
+}
+
+extern "C" int gpumpi_noalloc_test_hook(double timeout_s, int missing_arrivals) {
+    if (timeout_s < 0 || missing_arrivals < 0 || missing_arrivals > NOALLOC_MAX_RANKS) return GPUMPI_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    g_noalloc_timeout_ns = (unsigned long long)(timeout_s * 1e9);
+    g_noalloc_missing = missing_arrivals;
     return GPUMPI_SUCCESS;
 }

@@ -823,6 +823,77 @@ struct TinyMixed {
     }
 };
 
+// Attribute caching (MPI-1.3 section 5.7; the reference declares MPI_Keyval_create, MPI_NULL_COPY_FN,
+// MPI_NULL_DELETE_FN, mpi.cuh:95-110, and MPI_Attr_get/put, communicator.cuh:44-47, and does nothing or
+// traps in them) and the timer (MPI_Wtime, MPI_Wtick).  outi[r][0] = copy/delete counter,
+// outd[r][0..2] = Wtime before and after a world barrier, Wtick.
+__device__ int attrs_copy(MPI_Comm, int, void* extra, void* in, void* out, int* flag) {
+    (*(int*)extra) += 1;
+    *(void**)out = in;
+    *flag = 1;
+    return MPI_SUCCESS;
+}
+__device__ int attrs_delete(MPI_Comm, int, void*, void* extra) {
+    (*(int*)extra) += 100;
+    return MPI_SUCCESS;
+}
+struct Attrs {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        const int rank = wrank();
+        int n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        long long* oi = outi(p, rank);
+        double* od = outd(p, rank);
+        bool ok = true;
+        const double wt = MPI_Wtick();
+        ok = ok && wt > 0 && wt <= 1e-5;
+        double prev = MPI_Wtime();
+        for (int i = 0; i < 100; i++) {
+            const double t = MPI_Wtime();
+            ok = ok && t >= prev;
+            prev = t;
+        }
+        od[0] = MPI_Wtime();
+        MPI_Barrier(MPI_COMM_WORLD);
+        od[1] = MPI_Wtime();
+        od[2] = wt;
+        int counter = 0;  // copies + 100 x deletes
+        int value = 1000 + rank;
+        int kv = MPI_KEYVAL_INVALID, kv_null = MPI_KEYVAL_INVALID, flag = -1;
+        int* got = nullptr;
+        ok = ok && MPI_Keyval_create(attrs_copy, attrs_delete, &kv, &counter) == MPI_SUCCESS;
+        ok = ok && MPI_Keyval_create(MPI_NULL_COPY_FN, MPI_NULL_DELETE_FN, &kv_null, nullptr) == MPI_SUCCESS;
+        ok = ok && kv != MPI_KEYVAL_INVALID && kv_null != MPI_KEYVAL_INVALID && kv != kv_null;
+        MPI_Comm c1 = MPI_COMM_NULL, c2 = MPI_COMM_NULL;
+        ok = ok && MPI_Comm_dup(MPI_COMM_WORLD, &c1) == MPI_SUCCESS;
+        ok = ok && MPI_Attr_put(c1, kv, &value) == MPI_SUCCESS && MPI_Attr_put(c1, kv_null, &value) == MPI_SUCCESS;
+        ok = ok && MPI_Attr_get(c1, kv, &got, &flag) == MPI_SUCCESS && flag == 1 && got == &value;
+        ok = ok && MPI_Attr_get(MPI_COMM_WORLD, kv, &got, &flag) == MPI_SUCCESS && flag == 0;
+        ok = ok && MPI_Comm_dup(c1, &c2) == MPI_SUCCESS && counter == 1;   // kv's copy function ran once
+        got = nullptr;
+        ok = ok && MPI_Attr_get(c2, kv, &got, &flag) == MPI_SUCCESS && flag == 1 && got == &value;
+        ok = ok && MPI_Attr_get(c2, kv_null, &got, &flag) == MPI_SUCCESS && flag == 0;  // not copied
+        int sum = 0;
+        ok = ok && MPI_Allreduce(&value, &sum, 1, MPI_INT, MPI_SUM, c2) == MPI_SUCCESS;
+        ok = ok && sum == 1000 * n + n * (n - 1) / 2;
+        ok = ok && MPI_Attr_delete(c2, kv) == MPI_SUCCESS && counter == 101;
+        ok = ok && MPI_Attr_get(c2, kv, &got, &flag) == MPI_SUCCESS && flag == 0;
+        ok = ok && MPI_Attr_put(c1, kv, &value) == MPI_SUCCESS && counter == 201;  // replacing deletes first
+        ok = ok && MPI_Comm_free(&c1) == MPI_SUCCESS && c1 == MPI_COMM_NULL && counter == 301;
+        ok = ok && MPI_Comm_free(&c2) == MPI_SUCCESS && counter == 301;
+        int* ub = nullptr;
+        ok = ok && MPI_Attr_get(MPI_COMM_WORLD, MPI_TAG_UB, &ub, &flag) == MPI_SUCCESS && flag == 1 && ub &&
+             *ub == MPI_TAG_UB;
+        ok = ok && MPI_Keyval_free(&kv) == MPI_SUCCESS && kv == MPI_KEYVAL_INVALID;
+        ok = ok && MPI_Attr_put(MPI_COMM_WORLD, GPUMPI_MAX_KEYVALS + 5, &value) == MPI_ERR_ARG;
+        ok = ok && MPI_Keyval_free(&kv_null) == MPI_SUCCESS;
+        oi[0] = counter;
+        okp(p)[rank] = ok;
+        return MPI_Finalize();
+    }
+};
+
 }  // namespace
 
 extern const gpumpi_prog_entry g_test_programs[] = {
@@ -849,5 +920,6 @@ extern const gpumpi_prog_entry g_test_programs[] = {
     GPUMPI_PROGRAM(GPUMPI_T_CART, "cart", Cart),
     GPUMPI_PROGRAM(GPUMPI_T_TINY_STRESS, "tiny_stress", TinyStress),
     GPUMPI_PROGRAM(GPUMPI_T_TINY_MIXED, "tiny_mixed", TinyMixed),
+    GPUMPI_PROGRAM(GPUMPI_T_ATTRS, "attrs", Attrs),
 };
 extern const int g_num_test_programs = sizeof(g_test_programs) / sizeof(g_test_programs[0]);

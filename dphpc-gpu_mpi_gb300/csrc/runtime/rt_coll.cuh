@@ -430,8 +430,9 @@ __device__ __noinline__ void fold_chunk(const JobParams* j, long long idx, int t
     if (j->variant == GPUMPI_VARIANT_TREE && j->tile > 0) {
         if (fold_tree_dispatch(j, idx, tid, nt)) return;
     }
+    // after an abort no block issues bulk copies: a stage may still hold a copy that never landed
     if (j->variant == GPUMPI_VARIANT_STAGED && j->tile > 0 &&
-        ((min(j->chunk, j->count - e0) * j->esize) & 15) == 0) {
+        ((min(j->chunk, j->count - e0) * j->esize) & 15) == 0 && !ld_relaxed(c_rt.abort_flag)) {
         switch (j->dt) {
         case GPUMPI_FLOAT: done = fold_staged_t<float>(j, idx, tid, nt); break;
         case GPUMPI_DOUBLE: case GPUMPI_LONG_DOUBLE: done = fold_staged_t<double>(j, idx, tid, nt); break;

@@ -322,6 +322,7 @@ struct alignas(128) RankState {
     int sel_variant;
     float sel_y[4];                 // the network's predicted log-times of the cached shape
     unsigned long long coll_calls;
+    void* attrs;                    // keyvals and cached attributes (device heap, made on first use)
     Job p2p_job;
 };
 

@@ -353,15 +353,18 @@ __device__ __noinline__ bool staged_copy(PTab t, long long u0, long long u1, int
         issue(st);
         st ^= 1;
     }
+    bool drained = true;
     if (!ok) {
         // a stage did not complete in time: let any copy still in flight land before the shared memory is
-        // reused (bounded), and report
+        // reused (bounded), and report.  The error record raises the launch's abort flag, after which no
+        // block issues STAGED copies again, so barriers whose copies never landed are left as they are.
         if (lane == 0) record_error(GPUMPI_ERR_OTHER, GPUMPI_ERR_TIMEOUT, __LINE__, wb);
         for (int k = 0; k < 2; k++)
-            if (busy[k]) mbar_wait_bounded(&bar[k], par[k]);
+            if (busy[k]) drained = mbar_wait_bounded(&bar[k], par[k]) && drained;
+        drained = __all_sync(0xffffffffu, drained);
     }
     __syncwarp();
-    if (lane == 0) {
+    if (lane == 0 && drained) {
         mbar_inval(&bar[0]);
         mbar_inval(&bar[1]);
     }
@@ -370,7 +373,8 @@ __device__ __noinline__ bool staged_copy(PTab t, long long u0, long long u1, int
 
 __device__ __forceinline__ void copy_units(const JobParams* j, const PTab& t, long long u0, long long u1, bool mis,
                                            int lane, int warp, int nw, int wi, int nwk) {
-    if (j->variant == GPUMPI_VARIANT_STAGED) staged_copy(t, u0, u1, lane, warp, nw, wi, nwk);
+    if (j->variant == GPUMPI_VARIANT_STAGED && !ld_relaxed(c_rt.abort_flag))
+        staged_copy(t, u0, u1, lane, warp, nw, wi, nwk);
     else if (mis) flat_copy_mis(t, u0, u1, lane, wi, nwk);
     else flat_copy_aligned(t, u0, u1, lane, wi, nwk);
 }

@@ -40,6 +40,25 @@ __device__ __forceinline__ void stage_issue(unsigned long long* bar, T* sdst, lo
     for (int k = 0; k < mm; k++) tma_load_1d(sdst + (long long)k * E, (const T*)s_chunk.f.ptile[k0 + k] + e0, CB, bar);
 }
 
+// Thread 0 after an abort: groups gi .. gi+cnt-1 were issued and not consumed, so their bulk copies may
+// still be writing into the stages.  Waits (bounded) for every one of them before the stages can be
+// reused or the block exits, then retires the barriers.  If a copy still has not landed, the barriers are
+// left alone and the error record raises the launch's abort flag, after which no block issues STAGED
+// copies again (fold_chunk / copy_units check the flag).
+template <int S>
+__device__ __noinline__ void drain_stages(unsigned long long* full, unsigned gi, int cnt, long long idx) {
+    bool drained = true;
+    for (int k = 0; k < cnt; k++) {
+        const unsigned gq = gi + (unsigned)k;
+        drained = mbar_wait_bounded(&full[gq % S], (gq / S) & 1u) && drained;
+    }
+    if (!drained) {
+        record_error(GPUMPI_ERR_OTHER, GPUMPI_ERR_TIMEOUT, __LINE__, idx);
+        return;
+    }
+    for (int q = 0; q < S; q++) mbar_inval(&full[q]);
+}
+
 template <class T, int OP, int V>
 __device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int tid, int nt) {
     constexpr int S = 2;
@@ -87,7 +106,11 @@ __device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int 
             }
             bar_sync(BAR_TASK, nt);  // (a) everyone waited; abort flag visible
             aborted = s_stage_abort != 0;
-            if (aborted) break;
+            if (aborted) {
+                // groups g .. min(ng, g + S) - 1 of this tile have been issued and not consumed
+                if (tid == 0) drain_stages<S>(full, gi, min(ng, g + S) - g, idx);
+                break;
+            }
             const int mm = min(G, m - g * G);
             const T* st = stage + (long long)sidx * stage_elems + my;
             if (nv > 0) {

@@ -39,7 +39,7 @@ TESTS = {
     "single_int": 1, "transfer_array": 2, "send_recv": 3, "repeat_send_recv": 4, "network_flood": 5,
     "all_to_all": 6, "reduce_int16_prod": 7, "allreduce_f64_sum": 8, "allgather_int": 9, "scatter_int": 10,
     "scatterv_int": 11, "comm_rank": 12, "comm_dup_isolation": 13, "comm_split": 14, "sample": 15,
-    "p2p_matching": 16, "timeout": 17, "datatypes": 18, "subcomm_coll": 19, "errors": 20, "cart": 21, "tiny_stress": 22, "tiny_mixed": 23,
+    "p2p_matching": 16, "timeout": 17, "datatypes": 18, "subcomm_coll": 19, "errors": 20, "cart": 21, "tiny_stress": 22, "tiny_mixed": 23, "attrs": 24,
 }
 P_COLL, P_PINGPONG, P_RING, P_PI, P_BUCKET_SORT, P_HALO, P_BATCH = 100, 101, 102, 103, 104, 105, 106
 COLL = {"allreduce": 0, "reduce": 1, "bcast": 2, "alltoall": 3, "alltoallv": 4, "allgather": 5, "gather": 6,
@@ -61,7 +61,7 @@ EXPORTS = [
     "gpumpi_set_mlp", "gpumpi_read_trace", "gpumpi_run_program", "gpumpi_last_kernel_ms",
     "gpumpi_kernel_launches", "gpumpi_test_run", "gpumpi_allreduce", "gpumpi_reduce", "gpumpi_bcast",
     "gpumpi_alltoall", "gpumpi_alltoallv", "gpumpi_allgather", "gpumpi_pingpong", "gpumpi_ring",
-    "gpumpi_allreduce_noalloc", "gpumpi_mlp_forward", "gpumpi_mlp_loss_grad", "gpumpi_mlp_adam_step",
+    "gpumpi_allreduce_noalloc", "gpumpi_allreduce_noalloc_status", "gpumpi_noalloc_test_hook", "gpumpi_mlp_forward", "gpumpi_mlp_loss_grad", "gpumpi_mlp_adam_step",
     "gpumpi_graph_create", "gpumpi_graph_launch", "gpumpi_graph_destroy", "gpumpi_main",
 ]
 

@@ -442,7 +442,7 @@ def apply_policy(world, policy: str):
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["run"])
-    ap.add_argument("--out", default="gpurun_out/selector")
+    ap.add_argument("--out", required=True, help="folder for the recorded timings, table, network and report")
     ap.add_argument("--iters", type=int, default=30)
     a = ap.parse_args()
     run(Path(a.out), iters=a.iters)

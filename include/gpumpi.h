@@ -100,6 +100,7 @@ enum gpumpi_program {
     GPUMPI_T_CART,             /* Cartesian topologies: dims, coords, shifts, sub-grids, exchange */
     GPUMPI_T_TINY_STRESS,      /* back-to-back tiny collectives with skewed ranks, every result checked */
     GPUMPI_T_TINY_MIXED,       /* small collectives mixing thread-local/global buffers and datatypes */
+    GPUMPI_T_ATTRS,            /* keyvals and cached attributes, MPI_Wtime / MPI_Wtick */
     /* hot-path programs */
     GPUMPI_P_COLL = 100,       /* i[0]=kind i[1]=count i[2]=dt i[3]=op i[4]=root i[5]=iters i[6]=send stride
                                   i[7]=recv stride i[8]=variant p[0]=send p[1]=recv p[2..5]=count/displ matrices
@@ -227,19 +228,29 @@ int gpumpi_ring(gpumpi_world* w, const void* sendbuf, void* recvbuf, long long b
                 uint64_t* iter_ns, void* stream);
 
 /* Allocation-free MPI_Allreduce among `nranks` block-ranks (no counterpart in the reference).
- * For callers that cannot allocate device memory when they reduce — inside stream capture, inside an
- * allocator or memory-pool callback, or under a fixed device-memory budget — this call allocates
- * nothing: its scratch (rank table, barrier words, chunk counter) is a fixed static device array of
- * GPUMPI_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until exit.  sendbuf/recvbuf are
- * rank-major DEVICE buffers of nranks * count elements; nranks <= GPUMPI_NOALLOC_MAX_RANKS (else
- * GPUMPI_ERR_ARG); float/double/int32/int64 with SUM/MAX/MIN/PROD (else GPUMPI_ERR_TYPE).  Asynchronous
- * on `stream`; canonical rank order, bit-identical to gpumpi_allreduce.  All calls share the array:
- * calls that overlap on the GPU race.  The first call on a device looks up the array's address with
- * that device current; make it before any stream capture. */
+ * For callers that cannot allocate device memory when they reduce — code inside an allocator or
+ * memory-pool callback that must not re-enter the allocator, processes that reserve a fixed device-memory
+ * budget up front, loops that cannot take cudaMalloc's device-wide synchronisation — this call allocates
+ * nothing: its scratch (rank table, barrier words, chunk counter, error word) is a fixed static device
+ * array of GPUMPI_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until exit.
+ * sendbuf/recvbuf are rank-major buffers of nranks * count elements in device memory of the current
+ * device (else GPUMPI_ERR_BUFFER); nranks <= GPUMPI_NOALLOC_MAX_RANKS (else GPUMPI_ERR_ARG);
+ * float/double/int32/int64 with SUM/MAX/MIN/PROD (else GPUMPI_ERR_TYPE).  Asynchronous on `stream`;
+ * canonical rank order, bit-identical to gpumpi_allreduce.  All calls share the array: calls that
+ * overlap on the GPU race.  The first call on a device looks up the array's address with that device
+ * current; make it before any stream capture. */
 #define GPUMPI_NOALLOC_MAX_RANKS 4096
 #define GPUMPI_NOALLOC_SCRATCH_BYTES (64 * 1024 + 256)
 int gpumpi_allreduce_noalloc(const void* sendbuf, void* recvbuf, long long count, int datatype, int op, int nranks,
                              void* stream);
+/* Outcome of the most recent gpumpi_allreduce_noalloc on the current device, read from its error word
+ * after the caller synchronised that call's stream: GPUMPI_SUCCESS, or GPUMPI_ERR_TIMEOUT when the
+ * kernel's bounded grid barrier ran out (the kernel then returned without writing recvbuf). */
+int gpumpi_allreduce_noalloc_status(void);
+/* Test hook of the allocation-free allreduce's failure path: bounded-wait limit in seconds (0 = the
+ * default 20 s) and arrivals its grid barrier waits for beyond the launched blocks (0 = none), so a
+ * test can make the barrier run out without faulting the GPU.  (0, 0) restores the defaults. */
+int gpumpi_noalloc_test_hook(double timeout_s, int missing_arrivals);
 
 #define GPUMPI_MLP_NPARAMS (64 * 12 + 64 + 64 * 64 + 64 + 4 * 64 + 4)
 

@@ -232,6 +232,29 @@ __device__ int MPI_Group_size(MPI_Group group, int* size);
 __device__ int MPI_Group_rank(MPI_Group group, int* rank);
 __device__ int MPI_Group_translate_ranks(MPI_Group group1, int n, const int ranks1[], MPI_Group group2, int ranks2[]);
 
+// ---- attribute caching on communicators (reference mpi.cuh:95-110 declares the keyval part and
+//      traps in every function, mpi.cu:519-536; implemented here per MPI-1.3 section 5.7) ----
+// Keyvals and attributes belong to the calling rank.  MPI_Comm_dup calls each attribute's copy
+// function and caches the value it returns when it sets *flag; MPI_Comm_free and MPI_Attr_delete call
+// the delete function.  MPI_Attr_get(comm, MPI_TAG_UB, ...) returns the tag bound.
+typedef int MPI_Copy_function(MPI_Comm oldcomm, int keyval, void* extra_state, void* attribute_val_in,
+                              void* attribute_val_out, int* flag);
+typedef int MPI_Delete_function(MPI_Comm comm, int keyval, void* attribute_val, void* extra_state);
+#define MPI_KEYVAL_INVALID (-1)
+#define GPUMPI_MAX_KEYVALS 32          // keyvals a rank can hold at once
+#define GPUMPI_MAX_ATTRS 64            // attributes a rank can cache over all its communicators
+__device__ int MPI_NULL_COPY_FN(MPI_Comm oldcomm, int keyval, void* extra_state, void* attribute_val_in,
+                                void* attribute_val_out, int* flag);
+__device__ int MPI_DUP_FN(MPI_Comm oldcomm, int keyval, void* extra_state, void* attribute_val_in,
+                          void* attribute_val_out, int* flag);
+__device__ int MPI_NULL_DELETE_FN(MPI_Comm comm, int keyval, void* attribute_val, void* extra_state);
+__device__ int MPI_Keyval_create(MPI_Copy_function* copy_fn, MPI_Delete_function* delete_fn, int* keyval,
+                                 void* extra_state);
+__device__ int MPI_Keyval_free(int* keyval);
+__device__ int MPI_Attr_put(MPI_Comm comm, int keyval, void* attribute_val);
+__device__ int MPI_Attr_get(MPI_Comm comm, int keyval, void* attribute_val, int* flag);
+__device__ int MPI_Attr_delete(MPI_Comm comm, int keyval);
+
 // ---- Cartesian topologies (MPI-3.1 section 7.5; not in the reference) ----
 // Ranks keep their order (reorder is accepted and ignored); at most MPI_MAX_DIMS dimensions.
 __device__ int MPI_Dims_create(int nnodes, int ndims, int dims[]);

@@ -113,13 +113,12 @@ def test_allreduce_variants_agree(gpulib, oracle):
             if v in (0, 3):   # canonical order: bit-exact
                 assert np.array_equal(got, ref), v
             else:
-                # reordered (TREE groups, RING rotation): error against the fp64 sum, relative to sum |x|:
-                # mean <= 1e-6 (the stated fp32 tolerance) and max <= (n-1) * 2^-24 (the bound that holds
-                # for any summation order, the canonical one included)
+                # reordered (TREE groups, RING rotation): the error of every element against the fp64
+                # sum, relative to sum_r |x_r| (the scale of any summation order's rounding error), is at
+                # most 1e-6, the stated fp32 tolerance
                 scale = np.abs(x).astype(np.float64).sum(0) + 1e-30
                 rel = np.abs(got[0].astype(np.float64) - ref64) / scale
-                assert rel.mean() <= 1e-6, (v, rel.mean())
-                assert rel.max() <= (n - 1) * 2.0 ** -24, (v, rel.max())
+                assert rel.max() <= 1e-6, (v, rel.max())
                 assert (got == got[0]).all()
 
 
@@ -274,6 +273,20 @@ def test_extended_programs(gpulib, name, n):
     with gpulib.World(n, timeout_s=10.0) as w:
         rc, ok, oi, od = w.run_test(name)
     assert rc == 0 and ok.all(), (name, ok, oi[:, :10])
+
+
+@pytest.mark.parametrize("n", [2, 37])
+def test_attributes_and_timer(gpulib, n):
+    """Keyvals and cached attributes (copy functions on MPI_Comm_dup, delete functions on MPI_Attr_delete,
+    on replacement and on MPI_Comm_free; MPI_TAG_UB) and the timer: MPI_Wtime never goes backwards, is
+    one clock for all ranks (every rank's reading before a world barrier precedes every rank's reading
+    after it), and MPI_Wtick reports a positive step of at most 10 us."""
+    with gpulib.World(n, timeout_s=10.0) as w:
+        rc, ok, oi, od = w.run_test("attrs")
+    assert rc == 0 and ok.all(), (ok, oi[:, 0])
+    assert (oi[:, 0] == 301).all()
+    assert od[:, 0].max() <= od[:, 1].min()
+    assert (od[:, 2] > 0).all() and (od[:, 2] <= 1e-5).all()
 
 
 def test_timeout_returns_error_not_hang(gpulib):

@@ -1,11 +1,14 @@
 """GPU: the allocation-free allreduce entry point, called through the C ABI.
 
 gpumpi_allreduce_noalloc exists for callers that cannot allocate device memory when they need a
-reduction (inside stream capture, inside allocator callbacks, under a fixed memory budget); its scratch
-is a static device array of fixed size.  Its output must equal the existing entry point's
+reduction (code inside allocator or memory-pool callbacks, processes with a fixed device-memory budget
+reserved up front); its scratch is a static device array of fixed size.  Its output must equal the existing entry point's
 (gpumpi_allreduce, which runs inside a world with allocated state) bit for bit — both fold in the
 canonical rank order — on two calls in a row that share the static scratch.  Sizes beyond the stated
-maximum must be rejected with an error.  This file is collected last on purpose.
+maximum must be rejected with an error.  When the kernel's bounded grid barrier runs out, the caller
+learns it from gpumpi_allreduce_noalloc_status (tested through the test hook that makes the barrier wait
+for an arrival that never comes, with a 0.1 s limit: no fault, the GPU stays usable).  This file is
+collected last on purpose.
 """
 import ctypes
 
@@ -24,6 +27,17 @@ def noalloc_fn(gpumpi):
                   ctypes.c_void_p]
     f.restype = ctypes.c_int
     return f
+
+
+def status_fns(gpumpi):
+    L = ctypes.CDLL(str(gpumpi.LIB_PATH))
+    st = L.gpumpi_allreduce_noalloc_status
+    st.argtypes = []
+    st.restype = ctypes.c_int
+    hook = L.gpumpi_noalloc_test_hook
+    hook.argtypes = [ctypes.c_double, ctypes.c_int]
+    hook.restype = ctypes.c_int
+    return st, hook
 
 
 @pytest.mark.parametrize("n,count,dt,op,tdt", [
@@ -48,6 +62,7 @@ def test_noalloc_matches_existing_entry_point_twice(gpulib, n, count, dt, op, td
             assert rc == 0
             torch.cuda.synchronize()
             assert torch.equal(out, ref), f"call {call}: outputs differ"
+            assert status_fns(gpulib)[0]() == 0
 
 
 def test_noalloc_rejects_sizes_beyond_maximum(gpulib):
@@ -58,3 +73,24 @@ def test_noalloc_rejects_sizes_beyond_maximum(gpulib):
     assert f(x.data_ptr(), x.data_ptr(), 1, 29, 2, 2, None) == 4          # MPI_BYTE: GPUMPI_ERR_TYPE
     host = np.zeros(8, np.float32)
     assert f(host.ctypes.data, host.ctypes.data, 1, 12, 2, 2, None) == 2  # host memory: GPUMPI_ERR_BUFFER
+
+
+def test_noalloc_reports_barrier_timeout(gpulib):
+    f = noalloc_fn(gpulib)
+    status, hook = status_fns(gpulib)
+    n, count = 16, 1000
+    x = torch.ones((n, count), device="cuda")
+    out = torch.full_like(x, -7.0)
+    assert hook(0.1, 1) == 0          # the barrier waits for one arrival that never comes, 0.1 s at most
+    try:
+        assert f(x.data_ptr(), out.data_ptr(), count, 12, 2, n, None) == 0   # the launch itself succeeds
+        torch.cuda.synchronize()
+        assert status() == 15         # GPUMPI_ERR_TIMEOUT
+        assert bool((out == -7.0).all())  # nothing was written
+    finally:
+        assert hook(0.0, 0) == 0
+    # the GPU and the scratch stay usable: the next call succeeds and clears the error word
+    assert f(x.data_ptr(), out.data_ptr(), count, 12, 2, n, None) == 0
+    torch.cuda.synchronize()
+    assert status() == 0
+    assert bool((out == float(n)).all())
