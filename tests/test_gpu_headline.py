@@ -87,7 +87,7 @@ def test_alltoallv_1024ranks_bench_counts_bit_exact(gpulib, oracle):
         for v in (-1, 0, 1, 2, 3):
             if v >= 0:
                 w.set_policy(v, 0)
-            r = torch.full((n, R), -1, dtype=torch.int32, device="cuda")
+            r = torch.zeros((n, R), dtype=torch.int32, device="cuda")   # as the oracle's output
             w.alltoallv(s, S * 4, dsc, dsd, r, R * 4, drc, drd, gpulib.INT)
             torch.cuda.synchronize()
             got = r.cpu().numpy()
