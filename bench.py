@@ -18,7 +18,9 @@ Reported:
              per rank (uniform and uneven counts) per piece order; the bucket sort (2^25 keys, 256
              ranks), the 512^3 halo exchange and the batch of 64 communicators; the selector block:
              plain / tuned / learned policies on the headline Allreduce and the uneven Alltoallv, and the
-             held-out regret of the packaged tuned table and network.
+             held-out regret of the packaged tuned table and network; the reference gpu_mpi runtime
+             itself (its own sources, built for this GPU) against this runtime at the largest shapes it
+             completes (run last, in a separate process).
 
   parity     the headline result of every rank compared bit for bit with the CPU oracle's canonical
              rank-order fold of the same inputs (outside the timed region); a mismatch fails the run.
@@ -376,6 +378,80 @@ def bench_batch(gpumpi, torch, w_kw):
     return out
 
 
+# Shapes at which the reference gpu_mpi runtime completed on this GPU (bit-exact against the oracle).
+# Not run: Allreduce 256 ranks x 256 KiB and larger (an illegal memory access inside the reference's
+# MPI_Reduce, whose root allocates ranks x bytes from the device heap without a check, mpi.cu:201-202),
+# and Alltoallv among 1024 ranks (still running after 150 s).
+REF_RUNTIME_SHAPES = {"allreduce": (64, 16384), "alltoallv": (256, 128)}
+
+
+def bench_reference_runtime(gpumpi, torch, w_kw):
+    """The reference gpu_mpi runtime itself (built from its own sources, driven through its own MPI_Allreduce
+    and MPI_Alltoallv by every rank of one launch, one thread per rank as its launcher does) against this
+    runtime on the same inputs: fp32 SUM Allreduce among 64 ranks x 64 KiB, and int32 Alltoallv among 256
+    ranks with counts uniform in [1, 128] (the reference asserts on zero counts).  The reference runs in
+    its own process (its device heap must hold the Reduce root's ranks x bytes buffer)."""
+    import numpy as np
+    from oracle import refgpu
+    try:
+        refgpu.stage()
+        refgpu.build()
+    except Exception as e:  # sources not staged here: nothing to compare with
+        return {"unavailable": f"reference runtime not built: {str(e)[:200]}"}
+    out = {"not_run": {"allreduce_256ranks_256KiB_and_larger": "illegal memory access inside the reference's "
+                       "MPI_Reduce (root's unchecked ranks x bytes device-heap buffer, mpi.cu:201-202)",
+                       "alltoallv_1024ranks": "still running after 150 s, stopped by the host"}}
+    n, count = REF_RUNTIME_SHAPES["allreduce"]
+    ref = refgpu.run_allreduce(n, count, iters=3, seed=2026, limit_s=60)
+    from oracle import oracle
+    x = oracle.fill_f32(2026, n * count).reshape(n, count)
+    s = torch.from_numpy(x).cuda()
+    r = torch.empty_like(s)
+    with gpumpi.World(n, **w_kw) as w:
+        w.allreduce(s, r, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=5)
+        ns = np.zeros(50, dtype=np.uint64)
+        w.allreduce(s, r, count, gpumpi.FLOAT, gpumpi.OP_SUM, iters=50, iter_ns=ns)
+    ours_us = float(np.median(ns)) / 1e3
+    row = {"ranks": n, "bytes_per_rank": count * 4, "ours_p50_us": ours_us,
+           "ours_gbs": 2.0 * n * count * 4 / (ours_us * 1e-6) / 1e9}
+    if "error" in ref:
+        row["reference"] = ref
+    else:
+        ref_us = float(np.median(ref["t_ns"][1:])) / 1e3
+        row.update(reference_us=ref_us, reference_gbs=2.0 * n * count * 4 / (ref_us * 1e-6) / 1e9,
+                   reference_bit_exact_vs_oracle=ref["bit_exact_vs_oracle"], speedup=ref_us / ours_us)
+    out["allreduce_fp32_64ranks_64KiB"] = row
+    n, hi = REF_RUNTIME_SHAPES["alltoallv"]
+    sc = np.random.default_rng(4242).integers(1, hi + 1, (n, n)).astype(np.int32)
+    ref = refgpu.run_alltoallv(sc, iters=3, seed=99, limit_s=60)
+    rc = sc.T.copy()
+    sd, rd = (np.cumsum(sc, 1) - sc).astype(np.int32), (np.cumsum(rc, 1) - rc).astype(np.int32)
+    S, R = int(sc.sum(1).max()), int(rc.sum(1).max())
+    xs = torch.from_numpy(oracle.fill_i32(99, n * S).reshape(n, S)).cuda()
+    xr = torch.zeros((n, R), dtype=torch.int32, device="cuda")
+    dev = [torch.from_numpy(a).cuda() for a in (sc, sd, rc, rd)]
+    with gpumpi.World(n, **w_kw) as w:
+        w.alltoallv(xs, S * 4, *dev[:2], xr, R * 4, *dev[2:], gpumpi.INT, iters=5)
+        ns = np.zeros(50, dtype=np.uint64)
+        w.alltoallv(xs, S * 4, *dev[:2], xr, R * 4, *dev[2:], gpumpi.INT, iters=50, iter_ns=ns)
+    ours_us = float(np.median(ns)) / 1e3
+    moved = 2.0 * int(sc.sum()) * 4
+    row = {"ranks": n, "counts": f"uniform [1, {hi}] int32", "bytes_moved": moved / 2, "ours_p50_us": ours_us,
+           "ours_gbs": moved / (ours_us * 1e-6) / 1e9,
+           "ours_bit_exact_vs_oracle": bool(np.array_equal(refgpu.alltoallv_checksums(xr.cpu().numpy()),
+                                                           refgpu.alltoallv_checksums(oracle.alltoallv(
+                                                               xs.cpu().numpy(), sc, sd, R, rc, rd,
+                                                               threads=os.cpu_count() or 1))))}
+    if "error" in ref:
+        row["reference"] = ref
+    else:
+        ref_us = float(np.median(ref["t_ns"][1:])) / 1e3
+        row.update(reference_us=ref_us, reference_gbs=moved / (ref_us * 1e-6) / 1e9,
+                   reference_bit_exact_vs_oracle=ref["bit_exact_vs_oracle"], speedup=ref_us / ours_us)
+    out["alltoallv_int32_256ranks"] = row
+    return out
+
+
 def bench_selector(gpumpi, torch, w_kw):
     """The three selection policies on the headline Allreduce (1024 ranks x 1 MiB fp32) and the uneven
     Alltoallv (1024 ranks, 1 MiB per rank, int32), with the packaged tuned table and network; plus the
@@ -654,7 +730,8 @@ def main():
                         ("bucket_sort_2e25_keys_256ranks", lambda: bench_bucket_sort(gpumpi, torch, w_kw)),
                         ("halo_512cubed_512ranks", lambda: bench_halo(gpumpi, torch, w_kw)),
                         ("batch_64_communicators", lambda: bench_batch(gpumpi, torch, w_kw)),
-                        ("selector", lambda: bench_selector(gpumpi, torch, w_kw))):
+                        ("selector", lambda: bench_selector(gpumpi, torch, w_kw)),
+                        ("reference_gpu_mpi", lambda: bench_reference_runtime(gpumpi, torch, w_kw))):
             try:
                 extra[key] = fn()
             except Exception as e:  # reported, not hidden
