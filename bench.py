@@ -559,26 +559,28 @@ def coll_sweep(args, gpumpi, torch, local):
     32..2048 ranks, 4 B .. 16 MiB per rank, default (heuristic) variant choice.  Inputs: int32 uniform in
     [0, 1000] from a seed (read as fp32 / fp64 bit patterns, small finite values, for the floating-point
     Allreduces).  Per
-    shape: p50/p99 of rank 0's per-iteration time over 10 calls after 3 warm-up calls, and GB/s of the
+    shape: p50/p99 of rank 0's per-iteration time over 10 calls (50 for Allreduces of at most 1 KiB per
+    rank, where every variant is timed too) after 3 warm-up calls, and GB/s of the
     algorithmic bytes (Allreduce 2 n b, Bcast b + n b, Alltoall 2 n b with b = bytes a rank sends).  The
     int32 Allreduce, the Bcast and the Alltoall are checked bit for bit on sampled ranks."""
     import numpy as np
     iters, warm = 10, 3
     rows = []
-    sizes = [4, 64, 1 << 10, 1 << 14, 1 << 18, 1 << 22, 1 << 24]
+    sizes = [b for b in (4, 64, 1 << 10, 1 << 14, 1 << 18, 1 << 22, 1 << 24) if b <= args.max_bytes]
     rng = np.random.default_rng(11)
 
-    def timed(fn):
+    def timed(fn, k=iters):
         fn(warm, None)
-        ns = np.zeros(iters, dtype=np.uint64)
-        fn(iters, ns)
+        ns = np.zeros(k, dtype=np.uint64)
+        fn(k, ns)
         return float(np.percentile(ns, 50)) / 1e3, float(np.percentile(ns, 99)) / 1e3
 
     for n in (32, 128, 512, 1024, 2048):
         with gpumpi.World(n, device=local, timeout_s=120.0) as w:
             maxb = max(sizes)
             g = torch.Generator(device="cuda").manual_seed(n)
-            send = torch.randint(0, 1001, (n * maxb // 4,), generator=g, device="cuda", dtype=torch.int32)
+            send = torch.randint(0, 1001, (max(n * maxb // 4, n * n),), generator=g, device="cuda",
+                                 dtype=torch.int32)
             recv = torch.empty_like(send)
             for b in sizes:
                 cnt = b // 4
@@ -591,9 +593,22 @@ def coll_sweep(args, gpumpi, torch, local):
                         continue
                     s_, r_ = (s2, r2) if view is None else (s2.view(view), r2.view(view))
                     c_ = s_.shape[1]
-                    p50, p99 = timed(lambda k, ns: w.allreduce(s_, r_, c_, dt, gpumpi.OP_SUM, iters=k, iter_ns=ns))
+                    p50, p99 = timed(lambda k, ns: w.allreduce(s_, r_, c_, dt, gpumpi.OP_SUM, iters=k, iter_ns=ns),
+                                     50 if b <= 1024 else iters)
                     row = {"coll": name, "ranks": n, "bytes_per_rank": b, "p50_us": p50, "p99_us": p99,
                            "gbs": 2.0 * n * b / (p50 * 1e-6) / 1e9}
+                    if b <= 1024:
+                        # every variant forced (job path), against the default choice: integers may take
+                        # any order; floating point keeps the canonical order (DIRECT, STAGED)
+                        vt = {}
+                        for v in range(4):
+                            w.set_policy(v, 0)
+                            vt[gpumpi.VARIANT_NAMES[v]] = timed(
+                                lambda k, ns: w.allreduce(s_, r_, c_, dt, gpumpi.OP_SUM, iters=k, iter_ns=ns), 50)[0]
+                        w.set_policy(-1, 3)
+                        eligible = list(vt) if view is None else ["direct", "staged"]
+                        row["variants_p50_us"] = vt
+                        row["default_over_best"] = p50 / min(vt[k] for k in eligible)
                     if view is None:
                         ref = torch.zeros(cnt, dtype=torch.int64, device="cuda")
                         for i in range(0, n, 64):
@@ -648,6 +663,7 @@ def main():
                          "256 KiB; device timing only (the ncu capture cases); p2p_sweep / coll_sweep: the "
                          "point-to-point and collectives sweeps")
     ap.add_argument("--variant", type=int, default=-1, help="variant override for the small cases")
+    ap.add_argument("--max-bytes", type=int, default=1 << 24, help="largest bytes per rank of the collectives sweep")
     args = ap.parse_args()
     dist, rank, ws = dist_setup()
     if args.impl == "reference":

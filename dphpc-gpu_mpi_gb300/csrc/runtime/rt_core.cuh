@@ -314,13 +314,6 @@ struct alignas(128) RankState {
     int uq_free_top;
     int req_hwm;
     int uq_hwm;
-    int sel_key_kind;
-    long long sel_key_bytes;
-    int sel_key_n;
-    int sel_key_dt;
-    int sel_key_op;
-    int sel_variant;
-    float sel_y[4];                 // the network's predicted log-times of the cached shape
     unsigned long long coll_calls;
     void* attrs;                    // keyvals and cached attributes (device heap, made on first use)
     Job p2p_job;

@@ -45,6 +45,18 @@ __device__ int select_variant(int kind, long long bytes_per_rank, int n, int dt,
         const int tv = tuned_cell(kind, bytes_per_rank, n, aligned16);
         if (tv >= 0) return tv;
     }
+    // Heuristic default for small folds whose result does not depend on the order (integers with an
+    // associative operator): RING starts chunk k at member k + 1, so the one or two chunks of a small fold
+    // do not all read member 0 first.  Measured at 1 KiB int32 SUM per rank (p50 of 10 calls): 15.8 vs
+    // 17.8 us at 32 ranks, 20.7 vs 21.9 at 128, 38.1 vs 40.4 at 512, 55.6 vs 57.0 at 1024.  Floating point
+    // keeps the canonical order.
+    if (c_rt.selector_mode == 3 && (kind == JOB_ALLREDUCE || kind == JOB_REDUCE) && bytes_per_rank <= 4096 &&
+        (op == GPUMPI_OP_SUM || op == GPUMPI_OP_MAX || op == GPUMPI_OP_MIN || op == GPUMPI_OP_PROD ||
+         op == GPUMPI_OP_BAND || op == GPUMPI_OP_BOR || op == GPUMPI_OP_BXOR) &&
+        (dt == GPUMPI_INT || dt == GPUMPI_INT32_T || dt == GPUMPI_UNSIGNED || dt == GPUMPI_UINT32_T ||
+         dt == GPUMPI_LONG || dt == GPUMPI_LONG_LONG_INT || dt == GPUMPI_LONG_LONG || dt == GPUMPI_INT64_T ||
+         dt == GPUMPI_UNSIGNED_LONG || dt == GPUMPI_UNSIGNED_LONG_LONG || dt == GPUMPI_UINT64_T))
+        return GPUMPI_VARIANT_RING;
     return GPUMPI_VARIANT_DIRECT;
 }
 
