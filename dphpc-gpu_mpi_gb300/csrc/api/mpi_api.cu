@@ -466,7 +466,7 @@ __device__ void mlp_infer_task(void* arg, int tid, int nt) {
 // global-memory round trip (the check ran on the rank's critical path before every collective).
 struct SelCache {
     long long bytes;
-    int kind, n, dt, op, variant, valid;
+    int kind, n, dt, op, blocks, variant, valid;
     float y[4];
 };
 __shared__ SelCache s_sel;
@@ -477,7 +477,9 @@ __shared__ SelCache s_sel;
 // calls of one shape.
 __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, int dt, int op, float* pred) {
     SelCache* sc = &s_sel;
-    if (sc->valid && sc->bytes == bytes && sc->kind == kind && sc->n == n && sc->dt == dt && sc->op == op) {
+    const int blocks = c_rt.nranks + c_rt.nengines;  // the network's occupancy input depends on it
+    if (sc->valid && sc->bytes == bytes && sc->kind == kind && sc->n == n && sc->dt == dt && sc->op == op &&
+        sc->blocks == blocks) {
         for (int v = 0; v < 4; v++) pred[v] = sc->y[v];
         return sc->variant;
     }
@@ -508,8 +510,20 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     sc->n = n;
     sc->dt = dt;
     sc->op = op;
+    sc->blocks = blocks;
     sc->variant = best;
     sc->valid = 1;
+    // kept for the rank's later launches (loaded by selector_rank_begin)
+    SelCacheRec* g = &c_rt.sel_cache[me()];
+    g->bytes = bytes;
+    g->kind = kind;
+    g->n = n;
+    g->dt = dt;
+    g->op = op;
+    g->blocks = blocks;
+    g->variant = best;
+    for (int v = 0; v < 4; v++) g->y[v] = w->y[v];
+    g->epoch = c_rt.sel_epoch;
     return best;
 }
 
@@ -738,8 +752,23 @@ __device__ long long sample_counts(const int* counts, int n) {
 
 }  // namespace
 
-// Shared memory starts undefined in every launch: the learned choice cache starts empty.
-__device__ void gpumpi::selector_rank_begin() { s_sel.valid = 0; }
+// Shared memory starts undefined in every launch: the cache starts from the rank's record of its last
+// choice when that record belongs to the current selector epoch, else empty.
+__device__ void gpumpi::selector_rank_begin() {
+    s_sel.valid = 0;
+    if (c_rt.selector_mode != 2 || !c_rt.sel_cache) return;
+    const SelCacheRec g = c_rt.sel_cache[me()];
+    if (g.epoch != c_rt.sel_epoch) return;
+    s_sel.bytes = g.bytes;
+    s_sel.kind = g.kind;
+    s_sel.n = g.n;
+    s_sel.dt = g.dt;
+    s_sel.op = g.op;
+    s_sel.blocks = g.blocks;
+    s_sel.variant = g.variant;
+    for (int v = 0; v < 4; v++) s_sel.y[v] = g.y[v];
+    s_sel.valid = 1;
+}
 
 // ------------------------------------------------------------------------------------------------
 // environment

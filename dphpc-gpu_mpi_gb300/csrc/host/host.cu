@@ -263,6 +263,7 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     size_t o_pool = dc.take<unsigned char>(scratch_pool_bytes * (size_t)n);
     const size_t tree_bytes = 64ull << 20;
     size_t o_tree = dc.take<unsigned char>(tree_bytes);
+    size_t o_selc = dc.take<gpumpi::SelCacheRec>(n);
     w->data_bytes = align_up(dc.off, 256);
 
     CK(cudaMalloc(&w->d_ctrl, w->ctrl_bytes));
@@ -297,6 +298,8 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     r.trace_cap = cfg.trace_capacity;
     r.trace_enabled = cfg.trace_capacity > 0;
     r.ranks = (gpumpi::RankState*)(w->d_ctrl + o_ranks);
+    r.sel_cache = (gpumpi::SelCacheRec*)(w->d_data + o_selc);
+    r.sel_epoch = 1;  // the data region starts zeroed: epoch 0 records are never valid
     r.ring = (gpumpi::Envelope*)(w->d_ctrl + o_ring);
     r.types = (gpumpi::TypeDesc*)(w->d_ctrl + o_types);
     r.errors = (gpumpi::ErrorRecord*)(w->d_ctrl + o_errors);
@@ -387,6 +390,7 @@ int gpumpi_world_get_info(gpumpi_world* w, gpumpi_world_info* info) {
 
 int gpumpi_set_policy(gpumpi_world* w, int variant, int mode) {
     if (!w) return GPUMPI_ERR_ARG;
+    w->h_rt.sel_epoch++;
     w->variant_override = variant;
     w->selector_mode = mode;
     return GPUMPI_SUCCESS;
@@ -394,6 +398,7 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode) {
 
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
     if (!w) return GPUMPI_ERR_ARG;
+    w->h_rt.sel_epoch++;
     switch (key) {
     case GPUMPI_TUNE_VEC: w->tune_vec = (int)value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_DYN_SMEM: w->dyn_smem_cap = value; return GPUMPI_SUCCESS;
@@ -436,6 +441,7 @@ int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes) {
             for (int c = 0; c < 2; c++) memcpy(img.data() + (k * 2 + c) * cell, table + k * cell, cell);
     }
     cudaSetDevice(w->device);
+    w->h_rt.sel_epoch++;
     if (!w->d_table) CK(cudaMalloc(&w->d_table, 6 * cell));
     CK(cudaMemcpy(w->d_table, img.data(), 6 * cell, cudaMemcpyHostToDevice));
     return GPUMPI_SUCCESS;
@@ -444,6 +450,7 @@ int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes) {
 int gpumpi_set_mlp(gpumpi_world* w, const float* params, size_t count) {
     if (!w || !params || count != GPUMPI_MLP_NPARAMS) return GPUMPI_ERR_ARG;
     cudaSetDevice(w->device);
+    w->h_rt.sel_epoch++;
     if (!w->d_mlp) CK(cudaMalloc(&w->d_mlp, sizeof(float) * count));
     CK(cudaMemcpy(w->d_mlp, params, sizeof(float) * count, cudaMemcpyHostToDevice));
     return GPUMPI_SUCCESS;

@@ -319,6 +319,16 @@ struct alignas(128) RankState {
     Job p2p_job;
 };
 
+// A rank's last learned variant choice, kept across launches (data region, never zeroed by a launch):
+// valid while `epoch` equals the runtime's selector epoch, which the host advances whenever the policy,
+// the weights, the table or a tuning knob changes.
+struct SelCacheRec {
+    long long bytes;
+    int kind, n, dt, op, blocks, variant;
+    unsigned epoch;
+    float y[4];
+};
+
 struct Task {                       // block task record, one per block (global memory)
     int kind;
     int i0;
@@ -420,6 +430,8 @@ struct Runtime {
     // selector
     const signed char* tuned_table;   // [kind][alignment class][log2 bytes][log2 ranks] -> variant (or nullptr)
     const float* mlp_params;          // learned selector weights (or nullptr)
+    SelCacheRec* sel_cache;           // per rank: the last learned choice, across launches
+    unsigned sel_epoch;               // records of another epoch are stale
     float mlp_margin;                 // learned choice overrides the tuned table only if it predicts this
                                       // much lower log-time
 
