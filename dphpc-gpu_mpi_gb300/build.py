@@ -24,6 +24,7 @@ SOURCES = [
     CSRC / "programs" / "prog_apps.cu",
     CSRC / "host" / "host.cu",
     CSRC / "host" / "noalloc.cu",
+    CSRC / "host" / "host_io.cu",
     CSRC / "selector" / "mlp.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

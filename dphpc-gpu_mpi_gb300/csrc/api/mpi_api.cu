@@ -3,6 +3,7 @@
 // One translation unit holds the whole runtime so its internals inline into each MPI call; user
 // programs (and the library's own built-in programs) link against these extern __device__ symbols
 // with relocatable device code, as converted programs link against the reference's libgpu_mpi.a.
+#include <cstdarg>
 #include <cstdio>
 #include <cstring>
 
@@ -14,6 +15,7 @@
 #include "../runtime/rt_p2p.cuh"
 #include "../runtime/rt_comm.cuh"
 #include "../runtime/rt_select.cuh"
+#include "gpumpi_stdio.h.cuh"
 
 using namespace gpumpi;
 
@@ -2178,3 +2180,5 @@ __device__ MPI_Op gpumpi_predefined_op(int code) {
     return (code >= 0 && code < GPUMPI_NUM_PREDEFINED_OPS) ? &g_predef_ops[code] : nullptr;
 }
 
+// file and stream I/O over the device -> host channel
+#include "api_io.cuh"

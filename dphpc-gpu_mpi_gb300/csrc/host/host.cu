@@ -17,6 +17,7 @@
 
 #include "../programs/rt_kernel.cuh"
 #include "../runtime/rt_core.cuh"
+#include "host_io.h"
 
 using gpumpi::Runtime;
 
@@ -117,6 +118,7 @@ struct gpumpi_world {
     // host mirrors of the error/exit records
     std::vector<gpumpi::ErrorRecord> h_err;
     std::vector<int> h_exit;
+    HostService* hio = nullptr;  // the device -> host channel's service thread and mapped memory
 };
 
 #define CK(expr)                                                                               \
@@ -264,6 +266,8 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     const size_t tree_bytes = 64ull << 20;
     size_t o_tree = dc.take<unsigned char>(tree_bytes);
     size_t o_selc = dc.take<gpumpi::SelCacheRec>(n);
+    size_t o_hio_tail = dc.take<unsigned long long>(1);
+    size_t o_hio_broken = dc.take<unsigned>(n);
     w->data_bytes = align_up(dc.off, 256);
 
     CK(cudaMalloc(&w->d_ctrl, w->ctrl_bytes));
@@ -299,6 +303,19 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     r.trace_enabled = cfg.trace_capacity > 0;
     r.ranks = (gpumpi::RankState*)(w->d_ctrl + o_ranks);
     r.sel_cache = (gpumpi::SelCacheRec*)(w->d_data + o_selc);
+    // the device -> host channel: mapped ring, responses and windows, and the world's service thread
+    if (cfg.host_window_bytes >= 0) {
+        long long win = cfg.host_window_bytes;
+        if (win == 0) win = std::min<long long>(1 << 20, std::max<long long>(4096, (16LL << 20) / n));
+        win = std::max<long long>(4096, win & ~4095LL);
+        w->hio = hio_create(n, (size_t)win, (unsigned long long*)(w->d_data + o_hio_tail),
+                            (unsigned*)(w->d_data + o_hio_broken), &r.hio, &w->err);
+        if (!w->hio) {
+            g_create_error = w->err;
+            gpumpi_world_destroy(w);
+            return GPUMPI_ERR_NO_MEM;
+        }
+    }
     r.sel_epoch = 1;  // the data region starts zeroed: epoch 0 records are never valid
     r.ring = (gpumpi::Envelope*)(w->d_ctrl + o_ring);
     r.types = (gpumpi::TypeDesc*)(w->d_ctrl + o_types);
@@ -362,6 +379,7 @@ int gpumpi_world_destroy(gpumpi_world* w) {
     if (!w) return GPUMPI_SUCCESS;
     cudaSetDevice(w->device);
     if (w->stream) cudaStreamSynchronize(w->stream);
+    hio_destroy(w->hio);
     cudaFree(w->d_ctrl);
     cudaFree(w->d_data);
     cudaFree(w->d_fixed);

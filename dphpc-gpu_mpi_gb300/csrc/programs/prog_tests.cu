@@ -6,6 +6,7 @@
 // plus the received values so the host can compare them with the golden vectors.
 //   p[0] = uint8 ok[nranks], p[1] = int64 outi[nranks*64], p[2] = double outd[nranks*64]
 #include "rt_kernel.cuh"
+#include "gpumpi_stdio.h.cuh"
 
 namespace {
 
@@ -894,6 +895,147 @@ struct Attrs {
     }
 };
 
+
+// File and stream I/O over the device -> host channel (MPI-IO, MPI-3.1 chapter 13; the reference's
+// tests/test_io_file_open.cu, test_io_file_access.cu, test_io_file_write.cu and
+// toolchain_tests/basicIO cover open modes, size, read-back and views with its own semantics).
+// p[3] = device string: a directory the program may create files in.  Files left for the host to check:
+//   io_block.bin   rank r's ints r * 1000 + i, i < K, at ints [r K, (r + 1) K) (explicit offsets)
+//   io_view.bin    view of 2 blocks of NW ints NW * n apart at disp r NW ints: rank r's ints r * 100 + i
+//   io_shared.bin  one int per rank through the shared file pointer (a permutation of the ranks)
+//   io_stdio.txt   rank 0's formatted line (gpumpi_fprintf)
+// outi[r][0] = the first failed check (0 = all passed), outi[r][1..] = error codes seen.
+__device__ void io_path(char* dst, const char* dir, const char* name) {
+    int k = 0;
+    for (; dir[k] && k < 200; k++) dst[k] = dir[k];
+    dst[k++] = '/';
+    for (int j = 0; name[j]; j++) dst[k++] = name[j];
+    dst[k] = 0;
+}
+struct FileIO {
+    static __device__ int run(const gpumpi_params& p) {
+        MPI_Init(nullptr, nullptr);
+        const int rank = wrank();
+        int n = 0;
+        MPI_Comm_size(MPI_COMM_WORLD, &n);
+        long long* oi = outi(p, rank);
+        const char* dir = (const char*)p.p[3];
+        char path[256];
+        int fail = 0, check = 0;
+#define IO_CHECK(c)                      \
+    do {                                 \
+        check++;                         \
+        if (!(c) && !fail) fail = check; \
+    } while (0)
+        constexpr int K = 300, NW = 50;
+        MPI_File fh = MPI_FILE_NULL;
+        MPI_Status st;
+        // explicit offsets, read-back of the neighbour's block, size
+        io_path(path, dir, "io_block.bin");
+        IO_CHECK(MPI_File_open(MPI_COMM_WORLD, path, MPI_MODE_CREATE | MPI_MODE_RDWR, MPI_INFO_NULL, &fh) ==
+                 MPI_SUCCESS);
+        int* buf = (int*)malloc(sizeof(int) * 2 * K);
+        for (int i = 0; i < K; i++) buf[i] = rank * 1000 + i;
+        IO_CHECK(MPI_File_write_at(fh, (MPI_Offset)rank * K * 4, buf, K, MPI_INT, &st) == MPI_SUCCESS);
+        int cnt = -1;
+        MPI_Get_count(&st, MPI_INT, &cnt);
+        IO_CHECK(cnt == K);
+        MPI_Barrier(MPI_COMM_WORLD);
+        const int nb = (rank + 1) % n;
+        IO_CHECK(MPI_File_read_at(fh, (MPI_Offset)nb * K * 4, buf + K, K, MPI_INT, &st) == MPI_SUCCESS);
+        bool same = true;
+        for (int i = 0; i < K; i++) same = same && buf[K + i] == nb * 1000 + i;
+        IO_CHECK(same);
+        MPI_Offset size = -1;
+        IO_CHECK(MPI_File_get_size(fh, &size) == MPI_SUCCESS && size == (MPI_Offset)n * K * 4);
+        // individual pointer with an int view from this rank's block
+        IO_CHECK(MPI_File_set_view(fh, (MPI_Offset)rank * K * 4, MPI_INT, MPI_INT, "native", MPI_INFO_NULL) ==
+                 MPI_SUCCESS);
+        IO_CHECK(MPI_File_seek(fh, 10, MPI_SEEK_SET) == MPI_SUCCESS);
+        int two[2] = {-1, -1};
+        IO_CHECK(MPI_File_read(fh, two, 2, MPI_INT, &st) == MPI_SUCCESS && two[0] == rank * 1000 + 10 &&
+                 two[1] == rank * 1000 + 11);
+        MPI_Offset pos = -1, byte = -1;
+        IO_CHECK(MPI_File_get_position(fh, &pos) == MPI_SUCCESS && pos == 12);
+        IO_CHECK(MPI_File_get_byte_offset(fh, pos, &byte) == MPI_SUCCESS && byte == (MPI_Offset)rank * K * 4 + 48);
+        IO_CHECK(MPI_File_close(&fh) == MPI_SUCCESS && fh == MPI_FILE_NULL);
+        // a non-contiguous view: 2 blocks of NW ints, NW * n ints apart, starting at this rank's slot
+        io_path(path, dir, "io_view.bin");
+        MPI_Datatype fileblk;
+        MPI_Type_vector(2, NW, NW * n, MPI_INT, &fileblk);
+        MPI_Type_commit(&fileblk);
+        IO_CHECK(MPI_File_open(MPI_COMM_WORLD, path, MPI_MODE_CREATE | MPI_MODE_WRONLY, MPI_INFO_NULL, &fh) ==
+                 MPI_SUCCESS);
+        IO_CHECK(MPI_File_set_view(fh, (MPI_Offset)rank * NW * 4, MPI_INT, fileblk, "native", MPI_INFO_NULL) ==
+                 MPI_SUCCESS);
+        MPI_Datatype got_e, got_f;
+        MPI_Offset got_d = -1;
+        char rep[16];
+        IO_CHECK(MPI_File_get_view(fh, &got_d, &got_e, &got_f, rep) == MPI_SUCCESS &&
+                 got_d == (MPI_Offset)rank * NW * 4 && got_e == MPI_INT && got_f == fileblk && rep[0] == 'n');
+        for (int i = 0; i < 2 * NW; i++) buf[i] = rank * 100 + i;
+        IO_CHECK(MPI_File_write_all(fh, buf, 2 * NW, MPI_INT, &st) == MPI_SUCCESS);
+        int dummy = 0;
+        oi[1] = MPI_File_read(fh, &dummy, 1, MPI_INT, &st);  // write-only: MPI_ERR_AMODE
+        IO_CHECK(oi[1] == MPI_ERR_AMODE);
+        IO_CHECK(MPI_File_close(&fh) == MPI_SUCCESS);
+        MPI_Type_free(&fileblk);
+        // the shared file pointer: one int per rank, in the order the ranks arrive
+        io_path(path, dir, "io_shared.bin");
+        IO_CHECK(MPI_File_open(MPI_COMM_WORLD, path, MPI_MODE_CREATE | MPI_MODE_RDWR, MPI_INFO_NULL, &fh) ==
+                 MPI_SUCCESS);
+        IO_CHECK(MPI_File_set_view(fh, 0, MPI_INT, MPI_INT, "native", MPI_INFO_NULL) == MPI_SUCCESS);
+        IO_CHECK(MPI_File_write_shared(fh, &rank, 1, MPI_INT, &st) == MPI_SUCCESS);
+        MPI_Barrier(MPI_COMM_WORLD);
+        MPI_Offset sp = -1;
+        IO_CHECK(MPI_File_get_position_shared(fh, &sp) == MPI_SUCCESS && sp == n);
+        IO_CHECK(MPI_File_seek_shared(fh, 0, MPI_SEEK_SET) == MPI_SUCCESS);
+        int first = -1;
+        if (rank == 0) IO_CHECK(MPI_File_read_shared(fh, &first, 1, MPI_INT, &st) == MPI_SUCCESS && first >= 0 && first < n);
+        IO_CHECK(MPI_File_close(&fh) == MPI_SUCCESS);
+        // errors: bad access modes, a missing file, writing a read-only file
+        oi[2] = MPI_File_open(MPI_COMM_WORLD, path, MPI_MODE_RDONLY | MPI_MODE_RDWR, MPI_INFO_NULL, &fh);
+        IO_CHECK(oi[2] == MPI_ERR_AMODE && fh == MPI_FILE_NULL);
+        oi[3] = MPI_File_open(MPI_COMM_WORLD, path, MPI_MODE_CREATE | MPI_MODE_RDONLY, MPI_INFO_NULL, &fh);
+        IO_CHECK(oi[3] == MPI_ERR_AMODE);
+        io_path(path, dir, "io_missing.bin");
+        oi[4] = MPI_File_open(MPI_COMM_WORLD, path, MPI_MODE_RDONLY, MPI_INFO_NULL, &fh);
+        IO_CHECK(oi[4] == MPI_ERR_NO_SUCH_FILE);
+        io_path(path, dir, "io_block.bin");
+        IO_CHECK(MPI_File_open(MPI_COMM_WORLD, path, MPI_MODE_RDONLY, MPI_INFO_NULL, &fh) == MPI_SUCCESS);
+        oi[5] = MPI_File_write(fh, buf, 1, MPI_INT, &st);
+        IO_CHECK(oi[5] == MPI_ERR_READ_ONLY);
+        IO_CHECK(MPI_File_close(&fh) == MPI_SUCCESS);
+        // delete on close, and delete of a missing file
+        io_path(path, dir, "io_tmp.bin");
+        IO_CHECK(MPI_File_open(MPI_COMM_WORLD, path, MPI_MODE_CREATE | MPI_MODE_WRONLY | MPI_MODE_DELETE_ON_CLOSE,
+                               MPI_INFO_NULL, &fh) == MPI_SUCCESS);
+        IO_CHECK(MPI_File_close(&fh) == MPI_SUCCESS);
+        if (rank == 0) {
+            oi[6] = MPI_File_delete(path, MPI_INFO_NULL);
+            IO_CHECK(oi[6] == MPI_ERR_NO_SUCH_FILE);
+            // stdio through the host
+            io_path(path, dir, "io_stdio.txt");
+            gpumpi_FILE* f = gpumpi_fopen(path, "w");
+            IO_CHECK(f != nullptr);
+            IO_CHECK(gpumpi_fprintf(f, "rank %d of %d pi %.6f name %s hex %#x pad [%5d] [%-4s] %c%%\n", rank, n,
+                                    3.14159265358979, "gb300", 255, 42, "ab", 'z') > 0);
+            IO_CHECK(gpumpi_fputs("second line\n", f) == 0);
+            IO_CHECK(gpumpi_fclose(f) == 0);
+            f = gpumpi_fopen(path, "r");
+            char line[8] = {};
+            IO_CHECK(f && gpumpi_fread(line, 1, 4, f) == 4 && line[0] == 'r' && line[3] == 'k');
+            IO_CHECK(gpumpi_fclose(f) == 0);
+            IO_CHECK(gpumpi_printf("gpumpi_printf from rank %d of %d: %s %.3e\n", rank, n, "ok", 1234.5) > 0);
+        }
+        free(buf);
+#undef IO_CHECK
+        oi[0] = fail;
+        okp(p)[rank] = fail == 0;
+        return MPI_Finalize();
+    }
+};
+
 }  // namespace
 
 extern const gpumpi_prog_entry g_test_programs[] = {
@@ -921,5 +1063,6 @@ extern const gpumpi_prog_entry g_test_programs[] = {
     GPUMPI_PROGRAM(GPUMPI_T_TINY_STRESS, "tiny_stress", TinyStress),
     GPUMPI_PROGRAM(GPUMPI_T_TINY_MIXED, "tiny_mixed", TinyMixed),
     GPUMPI_PROGRAM(GPUMPI_T_ATTRS, "attrs", Attrs),
+    GPUMPI_PROGRAM(GPUMPI_T_FILE_IO, "file_io", FileIO),
 };
 extern const int g_num_test_programs = sizeof(g_test_programs) / sizeof(g_test_programs[0]);

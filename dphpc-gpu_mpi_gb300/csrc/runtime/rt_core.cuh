@@ -15,6 +15,7 @@
 
 #include "gpumpi_abi.h"
 #include "mpi.h.cuh"
+#include "rt_hostio.cuh"
 
 namespace gpumpi {
 
@@ -431,6 +432,7 @@ struct Runtime {
     const signed char* tuned_table;   // [kind][alignment class][log2 bytes][log2 ranks] -> variant (or nullptr)
     const float* mlp_params;          // learned selector weights (or nullptr)
     SelCacheRec* sel_cache;           // per rank: the last learned choice, across launches
+    HostIO hio;                       // the device -> host request channel (files, standard streams)
     unsigned sel_epoch;               // records of another epoch are stale
     float mlp_margin;                 // learned choice overrides the tuned table only if it predicts this
                                       // much lower log-time

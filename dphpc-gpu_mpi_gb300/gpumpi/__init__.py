@@ -39,7 +39,7 @@ TESTS = {
     "single_int": 1, "transfer_array": 2, "send_recv": 3, "repeat_send_recv": 4, "network_flood": 5,
     "all_to_all": 6, "reduce_int16_prod": 7, "allreduce_f64_sum": 8, "allgather_int": 9, "scatter_int": 10,
     "scatterv_int": 11, "comm_rank": 12, "comm_dup_isolation": 13, "comm_split": 14, "sample": 15,
-    "p2p_matching": 16, "timeout": 17, "datatypes": 18, "subcomm_coll": 19, "errors": 20, "cart": 21, "tiny_stress": 22, "tiny_mixed": 23, "attrs": 24,
+    "p2p_matching": 16, "timeout": 17, "datatypes": 18, "subcomm_coll": 19, "errors": 20, "cart": 21, "tiny_stress": 22, "tiny_mixed": 23, "attrs": 24, "file_io": 25,
 }
 P_COLL, P_PINGPONG, P_RING, P_PI, P_BUCKET_SORT, P_HALO, P_BATCH = 100, 101, 102, 103, 104, 105, 106
 COLL = {"allreduce": 0, "reduce": 1, "bcast": 2, "alltoall": 3, "alltoallv": 4, "allgather": 5, "gather": 6,
@@ -79,7 +79,8 @@ class Config(ctypes.Structure):
                 ("posted_depth", ctypes.c_int), ("device", ctypes.c_int), ("stack_bytes", ctypes.c_size_t),
                 ("heap_bytes", ctypes.c_size_t), ("arena_bytes", ctypes.c_size_t),
                 ("copy_chunk_bytes", ctypes.c_longlong), ("engine_min_bytes", ctypes.c_longlong),
-                ("timeout_s", ctypes.c_double), ("trace_capacity", ctypes.c_int)]
+                ("timeout_s", ctypes.c_double), ("trace_capacity", ctypes.c_int),
+                ("host_window_bytes", ctypes.c_longlong)]
 
 
 class WorldInfo(ctypes.Structure):

@@ -59,6 +59,8 @@ typedef struct gpumpi_config {
     long long engine_min_bytes;   /* jobs smaller than this are not offered to engine blocks */
     double timeout_s;         /* bound on every device-side wait */
     int trace_capacity;       /* per-call timing records kept (0 = tracing off) */
+    long long host_window_bytes;  /* per-rank payload window of the device -> host channel (file and
+                                     stream I/O); 0 = 16 MiB / ranks, 4 KiB .. 1 MiB; -1 = no channel */
 } gpumpi_config;
 
 typedef struct gpumpi_world_info {
@@ -101,6 +103,7 @@ enum gpumpi_program {
     GPUMPI_T_TINY_STRESS,      /* back-to-back tiny collectives with skewed ranks, every result checked */
     GPUMPI_T_TINY_MIXED,       /* small collectives mixing thread-local/global buffers and datatypes */
     GPUMPI_T_ATTRS,            /* keyvals and cached attributes, MPI_Wtime / MPI_Wtick */
+    GPUMPI_T_FILE_IO,          /* MPI-IO and gpumpi stdio over the host channel; p[3] = directory */
     /* hot-path programs */
     GPUMPI_P_COLL = 100,       /* i[0]=kind i[1]=count i[2]=dt i[3]=op i[4]=root i[5]=iters i[6]=send stride
                                   i[7]=recv stride i[8]=variant p[0]=send p[1]=recv p[2..5]=count/displ matrices

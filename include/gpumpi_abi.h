@@ -95,6 +95,22 @@
 #define GPUMPI_ERR_NOT_IMPL   17
 #define GPUMPI_ERR_LAUNCH     18   /* host side: launch / co-residency failure */
 #define GPUMPI_ERR_CUDA       19   /* host side: a CUDA runtime call failed */
+/* MPI-IO error classes (MPI-3.1 table 13.4).  The reference numbers its I/O classes 1..16 in a space of
+ * their own (gpu_libs/gpu_mpi/io.cuh:28-45), which overlaps MPI_ERR_OTHER..; here they are distinct. */
+#define GPUMPI_ERR_FILE                  20
+#define GPUMPI_ERR_NOT_SAME              21
+#define GPUMPI_ERR_AMODE                 22
+#define GPUMPI_ERR_UNSUPPORTED_DATAREP   23
+#define GPUMPI_ERR_UNSUPPORTED_OPERATION 24
+#define GPUMPI_ERR_NO_SUCH_FILE          25
+#define GPUMPI_ERR_FILE_EXISTS           26
+#define GPUMPI_ERR_BAD_FILE              27
+#define GPUMPI_ERR_ACCESS                28
+#define GPUMPI_ERR_NO_SPACE              29
+#define GPUMPI_ERR_QUOTA                 30
+#define GPUMPI_ERR_READ_ONLY             31
+#define GPUMPI_ERR_FILE_IN_USE           32
+#define GPUMPI_ERR_IO                    33
 
 /* ---- collective algorithm variants (what the tuned table and the learned selector pick) ---- */
 #define GPUMPI_VARIANT_AUTO     (-1)

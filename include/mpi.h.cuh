@@ -268,6 +268,77 @@ __device__ int MPI_Cartdim_get(MPI_Comm comm, int* ndims);
 __device__ int MPI_Cart_sub(MPI_Comm comm, const int remain_dims[], MPI_Comm* newcomm);
 __device__ int MPI_Topo_test(MPI_Comm comm, int* status);
 
+// ---- MPI-IO (reference gpu_libs/gpu_mpi/io.cuh:13-153; MPI-3.1 chapter 13) ----
+// File data and metadata travel over the device -> host request channel; the host process performs the
+// file system calls.  MPI_File is an opaque handle here (the reference passes a struct by value), read
+// and write calls return MPI_SUCCESS or an error class and report the amount in the status, and file
+// pointers count etypes of the current view.
+typedef long long MPI_Offset;
+struct MPI_Info_impl;
+typedef MPI_Info_impl* MPI_Info;
+#define MPI_INFO_NULL ((MPI_Info)0)
+struct MPI_File_impl;
+typedef MPI_File_impl* MPI_File;
+#define MPI_FILE_NULL ((MPI_File)0)
+#define MPI_MODE_RDONLY 1             // access modes: the reference's values (io.cuh:13-21)
+#define MPI_MODE_RDWR 2
+#define MPI_MODE_WRONLY 4
+#define MPI_MODE_CREATE 8
+#define MPI_MODE_EXCL 16
+#define MPI_MODE_DELETE_ON_CLOSE 32
+#define MPI_MODE_UNIQUE_OPEN 64
+#define MPI_MODE_SEQUENTIAL 128
+#define MPI_MODE_APPEND 256
+#define MPI_SEEK_SET 1                // the reference's values (io.cuh:52-54)
+#define MPI_SEEK_CUR 2
+#define MPI_SEEK_END 3
+#define MPI_DISPLACEMENT_CURRENT (-1)
+#define MPI_ERR_FILE GPUMPI_ERR_FILE
+#define MPI_ERR_NOT_SAME GPUMPI_ERR_NOT_SAME
+#define MPI_ERR_AMODE GPUMPI_ERR_AMODE
+#define MPI_ERR_UNSUPPORTED_DATAREP GPUMPI_ERR_UNSUPPORTED_DATAREP
+#define MPI_ERR_UNSUPPORTED_OPERATION GPUMPI_ERR_UNSUPPORTED_OPERATION
+#define MPI_ERR_NO_SUCH_FILE GPUMPI_ERR_NO_SUCH_FILE
+#define MPI_ERR_FILE_EXISTS GPUMPI_ERR_FILE_EXISTS
+#define MPI_ERR_BAD_FILE GPUMPI_ERR_BAD_FILE
+#define MPI_ERR_ACCESS GPUMPI_ERR_ACCESS
+#define MPI_ERR_NO_SPACE GPUMPI_ERR_NO_SPACE
+#define MPI_ERR_QUOTA GPUMPI_ERR_QUOTA
+#define MPI_ERR_READ_ONLY GPUMPI_ERR_READ_ONLY
+#define MPI_ERR_FILE_IN_USE GPUMPI_ERR_FILE_IN_USE
+#define MPI_ERR_IO GPUMPI_ERR_IO
+__device__ int MPI_File_open(MPI_Comm comm, const char* filename, int amode, MPI_Info info, MPI_File* fh);
+__device__ int MPI_File_close(MPI_File* fh);
+__device__ int MPI_File_delete(const char* filename, MPI_Info info);
+__device__ int MPI_File_get_size(MPI_File fh, MPI_Offset* size);
+__device__ int MPI_File_set_size(MPI_File fh, MPI_Offset size);
+__device__ int MPI_File_sync(MPI_File fh);
+__device__ int MPI_File_get_amode(MPI_File fh, int* amode);
+__device__ int MPI_File_set_view(MPI_File fh, MPI_Offset disp, MPI_Datatype etype, MPI_Datatype filetype,
+                                 const char* datarep, MPI_Info info);
+__device__ int MPI_File_get_view(MPI_File fh, MPI_Offset* disp, MPI_Datatype* etype, MPI_Datatype* filetype,
+                                 char* datarep);
+__device__ int MPI_File_read(MPI_File fh, void* buf, int count, MPI_Datatype datatype, MPI_Status* status);
+__device__ int MPI_File_write(MPI_File fh, const void* buf, int count, MPI_Datatype datatype, MPI_Status* status);
+__device__ int MPI_File_read_at(MPI_File fh, MPI_Offset offset, void* buf, int count, MPI_Datatype datatype,
+                                MPI_Status* status);
+__device__ int MPI_File_write_at(MPI_File fh, MPI_Offset offset, const void* buf, int count, MPI_Datatype datatype,
+                                 MPI_Status* status);
+__device__ int MPI_File_read_all(MPI_File fh, void* buf, int count, MPI_Datatype datatype, MPI_Status* status);
+__device__ int MPI_File_write_all(MPI_File fh, const void* buf, int count, MPI_Datatype datatype, MPI_Status* status);
+__device__ int MPI_File_read_at_all(MPI_File fh, MPI_Offset offset, void* buf, int count, MPI_Datatype datatype,
+                                    MPI_Status* status);
+__device__ int MPI_File_write_at_all(MPI_File fh, MPI_Offset offset, const void* buf, int count,
+                                     MPI_Datatype datatype, MPI_Status* status);
+__device__ int MPI_File_read_shared(MPI_File fh, void* buf, int count, MPI_Datatype datatype, MPI_Status* status);
+__device__ int MPI_File_write_shared(MPI_File fh, const void* buf, int count, MPI_Datatype datatype,
+                                     MPI_Status* status);
+__device__ int MPI_File_seek(MPI_File fh, MPI_Offset offset, int whence);
+__device__ int MPI_File_get_position(MPI_File fh, MPI_Offset* offset);
+__device__ int MPI_File_seek_shared(MPI_File fh, MPI_Offset offset, int whence);
+__device__ int MPI_File_get_position_shared(MPI_File fh, MPI_Offset* offset);
+__device__ int MPI_File_get_byte_offset(MPI_File fh, MPI_Offset offset, MPI_Offset* disp);
+
 // ---- block-rank extensions (no counterpart in the reference) ----
 // Rank of the calling block in MPI_COMM_WORLD, usable anywhere in the rank's block.
 __device__ int gpumpi_world_rank(void);

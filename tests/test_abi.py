@@ -74,14 +74,15 @@ def test_product_path_has_no_oracle_dependency():
 
 def test_device_header_declares_the_reference_surface():
     """Every __device__ MPI function the reference's headers declare (mpi.cuh, communicator.cuh,
-    group.cuh; names recorded in tests/golden/reference_device_api.json by make_api_list.py) is declared
+    group.cuh, io.cuh; names recorded in tests/golden/reference_device_api.json by make_api_list.py) is declared
     by include/mpi.h.cuh, so a converted program that calls any of them links."""
     import json
     names = json.loads((ROOT / "tests" / "golden" / "reference_device_api.json").read_text())
     text = (ROOT / "include" / "mpi.h.cuh").read_text()
     ours = set(re.findall(r"__device__[^;(]*?\b(MPI_\w+)\s*\(", text))
-    for header in ("mpi.cuh", "communicator.cuh", "group.cuh"):
-        missing = sorted(set(names[header]) - ours)
+    for header in ("mpi.cuh", "communicator.cuh", "group.cuh", "io.cuh"):
+        # io.cuh's MPI_File_View is the constructor of the reference's internal view struct, not an API call
+        missing = sorted(set(names[header]) - ours - {"MPI_File_View"})
         assert not missing, (header, missing)
     # the typedefs the keyval functions take
     for t in ("MPI_Copy_function", "MPI_Delete_function"):

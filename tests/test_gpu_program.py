@@ -54,3 +54,25 @@ def test_bad_options_fail_cleanly(pi_exe):
     r = subprocess.run([str(pi_exe), "1000", "---gpumpi", "-n", "8", "-b", "48"], capture_output=True, text=True,
                        timeout=120)
     assert r.returncode == 1 and "threads_per_block" in r.stderr
+
+
+@pytest.fixture(scope="module")
+def io_exe(tmp_path_factory, gpulib):
+    import build
+    out = tmp_path_factory.mktemp("prog") / "mpi_io_report"
+    return build.build_program([ROOT / "tests" / "programs" / "mpi_io_report.cu"], out)
+
+
+@pytest.mark.parametrize("ranks", [1, 16, 100])
+def test_converted_program_writes_files_and_prints(io_exe, tmp_path, ranks):
+    # fprintf(stdout, ...) and MPI_File_write_at from ranks, performed by the launcher's host channel
+    import numpy as np
+    n = 1000
+    out = tmp_path / "partial.bin"
+    r = subprocess.run([str(io_exe), str(out), str(n), "---gpumpi", "-n", str(ranks)], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    total = float(sum(i * i for i in range(n)))
+    assert f"sum of squares below {n} over {ranks} ranks: {total:.1f}" in r.stdout
+    parts = np.fromfile(out, dtype=np.float64)
+    assert parts.tolist() == [float(sum(i * i for i in range(k, n, ranks))) for k in range(ranks)]
