@@ -464,7 +464,8 @@ def bench_selector(gpumpi, torch, w_kw):
         rep = json.loads(rep_path.read_text())
         out["heldout_stream"] = {k: rep[k] for k in ("all", "allreduce", "alltoallv") if k in rep}
         out["training_timings"] = rep.get("train_records", 0) + rep.get("val_records", 0)
-        out["margin"] = rep.get("margin")
+        out["margins"] = rep.get("margins", rep.get("margin"))
+        out["heldout_shapes"] = rep.get("shapes")
     n, count = 1024, (1 << 20) // 4
     send = (torch.rand((n, count), device="cuda") * 2 - 1).contiguous()
     recv = torch.empty_like(send)

@@ -200,9 +200,10 @@ struct CollArgs {
     MPI_User_function* ufn;
     long long est_piece;   // pulls: estimated bytes per piece
     int variant;
-    bool learned = false;  // `variant` is the network's choice; pred = its predicted log-times
-    float pred[4] = {0.f, 0.f, 0.f, 0.f};
+    bool learned = false;  // the learned policy chooses (the setup evaluates the network)
 };
+
+__device__ int learned_variant(int kind, long long bytes, int n, int dt, int op, int aligned16, float* pred);
 
 // Elements per thread for a fold chunk (chunk = T * v elements).  Candidates: one 16-byte vector,
 // 8 bytes (4-byte types), one element.  Score = blocks busy per wave x bytes in flight per thread
@@ -311,8 +312,11 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
     if (a.kind == JOB_ALLREDUCE || a.kind == JOB_REDUCE) {
         j->count = a.count;
         bytes = a.count * a.esize * (long long)n;
-        int variant = select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, a.variant, j->aligned16,
-                                     a.learned ? a.pred : nullptr);
+        float pred[4];
+        const int ov = a.learned ? learned_variant(a.kind, a.count * a.esize, n, a.dt, a.op, j->aligned16, pred)
+                                 : a.variant;
+        int variant = select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, ov, j->aligned16,
+                                     a.learned ? pred : nullptr);
         may_post = may_post && bytes >= c_rt.engine_min_bytes;
         long long target = n + (may_post ? c_rt.nengines : 0);
         int vec = 1;
@@ -368,9 +372,13 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         long long P = matrix ? (long long)n * n : (long long)n;
         j->count = P;
         // piece order (DIRECT / TREE / RING, see piece_of) or bulk-copy staging (STAGED)
+        float pred[4];
+        const int ov = a.learned && a.kind == JOB_ALLTOALLV
+                           ? learned_variant(a.kind, a.est_piece * n, n, a.dt, -1, j->aligned16, pred)
+                           : a.variant;
         int variant = a.kind == JOB_ALLTOALLV
-                          ? select_variant(a.kind, a.est_piece * n, n, a.dt, -1, a.variant, j->aligned16,
-                                           a.learned ? a.pred : nullptr)
+                          ? select_variant(a.kind, a.est_piece * n, n, a.dt, -1, ov, j->aligned16,
+                                           a.learned ? pred : nullptr)
                           : (matrix && a.variant >= 0 && a.variant < GPUMPI_NUM_VARIANTS ? a.variant
                                                                                           : GPUMPI_VARIANT_DIRECT);
         // STAGED needs shared memory for two bulk-copy stages of at least 512 bytes per warp
@@ -431,8 +439,10 @@ __device__ __forceinline__ int op_code_of(MPI_Op op, MPI_User_function** ufn) {
 }
 
 // ---- learned selector: in-kernel inference of the MLP trained by csrc/selector/mlp.cu ----
-// Features (same formula as gpumpi/selector.py): log2 bytes per rank, log2 ranks, datatype one-hot
-// (f32, f64, i32, i64), operator one-hot (SUM, MAX, MIN, PROD), rank share of the launch's blocks, kind.
+// Features (same formula as gpumpi/selector.py, features()): log2 bytes per rank, log2 ranks, datatype
+// one-hot (f32, f64, i32, i64), SUM flag, 16-byte and 8-byte alignment flags of the members' buffers,
+// rank share of the launch's blocks, kind.  The alignment is known only once every member has arrived, so
+// the member that sets the collective up evaluates the network (the table's cell depends on it too).
 struct MlpWork {
     float f[12];
     float h1[64];
@@ -465,23 +475,30 @@ __device__ void mlp_infer_task(void* arg, int tid, int nt) {
 }
 
 // The rank's last learned choice, in shared memory: a repeated call of one shape is answered without a
-// global-memory round trip (the check ran on the rank's critical path before every collective).
+// global-memory round trip.
 struct SelCache {
     long long bytes;
-    int kind, n, dt, op, blocks, variant, valid;
+    int kind, n, dt, op, blocks, aligned, variant, valid;
     float y[4];
 };
 __shared__ SelCache s_sel;
 
+// Variants the selector chooses among: DIRECT, TREE, RING.  STAGED (bulk-copy staging through shared
+// memory) never measured fastest on this GPU: the 8 KiB of dynamic shared memory per rank block leaves it
+// stages of a few hundred bytes, and more shared memory takes L1 from the spilled registers of every
+// other path (1024 ranks x 1 MiB uneven Alltoallv: DIRECT 3,940 GB/s at 8 KiB, 3,079 at 12-24 KiB,
+// STAGED 2,385-2,780); it stays available as an explicit variant.
+constexpr int SEL_CHOICES = 3;
+
 // Variant with the smallest predicted time, and the predicted log-times in pred[4] (the setup weighs the
-// tuned table's choice against them once the buffers' alignment is known); every member computes it from
-// the same inputs with the same operation order, so all members agree.  Cached per rank for repeated
-// calls of one shape.
-__device__ __noinline__ int learned_variant(int kind, long long bytes, int n, int dt, int op, float* pred) {
+// tuned table's choice against them); every member computes the same features, so the choice does not
+// depend on which member sets up.  Cached per rank for repeated calls of one shape.
+__device__ __noinline__ int learned_variant(int kind, long long bytes, int n, int dt, int op, int aligned16, float* pred) {
     SelCache* sc = &s_sel;
     const int blocks = c_rt.nranks + c_rt.nengines;  // the network's occupancy input depends on it
+    const int al = aligned16 >= 16 ? 16 : aligned16 >= 8 ? 8 : 0;
     if (sc->valid && sc->bytes == bytes && sc->kind == kind && sc->n == n && sc->dt == dt && sc->op == op &&
-        sc->blocks == blocks) {
+        sc->blocks == blocks && sc->aligned == al) {
         for (int v = 0; v < 4; v++) pred[v] = sc->y[v];
         return sc->variant;
     }
@@ -492,11 +509,10 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     const int dslot = dt == GPUMPI_FLOAT ? 2 : (dt == GPUMPI_DOUBLE || dt == GPUMPI_LONG_DOUBLE) ? 3
                       : (dt == GPUMPI_INT || dt == GPUMPI_INT32_T) ? 4 : 5;
     w->f[dslot] = 1.f;
-    if (op >= 0) {  // pulls (Alltoall(v)) have no operator: all four slots stay 0
-        const int oslot = op == GPUMPI_OP_SUM ? 6 : op == GPUMPI_OP_MAX ? 7 : op == GPUMPI_OP_MIN ? 8 : 9;
-        w->f[oslot] = 1.f;
-    }
-    w->f[10] = (float)n / (float)(c_rt.nranks + c_rt.nengines);
+    w->f[6] = op == GPUMPI_OP_SUM ? 1.f : 0.f;  // pulls have no operator (op < 0)
+    w->f[7] = al >= 16 ? 1.f : 0.f;
+    w->f[8] = al >= 8 ? 1.f : 0.f;
+    w->f[10] = (float)n / (float)blocks;
     w->f[11] = kind == JOB_REDUCE ? 1.f : kind == JOB_ALLTOALLV ? -1.f : 0.f;
     Task t;
     t.kind = TASK_USER;
@@ -504,7 +520,7 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     t.p1 = w;
     dispatch(t);
     int best = 0;
-    for (int v = 1; v < 4; v++)
+    for (int v = 1; v < SEL_CHOICES; v++)
         if (w->y[v] < w->y[best]) best = v;
     for (int v = 0; v < 4; v++) sc->y[v] = pred[v] = w->y[v];
     sc->kind = kind;
@@ -513,6 +529,7 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     sc->dt = dt;
     sc->op = op;
     sc->blocks = blocks;
+    sc->aligned = al;
     sc->variant = best;
     sc->valid = 1;
     // kept for the rank's later launches (loaded by selector_rank_begin)
@@ -523,12 +540,12 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     g->dt = dt;
     g->op = op;
     g->blocks = blocks;
+    g->aligned = al;
     g->variant = best;
     for (int v = 0; v < 4; v++) g->y[v] = w->y[v];
     g->epoch = c_rt.sel_epoch;
     return best;
 }
-
 
 // ---- tiny reductions (at most TINY_BYTES per rank): one barrier, no job ----
 // Each member writes its operand into its inline slot of the parity of the barrier it is about to enter,
@@ -698,11 +715,7 @@ __device__ __noinline__ int fold_collective(int kind, const void* sendbuf, void*
     a.ufn = ufn;
     a.est_piece = 0;
     a.variant = c_rt.variant_override >= 0 ? c_rt.variant_override : route >= 0 ? route : GPUMPI_VARIANT_AUTO;
-    a.learned = false;
-    if (a.variant < 0 && c_rt.selector_mode == 2 && c_rt.mlp_params) {
-        a.variant = learned_variant(kind, bytes, c->size, dt, opc, a.pred);
-        a.learned = true;
-    }
+    a.learned = a.variant < 0 && c_rt.selector_mode == 2 && c_rt.mlp_params;
     int rc = coll_run(c, my, a, __LINE__);
     stage_out(ss, false);
     stage_out(rs, has_out);
@@ -733,11 +746,7 @@ __device__ __noinline__ int pull_collective(int kind, MPI_Comm_impl* c, CollSlot
     a.ufn = nullptr;
     a.est_piece = est_piece;
     a.variant = c_rt.variant_override;
-    a.learned = false;
-    if (a.variant < 0 && kind == JOB_ALLTOALLV && c_rt.selector_mode == 2 && c_rt.mlp_params) {
-        a.variant = learned_variant(kind, est_piece * c->size, c->size, my.stype, -1, a.pred);
-        a.learned = true;
-    }
+    a.learned = a.variant < 0 && kind == JOB_ALLTOALLV && c_rt.selector_mode == 2 && c_rt.mlp_params;
     int rc = coll_run(c, my, a, __LINE__);
     stage_out(ss, false);
     stage_out(rs, true);
@@ -767,6 +776,7 @@ __device__ void gpumpi::selector_rank_begin() {
     s_sel.dt = g.dt;
     s_sel.op = g.op;
     s_sel.blocks = g.blocks;
+    s_sel.aligned = g.aligned;
     s_sel.variant = g.variant;
     for (int v = 0; v < 4; v++) s_sel.y[v] = g.y[v];
     s_sel.valid = 1;

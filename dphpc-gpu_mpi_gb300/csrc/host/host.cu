@@ -426,6 +426,7 @@ int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
     case GPUMPI_TUNE_COPY_CHUNK: w->h_rt.copy_chunk_bytes = value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_ENGINE_MIN_BYTES: w->h_rt.engine_min_bytes = value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_MLP_MARGIN: w->h_rt.mlp_margin = (float)value * 1e-3f; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_MLP_MARGIN_PULL: w->h_rt.mlp_margin_pull = (float)value * 1e-3f; return GPUMPI_SUCCESS;
     default: return GPUMPI_ERR_ARG;
     }
 }
@@ -441,6 +442,7 @@ int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value) {
     case GPUMPI_TUNE_COPY_CHUNK: *value = w->h_rt.copy_chunk_bytes; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_ENGINE_MIN_BYTES: *value = w->h_rt.engine_min_bytes; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_MLP_MARGIN: *value = (long long)(w->h_rt.mlp_margin * 1e3f + 0.5f); return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_MLP_MARGIN_PULL: *value = (long long)(w->h_rt.mlp_margin_pull * 1e3f + 0.5f); return GPUMPI_SUCCESS;
     default: return GPUMPI_ERR_ARG;
     }
 }

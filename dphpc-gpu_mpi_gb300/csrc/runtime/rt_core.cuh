@@ -325,7 +325,7 @@ struct alignas(128) RankState {
 // the weights, the table or a tuning knob changes.
 struct SelCacheRec {
     long long bytes;
-    int kind, n, dt, op, blocks, variant;
+    int kind, n, dt, op, blocks, aligned, variant;
     unsigned epoch;
     float y[4];
 };
@@ -435,7 +435,8 @@ struct Runtime {
     HostIO hio;                       // the device -> host request channel (files, standard streams)
     unsigned sel_epoch;               // records of another epoch are stale
     float mlp_margin;                 // learned choice overrides the tuned table only if it predicts this
-                                      // much lower log-time
+                                      // much lower log-time (Allreduce / Reduce)
+    float mlp_margin_pull;            // the same for Alltoall(v)
 
     TraceRec* trace;
     unsigned long long* trace_count;

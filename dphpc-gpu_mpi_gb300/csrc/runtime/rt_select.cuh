@@ -37,7 +37,8 @@ __device__ int select_variant(int kind, long long bytes_per_rank, int n, int dt,
     if (override_v >= 0 && override_v < GPUMPI_NUM_VARIANTS) {
         if (pred) {
             const int tv = tuned_cell(kind, bytes_per_rank, n, aligned16);
-            if (tv >= 0 && pred[tv] <= pred[override_v] + c_rt.mlp_margin) return tv;
+            const float margin = kind == JOB_ALLTOALLV ? c_rt.mlp_margin_pull : c_rt.mlp_margin;
+            if (tv >= 0 && pred[tv] <= pred[override_v] + margin) return tv;
         }
         return override_v;
     }

@@ -31,7 +31,8 @@ if __package__ in (None, ""):
     sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
 import gpumpi  # noqa: E402
 
-NVAR = 4
+NVAR = 4          # network outputs (one per variant)
+NSEL = 3          # variants the policies choose among: DIRECT, TREE, RING (STAGED never measured fastest)
 KIND_ALLREDUCE, KIND_REDUCE, KIND_ALLTOALLV = 2, 3, 5   # JOB_* codes of the runtime
 DT_SLOT = {gpumpi.FLOAT: 2, gpumpi.DOUBLE: 3, gpumpi.INT: 4, gpumpi.INT64_T: 5}
 OP_SLOT = {gpumpi.OP_SUM: 6, gpumpi.OP_MAX: 7, gpumpi.OP_MIN: 8, gpumpi.OP_PROD: 9}
@@ -39,14 +40,18 @@ DT_SIZE = {gpumpi.FLOAT: 4, gpumpi.DOUBLE: 8, gpumpi.INT: 4, gpumpi.INT64_T: 8}
 NP_DT = {gpumpi.FLOAT: np.float32, gpumpi.DOUBLE: np.float64, gpumpi.INT: np.int32, gpumpi.INT64_T: np.int64}
 
 
-def features(kind: int, bytes_per_rank: float, n: int, dt: int, op: int, rank_share: float) -> np.ndarray:
-    """The 12 features (must match learned_variant in csrc/api/mpi_api.cu)."""
+def features(kind: int, bytes_per_rank: float, n: int, dt: int, op: int, rank_share: float,
+             aligned: int = 16) -> np.ndarray:
+    """The 12 features (must match learned_variant in csrc/api/mpi_api.cu): log2 bytes per rank, log2
+    ranks, datatype one-hot, SUM flag (Alltoall(v) has no operator: op = -1), 16-byte and 8-byte alignment
+    flags of the members' buffers, rank share of the launch's blocks, kind."""
     f = np.zeros(12, np.float32)
     f[0] = (math.log2(max(bytes_per_rank, 1.0)) - 16.0) / 8.0
     f[1] = (math.log2(n) - 8.0) / 3.0
     f[DT_SLOT.get(dt, 5)] = 1.0
-    if op >= 0:                              # Alltoall(v) has no operator: op = -1, slots stay 0
-        f[OP_SLOT.get(op, 9)] = 1.0
+    f[6] = 1.0 if op == gpumpi.OP_SUM else 0.0
+    f[7] = 1.0 if aligned >= 16 else 0.0
+    f[8] = 1.0 if aligned >= 8 else 0.0
     f[10] = rank_share
     f[11] = 1.0 if kind == KIND_REDUCE else -1.0 if kind == KIND_ALLTOALLV else 0.0
     return f
@@ -132,6 +137,7 @@ DTYPES = [gpumpi.FLOAT, gpumpi.INT, gpumpi.DOUBLE]
 BUDGET = 6 << 30                          # device bytes for send + recv buffers
 KINDS = (KIND_ALLREDUCE, KIND_ALLTOALLV)
 MARGIN = 0.05   # default predicted log-time gain the network needs to override the tuned table (5%)
+KIND_NAME = {KIND_ALLREDUCE: "allreduce", KIND_REDUCE: "allreduce", KIND_ALLTOALLV: "alltoallv"}
 TABLE_ROW = {KIND_ALLREDUCE: 0, KIND_REDUCE: 1, KIND_ALLTOALLV: 2}
 DATA = Path(__file__).resolve().parent / "data"
 
@@ -209,10 +215,10 @@ def autotune(iters: int = 30, log=print):
                 for kind in KINDS:
                     ex = Exchange(torch, n, nbytes, seed=n * 100 + nbytes) if kind == KIND_ALLTOALLV else None
                     for dt in _shapes_for(kind):
-                        for v in range(NVAR):
+                        for v in range(NSEL):
                             recs = _measure(w, torch, send, recv, n, nbytes, dt, kind, v, iters, ex)
                             recs = recs[2:] if len(recs) > 4 else recs    # drop the first calls (cold)
-                            records += [(kind, n, l2b, dt, v, u) for l2b, u, _ in recs]
+                            records += [(kind, n, l2b, dt, v, u, al) for l2b, u, al in recs]
                             # table cell: log2 bytes as the kernel sees them, alignment class
                             cell = int(math.floor(recs[0][0])) if recs and recs[0][0] > 0 else 0
                             cls = 0 if recs and recs[0][2] >= 16 else 1
@@ -231,7 +237,7 @@ def autotune(iters: int = 30, log=print):
     sums = {}
     for (kind, n, nbytes, dt, v), (cell, cls, t, _) in grid.items():
         key = (kind, n, cell, cls)
-        sums.setdefault(key, np.zeros(NVAR))[v] += t
+        sums.setdefault(key, np.zeros(NSEL))[v] += t
     table = np.full((3, 2, 32, 16), -1, np.int8)
     for (kind, n, cell, cls), tv in sums.items():
         best = int(np.argmin(tv))
@@ -245,75 +251,102 @@ def autotune(iters: int = 30, log=print):
     return records, table, grid, shares
 
 
-def choose_margin(mlp, table, grid, shares, candidates=(0.05, 0.1, 0.2, 0.3, 0.5, 1.0, 2.0)):
-    """The override margin of the learned policy, chosen on the sweep's own shapes (never on the held-out
-    stream): the one with the least total time of "the table's choice unless the network predicts at least
-    the margin lower log-time" (ties go to the larger margin)."""
+def choose_margin(mlp, table, grid, shares, candidates=(0.0, 0.02, 0.05, 0.1, 0.2, 0.3, 0.5, 1.0, 2.0)):
+    """The override margins of the learned policy, one for Allreduce and one for Alltoall(v), chosen on the
+    sweep's own shapes (never on the held-out stream): per kind, the margin with the least total time of
+    "the table's choice unless the network predicts at least the margin lower log-time" (ties go to the
+    larger margin)."""
     shapes = {}
     for (kind, n, nbytes, dt, v), (cell, cls, t, l2b) in grid.items():
-        s = shapes.setdefault((kind, n, nbytes, dt), {"t": [np.inf] * NVAR, "cell": cell, "cls": cls, "l2b": l2b})
-        s["t"][v] = t
+        sh = shapes.setdefault((kind, n, nbytes, dt), {"t": [np.inf] * NSEL, "cell": cell, "cls": cls, "l2b": l2b})
+        sh["t"][v] = t
     keys = [k for k in shapes if all(np.isfinite(shapes[k]["t"]))]
+    margins = {"allreduce": MARGIN, "alltoallv": MARGIN}
     if not keys:
-        return MARGIN
+        return margins
     X = np.stack([features(k, 2.0 ** shapes[(k, n, b, dt)]["l2b"], n, dt,
-                           gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1, shares[n]) for (k, n, b, dt) in keys])
+                           gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1, shares[n],
+                           16 if shapes[(k, n, b, dt)]["cls"] == 0 else 8) for (k, n, b, dt) in keys])
     pred = mlp.predict(X)
-    best_m, best_t = MARGIN, None
-    for m in candidates:
-        tot = 0.0
-        for i, key in enumerate(keys):
-            s = shapes[key]
-            tv = int(table[TABLE_ROW[key[0]], s["cls"], min(31, s["cell"]), int(math.log2(key[1]))])
-            pure = int(np.argmin(pred[i]))
-            pick = tv if (tv >= 0 and pred[i][tv] <= pred[i][pure] + m) else pure
-            tot += s["t"][pick]
-        if best_t is None or tot <= best_t:
-            best_m, best_t = m, tot
-    return best_m
+    for kname in ("allreduce", "alltoallv"):
+        if not any(KIND_NAME[key[0]] == kname for key in keys):
+            continue  # no complete shape of this kind: the default stays
+        best_m, best_t = MARGIN, None
+        for m in candidates:
+            tot = 0.0
+            for i, key in enumerate(keys):
+                if KIND_NAME[key[0]] != kname:
+                    continue
+                sh = shapes[key]
+                tv = int(table[TABLE_ROW[key[0]], sh["cls"], min(31, sh["cell"]), int(math.log2(key[1]))])
+                tot += sh["t"][policy_pick(pred[i], tv, m)]
+            if best_t is None or tot <= best_t:
+                best_m, best_t = m, tot
+        margins[kname] = best_m
+    return margins
+
+
+def policy_pick(pred_row, tv: int, margin: float) -> int:
+    """The learned policy's choice, as the kernel makes it (select_variant in rt_select.cuh): the network's
+    best selectable variant, unless the tuned table's choice is predicted within `margin`."""
+    pure = int(np.argmin(pred_row[:NSEL]))
+    return tv if (tv >= 0 and pred_row[tv] <= pred_row[pure] + margin) else pure
 
 
 def dataset(records, rank_share_of):
-    X = np.stack([features(k, 2.0 ** l2b, n, dt, gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1, rank_share_of[n])
-                  for k, n, l2b, dt, v, u in records])
+    X = np.stack([features(k, 2.0 ** l2b, n, dt, gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1, rank_share_of[n], al)
+                  for k, n, l2b, dt, v, u, al in records])
     T = np.zeros((len(records), NVAR), np.float32)
     M = np.zeros((len(records), NVAR), np.float32)
-    for i, (k, n, l2b, dt, v, u) in enumerate(records):
+    for i, (k, n, l2b, dt, v, u, al) in enumerate(records):
         T[i, v] = math.log(max(u, 1e-3))
         M[i, v] = 1.0
     return X, T, M
 
 
-def evaluate(mlp_params, table, calls: int = 10000, shapes_per_rank: int = 12, seed: int = 2026, iters: int = 12,
-             log=print, margin: float = None):
+def heldout_ranks(seed: int = 2026, count: int = 24) -> list:
+    """Rank counts of the held-out stream, drawn independently of the sweep's powers of two: log-uniform
+    integers in [16, 2048], every one off the grid (a power of two is redrawn)."""
+    rng = np.random.default_rng(seed + 1)
+    out = set()
+    while len(out) < count:
+        n = int(round(2 ** rng.uniform(4, 11)))
+        if 16 <= n <= 2048 and (n & (n - 1)) != 0:
+            out.add(n)
+    return sorted(out)
+
+
+def evaluate(mlp_params, table, calls: int = 10000, shapes_per_rank: int = 16, seed: int = 2026, iters: int = 12,
+             log=print, margins: dict = None):
     """Held-out stream: `calls` seeded calls, half Allreduce (fp32/int32/fp64 SUM) and half uneven int32
-    Alltoallv, sizes log-uniform 64 B .. 32 MiB per rank, 16 .. 2048 ranks, drawn from off-grid shapes;
-    every variant of every shape is measured, so the exhaustive best is known."""
+    Alltoallv, over shapes drawn independently of the sweep: rank counts off the power-of-two grid
+    (heldout_ranks), sizes log-uniform 64 B .. 32 MiB per rank and not powers of two.  Every selectable
+    variant of every shape is measured, so the exhaustive best is known."""
     import torch
-    margin = MARGIN if margin is None else margin
+    margins = margins or {"allreduce": MARGIN, "alltoallv": MARGIN}
     rng = np.random.default_rng(seed)
     shapes = []
-    for n in RANKS:
+    for n in heldout_ranks(seed):
         for j in range(shapes_per_rank):
             kind = KINDS[j % 2]
+            dt = int(rng.choice(DTYPES)) if kind == KIND_ALLREDUCE else gpumpi.INT
             while True:
                 b = int(2 ** rng.uniform(6, 25))
-                b -= b % 8
+                b -= b % DT_SIZE[dt]
                 if b >= 64 and 2 * n * b <= BUDGET and (b & (b - 1)) != 0:
                     break
-            dt = int(rng.choice(DTYPES)) if kind == KIND_ALLREDUCE else gpumpi.INT
             shapes.append((kind, n, b, dt))
     meas, seen, shares = {}, {}, {}
     mlp = MLP(params=mlp_params)
-    for n in RANKS:
-        sub = [s for s in shapes if s[1] == n]
+    for n in sorted({s_[1] for s_ in shapes}):
+        sub = [s_ for s_ in shapes if s_[1] == n]
         max_bytes = max(b for _, _, b, _ in sub)
         w = gpumpi.World(n, timeout_s=60.0, trace_capacity=4096)
         send, recv = _buffers(torch, n, max_bytes)
         for k, (kind, _, b, dt) in enumerate(sub):
             ex = Exchange(torch, n, b, seed=seed + 7 * k + n) if kind == KIND_ALLTOALLV else None
             times = []
-            for v in range(NVAR):
+            for v in range(NSEL):
                 recs = _measure(w, torch, send, recv, n, b, dt, kind, v, iters, ex)
                 recs = recs[2:] if len(recs) > 4 else recs
                 times.append(float(np.median([u for _, u, _ in recs])))
@@ -324,24 +357,38 @@ def evaluate(mlp_params, table, calls: int = 10000, shapes_per_rank: int = 12, s
         del send, recv
         torch.cuda.empty_cache()
     keys = list(meas)
-    # the learned and tuned choices use what the kernel computes per call (bytes estimate, rank share)
+    # the learned and tuned choices use what the kernel computes per call (bytes estimate, rank share,
+    # alignment of the members' buffers)
     X = np.stack([features(k, 2.0 ** seen[(k, n, b, dt)][0], n, dt, gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1,
-                           shares[n]) for (k, n, b, dt) in keys])
+                           shares[n], seen[(k, n, b, dt)][1]) for (k, n, b, dt) in keys])
     pred = mlp.predict(X)
     pick = {}
     for i, key in enumerate(keys):
         kind, n, b, dt = key
         l2b, al = seen[key]
         tv = int(table[TABLE_ROW[kind], 0 if al >= 16 else 1, min(31, max(0, int(math.floor(l2b)))), int(math.log2(n))])
-        pure = int(np.argmin(pred[i]))
-        learned = tv if (tv >= 0 and pred[i][tv] <= pred[i][pure] + margin) else pure  # same rule as the kernel
-        pick[key] = {"learned": learned, "learned_pure": pure, "tuned": tv if tv >= 0 else 0, "plain": 0}
-    idx = rng.integers(0, len(keys), calls)
-    pols = ("learned", "learned_pure", "tuned", "plain")
-    rep = {"calls": calls, "shapes": len(keys)}
+        pick[key] = {"learned": policy_pick(pred[i], tv, margins[KIND_NAME[kind]]),
+                     "learned_pure": int(np.argmin(pred[i][:NSEL])), "tuned": tv if tv >= 0 else 0, "plain": 0}
+    rep = summarize(keys, meas, pick, rng.integers(0, len(keys), calls))
+    rep["calls"] = calls
+    rep["shapes"] = len(keys)
+    rep["ranks"] = sorted({k[1] for k in keys})
+    rep["choices"] = {f"{k[0]}:{k[1]}x{k[2]}:{k[3]}": pick[k] for k in keys}
+    rep["measured_us"] = {f"{k[0]}:{k[1]}x{k[2]}:{k[3]}": meas[k] for k in keys}
+    rep["kernel_seen"] = {f"{k[0]}:{k[1]}x{k[2]}:{k[3]}": list(seen[k]) + [shares[k[1]]] for k in keys}
+    log(json.dumps({k: rep[k] for k in ("all", "allreduce", "alltoallv")}))
+    return rep
+
+
+POLICIES = ("learned", "learned_pure", "tuned", "plain")
+
+
+def summarize(keys, meas, pick, idx):
+    """Total and per-call regret of each policy over the calls `idx` (indices into keys)."""
+    rep = {}
     for label, kinds in (("all", KINDS), ("allreduce", (KIND_ALLREDUCE,)), ("alltoallv", (KIND_ALLTOALLV,))):
-        tot = {p: 0.0 for p in ("best",) + pols}
-        regrets = {p: [] for p in pols}
+        tot = {p_: 0.0 for p_ in ("best",) + POLICIES}
+        regrets = {p_: [] for p_ in POLICIES}
         for i in idx:
             key = keys[i]
             if key[0] not in kinds:
@@ -349,19 +396,16 @@ def evaluate(mlp_params, table, calls: int = 10000, shapes_per_rank: int = 12, s
             t = meas[key]
             best = min(t)
             tot["best"] += best
-            for pol in pols:
+            for pol in POLICIES:
                 tp = t[pick[key][pol]]
                 tot[pol] += tp
                 regrets[pol].append(tp / best - 1.0)
         rep[label] = {"calls": len(regrets["plain"]),
                       "total_time_ms": {k: v / 1e3 for k, v in tot.items()},
-                      "time_over_best": {p: tot[p] / tot["best"] - 1.0 for p in pols},
-                      "mean_regret": {p: float(np.mean(regrets[p])) for p in pols},
-                      "p90_regret": {p: float(np.percentile(regrets[p], 90)) for p in pols},
+                      "time_over_best": {p_: tot[p_] / tot["best"] - 1.0 for p_ in POLICIES},
+                      "mean_regret": {p_: float(np.mean(regrets[p_])) for p_ in POLICIES},
+                      "p90_regret": {p_: float(np.percentile(regrets[p_], 90)) for p_ in POLICIES},
                       "learned_vs_tuned_time": tot["learned"] / tot["tuned"]}
-    rep["choices"] = {f"{k[0]}:{k[1]}x{k[2]}:{k[3]}": pick[k] for k in keys}
-    rep["measured_us"] = {f"{k[0]}:{k[1]}x{k[2]}:{k[3]}": meas[k] for k in keys}
-    log(json.dumps({k: rep[k] for k in ("all", "allreduce", "alltoallv")}))
     return rep
 
 
@@ -385,16 +429,16 @@ def run(out: Path, iters: int = 30):
     mv = torch.from_numpy(M[va]).cuda()
     vloss, _ = mlp.loss_grad(xv, tv, mv)
     params = mlp.params()
-    margin = choose_margin(mlp, table, grid, shares)
-    print(f"override margin chosen on the sweep shapes: {margin}", flush=True)
+    margins = choose_margin(mlp, table, grid, shares)
+    print(f"override margins chosen on the sweep shapes: {margins}", flush=True)
     np.save(out / "tuned_table.npy", table)
     np.save(out / "mlp_params.npy", params)
-    rep = evaluate(params, table, margin=margin)
+    rep = evaluate(params, table, margins=margins)
     rep.update({"train_records": int(len(tr)), "val_records": int(len(va)), "train_loss": hist,
                 "val_loss": float(vloss.item()), "sweep_seconds": time.time() - t0,
                 "records_by_kind": {str(k): int(sum(1 for r in records if r[0] == k)) for k in KINDS},
                 "grid_median_us": {f"{k[0]}:{k[1]}:{k[2]}:{k[3]}:{k[4]}": g[2] for k, g in grid.items()}})
-    rep["margin"] = margin
+    rep["margins"] = margins
     (out / "selector_report.json").write_text(json.dumps(rep, indent=1))
     print(json.dumps({k: rep[k] for k in ("all", "allreduce", "alltoallv", "val_loss", "train_records")}))
 
@@ -407,12 +451,16 @@ def load_packaged():
     return np.load(t), np.load(p)
 
 
-def packaged_margin() -> float:
-    """The override margin the packaged network was evaluated with (chosen on its sweep), else MARGIN."""
+def packaged_margins() -> dict:
+    """The override margins (per kind) the packaged network was evaluated with (chosen on its sweep)."""
     rep = DATA / "selector_report.json"
     if rep.exists():
-        return float(json.loads(rep.read_text()).get("margin", MARGIN))
-    return MARGIN
+        r = json.loads(rep.read_text())
+        if "margins" in r:
+            return {k: float(v) for k, v in r["margins"].items()}
+        m = float(r.get("margin", MARGIN))
+        return {"allreduce": m, "alltoallv": m}
+    return {"allreduce": MARGIN, "alltoallv": MARGIN}
 
 
 def apply_policy(world, policy: str):
@@ -433,7 +481,9 @@ def apply_policy(world, policy: str):
     elif policy == "learned":
         world.set_tuned_table(table)
         world.set_mlp(params)
-        world.set_tuning(gpumpi.TUNE_MLP_MARGIN, int(round(packaged_margin() * 1000)))
+        m = packaged_margins()
+        world.set_tuning(gpumpi.TUNE_MLP_MARGIN, int(round(m["allreduce"] * 1000)))
+        world.set_tuning(gpumpi.TUNE_MLP_MARGIN_PULL, int(round(m["alltoallv"] * 1000)))
         world.set_policy(-1, 2)
     else:
         raise ValueError(policy)

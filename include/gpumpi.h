@@ -158,8 +158,10 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
 #define GPUMPI_TUNE_ENGINES 3
 #define GPUMPI_TUNE_COPY_CHUNK 4
 #define GPUMPI_TUNE_ENGINE_MIN_BYTES 5
-/* Learned policy: predicted log-time gain (in 1/1000) the network needs to override the tuned table. */
+/* Learned policy: predicted log-time gain (in 1/1000) the network needs to override the tuned table,
+ * for Allreduce / Reduce (MARGIN) and for Alltoall(v) (MARGIN_PULL). */
 #define GPUMPI_TUNE_MLP_MARGIN 6
+#define GPUMPI_TUNE_MLP_MARGIN_PULL 9
 /* Dynamic shared memory per rank block at most, in bytes (default 8192; -1 = all the SM leaves over).
  * It holds the TMA stages of the STAGED variants and block-parallel user scratch; what it does not take
  * stays L1 cache, which the executors' spilled registers and the ranks' private state use. */

@@ -28,25 +28,36 @@ def grid_entry(grid, n, nbytes, times):
 def test_margin_keeps_table_where_network_is_unsure_and_overrides_where_sure():
     n = 64
     grid = {}
-    grid_entry(grid, n, 1 << 10, [1.0, 2.0, 2.0, 2.0])   # the table is right (variant 0)
-    grid_entry(grid, n, 1 << 12, [3.0, 1.0, 3.0, 3.0])   # the table is wrong; variant 1 is 3x faster
+    grid_entry(grid, n, 1 << 10, [1.0, 2.0, 2.0])   # the table is right (variant 0)
+    grid_entry(grid, n, 1 << 12, [3.0, 1.0, 3.0])   # the table is wrong; variant 1 is 3x faster
     table = np.full((3, 2, 32, 16), -1, np.int8)
     table[0, :, 10, 6] = 0
     table[0, :, 12, 6] = 0
     # shape 1 KiB: the network prefers variant 1 by 0.08 (wrongly); shape 4 KiB: by 0.8 (rightly)
     net = TableNet({10: [0.50, 0.42, 1.0, 1.0], 12: [1.0, 0.2, 1.0, 1.0]})
     # margins 0.1 .. 0.5 keep the table at 1 KiB and override at 4 KiB (total 2.0); 0.05 overrides both
-    # (3.0); 1.0 and 2.0 override neither (4.0); ties go to the larger margin
-    assert sel.choose_margin(net, table, grid, {n: 0.8}) == 0.5
-    assert sel.choose_margin(net, table, grid, {n: 0.8}, candidates=(0.05, 1.0)) == 0.05
-    assert sel.choose_margin(net, table, grid, {n: 0.8}, candidates=(1.0, 2.0)) == 2.0
+    # (3.0); 1.0 and 2.0 override neither (4.0); ties go to the larger margin.  Margins are per kind: the
+    # Alltoall(v) margin has no shapes here and keeps the default.
+    m = sel.choose_margin(net, table, grid, {n: 0.8})
+    assert m == {"allreduce": 0.5, "alltoallv": sel.MARGIN}
+    assert sel.choose_margin(net, table, grid, {n: 0.8}, candidates=(0.05, 1.0))["allreduce"] == 0.05
+    assert sel.choose_margin(net, table, grid, {n: 0.8}, candidates=(1.0, 2.0))["allreduce"] == 2.0
+
+
+def test_policy_pick_never_chooses_staged():
+    # the network's output for STAGED (variant 3) is not a choice, however low it is
+    pred = np.array([1.0, 0.9, 0.8, -5.0], np.float32)
+    assert sel.policy_pick(pred, 0, 0.05) == 2
+    assert sel.policy_pick(pred, 0, 0.3) == 0      # within the margin: the table's choice stands
+    assert sel.policy_pick(pred, -1, 0.3) == 2     # no table cell: the network's choice
 
 
 def test_margin_defaults_without_complete_shapes():
     grid = {}
     grid[(sel.KIND_ALLREDUCE, 64, 1024, gpumpi.FLOAT, 0)] = (10, 0, 1.0, 10.0)   # one variant only
     table = np.zeros((3, 2, 32, 16), np.int8)
-    assert sel.choose_margin(TableNet({}), table, grid, {64: 0.8}) == sel.MARGIN
+    assert sel.choose_margin(TableNet({}), table, grid, {64: 0.8}) == {"allreduce": sel.MARGIN,
+                                                                        "alltoallv": sel.MARGIN}
 
 
 def test_packaged_artifacts_and_recorded_figures():
@@ -54,7 +65,7 @@ def test_packaged_artifacts_and_recorded_figures():
     if table is None:
         pytest.skip("no packaged selector")
     assert table.shape == (3, 2, 32, 16) and table.dtype == np.int8
-    assert set(np.unique(table)) <= {-1, 0, 1, 2, 3}
+    assert set(np.unique(table)) <= {-1, 0, 1, 2}        # STAGED is not a choice
     assert np.array_equal(table[0], table[1])          # Reduce follows the Allreduce sweep
     assert params.shape == (gpumpi.MLP_NPARAMS,) and params.dtype == np.float32
     assert np.isfinite(params).all()
@@ -65,7 +76,9 @@ def test_packaged_artifacts_and_recorded_figures():
     assert allr["time_over_best"]["learned"] <= 0.05
     assert allr["learned_vs_tuned_time"] <= 1.0
     assert allr["time_over_best"]["learned"] <= allr["time_over_best"]["plain"]
-    assert rep["margin"] == sel.packaged_margin() > 0
+    assert rep["margins"] == sel.packaged_margins()
+    assert min(rep["ranks"]) >= 16 and all(n & (n - 1) for n in rep["ranks"])   # off-grid rank counts
+    assert rep["shapes"] >= 300
 
 
 class FakeWorld:
@@ -97,7 +110,9 @@ def test_apply_policy_calls():
     w = FakeWorld()
     sel.apply_policy(w, "learned")
     assert w.calls == [("table", (3, 2, 32, 16)), ("mlp", (gpumpi.MLP_NPARAMS,)),
-                       ("tuning", gpumpi.TUNE_MLP_MARGIN, int(round(sel.packaged_margin() * 1000))),
+                       ("tuning", gpumpi.TUNE_MLP_MARGIN, int(round(sel.packaged_margins()["allreduce"] * 1000))),
+                       ("tuning", gpumpi.TUNE_MLP_MARGIN_PULL,
+                        int(round(sel.packaged_margins()["alltoallv"] * 1000))),
                        ("policy", -1, 2)]
     with pytest.raises(ValueError):
         sel.apply_policy(FakeWorld(), "nonsense")
