@@ -186,19 +186,21 @@ def _shapes_for(kind):
 
 
 def _sizes_for(lb):
-    """The power of two 2^lb and an off-grid size in the same octave that is 8 mod 16 bytes, so rank
-    buffers laid end to end lose 16-byte alignment (vector width and variant ranking change with it)."""
+    """The power of two 2^lb and two off-grid sizes in the same octave, 8 and 4 mod 16 bytes, so rank buffers
+    laid end to end lose 16-byte (and 8-byte) alignment: vector width and variant ranking change with it."""
     b = 1 << lb
-    off = int(round(b * 1.41 / 8)) * 8
-    if off % 16 == 0:
-        off += 8
-    return [b, off] if off < 2 * b else [b]
+    out = [b]
+    for f, rem in ((1.41, 8), (1.19, 4)):
+        off = int(round(b * f / 16)) * 16 + rem
+        if b < off < 2 * b:
+            out.append(off)
+    return out
 
 
 def autotune(iters: int = 30, log=print):
     """Sweep of Allreduce (SUM; fp32, int32, fp64) and uneven int32 Alltoallv over ranks x bytes per rank
     x variant.  Returns (records, table, median grid, rank share per n); a record is
-    (kind, n, log2 bytes seen by the kernel, dt, variant, us)."""
+    (kind, n, log2 bytes seen by the kernel, dt, variant, us, buffer alignment, bytes per rank asked)."""
     import torch
     records = []
     grid = {}
@@ -218,7 +220,7 @@ def autotune(iters: int = 30, log=print):
                         for v in range(NSEL):
                             recs = _measure(w, torch, send, recv, n, nbytes, dt, kind, v, iters, ex)
                             recs = recs[2:] if len(recs) > 4 else recs    # drop the first calls (cold)
-                            records += [(kind, n, l2b, dt, v, u, al) for l2b, u, al in recs]
+                            records += [(kind, n, l2b, dt, v, u, al, nbytes) for l2b, u, al in recs]
                             # table cell: log2 bytes as the kernel sees them, alignment class
                             cell = int(math.floor(recs[0][0])) if recs and recs[0][0] > 0 else 0
                             cls = 0 if recs and recs[0][2] >= 16 else 1
@@ -230,10 +232,14 @@ def autotune(iters: int = 30, log=print):
         w.close()
         del send, recv
         torch.cuda.empty_cache()
-    # table: per (kind, alignment class, cell of log2 bytes, log2 ranks) the variant with the least summed
-    # median time over every shape measured in the cell (every datatype); class 0 = 16-byte aligned buffers
-    # (the power-of-two sizes), 1 = not (the off-grid sizes, 8 mod 16 bytes); a class the sweep did not
-    # reach in a cell takes the other class's choice
+    return records, build_table(grid), grid, shares
+
+
+def build_table(grid):
+    """The tuned table: per (kind, alignment class, cell of log2 bytes, log2 ranks) the variant with the
+    least summed median time over every shape of `grid` in the cell (every datatype); class 0 = 16-byte
+    aligned buffers (the power-of-two sizes), 1 = not (the off-grid sizes, 8 or 4 mod 16 bytes); a class
+    the sweep did not reach in a cell takes the other class's choice."""
     sums = {}
     for (kind, n, nbytes, dt, v), (cell, cls, t, _) in grid.items():
         key = (kind, n, cell, cls)
@@ -248,42 +254,52 @@ def autotune(iters: int = 30, log=print):
         other = table[:, 1 - cls]
         mine = table[:, cls]
         mine[mine < 0] = other[mine < 0]
-    return records, table, grid, shares
+    return table
 
 
-def choose_margin(mlp, table, grid, shares, candidates=(0.0, 0.02, 0.05, 0.1, 0.2, 0.3, 0.5, 1.0, 2.0)):
-    """The override margins of the learned policy, one for Allreduce and one for Alltoall(v), chosen on the
-    sweep's own shapes (never on the held-out stream): per kind, the margin with the least total time of
-    "the table's choice unless the network predicts at least the margin lower log-time" (ties go to the
-    larger margin)."""
+MARGIN_CANDIDATES = (0.0, 0.02, 0.05, 0.1, 0.2, 0.3, 0.5, 1.0, 2.0)
+
+
+def margin_totals(mlp, table, grid, shares, candidates=MARGIN_CANDIDATES, rank_col=None):
+    """Per kind and candidate margin, the total median time over the complete shapes of `grid` of the learned
+    policy: "the table's choice unless the network predicts at least the margin lower log-time".  The table
+    column of a rank count is rank_col(n) (default: its log2, as the kernel indexes it)."""
+    rank_col = rank_col or (lambda n: int(math.log2(n)))
     shapes = {}
     for (kind, n, nbytes, dt, v), (cell, cls, t, l2b) in grid.items():
         sh = shapes.setdefault((kind, n, nbytes, dt), {"t": [np.inf] * NSEL, "cell": cell, "cls": cls, "l2b": l2b})
         sh["t"][v] = t
     keys = [k for k in shapes if all(np.isfinite(shapes[k]["t"]))]
-    margins = {"allreduce": MARGIN, "alltoallv": MARGIN}
+    tot = {"allreduce": {}, "alltoallv": {}}
     if not keys:
-        return margins
+        return tot
     X = np.stack([features(k, 2.0 ** shapes[(k, n, b, dt)]["l2b"], n, dt,
                            gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1, shares[n],
                            16 if shapes[(k, n, b, dt)]["cls"] == 0 else 8) for (k, n, b, dt) in keys])
     pred = mlp.predict(X)
+    for m in candidates:
+        for i, key in enumerate(keys):
+            sh = shapes[key]
+            tv = int(table[TABLE_ROW[key[0]], sh["cls"], min(31, sh["cell"]), rank_col(key[1])])
+            kn = KIND_NAME[key[0]]
+            tot[kn][m] = tot[kn].get(m, 0.0) + sh["t"][policy_pick(pred[i], tv, m)]
+    return tot
+
+
+def pick_margins(totals):
+    """Per kind, the candidate with the least total (ties go to the larger margin); the default without data."""
+    out = {}
     for kname in ("allreduce", "alltoallv"):
-        if not any(KIND_NAME[key[0]] == kname for key in keys):
-            continue  # no complete shape of this kind: the default stays
-        best_m, best_t = MARGIN, None
-        for m in candidates:
-            tot = 0.0
-            for i, key in enumerate(keys):
-                if KIND_NAME[key[0]] != kname:
-                    continue
-                sh = shapes[key]
-                tv = int(table[TABLE_ROW[key[0]], sh["cls"], min(31, sh["cell"]), int(math.log2(key[1]))])
-                tot += sh["t"][policy_pick(pred[i], tv, m)]
-            if best_t is None or tot <= best_t:
-                best_m, best_t = m, tot
-        margins[kname] = best_m
-    return margins
+        t = totals.get(kname, {})
+        out[kname] = min(t, key=lambda m: (t[m], -m)) if t else MARGIN
+    return out
+
+
+def choose_margin(mlp, table, grid, shares, candidates=MARGIN_CANDIDATES):
+    """The override margins of the learned policy, one for Allreduce and one for Alltoall(v): per kind, the
+    margin with the least total time over the shapes of `grid` (margin_totals; ties go to the larger
+    margin)."""
+    return pick_margins(margin_totals(mlp, table, grid, shares, candidates))
 
 
 def policy_pick(pred_row, tv: int, margin: float) -> int:
@@ -294,12 +310,20 @@ def policy_pick(pred_row, tv: int, margin: float) -> int:
 
 
 def dataset(records, rank_share_of):
+    """Features and targets of the timing records.  The target of a record is its log-time relative to its
+    shape: minus the mean over the shape's variants of their median log-times.  Only the differences
+    between variants decide the choice, and without the shape's own scale (microseconds to milliseconds)
+    the network spends its capacity on them."""
     X = np.stack([features(k, 2.0 ** l2b, n, dt, gpumpi.OP_SUM if k == KIND_ALLREDUCE else -1, rank_share_of[n], al)
-                  for k, n, l2b, dt, v, u, al in records])
+                  for k, n, l2b, dt, v, u, al, _ in records])
+    per = {}
+    for k, n, l2b, dt, v, u, al, _ in records:
+        per.setdefault((k, n, round(l2b, 4), dt, al), {}).setdefault(v, []).append(math.log(max(u, 1e-3)))
+    base = {key: float(np.mean([np.median(x) for x in d.values()])) for key, d in per.items()}
     T = np.zeros((len(records), NVAR), np.float32)
     M = np.zeros((len(records), NVAR), np.float32)
-    for i, (k, n, l2b, dt, v, u, al) in enumerate(records):
-        T[i, v] = math.log(max(u, 1e-3))
+    for i, (k, n, l2b, dt, v, u, al, _) in enumerate(records):
+        T[i, v] = math.log(max(u, 1e-3)) - base[(k, n, round(l2b, 4), dt, al)]
         M[i, v] = 1.0
     return X, T, M
 
@@ -409,6 +433,28 @@ def summarize(keys, meas, pick, idx):
     return rep
 
 
+def split_margins(records, grid, shares, epochs: int = 60):
+    """Override margins chosen without the held-out stream and without judging either side on shapes it
+    was fitted to: two folds over the sweep's rank counts (even and odd powers of two); in each, a table and
+    a network are fitted to one half and the other half is served as an off-grid rank count is at run time,
+    from the table column of the next lower fitted rank count."""
+    totals = {"allreduce": {}, "alltoallv": {}}
+    for fit in (RANKS[0::2], RANKS[1::2]):
+        score = [n for n in RANKS if n not in fit and any(f < n for f in fit)]
+        rec_f = [r for r in records if r[1] in fit]
+        X, T, M = dataset(rec_f, shares)
+        net = MLP(seed=1)
+        net.train(X, T, M, epochs=epochs)
+        table = build_table({k: g for k, g in grid.items() if k[1] in fit})
+        lower = {n: int(math.log2(max(f for f in fit if f < n))) for n in score}
+        t = margin_totals(net, table, {k: g for k, g in grid.items() if k[1] in score}, shares,
+                          rank_col=lambda n: lower[n])
+        for kname, d in t.items():
+            for m, v in d.items():
+                totals[kname][m] = totals[kname].get(m, 0.0) + v
+    return pick_margins(totals)
+
+
 def run(out: Path, iters: int = 30):
     import torch
     out.mkdir(parents=True, exist_ok=True)
@@ -423,14 +469,14 @@ def run(out: Path, iters: int = 30):
     cut = int(0.8 * len(X))
     tr, va = perm[:cut], perm[cut:]
     mlp = MLP(seed=0)
-    hist = mlp.train(X[tr], T[tr], M[tr], epochs=60)
+    hist = mlp.train(X[tr], T[tr], M[tr], epochs=100)
     xv = torch.from_numpy(X[va]).cuda()
     tv = torch.from_numpy(T[va]).cuda()
     mv = torch.from_numpy(M[va]).cuda()
     vloss, _ = mlp.loss_grad(xv, tv, mv)
     params = mlp.params()
-    margins = choose_margin(mlp, table, grid, shares)
-    print(f"override margins chosen on the sweep shapes: {margins}", flush=True)
+    margins = split_margins(records, grid, shares)
+    print(f"override margins chosen by the rank-count split of the sweep: {margins}", flush=True)
     np.save(out / "tuned_table.npy", table)
     np.save(out / "mlp_params.npy", params)
     rep = evaluate(params, table, margins=margins)
