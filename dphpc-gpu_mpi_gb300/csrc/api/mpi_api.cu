@@ -203,7 +203,8 @@ struct CollArgs {
     bool learned = false;  // the learned policy chooses (the setup evaluates the network)
 };
 
-__device__ int learned_variant(int kind, long long bytes, int n, int dt, int op, int aligned16, float* pred);
+__device__ int learned_variant(MPI_Comm_impl* c, int kind, long long bytes, int n, int dt, int op, int aligned16,
+                               float* pred);
 
 // Elements per thread for a fold chunk (chunk = T * v elements).  Candidates: one 16-byte vector,
 // 8 bytes (4-byte types), one element.  Score = blocks busy per wave x bytes in flight per thread
@@ -313,7 +314,7 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         j->count = a.count;
         bytes = a.count * a.esize * (long long)n;
         float pred[4];
-        const int ov = a.learned ? learned_variant(a.kind, a.count * a.esize, n, a.dt, a.op, j->aligned16, pred)
+        const int ov = a.learned ? learned_variant(c, a.kind, a.count * a.esize, n, a.dt, a.op, j->aligned16, pred)
                                  : a.variant;
         int variant = select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, ov, j->aligned16,
                                      a.learned ? pred : nullptr);
@@ -374,7 +375,7 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         // piece order (DIRECT / TREE / RING, see piece_of) or bulk-copy staging (STAGED)
         float pred[4];
         const int ov = a.learned && a.kind == JOB_ALLTOALLV
-                           ? learned_variant(a.kind, a.est_piece * n, n, a.dt, -1, j->aligned16, pred)
+                           ? learned_variant(c, a.kind, a.est_piece * n, n, a.dt, -1, j->aligned16, pred)
                            : a.variant;
         int variant = a.kind == JOB_ALLTOALLV
                           ? select_variant(a.kind, a.est_piece * n, n, a.dt, -1, ov, j->aligned16,
@@ -490,16 +491,39 @@ __shared__ SelCache s_sel;
 // STAGED 2,385-2,780); it stays available as an explicit variant.
 constexpr int SEL_CHOICES = 3;
 
+__device__ __forceinline__ bool sel_hit(const SelCacheRec& r, int kind, long long bytes, int n, int dt, int op,
+                                        int blocks, int al) {
+    return r.epoch == c_rt.sel_epoch && r.bytes == bytes && r.kind == kind && r.n == n && r.dt == dt &&
+           r.op == op && r.blocks == blocks && r.aligned == al;
+}
+
 // Variant with the smallest predicted time, and the predicted log-times in pred[4] (the setup weighs the
-// tuned table's choice against them); every member computes the same features, so the choice does not
-// depend on which member sets up.  Cached per rank for repeated calls of one shape.
-__device__ __noinline__ int learned_variant(int kind, long long bytes, int n, int dt, int op, int aligned16, float* pred) {
+// tuned table's choice against them).  Evaluated by the member that sets the collective up; the choice is
+// kept on the communicator (every later setup of the same shape reuses it, whoever arrives last) and in
+// the deciding rank's own cache, which outlives the launch.
+__device__ __noinline__ int learned_variant(MPI_Comm_impl* c, int kind, long long bytes, int n, int dt, int op,
+                                            int aligned16, float* pred) {
     SelCache* sc = &s_sel;
     const int blocks = c_rt.nranks + c_rt.nengines;  // the network's occupancy input depends on it
     const int al = aligned16 >= 16 ? 16 : aligned16 >= 8 ? 8 : 0;
+    if (sel_hit(c->sel, kind, bytes, n, dt, op, blocks, al)) {
+        for (int v = 0; v < 4; v++) pred[v] = c->sel.y[v];
+        return c->sel.variant;
+    }
     if (sc->valid && sc->bytes == bytes && sc->kind == kind && sc->n == n && sc->dt == dt && sc->op == op &&
         sc->blocks == blocks && sc->aligned == al) {
         for (int v = 0; v < 4; v++) pred[v] = sc->y[v];
+        SelCacheRec* cr = &c->sel;
+        cr->bytes = bytes;
+        cr->kind = kind;
+        cr->n = n;
+        cr->dt = dt;
+        cr->op = op;
+        cr->blocks = blocks;
+        cr->aligned = al;
+        cr->variant = sc->variant;
+        for (int v = 0; v < 4; v++) cr->y[v] = sc->y[v];
+        cr->epoch = c_rt.sel_epoch;
         return sc->variant;
     }
     MlpWork* w = &s_mlp;
@@ -544,6 +568,7 @@ __device__ __noinline__ int learned_variant(int kind, long long bytes, int n, in
     g->variant = best;
     for (int v = 0; v < 4; v++) g->y[v] = w->y[v];
     g->epoch = c_rt.sel_epoch;
+    c->sel = *g;
     return best;
 }
 

@@ -200,6 +200,19 @@ struct CollSlot {            // what each member publishes when it enters a coll
 
 }  // namespace gpumpi
 
+namespace gpumpi {
+// A rank's last learned variant choice, kept across launches (data region, never zeroed by a launch):
+// valid while `epoch` equals the runtime's selector epoch, which the host advances whenever the policy,
+// the weights, the table or a tuning knob changes.
+struct SelCacheRec {
+    long long bytes;
+    int kind, n, dt, op, blocks, aligned, variant;
+    unsigned epoch;
+    float y[4];
+};
+
+}  // namespace gpumpi
+
 struct alignas(128) MPI_Comm_impl {
     unsigned bar_count;
     char pad0[124];
@@ -222,6 +235,9 @@ struct alignas(128) MPI_Comm_impl {
     int topo_ndims;
     int topo_dims[8];
     int topo_periods[8];
+    // the learned selector's last choice on this communicator, made by whichever member set the
+    // collective up (setups of one communicator are ordered by its barriers)
+    gpumpi::SelCacheRec sel;
 };
 namespace gpumpi {
 constexpr int COMM_MAGIC = 0x434f4d4d;
@@ -318,16 +334,6 @@ struct alignas(128) RankState {
     unsigned long long coll_calls;
     void* attrs;                    // keyvals and cached attributes (device heap, made on first use)
     Job p2p_job;
-};
-
-// A rank's last learned variant choice, kept across launches (data region, never zeroed by a launch):
-// valid while `epoch` equals the runtime's selector epoch, which the host advances whenever the policy,
-// the weights, the table or a tuning knob changes.
-struct SelCacheRec {
-    long long bytes;
-    int kind, n, dt, op, blocks, aligned, variant;
-    unsigned epoch;
-    float y[4];
 };
 
 struct Task {                       // block task record, one per block (global memory)
