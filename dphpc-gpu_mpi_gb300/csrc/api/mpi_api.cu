@@ -206,6 +206,28 @@ struct CollArgs {
 __device__ int learned_variant(MPI_Comm_impl* c, int kind, long long bytes, int n, int dt, int op, int aligned16,
                                float* pred);
 
+// Bytes per piece of an Alltoallv, estimated the same way whichever member sets the collective up: the
+// mean of 64 counts, 8 entries of the count arrays of 8 members spread over the communicator (a member's
+// own estimate differs from another's, and the variant choice and the chunking would then depend on
+// which member arrived last).  -1 when a sampled member published no count array.
+__device__ __noinline__ long long shared_piece_estimate(const MPI_Comm_impl* c) {
+    const int n = c->size;
+    const CollSlot* sl = c->slots;
+    long long sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int m = (int)(((long long)(2 * q + 1) * n) / 16);
+        const int* cnt = (const int*)__ldcg((const unsigned long long*)&sl[m].scounts);
+        const TypeDesc* d = (const TypeDesc*)__ldcg((const unsigned long long*)&sl[m].sdesc);
+        if (!cnt || !d) return -1;
+        long long part = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) part += __ldcg(cnt + ((long long)(2 * i + 1) * n) / 16);
+        sum += part * d->size;
+    }
+    return sum / 64;
+}
+
 // Elements per thread for a fold chunk (chunk = T * v elements).  Candidates: one 16-byte vector,
 // 8 bytes (4-byte types), one element.  Score = blocks busy per wave x bytes in flight per thread
 // (the rank-unrolled loads of fold_fast keep ~128 bytes in flight, at most 16 loads): the canonical
@@ -312,6 +334,7 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
     bool may_post = c_rt.nengines > 0;
     if (a.kind == JOB_ALLREDUCE || a.kind == JOB_REDUCE) {
         j->count = a.count;
+        j->sel_bytes = a.count * a.esize;
         bytes = a.count * a.esize * (long long)n;
         float pred[4];
         const int ov = a.learned ? learned_variant(c, a.kind, a.count * a.esize, n, a.dt, a.op, j->aligned16, pred)
@@ -373,12 +396,17 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         long long P = matrix ? (long long)n * n : (long long)n;
         j->count = P;
         // piece order (DIRECT / TREE / RING, see piece_of) or bulk-copy staging (STAGED)
+        long long a_est = a.est_piece;
+        if (a.kind == JOB_ALLTOALLV && n >= 16) {
+            const long long est = shared_piece_estimate(c);
+            if (est >= 0) a_est = est;
+        }
         float pred[4];
         const int ov = a.learned && a.kind == JOB_ALLTOALLV
-                           ? learned_variant(c, a.kind, a.est_piece * n, n, a.dt, -1, j->aligned16, pred)
+                           ? learned_variant(c, a.kind, a_est * n, n, a.dt, -1, j->aligned16, pred)
                            : a.variant;
         int variant = a.kind == JOB_ALLTOALLV
-                          ? select_variant(a.kind, a.est_piece * n, n, a.dt, -1, ov, j->aligned16,
+                          ? select_variant(a.kind, a_est * n, n, a.dt, -1, ov, j->aligned16,
                                            a.learned ? pred : nullptr)
                           : (matrix && a.variant >= 0 && a.variant < GPUMPI_NUM_VARIANTS ? a.variant
                                                                                           : GPUMPI_VARIANT_DIRECT);
@@ -386,11 +414,12 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         if (variant == GPUMPI_VARIANT_STAGED && (!matrix || staged_pull_stage_bytes(T) < 512))
             variant = GPUMPI_VARIANT_DIRECT;
         j->variant = variant;
-        bytes = a.est_piece * P;
+        j->sel_bytes = a_est * n;
+        bytes = a_est * P;
         may_post = may_post && bytes >= c_rt.engine_min_bytes;
         long long target = n + (may_post ? c_rt.nengines : 0);
-        if (a.est_piece >= 65536) {
-            int parts = (int)((a.est_piece + 65535) / 65536);
+        if (a_est >= 65536) {
+            int parts = (int)((a_est + 65535) / 65536);
             j->vec = parts;
             j->tile = 1;
             nchunks = (int)(P * parts);
@@ -422,9 +451,7 @@ __device__ __noinline__ int coll_run(MPI_Comm_impl* c, const CollSlot& mine, con
     if (a.kind == JOB_BARRIER) return 0;
     rc = job_run_and_wait(&c->job, line);
     if (rc) return rc;
-    if (c_rt.trace_enabled && cr == 0) trace_record(c, a.kind, c->job.variant, a.dt, a.op,
-                                                    a.kind == JOB_ALLREDUCE || a.kind == JOB_REDUCE
-                                                        ? a.count * a.esize : a.est_piece * c->size,
+    if (c_rt.trace_enabled && cr == 0) trace_record(c, a.kind, c->job.variant, a.dt, a.op, c->job.sel_bytes,
                                                     now_ns() - t0);
     return ld_relaxed(&c->job.err) ? GPUMPI_ERR_TRUNCATE : 0;
 }
