@@ -533,9 +533,12 @@ __device__ __noinline__ int learned_variant(MPI_Comm_impl* c, int kind, long lon
     SelCache* sc = &s_sel;
     const int blocks = c_rt.nranks + c_rt.nengines;  // the network's occupancy input depends on it
     const int al = aligned16 >= 16 ? 16 : aligned16 >= 8 ? 8 : 0;
-    if (sel_hit(c->sel, kind, bytes, n, dt, op, blocks, al)) {
-        for (int v = 0; v < 4; v++) pred[v] = c->sel.y[v];
-        return c->sel.variant;
+    // one copy of the record (its loads issue together), then the comparisons: the setup runs while every
+    // other member waits, and each dependent global load is an L2 round trip
+    const SelCacheRec cs = c->sel;
+    if (sel_hit(cs, kind, bytes, n, dt, op, blocks, al)) {
+        for (int v = 0; v < 4; v++) pred[v] = cs.y[v];
+        return cs.variant;
     }
     if (sc->valid && sc->bytes == bytes && sc->kind == kind && sc->n == n && sc->dt == dt && sc->op == op &&
         sc->blocks == blocks && sc->aligned == al) {

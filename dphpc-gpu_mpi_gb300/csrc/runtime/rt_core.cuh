@@ -205,7 +205,7 @@ namespace gpumpi {
 // A rank's last learned variant choice, kept across launches (data region, never zeroed by a launch):
 // valid while `epoch` equals the runtime's selector epoch, which the host advances whenever the policy,
 // the weights, the table or a tuning knob changes.
-struct SelCacheRec {
+struct alignas(16) SelCacheRec {
     long long bytes;
     int kind, n, dt, op, blocks, aligned, variant;
     unsigned epoch;
