@@ -203,8 +203,8 @@ struct CollArgs {
     bool learned = false;  // the learned policy chooses (the setup evaluates the network)
 };
 
-__device__ int learned_variant(MPI_Comm_impl* c, int kind, long long bytes, int n, int dt, int op, int aligned16,
-                               float* pred);
+__device__ __forceinline__ int learned_choice(MPI_Comm_impl* c, int kind, long long bytes, int n, int dt, int op,
+                                              int aligned16);
 
 // Bytes per piece of an Alltoallv, estimated the same way whichever member sets the collective up: the
 // mean of 64 counts, 8 entries of the count arrays of 8 members spread over the communicator (a member's
@@ -336,11 +336,9 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         j->count = a.count;
         j->sel_bytes = a.count * a.esize;
         bytes = a.count * a.esize * (long long)n;
-        float pred[4];
-        const int ov = a.learned ? learned_variant(c, a.kind, a.count * a.esize, n, a.dt, a.op, j->aligned16, pred)
-                                 : a.variant;
-        int variant = select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, ov, j->aligned16,
-                                     a.learned ? pred : nullptr);
+        int variant = a.learned ? learned_choice(c, a.kind, a.count * a.esize, n, a.dt, a.op, j->aligned16)
+                                : select_variant(a.kind, a.count * a.esize, n, a.dt, a.op, a.variant, j->aligned16,
+                                                 nullptr);
         may_post = may_post && bytes >= c_rt.engine_min_bytes;
         long long target = n + (may_post ? c_rt.nengines : 0);
         int vec = 1;
@@ -401,15 +399,11 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             const long long est = shared_piece_estimate(c);
             if (est >= 0) a_est = est;
         }
-        float pred[4];
-        const int ov = a.learned && a.kind == JOB_ALLTOALLV
-                           ? learned_variant(c, a.kind, a_est * n, n, a.dt, -1, j->aligned16, pred)
-                           : a.variant;
-        int variant = a.kind == JOB_ALLTOALLV
-                          ? select_variant(a.kind, a_est * n, n, a.dt, -1, ov, j->aligned16,
-                                           a.learned ? pred : nullptr)
-                          : (matrix && a.variant >= 0 && a.variant < GPUMPI_NUM_VARIANTS ? a.variant
-                                                                                          : GPUMPI_VARIANT_DIRECT);
+        int variant = a.kind != JOB_ALLTOALLV
+                          ? (matrix && a.variant >= 0 && a.variant < GPUMPI_NUM_VARIANTS ? a.variant
+                                                                                          : GPUMPI_VARIANT_DIRECT)
+                      : a.learned ? learned_choice(c, a.kind, a_est * n, n, a.dt, -1, j->aligned16)
+                                  : select_variant(a.kind, a_est * n, n, a.dt, -1, a.variant, j->aligned16, nullptr);
         // STAGED needs shared memory for two bulk-copy stages of at least 512 bytes per warp
         if (variant == GPUMPI_VARIANT_STAGED && (!matrix || staged_pull_stage_bytes(T) < 512))
             variant = GPUMPI_VARIANT_DIRECT;
@@ -507,7 +501,6 @@ __device__ void mlp_infer_task(void* arg, int tid, int nt) {
 struct SelCache {
     long long bytes;
     int kind, n, dt, op, blocks, aligned, variant, valid;
-    float y[4];
 };
 __shared__ SelCache s_sel;
 
@@ -524,82 +517,74 @@ __device__ __forceinline__ bool sel_hit(const SelCacheRec& r, int kind, long lon
            r.op == op && r.blocks == blocks && r.aligned == al;
 }
 
-// Variant with the smallest predicted time, and the predicted log-times in pred[4] (the setup weighs the
-// tuned table's choice against them).  Evaluated by the member that sets the collective up; the choice is
-// kept on the communicator (every later setup of the same shape reuses it, whoever arrives last) and in
-// the deciding rank's own cache, which outlives the launch.
-__device__ __noinline__ int learned_variant(MPI_Comm_impl* c, int kind, long long bytes, int n, int dt, int op,
-                                            int aligned16, float* pred) {
+// The learned policy's choice when the communicator holds none for this shape: the rank's own last
+// choice if it matches, else the network (evaluated by this block's threads) weighed against the tuned
+// table by the kind's margin (select_variant).  The choice is recorded on the communicator, in shared
+// memory and in the rank's record that outlives the launch.
+__device__ __noinline__ int learned_decide(MPI_Comm_impl* c, int kind, long long bytes, int n, int dt, int op,
+                                           int aligned16, int blocks, int al) {
     SelCache* sc = &s_sel;
-    const int blocks = c_rt.nranks + c_rt.nengines;  // the network's occupancy input depends on it
-    const int al = aligned16 >= 16 ? 16 : aligned16 >= 8 ? 8 : 0;
-    // one copy of the record (its loads issue together), then the comparisons: the setup runs while every
-    // other member waits, and each dependent global load is an L2 round trip
-    const SelCacheRec cs = c->sel;
-    if (sel_hit(cs, kind, bytes, n, dt, op, blocks, al)) {
-        for (int v = 0; v < 4; v++) pred[v] = cs.y[v];
-        return cs.variant;
-    }
+    int choice;
     if (sc->valid && sc->bytes == bytes && sc->kind == kind && sc->n == n && sc->dt == dt && sc->op == op &&
         sc->blocks == blocks && sc->aligned == al) {
-        for (int v = 0; v < 4; v++) pred[v] = sc->y[v];
-        SelCacheRec* cr = &c->sel;
-        cr->bytes = bytes;
-        cr->kind = kind;
-        cr->n = n;
-        cr->dt = dt;
-        cr->op = op;
-        cr->blocks = blocks;
-        cr->aligned = al;
-        cr->variant = sc->variant;
-        for (int v = 0; v < 4; v++) cr->y[v] = sc->y[v];
-        cr->epoch = c_rt.sel_epoch;
-        return sc->variant;
+        choice = sc->variant;
+    } else {
+        MlpWork* w = &s_mlp;
+        for (int i = 0; i < 12; i++) w->f[i] = 0.f;
+        w->f[0] = (log2f((float)(bytes > 0 ? bytes : 1)) - 16.f) / 8.f;
+        w->f[1] = (log2f((float)n) - 8.f) / 3.f;
+        const int dslot = dt == GPUMPI_FLOAT ? 2 : (dt == GPUMPI_DOUBLE || dt == GPUMPI_LONG_DOUBLE) ? 3
+                          : (dt == GPUMPI_INT || dt == GPUMPI_INT32_T) ? 4 : 5;
+        w->f[dslot] = 1.f;
+        w->f[6] = op == GPUMPI_OP_SUM ? 1.f : 0.f;  // pulls have no operator (op < 0)
+        w->f[7] = al >= 16 ? 1.f : 0.f;
+        w->f[8] = al >= 8 ? 1.f : 0.f;
+        w->f[10] = (float)n / (float)blocks;
+        w->f[11] = kind == JOB_REDUCE ? 1.f : kind == JOB_ALLTOALLV ? -1.f : 0.f;
+        Task t;
+        t.kind = TASK_USER;
+        t.p0 = (const void*)&mlp_infer_task;
+        t.p1 = w;
+        dispatch(t);
+        int best = 0;
+        for (int v = 1; v < SEL_CHOICES; v++)
+            if (w->y[v] < w->y[best]) best = v;
+        choice = select_variant(kind, bytes, n, dt, op, best, aligned16, w->y);
+        sc->kind = kind;
+        sc->bytes = bytes;
+        sc->n = n;
+        sc->dt = dt;
+        sc->op = op;
+        sc->blocks = blocks;
+        sc->aligned = al;
+        sc->variant = choice;
+        sc->valid = 1;
     }
-    MlpWork* w = &s_mlp;
-    for (int i = 0; i < 12; i++) w->f[i] = 0.f;
-    w->f[0] = (log2f((float)(bytes > 0 ? bytes : 1)) - 16.f) / 8.f;
-    w->f[1] = (log2f((float)n) - 8.f) / 3.f;
-    const int dslot = dt == GPUMPI_FLOAT ? 2 : (dt == GPUMPI_DOUBLE || dt == GPUMPI_LONG_DOUBLE) ? 3
-                      : (dt == GPUMPI_INT || dt == GPUMPI_INT32_T) ? 4 : 5;
-    w->f[dslot] = 1.f;
-    w->f[6] = op == GPUMPI_OP_SUM ? 1.f : 0.f;  // pulls have no operator (op < 0)
-    w->f[7] = al >= 16 ? 1.f : 0.f;
-    w->f[8] = al >= 8 ? 1.f : 0.f;
-    w->f[10] = (float)n / (float)blocks;
-    w->f[11] = kind == JOB_REDUCE ? 1.f : kind == JOB_ALLTOALLV ? -1.f : 0.f;
-    Task t;
-    t.kind = TASK_USER;
-    t.p0 = (const void*)&mlp_infer_task;
-    t.p1 = w;
-    dispatch(t);
-    int best = 0;
-    for (int v = 1; v < SEL_CHOICES; v++)
-        if (w->y[v] < w->y[best]) best = v;
-    for (int v = 0; v < 4; v++) sc->y[v] = pred[v] = w->y[v];
-    sc->kind = kind;
-    sc->bytes = bytes;
-    sc->n = n;
-    sc->dt = dt;
-    sc->op = op;
-    sc->blocks = blocks;
-    sc->aligned = al;
-    sc->variant = best;
-    sc->valid = 1;
-    // kept for the rank's later launches (loaded by selector_rank_begin)
-    SelCacheRec* g = &c_rt.sel_cache[me()];
-    g->bytes = bytes;
-    g->kind = kind;
-    g->n = n;
-    g->dt = dt;
-    g->op = op;
-    g->blocks = blocks;
-    g->aligned = al;
-    g->variant = best;
-    for (int v = 0; v < 4; v++) g->y[v] = w->y[v];
-    g->epoch = c_rt.sel_epoch;
-    c->sel = *g;
-    return best;
+    SelCacheRec r;
+    r.bytes = bytes;
+    r.kind = kind;
+    r.n = n;
+    r.dt = dt;
+    r.op = op;
+    r.blocks = blocks;
+    r.aligned = al;
+    r.variant = choice;
+    r.epoch = c_rt.sel_epoch;
+    c_rt.sel_cache[me()] = r;   // loaded by selector_rank_begin in the rank's later launches
+    c->sel = r;
+    return choice;
+}
+
+// The learned policy's variant for a collective, decided by the member that sets it up.  A setup of the
+// shape the communicator last decided reads one record (its loads issue together) and compares: the setup
+// runs while every other member waits, so the common path is kept to one global round trip and no call.
+__device__ __forceinline__ int learned_choice(MPI_Comm_impl* c, int kind, long long bytes, int n, int dt, int op,
+                                              int aligned16) {
+    const int blocks = c_rt.nranks + c_rt.nengines;  // the network's occupancy input depends on it
+    const int al = aligned16 >= 16 ? 16 : aligned16 >= 8 ? 8 : 0;
+    const SelCacheRec cs = c->sel;
+    if (sel_hit(cs, kind, bytes, n, dt, op, blocks, al)) return cs.variant;
+    return learned_decide(c, kind, bytes, n, dt, op, aligned16, blocks, al);
 }
 
 // ---- tiny reductions (at most TINY_BYTES per rank): one barrier, no job ----
@@ -833,7 +818,6 @@ __device__ void gpumpi::selector_rank_begin() {
     s_sel.blocks = g.blocks;
     s_sel.aligned = g.aligned;
     s_sel.variant = g.variant;
-    for (int v = 0; v < 4; v++) s_sel.y[v] = g.y[v];
     s_sel.valid = 1;
 }
 

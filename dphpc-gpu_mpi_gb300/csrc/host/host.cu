@@ -425,8 +425,15 @@ int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
     case GPUMPI_TUNE_ENGINES: w->cfg.engine_blocks = (int)value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_COPY_CHUNK: w->h_rt.copy_chunk_bytes = value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_ENGINE_MIN_BYTES: w->h_rt.engine_min_bytes = value; return GPUMPI_SUCCESS;
-    case GPUMPI_TUNE_MLP_MARGIN: w->h_rt.mlp_margin = (float)value * 1e-3f; return GPUMPI_SUCCESS;
-    case GPUMPI_TUNE_MLP_MARGIN_PULL: w->h_rt.mlp_margin_pull = (float)value * 1e-3f; return GPUMPI_SUCCESS;
+    // the learned policy's cached choices include the margin rule: a new margin starts a new epoch
+    case GPUMPI_TUNE_MLP_MARGIN:
+        w->h_rt.mlp_margin = (float)value * 1e-3f;
+        w->h_rt.sel_epoch++;
+        return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_MLP_MARGIN_PULL:
+        w->h_rt.mlp_margin_pull = (float)value * 1e-3f;
+        w->h_rt.sel_epoch++;
+        return GPUMPI_SUCCESS;
     default: return GPUMPI_ERR_ARG;
     }
 }
@@ -448,22 +455,30 @@ int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value) {
 }
 
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes) {
-    // device layout [3 kinds][2 alignment classes][32][16]; kinds 0 Allreduce, 1 Reduce, 2 Alltoall(v);
-    // class 0: every member's buffers 16-byte aligned, 1: not.  A table without classes ([2 or 3][32][16])
-    // serves both classes; a two-kind table leaves kind 2 unset.
+    // device layout [3 kinds][3 datatype classes][2 alignment classes][32][16]; kinds 0 Allreduce,
+    // 1 Reduce, 2 Alltoall(v); datatype classes 0 float, 1 double / long double, 2 the rest; alignment
+    // class 0: every member's buffers 16-byte aligned, 1: not.  A table without datatype classes
+    // ([3][2][32][16]) serves every datatype; one without either class ([2 or 3][32][16]) serves both
+    // alignments as well; a two-kind table leaves kind 2 unset.
     constexpr size_t cell = 32 * 16;
-    if (!w || !table || (bytes != 2 * cell && bytes != 3 * cell && bytes != 6 * cell)) return GPUMPI_ERR_ARG;
-    std::vector<int8_t> img(6 * cell, (int8_t)-1);
-    if (bytes == 6 * cell) {
+    constexpr int D = 3, C = 2;
+    if (!w || !table || (bytes != 2 * cell && bytes != 3 * cell && bytes != 3 * C * cell && bytes != 3 * D * C * cell))
+        return GPUMPI_ERR_ARG;
+    std::vector<int8_t> img(3 * D * C * cell, (int8_t)-1);
+    if (bytes == 3 * D * C * cell) {
         memcpy(img.data(), table, bytes);
     } else {
-        for (size_t k = 0; k < bytes / cell; k++)
-            for (int c = 0; c < 2; c++) memcpy(img.data() + (k * 2 + c) * cell, table + k * cell, cell);
+        const bool classes = bytes == 3 * C * cell;
+        const size_t kinds = classes ? 3 : bytes / cell;
+        for (size_t k = 0; k < kinds; k++)
+            for (int d = 0; d < D; d++)
+                for (int c = 0; c < C; c++)
+                    memcpy(img.data() + ((k * D + d) * C + c) * cell, table + (classes ? k * C + c : k) * cell, cell);
     }
     cudaSetDevice(w->device);
     w->h_rt.sel_epoch++;
-    if (!w->d_table) CK(cudaMalloc(&w->d_table, 6 * cell));
-    CK(cudaMemcpy(w->d_table, img.data(), 6 * cell, cudaMemcpyHostToDevice));
+    if (!w->d_table) CK(cudaMalloc(&w->d_table, img.size()));
+    CK(cudaMemcpy(w->d_table, img.data(), img.size(), cudaMemcpyHostToDevice));
     return GPUMPI_SUCCESS;
 }
 

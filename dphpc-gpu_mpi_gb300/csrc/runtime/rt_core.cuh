@@ -202,14 +202,14 @@ struct CollSlot {            // what each member publishes when it enters a coll
 }  // namespace gpumpi
 
 namespace gpumpi {
-// A rank's last learned variant choice, kept across launches (data region, never zeroed by a launch):
-// valid while `epoch` equals the runtime's selector epoch, which the host advances whenever the policy,
-// the weights, the table or a tuning knob changes.
+// The learned policy's final choice for one call shape (network, tuned table and override margin
+// applied): kept on a communicator for its later setups, and per rank across launches (data region,
+// never zeroed by a launch).  Valid while `epoch` equals the runtime's selector epoch, which the host
+// advances whenever the policy, the weights, the table or a margin changes.
 struct alignas(16) SelCacheRec {
     long long bytes;
     int kind, n, dt, op, blocks, aligned, variant;
     unsigned epoch;
-    float y[4];
 };
 
 }  // namespace gpumpi
@@ -436,7 +436,7 @@ struct Runtime {
     unsigned* abort_flag;
     int* exit_codes;                  // nranks
     // selector
-    const signed char* tuned_table;   // [kind][alignment class][log2 bytes][log2 ranks] -> variant (or nullptr)
+    const signed char* tuned_table;   // [kind][datatype class][alignment class][log2 bytes][log2 ranks] -> variant (or nullptr)
     const float* mlp_params;          // learned selector weights (or nullptr)
     SelCacheRec* sel_cache;           // per rank: the last learned choice, across launches
     HostIO hio;                       // the device -> host request channel (files, standard streams)

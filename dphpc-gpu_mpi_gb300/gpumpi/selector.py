@@ -8,7 +8,8 @@ No counterpart in the reference (one algorithm per collective there).  Pieces:
     kernels (gpumpi_mlp_loss_grad / gpumpi_mlp_adam_step); torch only holds the device buffers;
   * `autotune()` — sweeps ranks x bytes-per-rank x datatype x variant; the per-call timings come from the
     runtime's own trace (each collective's rank 0 records its duration); produces the tuned table
-    (best variant per (kind, log2 bytes, log2 ranks) cell) and the training set;
+    (best variant per (kind, datatype class, alignment class, log2 bytes, log2 ranks) cell) and the
+    training set;
   * `evaluate()` — a held-out stream of seeded calls: time of the learned choice, the tuned table's choice
     and the plain DIRECT choice against the exhaustive best (every variant measured).
 
@@ -235,25 +236,48 @@ def autotune(iters: int = 30, log=print):
     return records, build_table(grid), grid, shares
 
 
+NDCLASS = 3   # datatype classes of the tuned table: 0 float, 1 double / long double, 2 every other type
+
+
+def dclass(dt: int) -> int:
+    """Datatype class of the tuned table (sel_dclass in rt_select.cuh)."""
+    return 0 if dt == gpumpi.FLOAT else 1 if dt in (gpumpi.DOUBLE, gpumpi.LONG_DOUBLE) else 2
+
+
+def table_choice(table, kind: int, dt: int, aligned: int, log2_bytes: float, col: int) -> int:
+    """The tuned table's variant for a call, indexed as the kernel does (tuned_cell in rt_select.cuh):
+    datatype class, alignment class, floor of log2 bytes per rank, rank column `col`; -1 when unset."""
+    cell = min(31, max(0, int(math.floor(log2_bytes))))
+    return int(table[TABLE_ROW[kind], dclass(dt), 0 if aligned >= 16 else 1, cell, col])
+
+
 def build_table(grid):
-    """The tuned table: per (kind, alignment class, cell of log2 bytes, log2 ranks) the variant with the
-    least summed median time over every shape of `grid` in the cell (every datatype); class 0 = 16-byte
-    aligned buffers (the power-of-two sizes), 1 = not (the off-grid sizes, 8 or 4 mod 16 bytes); a class
-    the sweep did not reach in a cell takes the other class's choice."""
-    sums = {}
+    """The tuned table: per (kind, datatype class, alignment class, cell of log2 bytes, log2 ranks) the
+    variant with the least summed median time over the shapes of `grid` in the cell; alignment class 0 =
+    16-byte aligned buffers (the power-of-two sizes), 1 = not (the off-grid sizes, 8 or 4 mod 16 bytes).
+    A cell the sweep did not reach in one alignment class takes the same datatype class's other alignment
+    class; a datatype class the sweep did not time at all (Alltoall(v) is timed with int32 only) takes the
+    choice over every datatype."""
+    per, pooled = {}, {}
     for (kind, n, nbytes, dt, v), (cell, cls, t, _) in grid.items():
-        key = (kind, n, cell, cls)
-        sums.setdefault(key, np.zeros(NSEL))[v] += t
-    table = np.full((3, 2, 32, 16), -1, np.int8)
-    for (kind, n, cell, cls), tv in sums.items():
-        best = int(np.argmin(tv))
-        table[TABLE_ROW[kind], cls, min(31, cell), int(math.log2(n))] = best
-        if kind == KIND_ALLREDUCE:
-            table[TABLE_ROW[KIND_REDUCE], cls, min(31, cell), int(math.log2(n))] = best
-    for cls in (0, 1):
-        other = table[:, 1 - cls]
-        mine = table[:, cls]
-        mine[mine < 0] = other[mine < 0]
+        per.setdefault((kind, dclass(dt), n, cell, cls), np.zeros(NSEL))[v] += t
+        pooled.setdefault((kind, n, cell, cls), np.zeros(NSEL))[v] += t
+
+    def fill(tab, sums, dcls_of):
+        for key, tv in sums.items():
+            kind, n, cell, cls = key[0], key[-3], key[-2], key[-1]
+            rows = (TABLE_ROW[kind],) + ((TABLE_ROW[KIND_REDUCE],) if kind == KIND_ALLREDUCE else ())
+            for row in rows:
+                for d in dcls_of(key):
+                    tab[row, d, cls, min(31, cell), int(math.log2(n))] = int(np.argmin(tv))
+        for cls in (0, 1):
+            mine, other = tab[:, :, cls], tab[:, :, 1 - cls]
+            mine[mine < 0] = other[mine < 0]
+        return tab
+
+    table = fill(np.full((3, NDCLASS, 2, 32, 16), -1, np.int8), per, lambda key: (key[1],))
+    every = fill(np.full((3, NDCLASS, 2, 32, 16), -1, np.int8), pooled, lambda key: range(NDCLASS))
+    table[table < 0] = every[table < 0]
     return table
 
 
@@ -280,7 +304,7 @@ def margin_totals(mlp, table, grid, shares, candidates=MARGIN_CANDIDATES, rank_c
     for m in candidates:
         for i, key in enumerate(keys):
             sh = shapes[key]
-            tv = int(table[TABLE_ROW[key[0]], sh["cls"], min(31, sh["cell"]), rank_col(key[1])])
+            tv = table_choice(table, key[0], key[3], 16 if sh["cls"] == 0 else 8, sh["cell"], rank_col(key[1]))
             kn = KIND_NAME[key[0]]
             tot[kn][m] = tot[kn].get(m, 0.0) + sh["t"][policy_pick(pred[i], tv, m)]
     return tot
@@ -390,7 +414,7 @@ def evaluate(mlp_params, table, calls: int = 10000, shapes_per_rank: int = 16, s
     for i, key in enumerate(keys):
         kind, n, b, dt = key
         l2b, al = seen[key]
-        tv = int(table[TABLE_ROW[kind], 0 if al >= 16 else 1, min(31, max(0, int(math.floor(l2b)))), int(math.log2(n))])
+        tv = table_choice(table, kind, dt, al, l2b, int(math.log2(n)))
         pick[key] = {"learned": policy_pick(pred[i], tv, margins[KIND_NAME[kind]]),
                      "learned_pure": int(np.argmin(pred[i][:NSEL])), "tuned": tv if tv >= 0 else 0, "plain": 0}
     rep = summarize(keys, meas, pick, rng.integers(0, len(keys), calls))
@@ -511,7 +535,8 @@ def packaged_margins() -> dict:
 
 def apply_policy(world, policy: str):
     """Sets a world's selection policy: "plain" (DIRECT), "tuned" (packaged table), "learned" (packaged
-    network, in-kernel inference per call), "heuristic" (the library default)."""
+    network evaluated in the kernel once per call shape, its choice cached), "heuristic" (the library
+    default)."""
     if policy == "plain":
         world.set_policy(-1, 0)
         return

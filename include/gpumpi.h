@@ -180,10 +180,11 @@ int gpumpi_main(int argc, char** argv, int program);
 #define GPUMPI_P_USER 200
 /* The current value of a GPUMPI_TUNE_* knob. */
 int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value);
-/* Tuned table: int8 [3][2][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; alignment class:
- * 0 when every member's buffers are 16-byte aligned, else 1; log2 bytes per rank; log2 ranks) -> variant
- * or -1, host memory.  A [3][32][16] table serves both classes; a [2][32][16] one leaves Alltoall(v)
- * untuned. */
+/* Tuned table: int8 [3][3][2][32][16] (kind: 0 Allreduce, 1 Reduce, 2 Alltoall/Alltoallv; datatype
+ * class: 0 MPI_FLOAT, 1 MPI_DOUBLE / MPI_LONG_DOUBLE, 2 every other type; alignment class: 0 when every
+ * member's buffers are 16-byte aligned, else 1; log2 bytes per rank; log2 ranks) -> variant or -1, host
+ * memory.  A [3][2][32][16] table serves every datatype class, a [3][32][16] one every class of both
+ * kinds; a [2][32][16] one leaves Alltoall(v) untuned. */
 int gpumpi_set_tuned_table(gpumpi_world* w, const int8_t* table, size_t bytes);
 /* Learned selector weights: float[GPUMPI_MLP_NPARAMS] in the layout of the training kernels. */
 int gpumpi_set_mlp(gpumpi_world* w, const float* params, size_t count);

@@ -104,7 +104,7 @@ def test_packaged_policies_give_exact_integer_results(gpulib, oracle):
     is exact on integer Allreduce and Alltoallv."""
     from gpumpi import selector
     table, params = selector.load_packaged()
-    assert table is not None and table.shape == (3, 2, 32, 16) and params.shape == (gpulib.MLP_NPARAMS,)
+    assert table is not None and table.shape == (3, selector.NDCLASS, 2, 32, 16) and params.shape == (gpulib.MLP_NPARAMS,)
     n, count = 96, 3000
     x = oracle.fill_i32(9, n * count).reshape(n, count) % 1000
     ref = oracle.allreduce(x, 2, 2)
@@ -148,13 +148,12 @@ def test_packaged_network_beats_table_on_recorded_heldout_timings(gpulib):
         l2b, al, share = rep["kernel_seen"][k]
         feats.append(sel.features(kind, 2.0 ** l2b, n, dt, gpulib.OP_SUM if kind == sel.KIND_ALLREDUCE else -1,
                                   share, int(al)))
-        cells.append((kind, n, l2b, int(al)))
+        cells.append((kind, n, l2b, int(al), dt))
     pred = sel.MLP(params=params).predict(np.stack(feats))
     tot = {"learned": 0.0, "tuned": 0.0, "best": 0.0}
     for i, k in enumerate(keys):
-        kind, n, l2b, al = cells[i]
-        tv = int(table[sel.TABLE_ROW[kind], 0 if al >= 16 else 1, min(31, max(0, int(np.floor(l2b)))),
-                       int(np.log2(n))])
+        kind, n, l2b, al, dt = cells[i]
+        tv = sel.table_choice(table, kind, dt, al, l2b, int(np.log2(n)))
         pick = sel.policy_pick(pred[i], tv, margins[sel.KIND_NAME[kind]])
         assert pick == rep["choices"][k]["learned"], k
         t = rep["measured_us"][k]

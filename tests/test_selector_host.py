@@ -30,9 +30,9 @@ def test_margin_keeps_table_where_network_is_unsure_and_overrides_where_sure():
     grid = {}
     grid_entry(grid, n, 1 << 10, [1.0, 2.0, 2.0])   # the table is right (variant 0)
     grid_entry(grid, n, 1 << 12, [3.0, 1.0, 3.0])   # the table is wrong; variant 1 is 3x faster
-    table = np.full((3, 2, 32, 16), -1, np.int8)
-    table[0, :, 10, 6] = 0
-    table[0, :, 12, 6] = 0
+    table = np.full((3, sel.NDCLASS, 2, 32, 16), -1, np.int8)
+    table[0, :, :, 10, 6] = 0
+    table[0, :, :, 12, 6] = 0
     # shape 1 KiB: the network prefers variant 1 by 0.08 (wrongly); shape 4 KiB: by 0.8 (rightly)
     net = TableNet({10: [0.50, 0.42, 1.0, 1.0], 12: [1.0, 0.2, 1.0, 1.0]})
     # margins 0.1 .. 0.5 keep the table at 1 KiB and override at 4 KiB (total 2.0); 0.05 overrides both
@@ -42,6 +42,31 @@ def test_margin_keeps_table_where_network_is_unsure_and_overrides_where_sure():
     assert m == {"allreduce": 0.5, "alltoallv": sel.MARGIN}
     assert sel.choose_margin(net, table, grid, {n: 0.8}, candidates=(0.05, 1.0))["allreduce"] == 0.05
     assert sel.choose_margin(net, table, grid, {n: 0.8}, candidates=(1.0, 2.0))["allreduce"] == 2.0
+
+
+def test_table_separates_datatypes_and_fills_untimed_classes():
+    # one cell (1024 ranks, 2^20 bytes, 16-byte aligned): float and int32 favour DIRECT, double favours RING
+    # by enough that the pooled sum would pick RING for every type
+    n, grid = 1024, {}
+    for dt, times in ((gpumpi.FLOAT, [367.5, 527.8, 403.2]), (gpumpi.INT, [377.7, 530.7, 400.6]),
+                      (gpumpi.DOUBLE, [962.1, 904.8, 601.9])):
+        for v, t in enumerate(times):
+            grid[(sel.KIND_ALLREDUCE, n, 1 << 20, dt, v)] = (20, 0, t, 20.0)
+    # Alltoall(v) timed with int32 only, and only its misaligned class
+    for v, t in enumerate([5.0, 6.0, 4.0]):
+        grid[(sel.KIND_ALLTOALLV, n, 3 << 19, gpumpi.INT, v)] = (20, 1, t, 20.58)
+    t = sel.build_table(grid)
+    assert t.shape == (3, sel.NDCLASS, 2, 32, 16)
+    assert t[0, sel.dclass(gpumpi.FLOAT), 0, 20, 10] == 0
+    assert t[0, sel.dclass(gpumpi.INT), 0, 20, 10] == 0
+    assert t[0, sel.dclass(gpumpi.DOUBLE), 0, 20, 10] == 2
+    assert sel.dclass(gpumpi.INT64_T) == sel.dclass(gpumpi.INT) == 2 and sel.dclass(gpumpi.LONG_DOUBLE) == 1
+    assert np.array_equal(t[0], t[1])                                  # Reduce follows Allreduce
+    assert (t[0, :, 1, 20, 10] == t[0, :, 0, 20, 10]).all()            # untimed alignment class: the other one
+    assert (t[2, :, :, 20, 10] == 2).all()                             # every datatype and alignment class
+    assert sel.table_choice(t, sel.KIND_ALLREDUCE, gpumpi.DOUBLE, 16, 20.3, 10) == 2
+    assert sel.table_choice(t, sel.KIND_ALLREDUCE, gpumpi.FLOAT, 8, 20.3, 10) == 0
+    assert sel.table_choice(t, sel.KIND_ALLREDUCE, gpumpi.FLOAT, 16, 21.0, 10) == -1
 
 
 def test_policy_pick_never_chooses_staged():
@@ -55,7 +80,7 @@ def test_policy_pick_never_chooses_staged():
 def test_margin_defaults_without_complete_shapes():
     grid = {}
     grid[(sel.KIND_ALLREDUCE, 64, 1024, gpumpi.FLOAT, 0)] = (10, 0, 1.0, 10.0)   # one variant only
-    table = np.zeros((3, 2, 32, 16), np.int8)
+    table = np.zeros((3, sel.NDCLASS, 2, 32, 16), np.int8)
     assert sel.choose_margin(TableNet({}), table, grid, {64: 0.8}) == {"allreduce": sel.MARGIN,
                                                                         "alltoallv": sel.MARGIN}
 
@@ -64,7 +89,7 @@ def test_packaged_artifacts_and_recorded_figures():
     table, params = sel.load_packaged()
     if table is None:
         pytest.skip("no packaged selector")
-    assert table.shape == (3, 2, 32, 16) and table.dtype == np.int8
+    assert table.shape == (3, sel.NDCLASS, 2, 32, 16) and table.dtype == np.int8
     assert set(np.unique(table)) <= {-1, 0, 1, 2}        # STAGED is not a choice
     assert np.array_equal(table[0], table[1])          # Reduce follows the Allreduce sweep
     assert params.shape == (gpumpi.MLP_NPARAMS,) and params.dtype == np.float32
@@ -106,10 +131,10 @@ def test_apply_policy_calls():
         pytest.skip("no packaged selector")
     w = FakeWorld()
     sel.apply_policy(w, "tuned")
-    assert w.calls == [("table", (3, 2, 32, 16)), ("policy", -1, 1)]
+    assert w.calls == [("table", (3, sel.NDCLASS, 2, 32, 16)), ("policy", -1, 1)]
     w = FakeWorld()
     sel.apply_policy(w, "learned")
-    assert w.calls == [("table", (3, 2, 32, 16)), ("mlp", (gpumpi.MLP_NPARAMS,)),
+    assert w.calls == [("table", (3, sel.NDCLASS, 2, 32, 16)), ("mlp", (gpumpi.MLP_NPARAMS,)),
                        ("tuning", gpumpi.TUNE_MLP_MARGIN, int(round(sel.packaged_margins()["allreduce"] * 1000))),
                        ("tuning", gpumpi.TUNE_MLP_MARGIN_PULL,
                         int(round(sel.packaged_margins()["alltoallv"] * 1000))),
