@@ -3,7 +3,7 @@ MPI_Allreduce/Reduce (fold orders, TMA staging) and MPI_Alltoall(v) (piece order
 
 No counterpart in the reference (one algorithm per collective there).  Pieces:
   * `features()` — the 12 call features; the same formula runs inside the kernel (mpi_api.cu,
-    learned_variant) when a world's policy is "learned";
+    learned_decide) when a world's policy is "learned";
   * `MLP` — the 12 -> 64 -> 64 -> 4 network, trained on the GPU by the library's own forward/backward
     kernels (gpumpi_mlp_loss_grad / gpumpi_mlp_adam_step); torch only holds the device buffers;
   * `autotune()` — sweeps ranks x bytes-per-rank x datatype x variant; the per-call timings come from the
@@ -43,7 +43,7 @@ NP_DT = {gpumpi.FLOAT: np.float32, gpumpi.DOUBLE: np.float64, gpumpi.INT: np.int
 
 def features(kind: int, bytes_per_rank: float, n: int, dt: int, op: int, rank_share: float,
              aligned: int = 16) -> np.ndarray:
-    """The 12 features (must match learned_variant in csrc/api/mpi_api.cu): log2 bytes per rank, log2
+    """The 12 features (must match learned_decide in csrc/api/mpi_api.cu): log2 bytes per rank, log2
     ranks, datatype one-hot, SUM flag (Alltoall(v) has no operator: op = -1), 16-byte and 8-byte alignment
     flags of the members' buffers, rank share of the launch's blocks, kind."""
     f = np.zeros(12, np.float32)
