@@ -47,4 +47,6 @@ __device__ int gpumpi_printf(const char* fmt, ...);
 #define fflush gpumpi_fflush
 #define remove gpumpi_remove
 #define fprintf gpumpi_fprintf
+#undef printf
+#define printf gpumpi_printf
 #endif

@@ -76,3 +76,43 @@ def test_converted_program_writes_files_and_prints(io_exe, tmp_path, ranks):
     assert f"sum of squares below {n} over {ranks} ranks: {total:.1f}" in r.stdout
     parts = np.fromfile(out, dtype=np.float64)
     assert parts.tolist() == [float(sum(i * i for i in range(k, n, ranks))) for k in range(ranks)]
+
+
+@pytest.fixture(scope="module")
+def report_exe(tmp_path_factory, gpulib):
+    import build
+    out = tmp_path_factory.mktemp("prog") / "mpi_pi_report"
+    return build.build_program([ROOT / "tests" / "programs" / "mpi_pi_report.cu"], out)
+
+
+def expected_pi_report(n: int, ranks: int) -> float:
+    """The program's sum in its own order: per rank every size-th interval from rank + 1, times h, then
+    the ranks' parts in rank order (the canonical MPI_Reduce fold)."""
+    h = 1.0 / n
+    total = 0.0
+    for r in range(ranks):
+        s = 0.0
+        for i in range(r + 1, n + 1, ranks):
+            x = h * (i - 0.5)
+            s += 4.0 / (1.0 + x * x)
+        total += h * s
+    return total
+
+
+@pytest.mark.parametrize("ranks,n", [(1, 10000), (16, 100000), (100, 100000)])
+def test_converted_pi_program_reports_through_host_streams(report_exe, ranks, n):
+    # MPI_Get_processor_name, MPI_Wtime, fprintf(stderr), printf and fflush(stdout) from ranks, performed
+    # by the launcher's host channel while the kernel runs
+    import math
+    r = subprocess.run([str(report_exe), str(n), "---gpumpi", "-n", str(ranks)], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    where = sorted(l for l in r.stderr.splitlines() if l.startswith("rank "))
+    assert where == sorted(f"rank {k} of {ranks} runs on GB300 block-rank" for k in range(ranks))
+    est = [l for l in r.stdout.splitlines() if l.startswith("pi estimate ")]
+    assert len(est) == 1, r.stdout
+    pi, err = (float(x) for x in est[0][len("pi estimate "):].replace(", error", "").split())
+    assert abs(pi - expected_pi_report(n, ranks)) <= 1e-12 * 3.2
+    assert abs(err - abs(pi - math.pi)) <= 1e-15
+    secs = [l for l in r.stdout.splitlines() if l.startswith("elapsed ")]
+    assert len(secs) == 1 and 0.0 <= float(secs[0].split()[1]) < 60.0
