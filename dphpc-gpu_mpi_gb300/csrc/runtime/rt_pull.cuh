@@ -193,8 +193,10 @@ __device__ __forceinline__ void flat_copy_t(const PTab& t, long long u0, long lo
                 const unsigned long long s = d + (unsigned long long)s_chunk.p.delta[i];
                 const int h = MIS ? (int)(s & 15) : 0;
                 const uint4* sa = (const uint4*)(s - (unsigned long long)h);
-                a[k] = __ldcg(sa);
-                if (MIS && h) b[k] = __ldcg(sa + 1);
+                // realigned units read two neighbouring vectors and lane l's second vector is lane l+1's
+                // first: allocating them in L1 serves the second read there instead of from L2
+                a[k] = MIS ? __ldca(sa) : __ldcg(sa);
+                if (MIS && h) b[k] = __ldca(sa + 1);
                 dst[k] = d;
                 sh[k] = h;
             }
@@ -212,6 +214,13 @@ __device__ __forceinline__ void flat_copy_t(const PTab& t, long long u0, long lo
 // same box): uniform 1 KiB pieces (aligned) K=3 5,154, K=4 4,888, K=6 4,780; uneven pieces of U[0,512]
 // int32 (misaligned) K=3 4,095, K=2 3,935, K=4 3,613 (more units spill under the 64-register cap);
 // K=3 is also the fastest on U[0,128] pieces and on the bucket-sort shape.
+// Cache operators, same box and shapes (uneven 1 MiB / uniform 1 MiB / bucket-sort shape): L2-only
+// loads and stores everywhere 4,068-4,078 / 5,073-5,080 / 2,484-2,498; misaligned loads through L1
+// 4,167-4,177 / 5,059-5,072 / 2,461-2,510; streaming (evict-first) loads on the misaligned path
+// 3,897-3,911 / - / 2,429-2,452; an L2 evict-first policy on every access 3,979-3,994 / 5,013-5,030 /
+// 2,656; evict-first loads and stores everywhere 4,097-4,109 / 5,032-5,039 / 2,650-2,658, whose gain on
+// the bucket-sort shape (2 x 128 MiB per call, about twice the L2) depends on how much of the previous
+// call's data the L2 still holds.
 __device__ __noinline__ void flat_copy_aligned(PTab t, long long u0, long long u1, int lane, int wi, int nwk) {
     flat_copy_t<3, false>(t, u0, u1, lane, wi, nwk);
 }
