@@ -10,7 +10,8 @@ Reported:
   value      algorithmic GB/s = 2 * ranks * bytes_per_rank / step time (every input read once, every
              output written once), summed over replicas when run on N GPUs (replicas only);
   e2e        the same metric through the C ABI with pinned HOST buffers: host->device copy of the
-             inputs, the collective, device->host copy of all outputs, every step;
+             inputs, the collective, device->host copy of all outputs, every step (the call cuts the
+             rows into column slices so later slices' inputs cross while earlier results cross back);
   roofline   against the measured HBM copy bandwidth (MEASURED_PEAKS.json, "of measured");
   cpu_baseline  the CPU oracle's multi-threaded allreduce on the same workload (bounded number of calls),
              on this host's cores;
@@ -736,7 +737,9 @@ def main():
     e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / ke)
     assert torch.equal(hr[0], recv[0].cpu())
     e2e = {"value": ws * algo_bytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": n * per,
-           "d2h_bytes_per_step": n * per, "ms_per_step": e2e_s * 1e3}
+           "d2h_bytes_per_step": n * per, "ms_per_step": e2e_s * 1e3,
+           "host_path": f"page-locked host buffers, TUNE_HOST_DIRECT {world.get_tuning(gpumpi.TUNE_HOST_DIRECT)} "
+                        "(3: column slices, inputs read in place, results copied back while later slices fold)"}
 
     peak, peak_kind = measured_peak()
     achieved = algo_bytes / (ms_total / K * 1e-3) / 1e9

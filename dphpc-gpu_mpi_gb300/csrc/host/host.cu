@@ -105,11 +105,18 @@ struct gpumpi_world {
     // 4.9 to 5.6 TB/s and uneven Alltoallv from 3.0 to 4.0 TB/s.
     long long dyn_smem_cap = 8192;
     // pinned host buffers: 1 = the kernel reads and writes them in place (device alias of the page-locked
-    // allocation, every byte crosses the host link once, both directions at once); 0 = staged through
-    // device memory by copies before and after the kernel.  Measured at 1024 ranks x 1 MiB Allreduce:
-    // 210 GB/s in place against 193 GB/s staged, the host link being the bound either way.
-    int host_direct = 1;
+    // allocation, every byte crosses the host link once); 0 = staged through device memory by copies
+    // before and after the kernel; 2..4: an Allreduce between host buffers is cut into column slices so
+    // both directions of the host link carry data at once (allreduce_host_sliced), other calls treat 2..4
+    // as 1.  Measured at 1024 ranks x 1 MiB fp32 Allreduce with page-locked buffers (GB/s of 2 x payload,
+    // host link: 211 GB/s host to device, 194 back, 343 both at once): in place 208, staged 193, slices of
+    // 256 KiB per rank 266 (mode 2) / 266 (mode 3) / 258 (mode 4); 128 KiB slices 207-224, 64 KiB 174-186
+    // (2D copies of narrow rows lose most of the two-way overlap).
+    int host_direct = 3;
     bool host_aliased = false;  // the launch being prepared reads host memory in place: no bulk copies
+    long long host_slice_bytes = 0;  // column slice per rank of the sliced path, bytes (0 = auto)
+    cudaStream_t xs_in = nullptr, xs_out = nullptr;  // the sliced path's copy streams (created on first use)
+    cudaEvent_t xev[4] = {};                         // input copied, slice folded, call start, call end
     signed char* d_table = nullptr;
     float* d_mlp = nullptr;
     // scratch for host-buffer staging
@@ -387,6 +394,10 @@ int gpumpi_world_destroy(gpumpi_world* w) {
     cudaFree(w->d_table);
     cudaFree(w->d_mlp);
     for (auto& p : w->d_stage) cudaFree(p);
+    if (w->xs_in) cudaStreamSynchronize(w->xs_in), cudaStreamDestroy(w->xs_in);
+    if (w->xs_out) cudaStreamSynchronize(w->xs_out), cudaStreamDestroy(w->xs_out);
+    for (auto& e : w->xev)
+        if (e) cudaEventDestroy(e);
     if (w->ev0) cudaEventDestroy(w->ev0);
     if (w->ev1) cudaEventDestroy(w->ev1);
     if (w->stream) cudaStreamDestroy(w->stream);
@@ -420,7 +431,14 @@ int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
     switch (key) {
     case GPUMPI_TUNE_VEC: w->tune_vec = (int)value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_DYN_SMEM: w->dyn_smem_cap = value; return GPUMPI_SUCCESS;
-    case GPUMPI_TUNE_HOST_DIRECT: w->host_direct = value != 0; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_HOST_DIRECT:
+        if (value < 0 || value > 4) return GPUMPI_ERR_ARG;
+        w->host_direct = (int)value;
+        return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_HOST_SLICE:
+        if (value < 0) return GPUMPI_ERR_ARG;
+        w->host_slice_bytes = value;
+        return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_STAGE_GROUP: w->tune_group = (int)value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_ENGINES: w->cfg.engine_blocks = (int)value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_COPY_CHUNK: w->h_rt.copy_chunk_bytes = value; return GPUMPI_SUCCESS;
@@ -444,6 +462,7 @@ int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value) {
     case GPUMPI_TUNE_VEC: *value = w->tune_vec; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_DYN_SMEM: *value = w->dyn_smem_cap; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_HOST_DIRECT: *value = w->host_direct; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_HOST_SLICE: *value = w->host_slice_bytes; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_STAGE_GROUP: *value = w->tune_group; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_ENGINES: *value = w->cfg.engine_blocks; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_COPY_CHUNK: *value = w->h_rt.copy_chunk_bytes; return GPUMPI_SUCCESS;
@@ -595,17 +614,11 @@ int prepare_runtime(gpumpi_world* w, const gpumpi_prog_entry* pe) {
     return GPUMPI_SUCCESS;
 }
 
-// Reads the device error records and exit codes after a finished launch.  Error records describe what
-// went wrong inside MPI calls; the calls also returned the codes to the program, so only a run that hit a
-// bounded-wait timeout fails here (other errors surface through the ranks' exit codes).
-int collect_results(gpumpi_world* w) {
-    const Runtime& r = w->h_rt;
-    const int nb = w->cfg.nranks + w->nengines;
-    CK(cudaMemcpy(w->h_err.data(), r.errors, sizeof(gpumpi::ErrorRecord) * nb, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(w->h_exit.data(), r.exit_codes, sizeof(int) * w->cfg.nranks, cudaMemcpyDeviceToHost));
+// Turns one launch's error records (nb blocks) and the ranks' exit codes into the call's status.
+int scan_results(gpumpi_world* w, const gpumpi::ErrorRecord* errs, int nb, const int* exits) {
     int timeout = 0;
     for (int b = 0; b < nb; b++) {
-        const gpumpi::ErrorRecord& e = w->h_err[b];
+        const gpumpi::ErrorRecord& e = errs[b];
         if (e.code) {
             char buf[256];
             snprintf(buf, sizeof buf, "rank %d: MPI error %d (detail %d) at runtime line %d, info %lld", e.rank,
@@ -616,11 +629,22 @@ int collect_results(gpumpi_world* w) {
     }
     if (timeout) return GPUMPI_ERR_TIMEOUT;
     for (int i = 0; i < w->cfg.nranks; i++)
-        if (w->h_exit[i] != 0) {
-            w->err = "rank " + std::to_string(i) + " returned " + std::to_string(w->h_exit[i]);
-            return w->h_exit[i];
+        if (exits[i] != 0) {
+            w->err = "rank " + std::to_string(i) + " returned " + std::to_string(exits[i]);
+            return exits[i];
         }
     return GPUMPI_SUCCESS;
+}
+
+// Reads the device error records and exit codes after a finished launch.  Error records describe what
+// went wrong inside MPI calls; the calls also returned the codes to the program, so only a run that hit a
+// bounded-wait timeout fails here (other errors surface through the ranks' exit codes).
+int collect_results(gpumpi_world* w) {
+    const Runtime& r = w->h_rt;
+    const int nb = w->cfg.nranks + w->nengines;
+    CK(cudaMemcpy(w->h_err.data(), r.errors, sizeof(gpumpi::ErrorRecord) * nb, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(w->h_exit.data(), r.exit_codes, sizeof(int) * w->cfg.nranks, cudaMemcpyDeviceToHost));
+    return scan_results(w, w->h_err.data(), nb, w->h_exit.data());
 }
 
 }  // namespace
@@ -857,6 +881,126 @@ size_t type_bytes(int dt) {
     return (dt >= 0 && dt < GPUMPI_NUM_PREDEFINED_TYPES) ? (size_t)sizes[dt] : 0;
 }
 
+static_assert(sizeof(gpumpi::ErrorRecord) % sizeof(int) == 0, "records are gathered as ints");
+
+// One launch's error records and exit codes, copied into slot `dst` on the launch's stream (no copy engine
+// between the slices' launches: their copies of user data keep the engines busy).
+__global__ void gather_records(const int* __restrict__ errs, int nerr, const int* __restrict__ exits, int nexit,
+                               int* __restrict__ dst) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nerr + nexit; i += gridDim.x * blockDim.x)
+        dst[i] = i < nerr ? errs[i] : exits[i - nerr];
+}
+
+// Allreduce between host buffers (rows of `count` elements, one per rank, `per` bytes apart), cut into
+// column slices: the same element range of every rank.  Slice j's inputs cross the host link while slice
+// j-1 is folded and slice j-2's results cross back, so both directions of the link carry data at once
+// (one launch over whole rows moves all inputs, then all results).  Each slice is one launch of the
+// collective over the slice's columns with the caller's row stride: every element gets the same fold (the
+// canonical rank order, or the variant the policy picks) as in one launch over whole rows.
+//   mode 2: inputs and results cross by 2D copies through device staging buffers;
+//   mode 3: the kernel reads page-locked inputs in place, results cross by 2D copies;
+//   mode 4: inputs cross by 2D copies, the kernel writes page-locked results in place.
+// Returns -1 when the call does not qualify (the caller takes the one-launch path).
+int allreduce_host_sliced(gpumpi_world* w, const void* sb, void* rb, long long count, int dt, int op,
+                          void* stream_v) {
+    const int n = w->cfg.nranks;
+    const size_t esz = type_bytes(dt);
+    const size_t per = (size_t)count * esz;
+    // slice width: by default 256 MiB per slice over all ranks and at least 128 KiB per rank (narrower 2D
+    // copies lose the two-way overlap); a multiple of 256 bytes per rank (keeps every slice's rows 16-byte
+    // aligned when the rows are), at most 64 slices
+    size_t sbytes = w->host_slice_bytes > 0 ? (size_t)w->host_slice_bytes
+                                            : std::max((size_t)128 << 10, ((size_t)256 << 20) / (size_t)n);
+    sbytes = std::max(align_up(sbytes, 256), align_up((per + 63) / 64, 256));
+    const long long selems = (long long)(sbytes / esz);
+    const int slices = (int)((count + selems - 1) / selems);
+    if (slices < 2 || per % 16 != 0) return -1;
+    const int mode = w->host_direct;
+    void* in_alias = mode == 3 ? pinned_alias(sb) : nullptr;
+    void* out_alias = mode == 4 ? pinned_alias(rb) : nullptr;
+
+    cudaStream_t s = stream_v ? (cudaStream_t)stream_v : w->stream;
+    CK(cudaSetDevice(w->device));
+    if (!w->xs_in) CK(cudaStreamCreateWithFlags(&w->xs_in, cudaStreamNonBlocking));
+    if (!w->xs_out) CK(cudaStreamCreateWithFlags(&w->xs_out, cudaStreamNonBlocking));
+    for (auto& e : w->xev)
+        if (!e) CK(cudaEventCreate(&e));
+    cudaEvent_t ev_in = w->xev[0], ev_fold = w->xev[1], ev_a = w->xev[2], ev_b = w->xev[3];
+
+    struct AliasScope {
+        gpumpi_world* w;
+        ~AliasScope() { w->host_aliased = false; }
+    } alias_scope{w};
+    w->host_aliased = in_alias || out_alias;  // no bulk asynchronous copy is pointed at host memory
+    const size_t all = per * (size_t)n;
+    void *dsend = in_alias, *drecv = out_alias, *drec = nullptr;
+    int rc;
+    if (!in_alias && (rc = stage(w, 0, nullptr, all, false, s, &dsend))) return rc;
+    if (!out_alias && (rc = stage(w, 1, nullptr, all, false, s, &drecv))) return rc;
+    const Runtime& r = w->h_rt;
+    const int nb = (int)w->h_err.size();  // records of every block the world can launch
+    const int nerr = (int)(sizeof(gpumpi::ErrorRecord) / sizeof(int)) * nb;
+    const int rec_ints = nerr + n;
+    if ((rc = stage(w, 6, nullptr, sizeof(int) * (size_t)rec_ints * slices, false, s, &drec))) return rc;
+
+    // copies wait for whatever the caller queued on its stream before this call
+    CK(cudaEventRecord(ev_a, s));
+    CK(cudaStreamWaitEvent(w->xs_in, ev_a, 0));
+    w->err.clear();
+    int launch_rc = GPUMPI_SUCCESS;
+    for (int j = 0; j < slices; j++) {
+        const long long c0 = (long long)j * selems;
+        const long long cn = std::min(selems, count - c0);
+        const size_t off = (size_t)c0 * esz, width = (size_t)cn * esz;
+        if (!in_alias) {
+            CK(cudaMemcpy2DAsync((char*)dsend + off, per, (const char*)sb + off, per, width, n,
+                                 cudaMemcpyHostToDevice, w->xs_in));
+            CK(cudaEventRecord(ev_in, w->xs_in));
+            CK(cudaStreamWaitEvent(s, ev_in, 0));
+        }
+        gpumpi_params prm;
+        memset(&prm, 0, sizeof(prm));
+        prm.i[0] = GPUMPI_COLL_ALLREDUCE;
+        prm.i[1] = cn;
+        prm.i[2] = dt;
+        prm.i[3] = op;
+        prm.i[5] = 1;
+        prm.i[6] = (long long)per;
+        prm.i[7] = (long long)per;
+        prm.p[0] = (char*)dsend + off;
+        prm.p[1] = (char*)drecv + off;
+        launch_rc = gpumpi_run_program(w, GPUMPI_P_COLL, &prm, s, 0);
+        if (launch_rc) break;
+        gather_records<<<8, 256, 0, s>>>((const int*)r.errors, nerr, r.exit_codes, n, (int*)drec + (size_t)j * rec_ints);
+        CK(cudaGetLastError());
+        g_launches++;
+        if (!out_alias) {
+            CK(cudaEventRecord(ev_fold, s));
+            CK(cudaStreamWaitEvent(w->xs_out, ev_fold, 0));
+            CK(cudaMemcpy2DAsync((char*)rb + off, per, (const char*)drecv + off, per, width, n,
+                                 cudaMemcpyDeviceToHost, w->xs_out));
+        }
+    }
+    // the call ends on the caller's stream after the last results have crossed
+    CK(cudaEventRecord(ev_fold, w->xs_out));
+    CK(cudaStreamWaitEvent(s, ev_fold, 0));
+    CK(cudaEventRecord(ev_b, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaStreamSynchronize(w->xs_in));  // inputs still in flight when a launch failed
+    if (launch_rc) return launch_rc;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev_a, ev_b);
+    w->last_ms = ms;
+    std::vector<int> rec((size_t)rec_ints * slices);
+    CK(cudaMemcpy(rec.data(), drec, sizeof(int) * rec.size(), cudaMemcpyDeviceToHost));
+    for (int j = 0; j < slices; j++) {
+        const int* base = rec.data() + (size_t)j * rec_ints;
+        rc = scan_results(w, reinterpret_cast<const gpumpi::ErrorRecord*>(base), nb, base + nerr);
+        if (rc) return rc;
+    }
+    return GPUMPI_SUCCESS;
+}
+
 int coll_call(gpumpi_world* w, int kind, const void* sb, size_t sbytes, long long sstride, void* rb, size_t rbytes,
               long long rstride, long long count, int dt, int op, int root, int iters, uint64_t* iter_ns,
               void* stream, const int* mats[4], size_t mat_bytes) {
@@ -886,6 +1030,12 @@ int coll_call(gpumpi_world* w, int kind, const void* sb, size_t sbytes, long lon
                 {mats ? mats[1] : nullptr, mat_bytes, true, false, nullptr, false},
                 {mats ? mats[2] : nullptr, mat_bytes, true, false, nullptr, false},
                 {mats ? mats[3] : nullptr, mat_bytes, true, false, nullptr, false}};
+    if (kind == GPUMPI_COLL_ALLREDUCE && w->host_direct >= 2 && iters == 1 && !iter_ns && sb && rb &&
+        sb != (const void*)(intptr_t)1 && sstride == rstride && (size_t)sstride == (size_t)count * type_bytes(dt) &&
+        !is_device_ptr(sb) && !is_device_ptr(rb)) {
+        int rc = allreduce_host_sliced(w, sb, rb, count, dt, op, stream);
+        if (rc >= 0) return rc;
+    }
     return run_with_buffers(w, GPUMPI_P_COLL, prm, b, 6, iters, iter_ns, stream);
 }
 

@@ -23,7 +23,8 @@
  *
  * Buffers: every data pointer may be device memory or host memory (pageable or pinned); pageable host
  * memory is staged through device memory inside the call (the host<->device copies are part of the
- * call), page-locked host memory is read and written in place by the kernel (GPUMPI_TUNE_HOST_DIRECT).
+ * call), page-locked host memory is read and written in place by the kernel; a large Allreduce between
+ * host buffers runs as column slices whose copies overlap (GPUMPI_TUNE_HOST_DIRECT).
  * Rank-major layout: rank r's buffer starts at base + r * stride_bytes.
  * Return value: GPUMPI_SUCCESS (0) or an error code from gpumpi_abi.h; never aborts the process.
  */
@@ -166,10 +167,19 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
  * It holds the TMA stages of the STAGED variants and block-parallel user scratch; what it does not take
  * stays L1 cache, which the executors' spilled registers and the ranks' private state use. */
 #define GPUMPI_TUNE_DYN_SMEM 7
-/* GPUMPI_TUNE_HOST_DIRECT: 1 (default) = page-locked host buffers are read and written in place by the
- * kernel through their device alias (every byte crosses the host link once, both directions at once;
- * the STAGED variants then run as DIRECT); 0 = staged through device memory around the kernel. */
+/* GPUMPI_TUNE_HOST_DIRECT: how page-locked host buffers reach the kernel.  1 = read and written in place
+ * by the kernel through their device alias (every byte crosses the host link once; the STAGED variants
+ * then run as DIRECT); 0 = staged through device memory around the kernel.  2..4 = an Allreduce between
+ * host buffers (one call, no per-iteration times, rows 16-byte multiples) runs as column slices, one
+ * launch per slice, so inputs of later slices cross the host link while results of earlier ones cross
+ * back: 2 = both directions by 2D copies through device staging, 3 (default) = page-locked inputs read in
+ * place and results copied back, 4 = inputs copied and page-locked results written in place.  Every
+ * element is folded as in one launch.  Other calls treat 2..4 as 1. */
 #define GPUMPI_TUNE_HOST_DIRECT 8
+/* GPUMPI_TUNE_HOST_SLICE: column slice of the sliced host-buffer Allreduce, bytes per rank (0 = auto:
+ * 256 MiB per slice over all ranks, at least 128 KiB per rank; rounded up to 256 bytes, at most 64
+ * slices; a call that would take one slice runs as one launch). */
+#define GPUMPI_TUNE_HOST_SLICE 10
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Launcher of a converted program (the reference's gpu_main): argv holds the program's arguments, then
  * optionally `---gpumpi` and the run's options (gpumpi_parse_args); creates the world, runs `program` on

@@ -99,6 +99,41 @@ def test_pinned_host_buffers_in_place_and_staged(gpulib, oracle):
                 assert np.array_equal(outv.numpy(), ref_v), (direct, v)
 
 
+@pytest.mark.parametrize("mode", [2, 3, 4])
+def test_sliced_host_allreduce_matches_oracle(gpulib, oracle, mode):
+    """An Allreduce between host buffers cut into column slices (TUNE_HOST_DIRECT 2..4, one launch per
+    slice, copies of later slices overlapping the folds of earlier ones) is bit-exact with the oracle:
+    page-locked and pageable buffers, a ragged last slice, floating point in the canonical order."""
+    n = 64
+    cases = [(20000, 12, 2, np.float32), (9000, 13, 2, np.float64), (12343, 2, 0, np.int32)]
+    with gpulib.World(n, timeout_s=10.0) as w:
+        w.set_tuning(gpulib.TUNE_HOST_DIRECT, mode)
+        w.set_tuning(gpulib.TUNE_HOST_SLICE, 16 << 10)
+        assert w.get_tuning(gpulib.TUNE_HOST_DIRECT) == mode
+        for count, dt, op, npdt in cases:
+            count -= count % (16 // np.dtype(npdt).itemsize)     # rows 16-byte aligned: the sliced path
+            x = make_input(oracle, n, count, npdt, 40 + count)
+            ref = oracle.allreduce(x, dt, op)
+            for pinned in (True, False):
+                hx = torch.from_numpy(x)
+                out = torch.zeros_like(hx)
+                if pinned:
+                    hx, out = hx.pin_memory(), out.pin_memory()
+                for _ in range(2):
+                    out.zero_()
+                    w.allreduce(hx.numpy(), out.numpy(), count, dt, op)
+                    assert np.array_equal(out.numpy().view(np.uint8), ref.view(np.uint8)), (count, dt, pinned)
+        # a rank's error reaches the caller through the slices' records: bitwise AND is illegal on floats
+        x = torch.from_numpy(make_input(oracle, n, 8192, np.float32, 3)).pin_memory()
+        out = torch.zeros_like(x).pin_memory()
+        with pytest.raises(gpulib.GpumpiError) as e:
+            w.allreduce(x.numpy(), out.numpy(), 8192, 12, gpulib.OP_BAND)
+        w.set_tuning(gpulib.TUNE_HOST_DIRECT, 1)
+        with pytest.raises(gpulib.GpumpiError) as e1:
+            w.allreduce(x.numpy(), out.numpy(), 8192, 12, gpulib.OP_BAND)
+        assert e.value.code == e1.value.code
+
+
 def test_allreduce_variants_agree(gpulib, oracle):
     n, count = 64, 1 << 14
     x = make_input(oracle, n, count, np.float32, 9)
