@@ -5,6 +5,8 @@
 // Compiled only by the program builder (build.py --program), together with the runtime's objects.
 #include "rt_kernel.cuh"
 
+#include <cstdio>
+
 #include "gpumpi.h"
 
 extern __device__ int __gpu_main(int argc, char* argv[]);
@@ -20,4 +22,21 @@ extern const gpumpi_prog_entry g_user_programs[] = {
 };
 extern const int g_num_user_programs = 1;
 
-int main(int argc, char** argv) { return gpumpi_main(argc, argv, GPUMPI_P_USER); }
+// A program written out by the source converter (gpumpi/converter.py) holds its globals in arrays of one
+// element per rank and records their length here; hand-written programs define nothing.
+extern "C" const int gpumpi_program_max_ranks __attribute__((weak));
+
+int main(int argc, char** argv) {
+    if (&gpumpi_program_max_ranks != nullptr) {
+        gpumpi_config cfg;
+        gpumpi_config_init(&cfg);
+        gpumpi_parse_args(argc, argv, &cfg);
+        if (cfg.nranks > gpumpi_program_max_ranks) {
+            fprintf(stderr, "gpumpi: %d ranks requested, but the program was converted for at most %d "
+                            "(its per-rank globals hold that many; convert it with GPU_MPI_MAX_RANKS raised)\n",
+                    cfg.nranks, gpumpi_program_max_ranks);
+            return 1;
+        }
+    }
+    return gpumpi_main(argc, argv, GPUMPI_P_USER);
+}

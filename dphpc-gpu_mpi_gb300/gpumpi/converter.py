@@ -1,0 +1,776 @@
+"""Source converter: turns a C MPI program into code that runs with one MPI rank per thread block.
+
+The reference project does this with a clang tool (source_converter/converter.cpp).  Neither this
+machine nor the GPU machine has clang or LLVM, so this module does the same rewrites over a C token
+stream, with a scope-aware pass over function bodies instead of an AST:
+
+* every function declaration and definition gets `__device__` (converter.cpp:49-75);
+* `main` becomes `__gpu_main(int argc, char** argv)`, `return 0;` is made explicit at its end (C99 main
+  returns 0 when it falls off its end; `__gpu_main` is an ordinary function), and after it come
+  `__device__ int __gpu_max_threads()` (converter.cpp:52-64) and a host constant the launcher reads to
+  refuse more ranks than the per-rank arrays hold;
+* old-style (K&R) parameter lists become prototype parameter lists (converter.cpp:77-108);
+* a variable with static storage (file scope, `extern`, or `static` inside a function) becomes an array
+  with one element per rank: `__device__ T name[MAX_RANKS]` with its C initializer repeated for every
+  rank (converter.cpp:118-144), and every reference to it becomes `__gpu_global(name)`, the calling
+  rank's element (converter.cpp:145-164) -- in function bodies, honouring local declarations and
+  parameters that shadow it, and in `#define` bodies;
+* results of malloc/calloc/realloc stored into typed pointers get an explicit cast, the implicit
+  `void*` conversion being invalid in CUDA C++ (the reference casts every implicit bit cast,
+  converter.cpp:112-116);
+* identifiers that are C++ keywords (`class`, `new`, `this`, ...) get the prefix `__decl_`
+  (converter.cpp:166-171 renames `class`);
+* `#include` lines: <mpi.h> / "mpi.h" -> <mpi.h.cuh>, <stdio.h> -> <gpumpi_stdio.h.cuh> (files and
+  streams through the host channel), <stdlib.h> / <string.h> -> <gpumpi_libc.h.cuh>; headers of the
+  project are converted too and included as `name.h.cuh` (the reference's gpumpicc.py renames the same
+  way).
+
+Limits (as for the reference's tool, plus those of working on tokens): a global initialised from another
+global's value, or a char array sized by its string initializer, does not compile after conversion;
+macros are rewritten where they are defined, so a macro whose body names a global is rewritten for every
+use; block-scope function prototypes are left alone; the program is expected to be C (C++ classes are
+not converted).  Output files: `x.c` -> `x.cu`, a project header `y.h` -> `y.h.cuh`.
+"""
+from __future__ import annotations
+
+import os
+import re
+from dataclasses import dataclass, field
+from pathlib import Path
+
+MAX_RANKS_ENV = "GPU_MPI_MAX_RANKS"   # the reference's variables (converter.cpp:24-25)
+PROJECT_ENV = "GPU_MPI_PROJECT"
+DEFAULT_MAX_RANKS = 1024
+
+
+class ConversionError(Exception):
+    pass
+
+
+def max_ranks_from_env() -> int:
+    v = os.environ.get(MAX_RANKS_ENV)
+    if v is None:
+        return DEFAULT_MAX_RANKS
+    try:
+        n = int(v)
+    except ValueError:
+        n = 0
+    if n <= 0:
+        raise ConversionError(f"{MAX_RANKS_ENV} should contain a positive number of ranks")
+    return n
+
+
+# ------------------------------------------------------------------------------------------------
+# tokens
+# ------------------------------------------------------------------------------------------------
+_TOKEN = re.compile(r"""
+  (?P<nl>\n)
+| (?P<ws>(?:[ \t\r\f\v]|\\\n)+)
+| (?P<comment>//(?:[^\n\\]|\\.)*|/\*.*?\*/)
+| (?P<str>(?:u8|[uUL])?"(?:\\.|[^"\\\n])*")
+| (?P<chr>(?:u8|[uUL])?'(?:\\.|[^'\\\n])*')
+| (?P<num>\.?[0-9](?:[eEpP][+-]|[0-9A-Za-z_.])*)
+| (?P<id>[A-Za-z_][A-Za-z_0-9]*)
+| (?P<op>\.\.\.|<<=|>>=|->|\+\+|--|<<|>>|<=|>=|==|!=|&&|\|\||[-+*/%&|^]=|\#\#|[][{}();,.<>+\-*/%&|^!~?:=\#])
+| (?P<other>.)
+""", re.S | re.X)
+
+STORAGE = {"typedef", "extern", "static", "auto", "register", "_Thread_local", "inline", "__inline",
+           "__inline__", "_Noreturn"}
+QUALS = {"const", "volatile", "restrict", "__restrict", "__restrict__", "_Atomic"}
+BASE = {"void", "char", "short", "int", "long", "float", "double", "signed", "unsigned", "_Bool", "_Complex",
+        "__int128"}
+TAGS = {"struct", "union", "enum"}
+ATTRS = {"__attribute__", "__declspec", "__extension__", "__asm__", "asm"}
+C_KEYWORDS = STORAGE | QUALS | BASE | TAGS | {
+    "break", "case", "continue", "default", "do", "else", "for", "goto", "if", "return", "sizeof", "switch",
+    "while", "_Alignas", "_Alignof", "_Generic", "_Static_assert"}
+CXX_KEYWORDS = {"class", "new", "delete", "this", "template", "typename", "namespace", "operator", "private",
+                "protected", "public", "virtual", "friend", "explicit", "mutable", "catch", "try", "throw",
+                "using", "nullptr", "export", "reinterpret_cast", "static_cast", "dynamic_cast",
+                "const_cast", "typeid", "decltype", "constexpr", "noexcept", "thread_local", "alignof",
+                "alignas", "char16_t", "char32_t", "static_assert"}
+KNOWN_TYPES = {
+    "MPI_Comm", "MPI_Datatype", "MPI_Status", "MPI_Request", "MPI_Op", "MPI_Group", "MPI_Aint", "MPI_Offset",
+    "MPI_File", "MPI_Info", "MPI_Fint", "MPI_Errhandler", "MPI_User_function", "MPI_Copy_function",
+    "MPI_Delete_function", "FILE", "va_list", "bool", "wchar_t", "div_t", "ldiv_t", "lldiv_t", "fpos_t"}
+ALLOCATORS = {"malloc", "calloc", "realloc", "aligned_alloc"}
+INCLUDE_MAP = {"mpi.h": "mpi.h.cuh", "stdio.h": "gpumpi_stdio.h.cuh", "stdlib.h": "gpumpi_libc.h.cuh",
+               "string.h": "gpumpi_libc.h.cuh"}
+PRELUDE = ("#define GPUMPI_STDIO_NAMES\n#define GPUMPI_LIBC_NAMES\n#include <gpumpi_libc.h.cuh>\n"
+           "#include <mpi.h.cuh>\n#include <gpumpi_stdio.h.cuh>\n")
+
+
+@dataclass
+class Tok:
+    kind: str
+    text: str
+
+
+def tokenize(src: str) -> list[Tok]:
+    """Lossless token list; a preprocessor directive (from a line-initial '#' to the end of its logical
+    line) is one token of kind 'dir'."""
+    raw = [Tok(m.lastgroup, m.group()) for m in _TOKEN.finditer(src)]
+    out: list[Tok] = []
+    line_start = True
+    i = 0
+    while i < len(raw):
+        t = raw[i]
+        if line_start and t.kind == "op" and t.text == "#":
+            j = i
+            while j < len(raw) and raw[j].kind != "nl":
+                j += 1
+            out.append(Tok("dir", "".join(x.text for x in raw[i:j])))
+            i = j
+            continue
+        if t.kind == "nl":
+            line_start = True
+        elif t.kind not in ("ws", "comment"):
+            line_start = False
+        out.append(t)
+        i += 1
+    return out
+
+
+def is_sig(t: Tok) -> bool:
+    return t.kind not in ("ws", "nl", "comment", "dir")
+
+
+# ------------------------------------------------------------------------------------------------
+# declarations
+# ------------------------------------------------------------------------------------------------
+@dataclass
+class Declarator:
+    start: int            # sig index range [start, end) of the declarator, initializer included
+    end: int
+    name: int | None      # sig index of the declared identifier
+    is_function: bool
+    init: int | None      # sig index of the first initializer token
+    stars: int
+    brackets: int
+
+
+@dataclass
+class Declaration:
+    start: int            # sig index of the first specifier
+    spec_end: int         # sig index after the specifiers
+    storage: set
+    decls: list
+    type_text: str        # specifiers without storage classes (for casts)
+
+
+class Converter:
+    def __init__(self, src: str, max_ranks: int, extra_types=(), is_main_file=True, globals_in=None,
+                 include_map=None):
+        self.toks = tokenize(src)
+        self.sig = [i for i, t in enumerate(self.toks) if is_sig(t)]
+        self.max_ranks = max_ranks
+        self.types = set(KNOWN_TYPES) | set(extra_types)
+        self.is_main_file = is_main_file
+        self.globals: dict[str, tuple] = dict(globals_in or {})   # name -> (type_text, stars, brackets)
+        self.include_map = include_map or {}
+        self.prefix: dict[int, str] = {}
+        self.suffix: dict[int, str] = {}
+        self.repl: dict[int, str] = {}
+        self.match = self._match_brackets()
+        self.saw_main = False
+
+    # ---- token helpers (k = sig index) ----
+    def t(self, k: int) -> str:
+        return self.toks[self.sig[k]].text if 0 <= k < len(self.sig) else ""
+
+    def kind(self, k: int) -> str:
+        return self.toks[self.sig[k]].kind if 0 <= k < len(self.sig) else ""
+
+    def is_id(self, k: int) -> bool:
+        return self.kind(k) == "id"
+
+    def _match_brackets(self) -> dict:
+        m, stack = {}, []
+        pairs = {")": "(", "]": "[", "}": "{"}
+        for k in range(len(self.sig)):
+            x = self.t(k)
+            if self.kind(k) != "op":
+                continue
+            if x in "([{":
+                stack.append(k)
+            elif x in ")]}":
+                if not stack or self.t(stack[-1]) != pairs[x]:
+                    raise ConversionError(f"unbalanced '{x}' near token {k}")
+                o = stack.pop()
+                m[o], m[k] = k, o
+        if stack:
+            raise ConversionError(f"unclosed '{self.t(stack[-1])}'")
+        return m
+
+    def add_prefix(self, k: int, s: str):
+        i = self.sig[k]
+        self.prefix[i] = self.prefix.get(i, "") + s
+
+    def add_suffix(self, k: int, s: str):
+        i = self.sig[k]
+        self.suffix[i] = s + self.suffix.get(i, "")
+
+    def replace(self, k: int, s: str):
+        self.repl[self.sig[k]] = s
+
+    def raw_text(self, a: int, b: int) -> str:
+        """Source text from sig token a through sig token b (inclusive), everything between included."""
+        return "".join(t.text for t in self.toks[self.sig[a]:self.sig[b] + 1])
+
+    def is_type_name(self, name: str) -> bool:
+        return name in self.types or (name.endswith("_t") and name not in self.globals)
+
+    # ---- declaration parsing over [a, b) ----
+    def parse_declaration(self, a: int, b: int) -> Declaration:
+        k = a
+        storage, has_base, type_parts = set(), False, []
+        while k < b:
+            x = self.t(k)
+            if x in STORAGE:
+                storage.add(x)
+                k += 1
+            elif x in QUALS or x in BASE:
+                has_base = has_base or x in BASE
+                type_parts.append(x)
+                k += 1
+            elif x in TAGS:
+                has_base = True
+                j = k + 1
+                if self.is_id(j):
+                    j += 1
+                if self.t(j) == "{":
+                    j = self.match[j] + 1
+                type_parts.append(self.raw_text(k, j - 1))
+                k = j
+            elif x in ATTRS:
+                k += 1
+                if self.t(k) == "(":
+                    k = self.match[k] + 1
+            elif self.is_id(k) and not has_base and self.is_type_name(x):
+                has_base = True
+                type_parts.append(x)
+                k += 1
+            else:
+                break
+        spec_end = k
+        decls = []
+        s = k
+        while s < b:
+            e, init = s, None
+            while e < b and self.t(e) != ",":
+                x = self.t(e)
+                if x == "=" and init is None:
+                    init = e + 1
+                if x in ("(", "[", "{"):
+                    e = self.match[e]
+                e += 1
+            decls.append(self._declarator(s, e, init))
+            s = e + 1
+        return Declaration(a, spec_end, storage, decls, " ".join(type_parts))
+
+    def _declarator(self, s: int, e: int, init) -> Declarator:
+        stop = (init - 1) if init is not None else e
+        name, stars, k = None, 0, s
+        while k < stop:
+            x = self.t(k)
+            if x == "*":
+                stars += 1
+            elif x in ATTRS:
+                if self.t(k + 1) == "(":
+                    k = self.match[k + 1]
+            elif self.is_id(k) and x not in QUALS:
+                name = k
+                break
+            k += 1
+        is_fn, brackets = False, 0
+        if name is not None:
+            j = name + 1
+            is_fn = self.t(j) == "("
+            while j < stop and self.t(j) == "[":
+                brackets += 1
+                j = self.match[j] + 1
+        return Declarator(s, e, name, is_fn, init, stars, brackets)
+
+    def starts_declaration(self, k: int) -> bool:
+        x = self.t(k)
+        if x in STORAGE or x in QUALS or x in BASE or x in TAGS:
+            return True
+        if self.is_id(k) and self.is_type_name(x):
+            return self.is_id(k + 1) or self.t(k + 1) == "*"
+        return False
+
+    # ---- the conversion ----
+    def run(self) -> str:
+        self._collect_typedefs_and_globals()
+        k = 0
+        n = len(self.sig)
+        while k < n:
+            k = self._top_level_item(k)
+        self._directives()
+        self._rename_cxx_keywords()
+        return self._emit()
+
+    def _collect_typedefs_and_globals(self):
+        """First pass: typedef names (for parsing) and the file-scope variables (for references that
+        come before a later tentative definition, and for macro bodies)."""
+        k, n = 0, len(self.sig)
+        while k < n:
+            end, body = self._item_extent(k)
+            if body is None and end > k:
+                d = self.parse_declaration(k, end)
+                for dd in d.decls:
+                    if dd.name is None:
+                        continue
+                    if "typedef" in d.storage:
+                        self.types.add(self.t(dd.name))
+                    elif not dd.is_function:
+                        self.globals[self.t(dd.name)] = (d.type_text, dd.stars, dd.brackets)
+            k = (body[1] + 1) if body else end + 1
+
+    def _item_extent(self, k: int):
+        """Extent of the top-level item starting at sig index k: (index of its ';' or of the token after
+        a function body, (body_open, body_close) or None)."""
+        n = len(self.sig)
+        j, seen_eq, prev = k, False, ""
+        while j < n:
+            x = self.t(j)
+            if x in ("(", "["):
+                j = self.match[j] + 1
+                prev = ")" if x == "(" else "]"
+                continue
+            if x == "{":
+                p1, p2 = self.t(j - 1), self.t(j - 2)
+                if seen_eq or p1 in TAGS or (self.is_id(j - 1) and p2 in TAGS):
+                    j = self.match[j] + 1
+                    prev = "}"
+                    continue
+                return j, (j, self.match[j])
+            if x == "=":
+                seen_eq = True
+            elif x == ",":
+                seen_eq = False
+            elif x == ";":
+                # an old-style definition continues with its parameter declarations up to the body
+                if self._knr_header(k, j):
+                    j2 = j
+                    while j2 < n and self.t(j2) != "{":
+                        if self.t(j2) in ("(", "["):
+                            j2 = self.match[j2]
+                        j2 += 1
+                    if j2 < n:
+                        return j2, (j2, self.match[j2])
+                return j, None
+            prev = x
+            j += 1
+        return j, None
+
+    def _knr_header(self, k: int, semi: int) -> bool:
+        """Does [k, semi) hold `... name ( ident, ident ) decl-specifiers ...` (an old-style definition's
+        header followed by its first parameter declaration)?"""
+        j = k
+        while j < semi:
+            if self.t(j) == "(" and self.is_id(j - 1):
+                close = self.match[j]
+                inner = list(range(j + 1, close))
+                if inner and all((self.is_id(q) and self.t(q) not in C_KEYWORDS and not self.is_type_name(self.t(q)))
+                                 or self.t(q) == "," for q in inner):
+                    nxt = close + 1
+                    return nxt < semi and self.starts_declaration(nxt)
+                j = close
+            j += 1
+        return False
+
+    def _top_level_item(self, k: int) -> int:
+        end, body = self._item_extent(k)
+        if body is None:
+            if end > k:
+                self._global_declaration(k, end)
+            return end + 1
+        open_, close = body
+        self._function_definition(k, open_, close)
+        return close + 1
+
+    def _global_declaration(self, a: int, b: int):
+        d = self.parse_declaration(a, b)
+        if "typedef" in d.storage or not d.decls:
+            return
+        if any(dd.name is not None for dd in d.decls):
+            self.add_prefix(a, "__device__ ")
+        for dd in d.decls:
+            if dd.name is None or dd.is_function:
+                continue
+            self._make_per_rank(d, dd)
+
+    def _make_per_rank(self, d: Declaration, dd: Declarator):
+        name = self.t(dd.name)
+        self.add_suffix(dd.name, f"[{self.max_ranks}]")
+        if dd.init is not None:
+            last = dd.end - 1
+            text = self.raw_text(dd.init, last).strip()
+            if self.t(dd.init) == "{" and self.match[dd.init] != last:
+                raise ConversionError(f"initializer of '{name}' is not a single braced list")
+            self.replace(dd.init, "{" + ", ".join([text] * self.max_ranks) + "}")
+            for q in range(dd.init + 1, last + 1):
+                self.replace(q, "")
+            # drop the layout between the removed tokens (their text is inside the replacement)
+            for i in range(self.sig[dd.init] + 1, self.sig[last] + 1):
+                if not is_sig(self.toks[i]):
+                    self.repl[i] = ""
+
+    def _function_definition(self, a: int, open_: int, close: int):
+        # declarator: find the function's name (the identifier before the '(' of its parameter list)
+        d = self.parse_declaration(a, open_)
+        fn = next((dd for dd in d.decls if dd.name is not None and dd.is_function), None)
+        if fn is None:
+            raise ConversionError(f"cannot find the name of the function defined before token {open_}")
+        self.add_prefix(a, "__device__ ")
+        name_k = fn.name
+        lp = name_k + 1
+        rp = self.match[lp]
+        params = self._parameters(lp, rp, open_)   # name -> (type, stars, brackets) or None
+        if self.t(name_k) == "main":
+            self.saw_main = True
+            self.replace(name_k, "__gpu_main")
+            if d.type_text.split() and d.type_text.split()[-1] != "int":
+                raise ConversionError("main must return int")
+            if len(params) == 0:
+                self.replace(lp, "(int argc, char** argv")
+                for q in range(lp + 1, rp):
+                    self.replace(q, "")
+            self.add_prefix(close, "    return 0;\n")
+            self.add_suffix(close, f"\n__device__ int __gpu_max_threads() {{ return {self.max_ranks}; }}\n"
+                                   f"extern \"C\" const int gpumpi_program_max_ranks = {self.max_ranks};")
+        scope = {p: ("local", info) for p, info in params.items()}
+        self._body(open_ + 1, close, [scope])
+
+    def _parameters(self, lp: int, rp: int, body_open: int) -> dict:
+        """The parameters, name -> (type text, stars, brackets); rewrites an old-style list (identifiers,
+        then declarations before the body) into a prototype list."""
+        inner = list(range(lp + 1, rp))
+        if not inner or (len(inner) == 1 and self.t(inner[0]) == "void"):
+            return {}
+        if rp + 1 < body_open:   # old-style: declarations between ')' and '{'
+            names = [self.t(q) for q in inner if self.is_id(q)]
+            typed, infos = {}, {}
+            k = rp + 1
+            while k < body_open:
+                e = k
+                while e < body_open and self.t(e) != ";":
+                    e += 1
+                d = self.parse_declaration(k, e)
+                spec = " ".join(x for x in self.raw_text(k, d.spec_end - 1).split() if x != "register")
+                for dd in d.decls:
+                    if dd.name is not None:
+                        typed[self.t(dd.name)] = spec + " " + self.raw_text(dd.start, dd.end - 1).strip()
+                        infos[self.t(dd.name)] = (d.type_text, dd.stars, dd.brackets)
+                k = e + 1
+            self.replace(lp, "(" + ", ".join(typed.get(nm, "int " + nm) for nm in names))
+            for q in range(lp + 1, rp):
+                self.replace(q, "")
+            for q in range(rp + 1, body_open):
+                self.replace(q, "")
+            for i in range(self.sig[rp] + 1, self.sig[body_open]):
+                if not is_sig(self.toks[i]):
+                    self.repl[i] = ""
+            self.add_suffix(rp, " ")
+            return {nm: infos.get(nm, ("int", 0, 0)) for nm in names}
+        names, s = {}, lp + 1
+        while s < rp:
+            e = s
+            while e < rp and self.t(e) != ",":
+                if self.t(e) in ("(", "["):
+                    e = self.match[e]
+                e += 1
+            if self.t(s) != "...":
+                d = self.parse_declaration(s, e)
+                for dd in d.decls:
+                    if dd.name is not None:
+                        names[self.t(dd.name)] = (d.type_text, dd.stars, dd.brackets)
+            s = e + 1
+        return names
+
+    # ---- function bodies ----
+    def _lookup(self, scopes: list, name: str):
+        for sc in reversed(scopes):
+            if name in sc:
+                return sc[name]
+        if name in self.globals:
+            return ("global", self.globals[name])
+        return None
+
+    def _body(self, a: int, b: int, scopes: list):
+        """Statements in sig range [a, b) of a block whose scopes are `scopes` (innermost last)."""
+        k = a
+        while k < b:
+            k = self._statement(k, b, scopes)
+
+    def _statement(self, k: int, b: int, scopes: list) -> int:
+        x = self.t(k)
+        if x == "{":
+            close = self.match[k]
+            scopes.append({})
+            self._body(k + 1, close, scopes)
+            scopes.pop()
+            return close + 1
+        if x == ";":
+            return k + 1
+        if x in ("if", "while", "switch") and self.t(k + 1) == "(":
+            close = self.match[k + 1]
+            self._expr(k + 2, close, scopes)
+            j = self._statement(close + 1, b, scopes)
+            if x == "if" and self.t(j) == "else":
+                j = self._statement(j + 1, b, scopes)
+            return j
+        if x == "for" and self.t(k + 1) == "(":
+            close = self.match[k + 1]
+            scopes.append({})
+            s = k + 2
+            first = s
+            while first < close and self.t(first) != ";":
+                if self.t(first) in ("(", "[", "{"):
+                    first = self.match[first]
+                first += 1
+            if self.starts_declaration(s):
+                self._local_declaration(s, first, scopes)
+            else:
+                self._expr(s, first, scopes)
+            self._expr(first + 1, close, scopes)
+            j = self._statement(close + 1, b, scopes)
+            scopes.pop()
+            return j
+        if x == "do":
+            j = self._statement(k + 1, b, scopes)
+            if self.t(j) == "while" and self.t(j + 1) == "(":
+                close = self.match[j + 1]
+                self._expr(j + 2, close, scopes)
+                return close + 2
+            return j
+        if x in ("case", "default"):
+            j = k + 1
+            while j < b and self.t(j) != ":":
+                if self.t(j) in ("(", "["):
+                    j = self.match[j]
+                j += 1
+            self._expr(k + 1, j, scopes)
+            return j + 1
+        if self.is_id(k) and self.t(k + 1) == ":" and x not in C_KEYWORDS:   # label
+            return k + 2
+        if x == "goto":
+            return self._skip_to_semicolon(k, b) + 1
+        end = self._skip_to_semicolon(k, b)
+        if self.starts_declaration(k):
+            self._local_declaration(k, end, scopes)
+        else:
+            self._expr(k, end, scopes)
+            self._cast_assignment(k, end, scopes)
+        return end + 1
+
+    def _skip_to_semicolon(self, k: int, b: int) -> int:
+        while k < b and self.t(k) != ";":
+            if self.t(k) in ("(", "[", "{"):
+                k = self.match[k]
+            k += 1
+        return k
+
+    def _local_declaration(self, a: int, b: int, scopes: list):
+        d = self.parse_declaration(a, b)
+        if "typedef" in d.storage:
+            for dd in d.decls:
+                if dd.name is not None:
+                    self.types.add(self.t(dd.name))
+            return
+        is_static = "static" in d.storage or "extern" in d.storage
+        for dd in d.decls:
+            if dd.name is None:
+                continue
+            nm = self.t(dd.name)
+            if dd.is_function:
+                scopes[-1][nm] = ("local", None)
+                continue
+            info = (d.type_text, dd.stars, dd.brackets)
+            # the initializer is evaluated in the scope where the name is already declared (C rules); a
+            # static's initializer is a constant
+            if dd.init is not None and not is_static:
+                self._expr(dd.init, dd.end, scopes)
+                self._cast_initializer(d, dd)
+            if is_static:
+                if "extern" in d.storage:
+                    scopes[-1][nm] = ("global", self.globals.get(nm, info))
+                else:
+                    self._make_per_rank(d, dd)
+                    scopes[-1][nm] = ("static", info)
+            else:
+                scopes[-1][nm] = ("local", info)
+            # array bounds inside the declarator
+            q = dd.name + 1
+            while q < (dd.init - 1 if dd.init is not None else dd.end) and self.t(q) == "[":
+                self._expr(q + 1, self.match[q], scopes)
+                q = self.match[q] + 1
+
+    def _expr(self, a: int, b: int, scopes: list):
+        """Wraps references to per-rank variables among the identifiers of sig range [a, b)."""
+        for k in range(a, b):
+            if not self.is_id(k):
+                continue
+            prev = self.t(k - 1)
+            if prev in (".", "->") or prev in TAGS or prev == "goto":
+                continue
+            r = self._lookup(scopes, self.t(k))
+            if r is not None and r[0] in ("global", "static"):
+                self._wrap(k)
+
+    def _wrap(self, k: int):
+        self.add_prefix(k, "__gpu_global(")
+        self.add_suffix(k, ")")
+
+    def _cast_type(self, type_text: str, stars: int) -> str:
+        return f"({type_text} {'*' * stars})".replace(" )", ")")
+
+    def _cast_initializer(self, d: Declaration, dd: Declarator):
+        if dd.init is None or dd.stars == 0 or dd.brackets:
+            return
+        if self.t(dd.init) in ALLOCATORS and self.t(dd.init + 1) == "(":
+            self.add_prefix(dd.init, self._cast_type(d.type_text, dd.stars))
+
+    def _cast_assignment(self, a: int, b: int, scopes: list):
+        """`p = malloc(...)` or `p[i] = malloc(...)` with p's declared pointer type known: an explicit cast."""
+        if not self.is_id(a):
+            return
+        k, subs = a + 1, 0
+        while k < b and self.t(k) == "[":
+            subs += 1
+            k = self.match[k] + 1
+        if self.t(k) != "=" or not (self.t(k + 1) in ALLOCATORS and self.t(k + 2) == "("):
+            return
+        r = self._lookup(scopes, self.t(a))
+        if r is None or r[1] is None:
+            return
+        type_text, stars, brackets = r[1]
+        if subs < brackets:            # still an array
+            return
+        left = stars - (subs - brackets)
+        if left <= 0:
+            return
+        self.add_prefix(k + 1, self._cast_type(type_text, left))
+
+    # ---- directives and keywords ----
+    def _directives(self):
+        for i, t in enumerate(self.toks):
+            if t.kind != "dir":
+                continue
+            m = re.match(r'(\s*#\s*include\s*)([<"])([^>"]+)([>"])(.*)$', t.text, re.S)
+            if m:
+                hdr = m.group(3).strip()
+                new = self.include_map.get(hdr)
+                if new is not None:
+                    self.repl[i] = f'{m.group(1)}"{new}"{m.group(5)}'
+                elif hdr in INCLUDE_MAP:
+                    self.repl[i] = f"{m.group(1)}<{INCLUDE_MAP[hdr]}>{m.group(5)}"
+                continue
+            m = re.match(r"(\s*#\s*define\s+)([A-Za-z_]\w*)(\([^)]*\))?(.*)$", t.text, re.S)
+            if m:
+                params = set(re.findall(r"[A-Za-z_]\w*", m.group(3) or ""))
+                body = tokenize(m.group(4))
+                out, prev = [], ""
+                for bt in body:
+                    txt = bt.text
+                    if bt.kind == "id" and txt in self.globals and txt not in params and prev not in (".", "->", "#"):
+                        txt = f"__gpu_global({txt})"
+                    elif bt.kind == "id" and txt in CXX_KEYWORDS:
+                        txt = "__decl_" + txt
+                    out.append(txt)
+                    if is_sig(bt):
+                        prev = bt.text
+                self.repl[i] = m.group(1) + m.group(2) + (m.group(3) or "") + "".join(out)
+
+    def _rename_cxx_keywords(self):
+        for i in self.sig:
+            t = self.toks[i]
+            if t.kind == "id" and t.text in CXX_KEYWORDS:
+                self.repl[i] = "__decl_" + self.repl.get(i, t.text)
+
+    def _emit(self) -> str:
+        parts = [PRELUDE]
+        for i, t in enumerate(self.toks):
+            parts.append(self.prefix.get(i, ""))
+            parts.append(self.repl.get(i, t.text))
+            parts.append(self.suffix.get(i, ""))
+        return "".join(parts)
+
+
+# ------------------------------------------------------------------------------------------------
+# files
+# ------------------------------------------------------------------------------------------------
+_INCLUDE = re.compile(r'^\s*#\s*include\s*"([^"]+)"', re.M)
+
+
+def convert_source(src: str, max_ranks: int = DEFAULT_MAX_RANKS, extra_types=(), include_map=None,
+                   globals_in=None) -> str:
+    """Converts one translation unit's text; see the module docstring for the rewrites."""
+    return Converter(src, max_ranks, extra_types, globals_in=globals_in, include_map=include_map).run()
+
+
+def _project_headers(path: Path, project: Path, include_dirs, seen: dict):
+    """Project headers a file includes with "...", recursively: {header path: include text}."""
+    text = path.read_text()
+    for name in _INCLUDE.findall(text):
+        for d in [path.parent, *include_dirs]:
+            cand = (Path(d) / name).resolve()
+            if cand.is_file() and str(cand).startswith(str(project)) and cand.name != "mpi.h":
+                if cand not in seen:
+                    seen[cand] = name
+                    _project_headers(cand, project, include_dirs, seen)
+                break
+    return seen
+
+
+def convert_files(sources, out_dir, max_ranks: int | None = None, include_dirs=(), project=None,
+                  extra_types=()) -> list:
+    """Converts C sources (and the project headers they include) into out_dir: x.c -> x.cu, y.h ->
+    y.h.cuh (the reference's gpumpicc.py naming).  Returns the converted sources' paths."""
+    max_ranks = max_ranks or max_ranks_from_env()
+    out_dir = Path(out_dir)
+    out_dir.mkdir(parents=True, exist_ok=True)
+    srcs = [Path(s).resolve() for s in sources]
+    project = Path(project or os.environ.get(PROJECT_ENV) or srcs[0].parent).resolve()
+    converted = []
+    for src in srcs:
+        headers = _project_headers(src, project, [Path(d).resolve() for d in include_dirs], {})
+        imap = {name: Path(name).name + ".cuh" for name in headers.values()}
+        # typedef names and file-scope variables declared in the project's headers
+        types, globs = set(extra_types), {}
+        for h in headers:
+            c = Converter(h.read_text(), max_ranks, types, include_map=imap)
+            c._collect_typedefs_and_globals()
+            types |= c.types
+            globs.update(c.globals)
+        for h in headers:
+            text = Converter(h.read_text(), max_ranks, types, include_map=imap, globals_in=globs).run()
+            (out_dir / (h.name + ".cuh")).write_text(text)
+        out = out_dir / (src.stem + ".cu")
+        out.write_text(Converter(src.read_text(), max_ranks, types, include_map=imap, globals_in=globs).run())
+        converted.append(out)
+    return converted
+
+
+def main(argv=None) -> int:
+    import argparse
+    ap = argparse.ArgumentParser(description="convert C MPI sources to block-rank device code")
+    ap.add_argument("sources", nargs="+")
+    ap.add_argument("-o", "--out-dir", default=".")
+    ap.add_argument("-I", dest="include_dirs", action="append", default=[])
+    ap.add_argument("--max-ranks", type=int, default=None)
+    ap.add_argument("--type", dest="types", action="append", default=[], help="extra typedef name")
+    a = ap.parse_args(argv)
+    try:
+        for p in convert_files(a.sources, a.out_dir, a.max_ranks, a.include_dirs, extra_types=a.types):
+            print(p)
+    except ConversionError as e:
+        print(f"gpumpi converter: {e}")
+        return 1
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -1,0 +1,149 @@
+"""CPU tests of the source converter (gpumpi/converter.py), the counterpart of the reference's clang tool
+(source_converter/converter.cpp): each rewrite on small inputs, and the converted test programs
+compiling for sm_103a (nvcc cross-compiles without a GPU)."""
+import re
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from gpumpi import converter as cv
+
+ROOT = Path(__file__).resolve().parents[1]
+PROGS = ROOT / "tests" / "programs" / "c"
+
+
+def conv(src: str, n: int = 4) -> str:
+    out = cv.convert_source(src, max_ranks=n)
+    assert out.startswith(cv.PRELUDE)
+    return out[len(cv.PRELUDE):]
+
+
+def squash(s: str) -> str:
+    return re.sub(r"\s+", " ", s).strip()
+
+
+def test_functions_get_device_and_main_is_renamed():
+    out = squash(conv("double f(double);\nstatic int g(void) { return 1; }\nint main() { return g(); }\n", 8))
+    assert "__device__ double f(double);" in out
+    assert "__device__ static int g(void) { return 1; }" in out
+    assert "__device__ int __gpu_main(int argc, char** argv) { return g(); return 0; }" in out
+    assert "__device__ int __gpu_max_threads() { return 8; }" in out
+    assert 'extern "C" const int gpumpi_program_max_ranks = 8;' in out
+
+
+def test_main_keeps_its_own_parameters():
+    out = squash(conv("int main(int ac, char **av) { return ac; }"))
+    assert "__device__ int __gpu_main(int ac, char **av) { return ac; return 0; }" in out
+
+
+def test_globals_become_per_rank_arrays_with_repeated_initializers():
+    out = squash(conv("int a = -1, *p, m[2][2] = {{1,2},{3,4}};\nextern int e;\nstatic char c;\n", 3))
+    assert "__device__ int a[3] = {-1, -1, -1}, *p[3], m[3][2][2] = {{{1,2},{3,4}}, {{1,2},{3,4}}, {{1,2},{3,4}}};" in out
+    assert "__device__ extern int e[3];" in out
+    assert "__device__ static char c[3];" in out
+
+
+def test_references_are_wrapped_unless_shadowed():
+    src = """int g = 1; int h[4];
+int f(int g) { return g + h[0]; }
+int k(void) { int r = g; { int h = 2; r += h; } for (int g = 0; g < 1; g++) r += g; return r + g; }
+"""
+    out = squash(conv(src))
+    assert "__device__ int f(int g) { return g + __gpu_global(h)[0]; }" in out
+    assert ("int r = __gpu_global(g); { int h = 2; r += h; } for (int g = 0; g < 1; g++) r += g; "
+            "return r + __gpu_global(g); }") in out
+
+
+def test_member_names_labels_and_tags_are_not_references():
+    src = """struct s { int g; } v; int g;
+int f(void) { struct s g2; g2.g = g; v.g = 1; goto g_end; g_end: return v.g; }
+"""
+    out = squash(conv(src))
+    assert "g2.g = __gpu_global(g); __gpu_global(v).g = 1; goto g_end; g_end: return __gpu_global(v).g;" in out
+
+
+def test_function_static_becomes_per_rank():
+    out = squash(conv("int f(void) { static int n = 5; n++; return n; }", 2))
+    assert "static int n[2] = {5, 5}; __gpu_global(n)++; return __gpu_global(n);" in out
+
+
+def test_old_style_definition_gets_a_prototype_list():
+    out = squash(conv("int f(a, b, c) double a; char *b; { return a + b[0] + c; }"))
+    assert "__device__ int f(double a, char *b, int c ) { return a + b[0] + c; }" in out
+
+
+def test_allocations_get_casts():
+    src = """typedef struct node { int v; } node;
+node *head; int **grid;
+void f(int n) { double *x = malloc(n * sizeof(double)); node *t; t = calloc(1, sizeof(node));
+  head = malloc(8); grid = malloc(8); grid[0] = malloc(4); }
+"""
+    out = squash(conv(src))
+    assert "double *x = (double *)malloc(n * sizeof(double));" in out
+    assert "t = (node *)calloc(1, sizeof(node));" in out
+    assert "__gpu_global(head) = (node *)malloc(8);" in out
+    assert "__gpu_global(grid) = (int **)malloc(8); __gpu_global(grid)[0] = (int *)malloc(4);" in out
+
+
+def test_cxx_keywords_are_renamed():
+    out = squash(conv("int f(int class) { int new = class, this = 1; return new + this; }"))
+    assert "int f(int __decl_class) { int __decl_new = __decl_class, __decl_this = 1; return __decl_new + __decl_this; }" in out
+
+
+def test_includes_and_macros():
+    src = """#include "mpi.h"
+#include <stdio.h>
+#include <stdlib.h>
+#include <math.h>
+int total;
+#define TOTAL total
+#define ADD(total, x) ((total) + (x))
+"""
+    out = conv(src)
+    assert "#include <mpi.h.cuh>" in out and "#include <gpumpi_stdio.h.cuh>" in out
+    assert "#include <gpumpi_libc.h.cuh>" in out and "#include <math.h>" in out
+    assert "#define TOTAL __gpu_global(total)" in out
+    assert "#define ADD(total, x) ((total) + (x))" in out   # a macro parameter, not the global
+
+
+def test_typedef_names_parse_as_types():
+    src = "typedef unsigned long long u64; u64 count = 3; MPI_Status st;\nint f(void) { u64 x = count; return (int)x; }"
+    out = squash(conv(src, 2))
+    assert "__device__ u64 count[2] = {3, 3}; __device__ MPI_Status st[2];" in out
+    assert "u64 x = __gpu_global(count);" in out
+
+
+def test_max_ranks_from_environment(monkeypatch):
+    monkeypatch.setenv(cv.MAX_RANKS_ENV, "16")
+    assert cv.max_ranks_from_env() == 16
+    monkeypatch.setenv(cv.MAX_RANKS_ENV, "zero")
+    with pytest.raises(cv.ConversionError):
+        cv.max_ranks_from_env()
+
+
+def test_unbalanced_input_is_an_error():
+    with pytest.raises(cv.ConversionError):
+        cv.convert_source("int f( { return 0; }")
+
+
+def test_project_headers_are_converted(tmp_path):
+    out = cv.convert_files([PROGS / "oldstyle.c", PROGS / "oldstyle_lib.c"], tmp_path, max_ranks=4)
+    assert [p.name for p in out] == ["oldstyle.cu", "oldstyle_lib.cu"]
+    hdr = (tmp_path / "oldstyle.h.cuh").read_text()
+    assert "__device__ extern int lib_calls[4];" in hdr
+    assert '#include "oldstyle.h.cuh"' in out[0].read_text()
+    assert "__device__ int lib_calls[4] = {0, 0, 0, 0};" in out[1].read_text()
+
+
+@pytest.mark.skipif(shutil.which("nvcc") is None and not Path("/usr/local/cuda/bin/nvcc").exists(),
+                    reason="no nvcc")
+@pytest.mark.parametrize("progs", [["rect_pi.c"], ["globals.c"], ["oldstyle.c", "oldstyle_lib.c"]])
+def test_converted_programs_compile_for_sm103a(tmp_path, progs):
+    import build as gbuild
+    out = cv.convert_files([PROGS / p for p in progs], tmp_path, max_ranks=64)
+    for f in out:
+        r = subprocess.run([gbuild.nvcc(), *gbuild.common_flags(), "-I", str(tmp_path), "-I", str(PROGS), "-c",
+                            str(f), "-o", str(f.with_suffix(".o"))], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-4000:]

@@ -116,3 +116,74 @@ def test_converted_pi_program_reports_through_host_streams(report_exe, ranks, n)
     assert abs(err - abs(pi - math.pi)) <= 1e-15
     secs = [l for l in r.stdout.splitlines() if l.startswith("elapsed ")]
     assert len(secs) == 1 and 0.0 <= float(secs[0].split()[1]) < 60.0
+
+
+# ---- plain C programs through gpumpicc (source converter + program builder) ----
+
+CPROGS = ROOT / "tests" / "programs" / "c"
+
+
+def gpumpicc(sources, out, max_ranks=None):
+    from gpumpi import gpumpicc as cc
+    return cc.compile_program([CPROGS / s for s in sources], out, max_ranks=max_ranks)
+
+
+@pytest.fixture(scope="module")
+def c_programs(tmp_path_factory, gpulib):
+    d = tmp_path_factory.mktemp("cprog")
+    return {"rect_pi": gpumpicc(["rect_pi.c"], d / "rect_pi"),
+            "globals": gpumpicc(["globals.c"], d / "globals"),
+            "globals8": gpumpicc(["globals.c"], d / "globals8", max_ranks=8),
+            "oldstyle": gpumpicc(["oldstyle.c", "oldstyle_lib.c"], d / "oldstyle")}
+
+
+@pytest.mark.parametrize("ranks,n", [(1, 10000), (7, 10000), (64, 100000)])
+def test_c_pi_program_runs_unchanged(c_programs, ranks, n):
+    # a classic C pi program: atoi, fabs, fprintf(stdout)/printf/fflush, MPI_Get_processor_name, MPI_Wtime
+    import math
+    r = subprocess.run([str(c_programs["rect_pi"]), str(n), "---gpumpi", "-n", str(ranks)], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    where = sorted(l for l in r.stdout.splitlines() if l.startswith("rank "))
+    assert where == sorted(f"rank {k}/{ranks} on GB300 block-rank" for k in range(ranks))
+    est = [l for l in r.stdout.splitlines() if l.startswith("pi = ")]
+    assert len(est) == 1, r.stdout
+    pi, err = (float(x) for x in est[0][len("pi = "):].replace(", error =", "").split())
+    assert abs(pi - expected_pi_report(n, ranks)) <= 1e-12 * 3.2
+    assert abs(err - abs(pi - math.pi)) <= 1e-15
+
+
+@pytest.mark.parametrize("ranks", [1, 8, 100])
+def test_c_globals_are_per_rank(c_programs, ranks):
+    r = subprocess.run([str(c_programs["globals"]), "---gpumpi", "-n", str(ranks)], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, (r.stdout, r.stderr)
+    assert f"globals: {ranks} ranks, ok" in r.stdout
+
+
+def test_c_program_refuses_more_ranks_than_it_was_converted_for(c_programs):
+    ok = subprocess.run([str(c_programs["globals8"]), "---gpumpi", "-n", "8"], capture_output=True, text=True,
+                        timeout=120)
+    assert ok.returncode == 0 and "globals: 8 ranks, ok" in ok.stdout, ok.stderr
+    r = subprocess.run([str(c_programs["globals8"]), "---gpumpi", "-n", "9"], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 1 and "converted for at most 8" in r.stderr
+
+
+def _checksum(text: str) -> int:
+    s = 0
+    for ch in text:
+        s = (s * 31 + ord(ch)) & 0xFFFFFFFF
+    return s - (1 << 32) if s >= 1 << 31 else s
+
+
+@pytest.mark.parametrize("ranks", [1, 2, 5])
+def test_c_oldstyle_program(c_programs, ranks):
+    # K&R definitions, implicit void* conversions, C++-keyword identifiers, libc strings and numbers,
+    # a contiguous datatype, two translation units sharing a global through a project header
+    r = subprocess.run([str(c_programs["oldstyle"]), "---gpumpi", "-n", str(ranks)], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, (r.stdout, r.stderr)
+    labels = ["rec-a", "rec-b", "rec-b"]
+    total = sum(_checksum(labels[k % 3]) + k for k in range(ranks))
+    assert f"oldstyle: {ranks} ranks, total {total}, failures 0" in r.stdout, r.stdout
