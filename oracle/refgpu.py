@@ -4,7 +4,8 @@ COMPARATOR / TEST INFRASTRUCTURE ONLY: used by bench.py's reference-runtime leg 
 product).  The reference's own sources are never committed here:
 
 * stage(): where the reference checkout exists (REFERENCE_SRC, default /root/reference), copies its
-  runtime sources - gpu_libs/gpu_libc, gpu_libs/gpu_mpi, gpu_libs/gpu_main (without main.cu, whose
+  toolchain test programs (plain C MPI programs, for the source converter's tests) into
+  baseline/_ref/toolchain/ and its runtime sources - gpu_libs/gpu_libc, gpu_libs/gpu_mpi, gpu_libs/gpu_main (without main.cu, whose
   launcher is replaced by oracle/refgpu/driver.cu) and common/ - unchanged into baseline/_ref/src/
   (git-ignored; it travels with the working tree to the GPU machine, which has no reference checkout);
 * build(): compiles those sources for sm_103a with relocatable device code, exactly as the reference's
@@ -41,7 +42,9 @@ def reference_root() -> Path:
 
 
 def stage() -> bool:
-    """Copies the reference runtime sources into baseline/_ref/src (when the checkout is present)."""
+    """Copies the reference runtime sources into baseline/_ref/src (when the checkout is present), and
+    its toolchain test programs into baseline/_ref/toolchain."""
+    stage_toolchain()
     ref = reference_root()
     if not (ref / "gpu_libs" / "gpu_mpi" / "mpi.cu").exists():
         return STAGE.exists()
@@ -50,6 +53,25 @@ def stage() -> bool:
         if dst.exists():
             shutil.rmtree(dst)
         shutil.copytree(ref / d, dst, ignore=shutil.ignore_patterns("main.cu", "CMakeLists.txt", "*.md"))
+    return True
+
+
+TOOLCHAIN = ROOT / "baseline" / "_ref" / "toolchain"
+# the reference's own plain C MPI programs that its toolchain tests convert and run (toolchain_tests/)
+TOOLCHAIN_PROGRAMS = ["pi/cpi.c", "global_var/global_var.c", "datatype/contiguous.c", "basicIO/basicIO.c",
+                      "basicIO/file_view1.c", "basicIO/file_view2.c"]
+
+
+def stage_toolchain() -> bool:
+    """Copies the reference's toolchain test programs unchanged into baseline/_ref/toolchain/ (git-ignored)
+    for the source converter's tests: they are the converter's inputs in the reference, so converting,
+    building and running them here checks the converter against the reference's own programs."""
+    ref = reference_root() / "toolchain_tests"
+    if not all((ref / p).exists() for p in TOOLCHAIN_PROGRAMS):
+        return all((TOOLCHAIN / p).exists() for p in TOOLCHAIN_PROGRAMS)
+    for p in TOOLCHAIN_PROGRAMS:
+        (TOOLCHAIN / p).parent.mkdir(parents=True, exist_ok=True)
+        shutil.copyfile(ref / p, TOOLCHAIN / p)
     return True
 
 

@@ -9,6 +9,7 @@ from pathlib import Path
 import pytest
 
 from gpumpi import converter as cv
+from oracle import refgpu
 
 ROOT = Path(__file__).resolve().parents[1]
 PROGS = ROOT / "tests" / "programs" / "c"
@@ -147,3 +148,16 @@ def test_converted_programs_compile_for_sm103a(tmp_path, progs):
         r = subprocess.run([gbuild.nvcc(), *gbuild.common_flags(), "-I", str(tmp_path), "-I", str(PROGS), "-c",
                             str(f), "-o", str(f.with_suffix(".o"))], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr[-4000:]
+
+
+# the reference's own toolchain test programs (staged unchanged, git-ignored, by oracle/refgpu.py)
+
+@pytest.mark.skipif(not all((refgpu.TOOLCHAIN / p).exists() for p in refgpu.TOOLCHAIN_PROGRAMS),
+                    reason="the reference's toolchain programs are not staged")
+@pytest.mark.parametrize("prog", refgpu.TOOLCHAIN_PROGRAMS)
+def test_reference_toolchain_programs_convert_and_compile(tmp_path, prog):
+    import build as gbuild
+    (out,) = cv.convert_files([refgpu.TOOLCHAIN / prog], tmp_path, max_ranks=64)
+    r = subprocess.run([gbuild.nvcc(), *gbuild.common_flags(), "-I", str(tmp_path), "-c", str(out), "-o",
+                        str(out.with_suffix(".o"))], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]

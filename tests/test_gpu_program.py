@@ -187,3 +187,68 @@ def test_c_oldstyle_program(c_programs, ranks):
     labels = ["rec-a", "rec-b", "rec-b"]
     total = sum(_checksum(labels[k % 3]) + k for k in range(ranks))
     assert f"oldstyle: {ranks} ranks, total {total}, failures 0" in r.stdout, r.stdout
+
+
+# ---- the reference's own toolchain programs (toolchain_tests/, staged unchanged by oracle/refgpu.py) ----
+
+def _toolchain():
+    sys.path.insert(0, str(ROOT))
+    from oracle import refgpu
+    return refgpu
+
+
+@pytest.fixture(scope="module")
+def ref_programs(tmp_path_factory, gpulib):
+    refgpu = _toolchain()
+    if not all((refgpu.TOOLCHAIN / p).exists() for p in refgpu.TOOLCHAIN_PROGRAMS):
+        pytest.skip("the reference's toolchain programs are not staged")
+    from gpumpi import gpumpicc as cc
+    d = tmp_path_factory.mktemp("refprog")
+    return {Path(p).stem: cc.compile_program([refgpu.TOOLCHAIN / p], d / Path(p).stem, max_ranks=256)
+            for p in refgpu.TOOLCHAIN_PROGRAMS}
+
+
+@pytest.mark.parametrize("ranks,n", [(4, 10000), (33, 100000)])
+def test_reference_cpi_runs_converted(ref_programs, ranks, n):
+    # toolchain_tests/pi/test.sh runs `./pi ---gpumpi -g 4 -b 1 -s 8192`
+    import math
+    r = subprocess.run([str(ref_programs["cpi"]), str(n), "---gpumpi", "-n", str(ranks)], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    procs = sorted(l for l in r.stdout.splitlines() if l.startswith("Process "))
+    assert procs == sorted(f"Process {k} of {ranks} is on GB300 block-rank" for k in range(ranks))
+    est = [l for l in r.stdout.splitlines() if l.startswith("pi is approximately ")]
+    assert len(est) == 1, r.stdout
+    pi, err = (float(x) for x in est[0][len("pi is approximately "):].replace(", Error is", "").split())
+    assert abs(pi - expected_pi_report(n, ranks)) <= 1e-12 * 3.2
+    assert abs(err - abs(pi - math.pi)) <= 1e-15
+    assert any(l.startswith("wall clock time = ") for l in r.stdout.splitlines())
+
+
+@pytest.mark.parametrize("ranks", [4, 64, 256])
+def test_reference_global_var_runs_converted(ref_programs, ranks):
+    # toolchain_tests/global_var/test.sh runs it on 4 ranks; it returns 1 and prints "error ..." when a
+    # per-rank global does not behave as a process's global
+    r = subprocess.run([str(ref_programs["global_var"]), "---gpumpi", "-n", str(ranks)], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0 and "error" not in r.stdout, (r.stdout, r.stderr)
+
+
+def test_reference_contiguous_runs_converted(ref_programs):
+    r = subprocess.run([str(ref_programs["contiguous"]), "---gpumpi", "-n", "2"], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("ranks", [1, 4, 16])
+def test_reference_io_programs_run_converted(ref_programs, tmp_path, ranks):
+    import numpy as np
+    for name in ("basicIO", "file_view1", "file_view2"):
+        r = subprocess.run([str(ref_programs[name]), "---gpumpi", "-n", str(ranks)], capture_output=True, text=True,
+                           timeout=120, cwd=tmp_path)
+        assert r.returncode == 0, (name, r.stderr)
+    assert (tmp_path / "test.out").read_bytes() == b"hello world from GPUMPI IO"
+    v1 = np.fromfile(tmp_path / "test_file_view1.out", dtype=np.int32)
+    assert v1.tolist() == list(range(100)) * ranks      # each rank's 100 ints at rank * 400 bytes
+    # two blocks of 50 ints per rank, 50 * ranks ints apart (the buffer itself is uninitialised)
+    assert (tmp_path / "test_file_view2.out").stat().st_size == 2 * 50 * ranks * 4
