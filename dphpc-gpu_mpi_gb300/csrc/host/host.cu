@@ -115,7 +115,8 @@ struct gpumpi_world {
     int host_direct = 3;
     bool host_aliased = false;  // the launch being prepared reads host memory in place: no bulk copies
     long long host_slice_bytes = 0;  // column slice per rank of the sliced path, bytes (0 = auto)
-    cudaStream_t xs_in = nullptr, xs_out = nullptr;  // the sliced path's copy streams (created on first use)
+    int host_streams = 1;            // copy streams per direction of the sliced path (row groups)
+    cudaStream_t xs_in[4] = {}, xs_out[4] = {};  // the sliced path's copy streams (created on first use)
     cudaEvent_t xev[4] = {};                         // input copied, slice folded, call start, call end
     signed char* d_table = nullptr;
     float* d_mlp = nullptr;
@@ -394,8 +395,9 @@ int gpumpi_world_destroy(gpumpi_world* w) {
     cudaFree(w->d_table);
     cudaFree(w->d_mlp);
     for (auto& p : w->d_stage) cudaFree(p);
-    if (w->xs_in) cudaStreamSynchronize(w->xs_in), cudaStreamDestroy(w->xs_in);
-    if (w->xs_out) cudaStreamSynchronize(w->xs_out), cudaStreamDestroy(w->xs_out);
+    for (auto* xs : {w->xs_in, w->xs_out})
+        for (int k = 0; k < 4; k++)
+            if (xs[k]) cudaStreamSynchronize(xs[k]), cudaStreamDestroy(xs[k]);
     for (auto& e : w->xev)
         if (e) cudaEventDestroy(e);
     if (w->ev0) cudaEventDestroy(w->ev0);
@@ -439,6 +441,10 @@ int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
         if (value < 0) return GPUMPI_ERR_ARG;
         w->host_slice_bytes = value;
         return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_HOST_STREAMS:
+        if (value < 1 || value > 4) return GPUMPI_ERR_ARG;
+        w->host_streams = (int)value;
+        return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_STAGE_GROUP: w->tune_group = (int)value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_ENGINES: w->cfg.engine_blocks = (int)value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_COPY_CHUNK: w->h_rt.copy_chunk_bytes = value; return GPUMPI_SUCCESS;
@@ -463,6 +469,7 @@ int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value) {
     case GPUMPI_TUNE_DYN_SMEM: *value = w->dyn_smem_cap; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_HOST_DIRECT: *value = w->host_direct; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_HOST_SLICE: *value = w->host_slice_bytes; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_HOST_STREAMS: *value = w->host_streams; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_STAGE_GROUP: *value = w->tune_group; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_ENGINES: *value = w->cfg.engine_blocks; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_COPY_CHUNK: *value = w->h_rt.copy_chunk_bytes; return GPUMPI_SUCCESS;
@@ -921,8 +928,13 @@ int allreduce_host_sliced(gpumpi_world* w, const void* sb, void* rb, long long c
 
     cudaStream_t s = stream_v ? (cudaStream_t)stream_v : w->stream;
     CK(cudaSetDevice(w->device));
-    if (!w->xs_in) CK(cudaStreamCreateWithFlags(&w->xs_in, cudaStreamNonBlocking));
-    if (!w->xs_out) CK(cudaStreamCreateWithFlags(&w->xs_out, cudaStreamNonBlocking));
+    // each slice's 2D copy in each direction is split into P row groups on P streams: 2D copies of short
+    // rows run at a fraction of the link on one stream
+    const int P = std::min(w->host_streams, n);
+    for (int k = 0; k < P; k++) {
+        if (!w->xs_in[k]) CK(cudaStreamCreateWithFlags(&w->xs_in[k], cudaStreamNonBlocking));
+        if (!w->xs_out[k]) CK(cudaStreamCreateWithFlags(&w->xs_out[k], cudaStreamNonBlocking));
+    }
     for (auto& e : w->xev)
         if (!e) CK(cudaEventCreate(&e));
     cudaEvent_t ev_in = w->xev[0], ev_fold = w->xev[1], ev_a = w->xev[2], ev_b = w->xev[3];
@@ -943,9 +955,10 @@ int allreduce_host_sliced(gpumpi_world* w, const void* sb, void* rb, long long c
     const int rec_ints = nerr + n;
     if ((rc = stage(w, 6, nullptr, sizeof(int) * (size_t)rec_ints * slices, false, s, &drec))) return rc;
 
-    // copies wait for whatever the caller queued on its stream before this call
+    // copies wait for whatever the caller queued on its stream before this call (an event's wait refers
+    // to its record at the time of the wait call, so one event serves every record-wait pair below)
     CK(cudaEventRecord(ev_a, s));
-    CK(cudaStreamWaitEvent(w->xs_in, ev_a, 0));
+    for (int k = 0; k < P; k++) CK(cudaStreamWaitEvent(w->xs_in[k], ev_a, 0));
     w->err.clear();
     int launch_rc = GPUMPI_SUCCESS;
     for (int j = 0; j < slices; j++) {
@@ -953,10 +966,13 @@ int allreduce_host_sliced(gpumpi_world* w, const void* sb, void* rb, long long c
         const long long cn = std::min(selems, count - c0);
         const size_t off = (size_t)c0 * esz, width = (size_t)cn * esz;
         if (!in_alias) {
-            CK(cudaMemcpy2DAsync((char*)dsend + off, per, (const char*)sb + off, per, width, n,
-                                 cudaMemcpyHostToDevice, w->xs_in));
-            CK(cudaEventRecord(ev_in, w->xs_in));
-            CK(cudaStreamWaitEvent(s, ev_in, 0));
+            for (int k = 0; k < P; k++) {
+                const size_t r0 = (size_t)n * k / P, r1 = (size_t)n * (k + 1) / P;
+                CK(cudaMemcpy2DAsync((char*)dsend + r0 * per + off, per, (const char*)sb + r0 * per + off, per,
+                                     width, r1 - r0, cudaMemcpyHostToDevice, w->xs_in[k]));
+                CK(cudaEventRecord(ev_in, w->xs_in[k]));
+                CK(cudaStreamWaitEvent(s, ev_in, 0));
+            }
         }
         gpumpi_params prm;
         memset(&prm, 0, sizeof(prm));
@@ -976,17 +992,22 @@ int allreduce_host_sliced(gpumpi_world* w, const void* sb, void* rb, long long c
         g_launches++;
         if (!out_alias) {
             CK(cudaEventRecord(ev_fold, s));
-            CK(cudaStreamWaitEvent(w->xs_out, ev_fold, 0));
-            CK(cudaMemcpy2DAsync((char*)rb + off, per, (const char*)drecv + off, per, width, n,
-                                 cudaMemcpyDeviceToHost, w->xs_out));
+            for (int k = 0; k < P; k++) {
+                const size_t r0 = (size_t)n * k / P, r1 = (size_t)n * (k + 1) / P;
+                CK(cudaStreamWaitEvent(w->xs_out[k], ev_fold, 0));
+                CK(cudaMemcpy2DAsync((char*)rb + r0 * per + off, per, (const char*)drecv + r0 * per + off, per,
+                                     width, r1 - r0, cudaMemcpyDeviceToHost, w->xs_out[k]));
+            }
         }
     }
     // the call ends on the caller's stream after the last results have crossed
-    CK(cudaEventRecord(ev_fold, w->xs_out));
-    CK(cudaStreamWaitEvent(s, ev_fold, 0));
+    for (int k = 0; k < P; k++) {
+        CK(cudaEventRecord(ev_fold, w->xs_out[k]));
+        CK(cudaStreamWaitEvent(s, ev_fold, 0));
+    }
     CK(cudaEventRecord(ev_b, s));
     CK(cudaStreamSynchronize(s));
-    CK(cudaStreamSynchronize(w->xs_in));  // inputs still in flight when a launch failed
+    for (int k = 0; k < P; k++) CK(cudaStreamSynchronize(w->xs_in[k]));  // inputs in flight when a launch failed
     if (launch_rc) return launch_rc;
     float ms = 0;
     cudaEventElapsedTime(&ms, ev_a, ev_b);

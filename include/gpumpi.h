@@ -180,6 +180,9 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
  * 256 MiB per slice over all ranks, at least 128 KiB per rank; rounded up to 256 bytes, at most 64
  * slices; a call that would take one slice runs as one launch). */
 #define GPUMPI_TUNE_HOST_SLICE 10
+/* GPUMPI_TUNE_HOST_STREAMS: copy streams per direction of the sliced host-buffer Allreduce (1..4): each
+ * slice's 2D copy is split into that many row groups copied concurrently. */
+#define GPUMPI_TUNE_HOST_STREAMS 11
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Launcher of a converted program (the reference's gpu_main): argv holds the program's arguments, then
  * optionally `---gpumpi` and the run's options (gpumpi_parse_args); creates the world, runs `program` on

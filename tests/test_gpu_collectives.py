@@ -103,7 +103,8 @@ def test_pinned_host_buffers_in_place_and_staged(gpulib, oracle):
 def test_sliced_host_allreduce_matches_oracle(gpulib, oracle, mode):
     """An Allreduce between host buffers cut into column slices (TUNE_HOST_DIRECT 2..4, one launch per
     slice, copies of later slices overlapping the folds of earlier ones) is bit-exact with the oracle:
-    page-locked and pageable buffers, a ragged last slice, floating point in the canonical order."""
+    page-locked and pageable buffers, a ragged last slice, copies split over one or three streams,
+    floating point in the canonical order."""
     n = 64
     cases = [(20000, 12, 2, np.float32), (9000, 13, 2, np.float64), (12343, 2, 0, np.int32)]
     with gpulib.World(n, timeout_s=10.0) as w:
@@ -111,6 +112,7 @@ def test_sliced_host_allreduce_matches_oracle(gpulib, oracle, mode):
         w.set_tuning(gpulib.TUNE_HOST_SLICE, 16 << 10)
         assert w.get_tuning(gpulib.TUNE_HOST_DIRECT) == mode
         for count, dt, op, npdt in cases:
+            w.set_tuning(gpulib.TUNE_HOST_STREAMS, 3 if dt == 13 else 1)   # row groups of 21, 21 and 22 ranks
             count -= count % (16 // np.dtype(npdt).itemsize)     # rows 16-byte aligned: the sliced path
             x = make_input(oracle, n, count, npdt, 40 + count)
             ref = oracle.allreduce(x, dt, op)
