@@ -5,6 +5,7 @@
 //    fprintf/printf formatted by the host's own printf.  The reference's device libc returns nullptr
 //    from fopen and traps in fclose/fputs/puts (gpu_libs/gpu_libc/stdio.cu:32-66) and prints through
 //    CUDA's buffered device printf; these reach real files and the host's standard streams in call order.
+//  * gpumpi_getenv (include/gpumpi_libc.h.cuh): the host process's environment.
 //  * MPI-IO (MPI-3.1 chapter 13; the reference's gpu_libs/gpu_mpi/io.cu:139-559 and io.cuh:125-153):
 //    collective open/close with the comm's rank 0 talking to the host, file views with any derived
 //    filetype (positions are etypes of the view; a position maps to file byte disp + typemap(filetype,
@@ -73,7 +74,7 @@ __device__ __noinline__ long long host_call(int op, long long a0, long long a1, 
 
 // Copies the NUL-terminated string s into the window (truncated to the window); returns false if s is null.
 __device__ bool window_put_string(const char* s) {
-    if (!s) return false;
+    if (!s || !c_rt.hio.ring) return false;  // a world made without the channel has no window
     unsigned char* w = hio_window();
     const long long cap = c_rt.hio.window_bytes;
     long long n = 0;
@@ -142,6 +143,7 @@ __device__ long long put_arg(unsigned char* w, long long off, long long cap, int
 
 __device__ long long host_vprintf(long long handle, const char* fmt, va_list ap) {
     if (!fmt) return HIO_EIO;
+    if (!c_rt.hio.ring) return HIO_ENOSYS;
     unsigned char* w = hio_window();
     const long long cap = c_rt.hio.window_bytes;
     long long flen = 0;
@@ -241,7 +243,7 @@ __device__ int gpumpi_fclose(gpumpi_FILE* f) {
 
 // Sequential transfer through the window in pieces of at most the window (less one run record).
 __device__ long long stream_xfer(gpumpi_FILE* f, void* buf, long long bytes, bool write) {
-    if (!f || !buf || bytes <= 0) return 0;
+    if (!f || !buf || bytes <= 0 || !c_rt.hio.ring) return 0;
     unsigned char* w = hio_window();
     const long long data_off = 16;
     const long long room = c_rt.hio.window_bytes - data_off;
@@ -289,6 +291,19 @@ __device__ int gpumpi_fflush(gpumpi_FILE* f) {
 __device__ int gpumpi_remove(const char* path) {
     if (!window_put_string(path)) return -1;
     return host_call(gpumpi::HIO_REMOVE, 0, 0, 0, 0) == 0 ? 0 : -1;
+}
+// The host process's environment variable `name`, or nullptr.  The value is copied into the calling
+// rank's block (shared memory, at most 255 bytes) and stays valid until the rank's next gpumpi_getenv.
+__shared__ char s_getenv_value[256];
+__device__ char* gpumpi_getenv(const char* name) {
+    if (!window_put_string(name)) return nullptr;
+    const long long n = host_call(gpumpi::HIO_GETENV, 0, 0, 0, 0);
+    if (n < 0) return nullptr;
+    const unsigned char* w = hio_window();
+    const long long m = n < 255 ? n : 255;
+    for (long long k = 0; k < m; k++) s_getenv_value[k] = (char)w[k];
+    s_getenv_value[m] = 0;
+    return s_getenv_value;
 }
 __device__ int gpumpi_fprintf(gpumpi_FILE* f, const char* fmt, ...) {
     if (!f) return -1;

@@ -853,6 +853,18 @@ __device__ int MPI_Abort(MPI_Comm comm, int errorcode) {
     atomicExch(c_rt.abort_flag, 1u);
     return MPI_SUCCESS;
 }
+// exit() for converted programs: the calling rank ends as if its program had returned `status` (its block
+// releases its helper threads, records the status and leaves; the launcher reports a non-zero status as
+// the run's failure) and the call does not return.  Ranks still waiting on it get bounded-wait errors, as
+// an MPI job fails when one of its processes exits early.  Only the rank's program thread can leave this
+// way; a call from another thread records an error and returns.
+__device__ void gpumpi_exit(int status) {
+    if (threadIdx.x == 0 && is_rank_block()) {
+        rank_finish(status);
+        asm volatile("exit;" ::: "memory");
+    }
+    record_error(GPUMPI_ERR_OTHER, GPUMPI_ERR_ARG, __LINE__, status);
+}
 __device__ int MPI_Get_processor_name(char* name, int* resultlen) {
     const char n[] = "GB300 block-rank";
     for (int i = 0; i < (int)sizeof(n); i++) name[i] = n[i];

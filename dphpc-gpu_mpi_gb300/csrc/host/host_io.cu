@@ -12,10 +12,12 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cerrno>
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -275,6 +277,15 @@ long long serve(HostService* s, const HostReq& r) {
         const int fd = handle_fd(s, r.a0);
         if (fd < 0) return -EBADF;
         return ftruncate(fd, (off_t)r.a1) == 0 ? 0 : -errno;
+    }
+    case gpumpi::HIO_GETENV: {
+        const std::string name = window_string(win, s->window_bytes);
+        const char* v = getenv(name.c_str());
+        if (!v) return -ENOENT;
+        const size_t n = std::min(strlen(v), s->window_bytes - 1);
+        memcpy(win, v, n);
+        win[n] = 0;
+        return (long long)n;
     }
     default: return -ENOSYS;
     }

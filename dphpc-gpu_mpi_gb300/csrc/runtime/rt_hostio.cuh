@@ -37,6 +37,8 @@ enum HostOp : int {
     HIO_FLUSH = 7,    // a0 = handle: data reaches the file (fsync) or the stream is flushed -> 0 or -errno
     HIO_PRINTF = 8,   // a0 = handle; window: format string then packed arguments (HostArg) -> characters
     HIO_TRUNCATE = 9, // a0 = handle, a1 = size -> 0 or -errno
+    HIO_GETENV = 10,  // window: NUL-terminated name -> the value, NUL-terminated, in the window: its length,
+                      // or -ENOENT when the host process has no such variable
 };
 
 // open flags (host maps them to open(2) flags)

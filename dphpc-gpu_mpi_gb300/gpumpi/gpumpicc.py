@@ -31,11 +31,13 @@ def _build_module():
 
 
 def compile_program(sources, out, include_dirs=(), defines=(), max_ranks=None, workdir=None,
-                    extra_types=()) -> Path:
-    """Converts `sources` (C files) and links them into the executable `out`; returns its path."""
+                    extra_types=(), project=None) -> Path:
+    """Converts `sources` (C files, with the project's headers they include) and links them into the
+    executable `out`; returns its path."""
     out = Path(out).resolve()
     work = Path(workdir) if workdir else out.parent / (out.name + ".gpumpi")
-    converted = converter.convert_files(sources, work, max_ranks, include_dirs, extra_types=extra_types)
+    converted = converter.convert_files(sources, work, max_ranks, include_dirs, project=project,
+                                        extra_types=extra_types)
     flags = []
     for d in [*(Path(s).resolve().parent for s in sources), work, *include_dirs]:
         flags += ["-I", str(Path(d).resolve())]
@@ -54,9 +56,11 @@ def main(argv=None) -> int:
     ap.add_argument("--max-ranks", type=int, default=None)
     ap.add_argument("--workdir", default=None, help="where the converted sources go (default OUT.gpumpi/)")
     ap.add_argument("--type", dest="types", action="append", default=[], help="extra typedef name")
+    ap.add_argument("--project", default=None, help="project directory (default $GPU_MPI_PROJECT)")
     a = ap.parse_args(argv)
     try:
-        print(compile_program(a.sources, a.out, a.include_dirs, a.defines, a.max_ranks, a.workdir, a.types))
+        print(compile_program(a.sources, a.out, a.include_dirs, a.defines, a.max_ranks, a.workdir, a.types,
+                              a.project))
     except (converter.ConversionError, RuntimeError) as e:
         print(f"gpumpicc: {e}", file=sys.stderr)
         return 1

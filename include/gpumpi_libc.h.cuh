@@ -101,6 +101,13 @@ __device__ inline void* gpumpi_calloc(size_t n, size_t size) {
     return p;
 }
 
+// getenv: the host process's environment, asked over the world's host channel (nullptr without one); the
+// value (at most 255 bytes) stays valid until the rank's next call.  Defined by the runtime library.
+__device__ char* gpumpi_getenv(const char* name);
+// exit: the calling rank ends with `status` as if its program had returned it (from the rank's program
+// thread; ranks still waiting on it get bounded-wait errors).  Defined by the runtime library.
+__device__ void gpumpi_exit(int status);
+
 __device__ inline int gpumpi_isspace_(int c) { return c == ' ' || (c >= '\t' && c <= '\r'); }
 __device__ inline int gpumpi_digit_(int c, int base) {
     int v = c >= '0' && c <= '9' ? c - '0' : c >= 'a' && c <= 'z' ? c - 'a' + 10 : c >= 'A' && c <= 'Z' ? c - 'A' + 10 : 99;
@@ -273,4 +280,6 @@ __device__ inline double gpumpi_atof(const char* s) { return gpumpi_strtod(s, nu
 #define atoll gpumpi_atoll
 #define atof gpumpi_atof
 #define calloc gpumpi_calloc
+#define getenv gpumpi_getenv
+#define exit gpumpi_exit
 #endif

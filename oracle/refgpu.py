@@ -62,17 +62,32 @@ TOOLCHAIN_PROGRAMS = ["pi/cpi.c", "global_var/global_var.c", "datatype/contiguou
                       "basicIO/file_view1.c", "basicIO/file_view2.c"]
 
 
+# NPB IS (the integer sort of the NAS Parallel Benchmarks, which the reference's toolchain test converts
+# and runs: toolchain_tests/npb/is_test.sh): its sources and the common files it links
+NPB_IS = ["npb/NPB3.4.1/NPB3.4-MPI/IS/is.c", "npb/NPB3.4.1/NPB3.4-MPI/common/c_print_results.c",
+          "npb/NPB3.4.1/NPB3.4-MPI/common/c_timers.c", "npb/NPB3.4.1/NPB3.4-MPI/common/c_timers.h"]
+
+
 def stage_toolchain() -> bool:
-    """Copies the reference's toolchain test programs unchanged into baseline/_ref/toolchain/ (git-ignored)
-    for the source converter's tests: they are the converter's inputs in the reference, so converting,
-    building and running them here checks the converter against the reference's own programs."""
+    """Copies the reference's toolchain test programs (and NPB IS) unchanged into baseline/_ref/toolchain/
+    (git-ignored) for the source converter's tests: they are the converter's inputs in the reference, so
+    converting, building and running them here checks the converter against the reference's own programs."""
     ref = reference_root() / "toolchain_tests"
-    if not all((ref / p).exists() for p in TOOLCHAIN_PROGRAMS):
-        return all((TOOLCHAIN / p).exists() for p in TOOLCHAIN_PROGRAMS)
-    for p in TOOLCHAIN_PROGRAMS:
+    files = TOOLCHAIN_PROGRAMS + NPB_IS
+    if not all((ref / p).exists() for p in files):
+        return all((TOOLCHAIN / p).exists() for p in files)
+    for p in files:
         (TOOLCHAIN / p).parent.mkdir(parents=True, exist_ok=True)
         shutil.copyfile(ref / p, TOOLCHAIN / p)
     return True
+
+
+def npb_is_params(cls: str = "S") -> str:
+    """npbparams.h of NPB IS for class `cls`, with the entries NPB's setparams writes for a C benchmark
+    (sys/setparams.c; the build-information strings name this toolchain)."""
+    return (f"#define CLASS '{cls}'\n#define NPBVERSION \"3.4.1\"\n#define COMPILETIME \"gpumpicc\"\n"
+            "#define MPICC \"gpumpicc\"\n#define CLINK \"gpumpicc\"\n#define CMPI_LIB \"\"\n"
+            "#define CMPI_INC \"\"\n#define CFLAGS \"-O3\"\n#define CLINKFLAGS \"\"\n")
 
 
 def sources() -> list:

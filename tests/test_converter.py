@@ -161,3 +161,20 @@ def test_reference_toolchain_programs_convert_and_compile(tmp_path, prog):
     r = subprocess.run([gbuild.nvcc(), *gbuild.common_flags(), "-I", str(tmp_path), "-c", str(out), "-o",
                         str(out.with_suffix(".o"))], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
+
+
+@pytest.mark.skipif(not all((refgpu.TOOLCHAIN / p).exists() for p in refgpu.NPB_IS),
+                    reason="NPB IS is not staged")
+def test_npb_is_converts_and_compiles(tmp_path):
+    import build as gbuild
+    npb = tmp_path / "npb"
+    shutil.copytree(refgpu.TOOLCHAIN / "npb", npb)
+    mpi = npb / "NPB3.4.1" / "NPB3.4-MPI"
+    (mpi / "IS" / "npbparams.h").write_text(refgpu.npb_is_params("S"))
+    srcs = [mpi / "IS" / "is.c", mpi / "common" / "c_print_results.c", mpi / "common" / "c_timers.c"]
+    out = cv.convert_files(srcs, tmp_path / "conv", max_ranks=8, project=npb)
+    assert (tmp_path / "conv" / "npbparams.h.cuh").exists() and (tmp_path / "conv" / "c_timers.h.cuh").exists()
+    for f in out:
+        r = subprocess.run([gbuild.nvcc(), *gbuild.common_flags(), "-I", str(tmp_path / "conv"), "-c", str(f), "-o",
+                            str(f.with_suffix(".o"))], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-4000:]

@@ -252,3 +252,44 @@ def test_reference_io_programs_run_converted(ref_programs, tmp_path, ranks):
     assert v1.tolist() == list(range(100)) * ranks      # each rank's 100 ints at rank * 400 bytes
     # two blocks of 50 ints per rank, 50 * ranks ints apart (the buffer itself is uninitialised)
     assert (tmp_path / "test_file_view2.out").stat().st_size == 2 * 50 * ranks * 4
+
+
+@pytest.fixture(scope="module")
+def npb_is(tmp_path_factory, gpulib):
+    import shutil
+    refgpu = _toolchain()
+    if not all((refgpu.TOOLCHAIN / p).exists() for p in refgpu.NPB_IS):
+        pytest.skip("NPB IS is not staged")
+    from gpumpi import gpumpicc as cc
+    d = tmp_path_factory.mktemp("npb")
+    shutil.copytree(refgpu.TOOLCHAIN / "npb", d / "npb")
+    mpi = d / "npb" / "NPB3.4.1" / "NPB3.4-MPI"
+    (mpi / "IS" / "npbparams.h").write_text(refgpu.npb_is_params("S"))
+    srcs = [mpi / "IS" / "is.c", mpi / "common" / "c_print_results.c", mpi / "common" / "c_timers.c"]
+    return cc.compile_program(srcs, d / "is.S.x", max_ranks=16, project=d / "npb")
+
+
+@pytest.mark.parametrize("ranks,strict", [(2, None), (8, None), (16, None), (3, "off")])
+def test_npb_is_class_s_verifies(npb_is, tmp_path, ranks, strict):
+    # toolchain_tests/npb/is_test.sh: `make IS CLASS=S` through gpumpicc, then `./bin/is.S.x ---gpumpi -g 2`.
+    # IS verifies its own sort.  With 3 ranks and NPB_NPROCS_STRICT=off (read through getenv, answered by
+    # the launcher's environment) IS runs on the largest power of two and the third rank leaves through
+    # MPI_Finalize and exit(0)
+    import os
+    env = {**os.environ, "NPB_NPROCS_STRICT": strict} if strict else None
+    r = subprocess.run([str(npb_is), "---gpumpi", "-n", str(ranks)], capture_output=True, text=True, timeout=300,
+                       cwd=tmp_path, env=env)
+    assert r.returncode == 0, (r.stdout[-3000:], r.stderr[-3000:])
+    assert "Verification    =               SUCCESSFUL" in r.stdout, r.stdout[-3000:]
+    assert " Class           =                        S" in r.stdout
+
+
+def test_npb_is_exit_status_reaches_the_launcher(npb_is, tmp_path):
+    # without NPB_NPROCS_STRICT, 3 ranks are refused: every rank calls MPI_Abort and exit(1), ends with
+    # status 1, and the launcher exits with 1
+    import os
+    env = {k: v for k, v in os.environ.items() if k != "NPB_NPROCS_STRICT"}
+    r = subprocess.run([str(npb_is), "---gpumpi", "-n", "3", "--timeout", "5"], capture_output=True, text=True,
+                       timeout=300, cwd=tmp_path, env=env)
+    assert r.returncode == 1, (r.stdout[-2000:], r.stderr[-2000:])
+    assert "is not a power of two" in r.stdout
