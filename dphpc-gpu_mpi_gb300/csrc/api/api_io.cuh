@@ -5,6 +5,7 @@
 //    fprintf/printf formatted by the host's own printf.  The reference's device libc returns nullptr
 //    from fopen and traps in fclose/fputs/puts (gpu_libs/gpu_libc/stdio.cu:32-66) and prints through
 //    CUDA's buffered device printf; these reach real files and the host's standard streams in call order.
+//  * gpumpi_sprintf / snprintf / vsprintf / vsnprintf: formatted by the host into the rank's window.
 //  * gpumpi_getenv (include/gpumpi_libc.h.cuh): the host process's environment.
 //  * MPI-IO (MPI-3.1 chapter 13; the reference's gpu_libs/gpu_mpi/io.cu:139-559 and io.cuh:125-153):
 //    collective open/close with the comm's rank 0 talking to the host, file views with any derived
@@ -141,7 +142,7 @@ __device__ long long put_arg(unsigned char* w, long long off, long long cap, int
     return off + (long long)sizeof(HostArg) + ((n + 7) & ~7LL);
 }
 
-__device__ long long host_vprintf(long long handle, const char* fmt, va_list ap) {
+__device__ long long host_vformat(int op, long long handle, const char* fmt, va_list ap) {
     if (!fmt) return HIO_EIO;
     if (!c_rt.hio.ring) return HIO_ENOSYS;
     unsigned char* w = hio_window();
@@ -210,7 +211,10 @@ __device__ long long host_vprintf(long long handle, const char* fmt, va_list ap)
         nargs++;
     }
     if (off < 0) return HIO_EIO;
-    return host_call(gpumpi::HIO_PRINTF, handle, a1, nargs, 0);
+    return host_call(op, handle, a1, nargs, 0);
+}
+__device__ long long host_vprintf(long long handle, const char* fmt, va_list ap) {
+    return host_vformat(gpumpi::HIO_PRINTF, handle, fmt, ap);
 }
 
 }  // namespace
@@ -291,6 +295,40 @@ __device__ int gpumpi_fflush(gpumpi_FILE* f) {
 __device__ int gpumpi_remove(const char* path) {
     if (!window_put_string(path)) return -1;
     return host_call(gpumpi::HIO_REMOVE, 0, 0, 0, 0) == 0 ? 0 : -1;
+}
+// sprintf family: the host formats (as for printf) into the rank's window; the text is copied to dst.  The
+// result is cut to the window (host_window_bytes - 1 characters); the return value is the full length.
+__device__ int gpumpi_vsnprintf(char* dst, size_t size, const char* fmt, va_list ap) {
+    const long long n = host_vformat(gpumpi::HIO_SPRINTF, 0, fmt, ap);
+    if (n < 0) {
+        if (dst && size) dst[0] = 0;
+        return -1;
+    }
+    if (dst && size) {
+        const unsigned char* w = hio_window();
+        long long m = n < c_rt.hio.window_bytes - 1 ? n : c_rt.hio.window_bytes - 1;
+        if ((unsigned long long)m > size - 1) m = (long long)(size - 1);
+        for (long long k = 0; k < m; k++) dst[k] = (char)w[k];
+        dst[m] = 0;
+    }
+    return (int)n;
+}
+__device__ int gpumpi_vsprintf(char* dst, const char* fmt, va_list ap) {
+    return gpumpi_vsnprintf(dst, ~(size_t)0, fmt, ap);
+}
+__device__ int gpumpi_snprintf(char* dst, size_t size, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    const int n = gpumpi_vsnprintf(dst, size, fmt, ap);
+    va_end(ap);
+    return n;
+}
+__device__ int gpumpi_sprintf(char* dst, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    const int n = gpumpi_vsnprintf(dst, ~(size_t)0, fmt, ap);
+    va_end(ap);
+    return n;
 }
 // The host process's environment variable `name`, or nullptr.  The value is copied into the calling
 // rank's block (shared memory, at most 255 bytes) and stays valid until the rank's next gpumpi_getenv.

@@ -122,9 +122,10 @@ long long do_rw(HostService* s, const HostReq& r, unsigned char* win, bool write
 
 // printf with the host's own formatter: the device sent the format string and one HostArg per value the
 // conversions consume, in order ('*' widths and precisions included).
-long long do_printf(HostService* s, const HostReq& r, const unsigned char* win) {
+// Formats a HIO_PRINTF / HIO_SPRINTF request (format string at the window's start, packed arguments at a1).
+std::string format_request(HostService* s, const HostReq& r, const unsigned char* win) {
     const std::string fmt = window_string(win, s->window_bytes);
-    if (r.a1 < 0 || (size_t)r.a1 > s->window_bytes) return -EINVAL;
+    if (r.a1 < 0 || (size_t)r.a1 > s->window_bytes) return std::string();
     const unsigned char* ap = win + r.a1;
     const unsigned char* end = win + s->window_bytes;
     long long left = r.a2;
@@ -211,6 +212,12 @@ long long do_printf(HostService* s, const HostReq& r, const unsigned char* win) 
         if (n > 0) out.append(buf, (size_t)(n < (int)sizeof(buf) ? n : (int)sizeof(buf) - 1));
         i = j;
     }
+    return out;
+}
+
+long long do_printf(HostService* s, const HostReq& r, const unsigned char* win) {
+    if (r.a1 < 0 || (size_t)r.a1 > s->window_bytes) return -EINVAL;
+    const std::string out = format_request(s, r, win);
     const long long h = r.a0;
     if (h == gpumpi::HIO_STDOUT || h == gpumpi::HIO_STDERR) return stream_write(h, out.data(), out.size());
     const int fd = handle_fd(s, h);
@@ -273,6 +280,14 @@ long long serve(HostService* s, const HostReq& r) {
         return fsync(fd) == 0 ? 0 : -errno;
     }
     case gpumpi::HIO_PRINTF: return do_printf(s, r, win);
+    case gpumpi::HIO_SPRINTF: {
+        if (r.a1 < 0 || (size_t)r.a1 > s->window_bytes) return -EINVAL;
+        const std::string out = format_request(s, r, win);
+        const size_t n = std::min(out.size(), s->window_bytes - 1);
+        memcpy(win, out.data(), n);
+        win[n] = 0;
+        return (long long)out.size();
+    }
     case gpumpi::HIO_TRUNCATE: {
         const int fd = handle_fd(s, r.a0);
         if (fd < 0) return -EBADF;

@@ -39,6 +39,8 @@ enum HostOp : int {
     HIO_TRUNCATE = 9, // a0 = handle, a1 = size -> 0 or -errno
     HIO_GETENV = 10,  // window: NUL-terminated name -> the value, NUL-terminated, in the window: its length,
                       // or -ENOENT when the host process has no such variable
+    HIO_SPRINTF = 11, // as HIO_PRINTF, the text is written into the window (NUL-terminated, cut to the
+                      // window) instead of a stream -> its full length
 };
 
 // open flags (host maps them to open(2) flags)

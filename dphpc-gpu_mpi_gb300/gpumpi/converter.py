@@ -161,7 +161,7 @@ class Declaration:
 
 class Converter:
     def __init__(self, src: str, max_ranks: int, extra_types=(), is_main_file=True, globals_in=None,
-                 include_map=None):
+                 include_map=None, structs_in=None, functions_in=None):
         self.toks = tokenize(src)
         self.sig = [i for i, t in enumerate(self.toks) if is_sig(t)]
         self.max_ranks = max_ranks
@@ -174,6 +174,9 @@ class Converter:
         self.repl: dict[int, str] = {}
         self.match = self._match_brackets()
         self.saw_main = False
+        self.structs: dict[str, dict] = dict(structs_in or {})  # struct key -> member -> (type, stars, brackets)
+        self.functions: dict[str, tuple] = dict(functions_in or {})  # name -> (return type, parameters or None)
+        self._ret = None                       # return type of the function being converted
 
     # ---- token helpers (k = sig index) ----
     def t(self, k: int) -> str:
@@ -312,21 +315,175 @@ class Converter:
         return self._emit()
 
     def _collect_typedefs_and_globals(self):
-        """First pass: typedef names (for parsing) and the file-scope variables (for references that
-        come before a later tentative definition, and for macro bodies)."""
+        """First pass: typedef names (for parsing), the file-scope variables (for references that come
+        before a later tentative definition, and for macro bodies), struct members and function signatures
+        (for the casts of void* values)."""
         k, n = 0, len(self.sig)
         while k < n:
             end, body = self._item_extent(k)
             if body is None and end > k:
                 d = self.parse_declaration(k, end)
+                self._record_structs(d)
                 for dd in d.decls:
                     if dd.name is None:
                         continue
                     if "typedef" in d.storage:
                         self.types.add(self.t(dd.name))
-                    elif not dd.is_function:
+                    elif dd.is_function:
+                        self.functions[self.t(dd.name)] = (
+                            (d.type_text, dd.stars, 0), self._param_infos(dd.name + 1, self.match[dd.name + 1]))
+                    else:
                         self.globals[self.t(dd.name)] = (d.type_text, dd.stars, dd.brackets)
+            elif body is not None:
+                d = self.parse_declaration(k, body[0])
+                fn = next((dd for dd in d.decls if dd.name is not None and dd.is_function), None)
+                if fn is not None:
+                    self.functions[self.t(fn.name)] = (
+                        (d.type_text, fn.stars, 0), self._param_infos(fn.name + 1, self.match[fn.name + 1]))
             k = (body[1] + 1) if body else end + 1
+
+    # ---- types of simple expressions (the casts of void* values) ----
+    @staticmethod
+    def _type_key(type_text: str) -> str:
+        words = [w for w in type_text.replace("{", " { ").split() if w not in QUALS]
+        if words and words[0] in TAGS:
+            return " ".join(words[:2]) if len(words) > 1 and words[1] != "{" else ""
+        return " ".join(words)
+
+    def _record_structs(self, d: Declaration):
+        """Members of a struct/union body in the specifiers of declaration d, under `struct Tag` and under
+        the typedef names that denote the struct itself; `typedef struct Tag Name;` aliases a known one."""
+        k = d.start
+        while k < d.spec_end:
+            if self.t(k) in TAGS:
+                tag = self.t(k + 1) if self.is_id(k + 1) else None
+                j = k + (2 if tag else 1)
+                names = [f"{self.t(k)} {tag}"] if tag else []
+                if "typedef" in d.storage:
+                    names += [self.t(dd.name) for dd in d.decls if dd.name is not None and dd.stars == 0
+                              and dd.brackets == 0 and not dd.is_function]
+                if self.t(j) == "{":
+                    members, s = {}, j + 1
+                    while s < self.match[j]:
+                        e = s
+                        while e < self.match[j] and self.t(e) != ";":
+                            if self.t(e) in ("(", "[", "{"):
+                                e = self.match[e]
+                            e += 1
+                        md = self.parse_declaration(s, e)
+                        self._record_structs(md)
+                        for dd in md.decls:
+                            if dd.name is not None and not dd.is_function:
+                                members[self.t(dd.name)] = (md.type_text, dd.stars, dd.brackets)
+                        s = e + 1
+                    for nm in names:
+                        self.structs[nm] = members
+                    k = self.match[j] + 1
+                    continue
+                if tag and f"{self.t(k)} {tag}" in self.structs:
+                    for nm in names[1:]:
+                        self.structs[nm] = self.structs[f"{self.t(k)} {tag}"]
+            k += 1
+
+    def _param_infos(self, lp: int, rp: int):
+        """Parameter types of a prototype list, or None for an old-style list (types unknown here)."""
+        inner = list(range(lp + 1, rp))
+        if not inner or (len(inner) == 1 and self.t(inner[0]) == "void"):
+            return []
+        out, s = [], lp + 1
+        while s < rp:
+            e = s
+            while e < rp and self.t(e) != ",":
+                if self.t(e) in ("(", "["):
+                    e = self.match[e]
+                e += 1
+            if self.t(s) == "...":
+                break
+            if e - s == 1 and self.is_id(s) and not self.is_type_name(self.t(s)) and self.t(s) not in C_KEYWORDS:
+                return None   # an identifier list
+            d = self.parse_declaration(s, e)
+            dd = d.decls[0] if d.decls else None
+            out.append((d.type_text, dd.stars if dd else 0, dd.brackets if dd else 0))
+            s = e + 1
+        return out
+
+    def _chain_info(self, a: int, b: int, scopes: list):
+        """Type of sig range [a, b) when it is `name` followed by member accesses and subscripts, else
+        None."""
+        if a >= b or not self.is_id(a):
+            return None
+        r = self._lookup(scopes, self.t(a))
+        if r is None or r[1] is None:
+            return None
+        tt, st, br = r[1]
+        k = a + 1
+        while k < b:
+            x = self.t(k)
+            if x == "[":
+                if self.match[k] >= b:
+                    return None
+                if br > 0:
+                    br -= 1
+                elif st > 0:
+                    st -= 1
+                else:
+                    return None
+                k = self.match[k] + 1
+            elif x in ("->", ".") and self.is_id(k + 1):
+                if x == "->":
+                    if br > 0:
+                        br -= 1
+                    elif st > 0:
+                        st -= 1
+                    else:
+                        return None
+                if st or br:
+                    return None
+                mem = self.structs.get(self._type_key(tt))
+                if mem is None or self.t(k + 1) not in mem:
+                    return None
+                tt, st, br = mem[self.t(k + 1)]
+                k += 2
+            else:
+                return None
+        return (tt, st, br)
+
+    def _void_ptr(self, info) -> bool:
+        return info is not None and self._type_key(info[0]) == "void" and info[1] == 1 and info[2] == 0
+
+    def _typed_ptr(self, info) -> bool:
+        return (info is not None and info[2] == 0 and info[1] >= 1 and
+                not (self._type_key(info[0]) == "void" and info[1] == 1))
+
+    def _cast_void_value(self, a: int, b: int, target, scopes: list):
+        """An explicit cast to `target` before sig range [a, b) when it is a void* chain."""
+        if self._typed_ptr(target) and self._void_ptr(self._chain_info(a, b, scopes)):
+            i = self.sig[a]
+            self.prefix[i] = self._cast_type(target[0], target[1]) + self.prefix.get(i, "")
+
+    def _cast_call_args(self, a: int, b: int, scopes: list):
+        """Arguments that are void* chains passed to typed pointer parameters of known functions."""
+        for k in range(a, b):
+            if not (self.is_id(k) and self.t(k + 1) == "(" and self.t(k) in self.functions):
+                continue
+            if self.t(k - 1) in (".", "->"):
+                continue
+            r = self._lookup(scopes, self.t(k))
+            if r is not None and r[0] != "global":
+                continue
+            params = self.functions[self.t(k)][1]
+            close = self.match[k + 1]
+            if not params or close > b:
+                continue
+            s, i = k + 2, 0
+            while s < close and i < len(params):
+                e = s
+                while e < close and self.t(e) != ",":
+                    if self.t(e) in ("(", "[", "{"):
+                        e = self.match[e]
+                    e += 1
+                self._cast_void_value(s, e, params[i], scopes)
+                s, i = e + 1, i + 1
 
     def _item_extent(self, k: int):
         """Extent of the top-level item starting at sig index k: (index of its ';' or of the token after
@@ -442,7 +599,9 @@ class Converter:
             self.add_suffix(close, f"\n__device__ int __gpu_max_threads() {{ return {self.max_ranks}; }}\n"
                                    f"extern \"C\" const int gpumpi_program_max_ranks = {self.max_ranks};")
         scope = {p: ("local", info) for p, info in params.items()}
+        self._ret = (d.type_text, fn.stars, 0)
         self._body(open_ + 1, close, [scope])
+        self._ret = None
 
     def _parameters(self, lp: int, rp: int, body_open: int) -> dict:
         """The parameters, name -> (type text, stars, brackets); rewrites an old-style list (identifiers,
@@ -561,6 +720,10 @@ class Converter:
         end = self._skip_to_semicolon(k, b)
         if self.starts_declaration(k):
             self._local_declaration(k, end, scopes)
+        elif x == "return":
+            self._expr(k + 1, end, scopes)
+            if self._ret is not None:
+                self._cast_void_value(k + 1, end, self._ret, scopes)
         else:
             self._expr(k, end, scopes)
             self._cast_assignment(k, end, scopes)
@@ -594,6 +757,8 @@ class Converter:
             if dd.init is not None and not is_static:
                 self._expr(dd.init, dd.end, scopes)
                 self._cast_initializer(d, dd)
+                if dd.brackets == 0:
+                    self._cast_void_value(dd.init, dd.end, (d.type_text, dd.stars, 0), scopes)
             if is_static:
                 if "extern" in d.storage:
                     scopes[-1][nm] = ("global", self.globals.get(nm, info))
@@ -619,6 +784,7 @@ class Converter:
             r = self._lookup(scopes, self.t(k))
             if r is not None and r[0] in ("global", "static"):
                 self._wrap(k)
+        self._cast_call_args(a, b, scopes)
 
     def _wrap(self, k: int):
         self.add_prefix(k, "__gpu_global(")
@@ -634,8 +800,17 @@ class Converter:
             self.add_prefix(dd.init, self._cast_type(d.type_text, dd.stars))
 
     def _cast_assignment(self, a: int, b: int, scopes: list):
-        """`p = malloc(...)` or `p[i] = malloc(...)` with p's declared pointer type known: an explicit cast."""
+        """`p = malloc(...)` or `p[i] = malloc(...)` with p's declared pointer type known, or `lhs = chain`
+        where the chain has type void* and lhs a typed pointer: an explicit cast."""
         if not self.is_id(a):
+            return
+        eq = a
+        while eq < b and self.t(eq) != "=":
+            if self.t(eq) in ("(", "[", "{"):
+                eq = self.match[eq]
+            eq += 1
+        if eq < b and not (self.t(eq + 1) in ALLOCATORS and self.t(eq + 2) == "("):
+            self._cast_void_value(eq + 1, b, self._chain_info(a, eq, scopes), scopes)
             return
         k, subs = a + 1, 0
         while k < b and self.t(k) == "[":
@@ -738,18 +913,22 @@ def convert_files(sources, out_dir, max_ranks: int | None = None, include_dirs=(
     for src in srcs:
         headers = _project_headers(src, project, [Path(d).resolve() for d in include_dirs], {})
         imap = {name: Path(name).name + ".cuh" for name in headers.values()}
-        # typedef names and file-scope variables declared in the project's headers
-        types, globs = set(extra_types), {}
+        # typedef names, file-scope variables, struct members and function signatures of the project's
+        # headers
+        types, globs, structs, funcs = set(extra_types), {}, {}, {}
         for h in headers:
-            c = Converter(h.read_text(), max_ranks, types, include_map=imap)
+            c = Converter(h.read_text(), max_ranks, types, include_map=imap, structs_in=structs)
             c._collect_typedefs_and_globals()
             types |= c.types
             globs.update(c.globals)
+            structs.update(c.structs)
+            funcs.update(c.functions)
+        known = dict(include_map=imap, globals_in=globs, structs_in=structs, functions_in=funcs)
         for h in headers:
-            text = Converter(h.read_text(), max_ranks, types, include_map=imap, globals_in=globs).run()
+            text = Converter(h.read_text(), max_ranks, types, **known).run()
             (out_dir / (h.name + ".cuh")).write_text(text)
         out = out_dir / (src.stem + ".cu")
-        out.write_text(Converter(src.read_text(), max_ranks, types, include_map=imap, globals_in=globs).run())
+        out.write_text(Converter(src.read_text(), max_ranks, types, **known).run())
         converted.append(out)
     return converted
 

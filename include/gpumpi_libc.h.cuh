@@ -93,6 +93,18 @@ __device__ inline void* gpumpi_memchr(const void* s, int c, size_t n) {
     return nullptr;
 }
 
+// strdup / strndup: copies on CUDA's device heap (released with free)
+__device__ inline char* gpumpi_strndup(const char* s, size_t n) {
+    const size_t len = gpumpi_strnlen(s, n);
+    char* d = (char*)malloc(len + 1);
+    if (d) {
+        for (size_t i = 0; i < len; i++) d[i] = s[i];
+        d[len] = 0;
+    }
+    return d;
+}
+__device__ inline char* gpumpi_strdup(const char* s) { return gpumpi_strndup(s, (size_t)-1); }
+
 // calloc: CUDA's device malloc, zeroed (the block can be released with free)
 __device__ inline void* gpumpi_calloc(size_t n, size_t size) {
     if (size && n > ((size_t)-1) / size) return nullptr;
@@ -280,6 +292,8 @@ __device__ inline double gpumpi_atof(const char* s) { return gpumpi_strtod(s, nu
 #define atoll gpumpi_atoll
 #define atof gpumpi_atof
 #define calloc gpumpi_calloc
+#define strdup gpumpi_strdup
+#define strndup gpumpi_strndup
 #define getenv gpumpi_getenv
 #define exit gpumpi_exit
 #endif

@@ -11,6 +11,7 @@
 // GPUMPI_STDIO_NAMES before including this header gets the standard names (FILE, fopen, fprintf, ...)
 // mapped onto these functions.
 #pragma once
+#include <stdarg.h>
 #include <stddef.h>
 
 struct gpumpi_FILE_impl;
@@ -31,6 +32,12 @@ __device__ int gpumpi_remove(const char* path);
 // modifiers; the values are read on the device and formatted by the host.
 __device__ int gpumpi_fprintf(gpumpi_FILE* f, const char* fmt, ...);
 __device__ int gpumpi_printf(const char* fmt, ...);
+// Formatted into dst by the host (the same conversions); the text is cut to the rank's host-channel window
+// (host_window_bytes - 1 characters) and to size - 1 for the n forms; returns the full length, -1 on error.
+__device__ int gpumpi_sprintf(char* dst, const char* fmt, ...);
+__device__ int gpumpi_snprintf(char* dst, size_t size, const char* fmt, ...);
+__device__ int gpumpi_vsprintf(char* dst, const char* fmt, va_list ap);
+__device__ int gpumpi_vsnprintf(char* dst, size_t size, const char* fmt, va_list ap);
 
 #ifdef GPUMPI_STDIO_NAMES
 #define FILE gpumpi_FILE
@@ -49,4 +56,8 @@ __device__ int gpumpi_printf(const char* fmt, ...);
 #define fprintf gpumpi_fprintf
 #undef printf
 #define printf gpumpi_printf
+#define sprintf gpumpi_sprintf
+#define snprintf gpumpi_snprintf
+#define vsprintf gpumpi_vsprintf
+#define vsnprintf gpumpi_vsnprintf
 #endif

@@ -62,18 +62,24 @@ TOOLCHAIN_PROGRAMS = ["pi/cpi.c", "global_var/global_var.c", "datatype/contiguou
                       "basicIO/file_view1.c", "basicIO/file_view2.c"]
 
 
-# NPB IS (the integer sort of the NAS Parallel Benchmarks, which the reference's toolchain test converts
-# and runs: toolchain_tests/npb/is_test.sh): its sources and the common files it links
-NPB_IS = ["npb/NPB3.4.1/NPB3.4-MPI/IS/is.c", "npb/NPB3.4.1/NPB3.4-MPI/common/c_print_results.c",
-          "npb/NPB3.4.1/NPB3.4-MPI/common/c_timers.c", "npb/NPB3.4.1/NPB3.4-MPI/common/c_timers.h"]
+# NPB IS and DT (the integer sort and data traffic benchmarks of the NAS Parallel Benchmarks, which the
+# reference's toolchain tests convert and run: toolchain_tests/npb/is_test.sh, dt_test.sh): their sources,
+# the common files they link, and NPB's own parameter generator with its configuration template
+NPB = "npb/NPB3.4.1/NPB3.4-MPI"
+NPB_FILES = [f"{NPB}/{p}" for p in (
+    "IS/is.c", "DT/dt.c", "DT/DGraph.c", "DT/DGraph.h", "common/c_print_results.c", "common/c_timers.c",
+    "common/c_timers.h", "common/randdp.c", "sys/setparams.c", "config/make.def.template")]
+NPB_SOURCES = {"is": ["IS/is.c", "common/c_print_results.c", "common/c_timers.c"],
+               "dt": ["DT/dt.c", "DT/DGraph.c", "common/c_print_results.c", "common/c_timers.c", "common/randdp.c"]}
 
 
 def stage_toolchain() -> bool:
-    """Copies the reference's toolchain test programs (and NPB IS) unchanged into baseline/_ref/toolchain/
-    (git-ignored) for the source converter's tests: they are the converter's inputs in the reference, so
-    converting, building and running them here checks the converter against the reference's own programs."""
+    """Copies the reference's toolchain test programs (and NPB IS and DT) unchanged into
+    baseline/_ref/toolchain/ (git-ignored) for the source converter's tests: they are the converter's inputs in
+    the reference, so converting, building and running them here checks the converter against the reference's
+    own programs."""
     ref = reference_root() / "toolchain_tests"
-    files = TOOLCHAIN_PROGRAMS + NPB_IS
+    files = TOOLCHAIN_PROGRAMS + NPB_FILES
     if not all((ref / p).exists() for p in files):
         return all((TOOLCHAIN / p).exists() for p in files)
     for p in files:
@@ -82,12 +88,19 @@ def stage_toolchain() -> bool:
     return True
 
 
-def npb_is_params(cls: str = "S") -> str:
-    """npbparams.h of NPB IS for class `cls`, with the entries NPB's setparams writes for a C benchmark
-    (sys/setparams.c; the build-information strings name this toolchain)."""
-    return (f"#define CLASS '{cls}'\n#define NPBVERSION \"3.4.1\"\n#define COMPILETIME \"gpumpicc\"\n"
-            "#define MPICC \"gpumpicc\"\n#define CLINK \"gpumpicc\"\n#define CMPI_LIB \"\"\n"
-            "#define CMPI_INC \"\"\n#define CFLAGS \"-O3\"\n#define CLINKFLAGS \"\"\n")
+def npb_prepare(dst: Path, bench: str, cls: str = "S") -> list:
+    """Copies the staged NPB tree to dst and writes `bench`'s npbparams.h for class `cls` the way NPB's build
+    does (sys/setparams, compiled with the host C compiler, run in the benchmark's directory with the
+    configuration template as config/make.def); returns the benchmark's source files under dst."""
+    shutil.copytree(TOOLCHAIN / "npb", dst / "npb")
+    mpi = dst / NPB
+    shutil.copyfile(mpi / "config" / "make.def.template", mpi / "config" / "make.def")
+    cc = shutil.which("gcc") or shutil.which("cc")
+    subprocess.run([cc, "-o", str(mpi / "sys" / "setparams"), str(mpi / "sys" / "setparams.c")], check=True,
+                   capture_output=True)
+    bdir = mpi / bench.upper()
+    subprocess.run([str(mpi / "sys" / "setparams"), bench, cls], cwd=bdir, check=True, capture_output=True)
+    return [mpi / p for p in NPB_SOURCES[bench]]
 
 
 def sources() -> list:

@@ -88,6 +88,29 @@ void f(int n) { double *x = malloc(n * sizeof(double)); node *t; t = calloc(1, s
     assert "__gpu_global(grid) = (int **)malloc(8); __gpu_global(grid)[0] = (int *)malloc(4);" in out
 
 
+def test_void_pointer_members_get_casts():
+    # the reference's converter casts every implicit conversion from void*; here: values of void* struct
+    # members reaching typed pointers through assignment, initialisation, return and call arguments
+    src = """typedef struct { int id; void *head, *tail; } Arc;
+typedef struct node { Arc **in; void *feat; } Node;
+typedef struct { double *v; } Arr;
+double total(Arr *a, int w);
+Arr *feat_of(Node *n) { return n->feat; }
+double f(Arc *ar, Node *nd, int j) {
+  Node *h = ar->head, *t;
+  t = nd->in[j]->tail;
+  void *keep = ar->tail;
+  return total(nd->feat, j) + total(feat_of(h), 0);
+}
+"""
+    out = squash(conv(src))
+    assert "Arr *feat_of(Node *n) { return (Arr *)n->feat; }" in out
+    assert "Node *h = (Node *)ar->head, *t;" in out
+    assert "t = (Node *)nd->in[j]->tail;" in out
+    assert "void *keep = ar->tail;" in out
+    assert "return total((Arr *)nd->feat, j) + total(feat_of(h), 0);" in out
+
+
 def test_cxx_keywords_are_renamed():
     out = squash(conv("int f(int class) { int new = class, this = 1; return new + this; }"))
     assert "int f(int __decl_class) { int __decl_new = __decl_class, __decl_this = 1; return __decl_new + __decl_this; }" in out
@@ -163,16 +186,14 @@ def test_reference_toolchain_programs_convert_and_compile(tmp_path, prog):
     assert r.returncode == 0, r.stderr[-4000:]
 
 
-@pytest.mark.skipif(not all((refgpu.TOOLCHAIN / p).exists() for p in refgpu.NPB_IS),
-                    reason="NPB IS is not staged")
-def test_npb_is_converts_and_compiles(tmp_path):
+@pytest.mark.skipif(not all((refgpu.TOOLCHAIN / p).exists() for p in refgpu.NPB_FILES),
+                    reason="NPB is not staged")
+@pytest.mark.parametrize("bench", ["is", "dt"])
+def test_npb_converts_and_compiles(tmp_path, bench):
+    # NPB IS and DT class S, npbparams.h from NPB's own setparams, converted with their project headers
     import build as gbuild
-    npb = tmp_path / "npb"
-    shutil.copytree(refgpu.TOOLCHAIN / "npb", npb)
-    mpi = npb / "NPB3.4.1" / "NPB3.4-MPI"
-    (mpi / "IS" / "npbparams.h").write_text(refgpu.npb_is_params("S"))
-    srcs = [mpi / "IS" / "is.c", mpi / "common" / "c_print_results.c", mpi / "common" / "c_timers.c"]
-    out = cv.convert_files(srcs, tmp_path / "conv", max_ranks=8, project=npb)
+    srcs = refgpu.npb_prepare(tmp_path, bench, "S")
+    out = cv.convert_files(srcs, tmp_path / "conv", max_ranks=8, project=tmp_path / "npb")
     assert (tmp_path / "conv" / "npbparams.h.cuh").exists() and (tmp_path / "conv" / "c_timers.h.cuh").exists()
     for f in out:
         r = subprocess.run([gbuild.nvcc(), *gbuild.common_flags(), "-I", str(tmp_path / "conv"), "-c", str(f), "-o",

@@ -254,19 +254,24 @@ def test_reference_io_programs_run_converted(ref_programs, tmp_path, ranks):
     assert (tmp_path / "test_file_view2.out").stat().st_size == 2 * 50 * ranks * 4
 
 
+def _npb(tmp_path_factory, bench):
+    refgpu = _toolchain()
+    if not all((refgpu.TOOLCHAIN / p).exists() for p in refgpu.NPB_FILES):
+        pytest.skip("NPB is not staged")
+    from gpumpi import gpumpicc as cc
+    d = tmp_path_factory.mktemp("npb_" + bench)
+    srcs = refgpu.npb_prepare(d, bench, "S")   # npbparams.h from NPB's own setparams
+    return cc.compile_program(srcs, d / f"{bench}.S.x", max_ranks=64, project=d / "npb")
+
+
 @pytest.fixture(scope="module")
 def npb_is(tmp_path_factory, gpulib):
-    import shutil
-    refgpu = _toolchain()
-    if not all((refgpu.TOOLCHAIN / p).exists() for p in refgpu.NPB_IS):
-        pytest.skip("NPB IS is not staged")
-    from gpumpi import gpumpicc as cc
-    d = tmp_path_factory.mktemp("npb")
-    shutil.copytree(refgpu.TOOLCHAIN / "npb", d / "npb")
-    mpi = d / "npb" / "NPB3.4.1" / "NPB3.4-MPI"
-    (mpi / "IS" / "npbparams.h").write_text(refgpu.npb_is_params("S"))
-    srcs = [mpi / "IS" / "is.c", mpi / "common" / "c_print_results.c", mpi / "common" / "c_timers.c"]
-    return cc.compile_program(srcs, d / "is.S.x", max_ranks=16, project=d / "npb")
+    return _npb(tmp_path_factory, "is")
+
+
+@pytest.fixture(scope="module")
+def npb_dt(tmp_path_factory, gpulib):
+    return _npb(tmp_path_factory, "dt")
 
 
 @pytest.mark.parametrize("ranks,strict", [(2, None), (8, None), (16, None), (3, "off")])
@@ -293,3 +298,13 @@ def test_npb_is_exit_status_reaches_the_launcher(npb_is, tmp_path):
                        timeout=300, cwd=tmp_path, env=env)
     assert r.returncode == 1, (r.stdout[-2000:], r.stderr[-2000:])
     assert "is not a power of two" in r.stdout
+
+
+@pytest.mark.parametrize("graph,ranks", [("BH", 5), ("WH", 5), ("SH", 32)])
+def test_npb_dt_class_s_verifies(npb_dt, tmp_path, graph, ranks):
+    # toolchain_tests/npb/dt_test.sh: `make DT CLASS=S` through gpumpicc, then
+    # `./bin/dt.S.x BH ---gpumpi -g 5 -b 1 -s 16000 -p 80000000`; DT checks its own result
+    r = subprocess.run([str(npb_dt), graph, "---gpumpi", "-n", str(ranks), "-s", "16000"], capture_output=True,
+                       text=True, timeout=300, cwd=tmp_path)
+    assert r.returncode == 0, (r.stdout[-3000:], r.stderr[-3000:])
+    assert "Verification    =               SUCCESSFUL" in r.stdout, (r.stdout[-3000:], r.stderr[-3000:])
