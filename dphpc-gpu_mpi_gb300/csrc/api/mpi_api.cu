@@ -450,6 +450,68 @@ __device__ __noinline__ int coll_run(MPI_Comm_impl* c, const CollSlot& mine, con
     return ld_relaxed(&c->job.err) ? GPUMPI_ERR_TRUNCATE : 0;
 }
 
+// ---- small reductions without a job: the members split the chunks statically ----
+// Each member publishes its buffers in its slot and enters a barrier; member r then folds chunks r, r + n,
+// ... of the result, each over every member in rank order (the canonical order, bit-identical to the job
+// path), writes them where they go (every member's receive buffer, or the root's), and a second barrier
+// ends the call: the members' reads of the inputs and writes of the results are complete when the
+// barrier releases.  At these sizes the job path's set-up by the last arriver, chunk claims and
+// completion count cost more than the second barrier.
+struct StaticFold {
+    JobParams j;
+    long long first, step, nch;
+};
+__shared__ StaticFold s_sfold;
+
+__device__ void static_fold_task(void* arg, int tid, int nt) {
+    StaticFold* w = (StaticFold*)arg;
+    for (long long k = w->first; k < w->nch; k += w->step) fold_chunk(&w->j, k, tid, nt);
+}
+
+// Whether a reduction takes the static split: every member computes the same answer from what all share.
+__device__ __forceinline__ bool static_fold_ok(long long count, int es, int n) {
+    const long long bytes = count * es;
+    return c_rt.static_fold_bytes > 0 && bytes <= c_rt.static_fold_bytes && n >= 2 &&
+           count <= (long long)n * nthreads();
+}
+
+__device__ __noinline__ int coll_run_static(MPI_Comm_impl* c, const CollSlot& mine, const CollArgs& a, int line) {
+    const int cr = comm_rank_of(c, me());
+    c->slots[cr] = mine;
+    c_rt.ranks[me()].coll_calls++;
+    int rc = comm_barrier(c, []() {}, line);
+    if (rc) return rc;
+    StaticFold* w = &s_sfold;
+    JobParams& j = w->j;
+    j.kind = a.kind;
+    j.dt = a.dt;
+    j.op = a.op;
+    j.root = a.root;
+    j.esize = a.esize;
+    j.vec = 1;
+    j.tile = 0;
+    j.aligned16 = 0;  // element-wide loads: no member's alignment is needed
+    j.variant = GPUMPI_VARIANT_DIRECT;
+    j.epoch = 0;
+    j.count = a.count;
+    j.chunk = nthreads();
+    j.comm = c;
+    j.src = nullptr;
+    j.dst = nullptr;
+    j.ufn = a.ufn;
+    w->first = cr;
+    w->step = c->size;
+    w->nch = (a.count + j.chunk - 1) / j.chunk;
+    if (w->first < w->nch) {
+        Task t;
+        t.kind = TASK_USER;
+        t.p0 = (const void*)&static_fold_task;
+        t.p1 = w;
+        dispatch(t);
+    }
+    return comm_barrier(c, []() {}, line);
+}
+
 __device__ __forceinline__ int op_code_of(MPI_Op op, MPI_User_function** ufn) {
     *ufn = nullptr;
     if (!op) return -1;
@@ -756,7 +818,9 @@ __device__ __noinline__ int fold_collective(int kind, const void* sendbuf, void*
     a.est_piece = 0;
     a.variant = c_rt.variant_override >= 0 ? c_rt.variant_override : route >= 0 ? route : GPUMPI_VARIANT_AUTO;
     a.learned = a.variant < 0 && c_rt.selector_mode == 2 && c_rt.mlp_params;
-    int rc = coll_run(c, my, a, __LINE__);
+    // (a forced variant or a route the small-message rules chose keeps the job path)
+    const bool stat = c_rt.variant_override < 0 && route == GPUMPI_VARIANT_AUTO && static_fold_ok(count, es, c->size);
+    int rc = stat ? coll_run_static(c, my, a, __LINE__) : coll_run(c, my, a, __LINE__);
     stage_out(ss, false);
     stage_out(rs, has_out);
     return rc;

@@ -183,6 +183,10 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
 /* GPUMPI_TUNE_HOST_STREAMS: copy streams per direction of the sliced host-buffer Allreduce (1..4): each
  * slice's 2D copy is split into that many row groups copied concurrently. */
 #define GPUMPI_TUNE_HOST_STREAMS 11
+/* GPUMPI_TUNE_STATIC_FOLD: an Allreduce / Reduce of more than 64 bytes and at most this many bytes per member,
+ * with at most one chunk (a block's threads' elements) per member, runs without a job: the members split
+ * the chunks statically between two barriers (0 = always the job path; default 4 KiB). */
+#define GPUMPI_TUNE_STATIC_FOLD 13
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Launcher of a converted program (the reference's gpu_main): argv holds the program's arguments, then
  * optionally `---gpumpi` and the run's options (gpumpi_parse_args); creates the world, runs `program` on

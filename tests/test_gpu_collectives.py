@@ -136,6 +136,31 @@ def test_sliced_host_allreduce_matches_oracle(gpulib, oracle, mode):
         assert e.value.code == e1.value.code
 
 
+@pytest.mark.parametrize("n,count,dt,npdt", [(32, 1000, 12, np.float32), (128, 257, 13, np.float64),
+                                              (200, 1024, 2, np.int32), (513, 100, 12, np.float32)])
+def test_static_split_reductions_match_the_job_path(gpulib, oracle, n, count, dt, npdt):
+    """Reductions of at most TUNE_STATIC_FOLD bytes per member run without a job (the members split the
+    chunks statically between two barriers): bit-exact with the oracle and with the job path, for
+    Allreduce, Allreduce in place and Reduce to a non-zero root."""
+    x = make_input(oracle, n, count, npdt, 77 + n)
+    ref = oracle.allreduce(x, dt, 2)
+    root = n // 3
+    with gpulib.World(n, timeout_s=10.0) as w:
+        for thr in (1 << 20, 0):           # static split, then the job path
+            w.set_tuning(gpulib.TUNE_STATIC_FOLD, thr)
+            assert w.get_tuning(gpulib.TUNE_STATIC_FOLD) == thr
+            s, r = dev(x), dev(np.zeros_like(x))
+            w.allreduce(s, r, count, dt, 2)
+            assert np.array_equal(host(r).view(np.uint8), ref.view(np.uint8)), thr
+            buf = dev(x)
+            rc = w.coll("allreduce", 1, buf, count, dt, 2, send_stride=0, recv_stride=count * x.itemsize)
+            assert rc == 0 and np.array_equal(host(buf).view(np.uint8), ref.view(np.uint8)), thr
+            r = dev(np.zeros_like(x))
+            w.reduce(dev(x), r, count, dt, 2, root=root)
+            got = host(r)
+            assert np.array_equal(got[root].view(np.uint8), ref[root].view(np.uint8)), thr
+
+
 def test_allreduce_variants_agree(gpulib, oracle):
     n, count = 64, 1 << 14
     x = make_input(oracle, n, count, np.float32, 9)
