@@ -1236,6 +1236,21 @@ __device__ int MPI_Bcast(void* buffer, int count, MPI_Datatype datatype, int roo
     my.rdesc = t;
     my.stype = datatype;
     my.rtype = datatype;
+    if (c_rt.variant_override < 0 && bytes <= c_rt.static_fold_bytes) {
+        // small broadcast without a job: every member copies its own piece from the root's buffer between
+        // two barriers (the second keeps the root's buffer valid until every member has read it)
+        c->slots[cr] = my;
+        int rc = comm_barrier(c, []() {}, __LINE__);
+        if (!rc && cr != root) {
+            const CollSlot* rs = &c->slots[root];
+            const void* src = (const void*)__ldcg((const unsigned long long*)&rs->sbuf);
+            const TypeDesc* sd = (const TypeDesc*)__ldcg((const unsigned long long*)&rs->sdesc);
+            t0_copy(gb, desc_contiguous(t) ? nullptr : t, src, desc_contiguous(sd) ? nullptr : sd, bytes);
+        }
+        const int rc2 = comm_barrier(c, []() {}, __LINE__);
+        stage_out(st, cr != root);
+        return rc ? rc : rc2;
+    }
     CollArgs a;
     a.kind = JOB_BCAST;
     a.count = 0;
