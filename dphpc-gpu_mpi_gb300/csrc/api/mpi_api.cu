@@ -1236,7 +1236,7 @@ __device__ int MPI_Bcast(void* buffer, int count, MPI_Datatype datatype, int roo
     my.rdesc = t;
     my.stype = datatype;
     my.rtype = datatype;
-    if (c_rt.variant_override < 0 && bytes <= c_rt.static_fold_bytes) {
+    if (c_rt.variant_override < 0 && bytes <= c_rt.static_bcast_bytes) {
         // small broadcast without a job: every member copies its own piece from the root's buffer between
         // two barriers (the second keeps the root's buffer valid until every member has read it)
         c->slots[cr] = my;

@@ -399,6 +399,7 @@ struct Runtime {
     long long engine_min_bytes;       // smaller jobs are not posted to the engines
     long long static_fold_bytes;      // reductions of at most this many bytes per member (and at most one
                                       // chunk per member) split their chunks statically, without a job
+    long long static_bcast_bytes;     // broadcasts of at most this many bytes copy from the root without a job
     int variant_override;             // -1: selector decides
     int selector_mode;                // 0 plain (DIRECT), 1 tuned table, 2 learned MLP, 3 heuristic
     int dyn_smem;                     // dynamic shared memory bytes of this launch (STAGED stages)

@@ -185,10 +185,11 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
 #define GPUMPI_TUNE_HOST_STREAMS 11
 /* GPUMPI_TUNE_STATIC_FOLD: an Allreduce / Reduce of more than 64 bytes and at most this many bytes per member,
  * with at most one chunk (a block's threads' elements) per member, runs without a job: the members split
- * the chunks statically between two barriers; a Bcast of more than 64 bytes and at most this many runs
- * without a job too, every member copying its piece from the root between two barriers (0 = always the
- * job path; default 4 KiB). */
+ * the chunks statically between two barriers (0 = always the job path; default 4 KiB). */
 #define GPUMPI_TUNE_STATIC_FOLD 13
+/* GPUMPI_TUNE_STATIC_BCAST: a Bcast of more than 64 bytes and at most this many runs without a job, every
+ * member copying its piece from the root between two barriers (0 = always the job path; default 64 KiB). */
+#define GPUMPI_TUNE_STATIC_BCAST 14
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Launcher of a converted program (the reference's gpu_main): argv holds the program's arguments, then
  * optionally `---gpumpi` and the run's options (gpumpi_parse_args); creates the world, runs `program` on
