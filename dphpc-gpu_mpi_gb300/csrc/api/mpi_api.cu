@@ -1379,39 +1379,46 @@ __device__ void piece_gather_task(void* arg, int tid, int nt) {
 __device__ __forceinline__ void piece_gather(const unsigned char* tiny, const CollSlot* slots, void* dst, int n,
                                              int parity, int bytes, int cr);
 
-// Small uniform alltoall (at most 256 bytes per pair, 64 KiB per member, contiguous, device buffers): each
-// member publishes its send buffer, a barrier, every member pulls its n pieces straight from the senders'
-// buffers, and a second barrier before any sender may reuse its buffer.  Two barriers instead of a job of
-// n^2 pieces (1024 ranks x 4 bytes: about 90 us as a job).  Returns -1 when the call does not qualify.
-__device__ int small_alltoall(MPI_Comm_impl* c, const void* sendbuf, int sendcount, const TypeDesc* st, void* recvbuf,
-                              int recvcount, const TypeDesc* rt) {
-    // the choice depends only on what every member shares (sizes, the policy); a member whose buffers
-    // are thread-local or whose types are not contiguous packs and unpacks through its scratch pool
+// Small uniform alltoall and allgather (at most SMALL_PIECE bytes per pair or contribution and 64 KiB per
+// member, any datatypes and buffers): each member publishes its send buffer, a barrier, every member pulls
+// its n pieces straight from the senders' buffers, and a second barrier before any sender may reuse its
+// buffer.  Two barriers instead of a job of n^2 (or n) pieces: 1024 ranks x 4 bytes of alltoall took about
+// 90 us as a job.  A member whose buffers are thread-local or whose types are not contiguous packs and
+// unpacks through its scratch pool.  Returns -1 when the call does not qualify (the choice depends only on
+// what every member shares: sizes and the policy).
+constexpr long long SMALL_PIECE = 4096;
+__device__ int small_pull(MPI_Comm_impl* c, const void* sendbuf, int sendcount, const TypeDesc* st, void* recvbuf,
+                          int recvcount, const TypeDesc* rt, bool gather) {
     const long long pb = (long long)sendcount * st->size;
-    if (sendbuf == MPI_IN_PLACE || sendcount < 0 || pb != (long long)recvcount * rt->size || pb > 256 ||
+    if (sendbuf == MPI_IN_PLACE || sendcount < 0 || pb != (long long)recvcount * rt->size || pb > SMALL_PIECE ||
         pb * c->size > 65536 || c_rt.variant_override >= 0)
         return -1;
     const int bytes = (int)pb, n = c->size;
     const int cr = comm_rank_of(c, me());
-    const long long all = (long long)n * bytes;
+    const long long all = (long long)n * bytes, sall = gather ? bytes : all;
     const bool direct_send = desc_contiguous(st) && is_global_ptr(sendbuf);
     const bool direct_recv = desc_contiguous(rt) && is_global_ptr(recvbuf);
-    void* sstage = direct_send || all == 0 ? nullptr : scratch_alloc((unsigned long long)all);
+    void* sstage = direct_send || sall == 0 ? nullptr : scratch_alloc((unsigned long long)sall);
     void* rstage = direct_recv || all == 0 ? nullptr : scratch_alloc((unsigned long long)all);
     int rc = 0;
-    if ((!direct_send && all && !sstage) || (!direct_recv && all && !rstage)) rc = GPUMPI_ERR_NO_MEM;
-    if (sstage) t0_copy(sstage, nullptr, sendbuf, desc_contiguous(st) ? nullptr : st, all);
+    if ((!direct_send && sall && !sstage) || (!direct_recv && all && !rstage)) rc = GPUMPI_ERR_NO_MEM;
+    if (sstage) t0_copy(sstage, nullptr, sendbuf, desc_contiguous(st) ? nullptr : st, sall);
     c->slots[cr].sbuf = direct_send ? sendbuf : sstage;  // nullptr when staging failed: the others skip it
     // (a member that could not stage still takes part in both barriers, so the others do not wait)
     const int rb = comm_barrier(c, []() {}, __LINE__);
     if (!rc) rc = rb;
-    if (!rc && bytes > 0) piece_gather(nullptr, c->slots, rstage ? rstage : recvbuf, n, 0, bytes, cr);
+    // piece q of member cr: member q's send buffer at cr * bytes (alltoall) or at 0 (allgather)
+    if (!rc && bytes > 0) piece_gather(nullptr, c->slots, rstage ? rstage : recvbuf, n, 0, bytes, gather ? 0 : cr);
     const int rb2 = comm_barrier(c, []() {}, __LINE__);
     if (!rc) rc = rb2;
     if (!rc && rstage) t0_copy(recvbuf, desc_contiguous(rt) ? nullptr : rt, rstage, nullptr, all);
     scratch_free(rstage);
     scratch_free(sstage);
     return rc;
+}
+__device__ int small_alltoall(MPI_Comm_impl* c, const void* sendbuf, int sendcount, const TypeDesc* st, void* recvbuf,
+                              int recvcount, const TypeDesc* rt) {
+    return small_pull(c, sendbuf, sendcount, st, recvbuf, recvcount, rt, false);
 }
 
 __device__ __forceinline__ void piece_gather(const unsigned char* tiny, const CollSlot* slots, void* dst, int n,
@@ -1461,6 +1468,9 @@ __device__ int MPI_Allgather(const void* sendbuf, int sendcount, MPI_Datatype se
                         c->tiny + ((size_t)q * 2 + (g & 1)) * TINY_BYTES, nullptr, bytes);
         }
         return MPI_SUCCESS;
+    }
+    if (sendbuf != MPI_IN_PLACE) {
+        if (int rc = small_pull(c, sendbuf, sendcount, st, recvbuf, recvcount, rt, true); rc != -1) return rc;
     }
     CollSlot my{};
     my.rbuf = recvbuf;
