@@ -659,6 +659,7 @@ __device__ __forceinline__ int learned_choice(MPI_Comm_impl* c, int kind, long l
 struct TinyFold {
     const unsigned char* tiny;
     int n, parity, count, es, dt, op;
+    int stride;  // bytes per staged operand in shared memory: the operand's 16-byte vectors only
     unsigned char out[TINY_BYTES];  // the result, also the accumulators (element e at e * es)
 };
 __shared__ TinyFold s_tiny_fold;
@@ -668,8 +669,9 @@ __shared__ TinyFold s_tiny_fold;
 template <class T, int OP>
 __device__ __forceinline__ void tiny_fold_typed(TinyFold* w, const unsigned char* buf, int m, int r0, int tid) {
     T* acc = (T*)w->out + tid;
+    const int st = w->stride;
     T a = r0 == 0 ? ((const T*)buf)[tid] : *acc;
-    for (int i = r0 == 0 ? 1 : 0; i < m; i++) a = op_apply<OP, T>(((const T*)(buf + (size_t)i * TINY_BYTES))[tid], a);
+    for (int i = r0 == 0 ? 1 : 0; i < m; i++) a = op_apply<OP, T>(((const T*)(buf + (size_t)i * st))[tid], a);
     *acc = a;
 }
 
@@ -697,21 +699,22 @@ __device__ __forceinline__ bool tiny_fold_fast(TinyFold* w, const unsigned char*
 
 __device__ void tiny_fold_task(void* arg, int tid, int nt) {
     TinyFold* w = (TinyFold*)arg;
-    unsigned char* buf = (unsigned char*)g_dyn_smem;  // staged operands, TINY_BYTES per rank
-    const int tile = c_rt.dyn_smem / TINY_BYTES;
+    unsigned char* buf = (unsigned char*)g_dyn_smem;  // staged operands, w->stride bytes per rank
     const int vecs = (w->count * w->es + 15) / 16;
+    // as many operands per tile as the dynamic shared memory holds (8 KiB: 512 operands of 16 bytes)
+    const int tile = c_rt.dyn_smem / w->stride;
     unsigned char* acc = w->out + tid * w->es;
     for (int r0 = 0; r0 < w->n; r0 += tile) {
         const int m = min(tile, w->n - r0);
         for (int x = tid; x < m * vecs; x += nt) {
             const int i = x / vecs, k = x % vecs;
             const uint4* src = (const uint4*)(w->tiny + ((size_t)(r0 + i) * 2 + w->parity) * TINY_BYTES) + k;
-            ((uint4*)(buf + (size_t)i * TINY_BYTES))[k] = __ldcg(src);
+            ((uint4*)(buf + (size_t)i * w->stride))[k] = __ldcg(src);
         }
         bar_sync(BAR_TASK, nt);
         if (tid < w->count && !tiny_fold_fast(w, buf, m, r0, tid)) {
             for (int i = 0; i < m; i++) {
-                const unsigned char* src = buf + (size_t)i * TINY_BYTES + tid * w->es;
+                const unsigned char* src = buf + (size_t)i * w->stride + tid * w->es;
                 if (r0 + i == 0) {
                     for (int b = 0; b < w->es; b++) acc[b] = src[b];
                 } else {
@@ -740,6 +743,7 @@ __device__ __noinline__ int tiny_fold(MPI_Comm_impl* c, int kind, const void* sb
     w->es = es;
     w->dt = dt;
     w->op = op;
+    w->stride = (bytes + 15) / 16 * 16;
     Task t;
     t.kind = TASK_USER;
     t.p0 = (const void*)&tiny_fold_task;
