@@ -660,8 +660,10 @@ struct TinyFold {
     const unsigned char* tiny;
     int n, parity, count, es, dt, op;
     int stride;  // bytes per staged operand in shared memory: the operand's 16-byte vectors only
-    unsigned char out[TINY_BYTES];  // the result, also the accumulators (element e at e * es)
+    alignas(16) unsigned char out[TINY_BYTES];  // the result, also the accumulators (element e at e * es,
+                                                // read and written as the element type)
 };
+static_assert(offsetof(TinyFold, out) % 16 == 0, "the accumulators are accessed as 8- and 16-byte values");
 __shared__ TinyFold s_tiny_fold;
 
 // fold of a staged tile of m ranks (the first at r0) into the accumulators, element tid; typed for the
