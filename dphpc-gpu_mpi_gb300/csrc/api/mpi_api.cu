@@ -863,6 +863,82 @@ __device__ __noinline__ int pull_collective(int kind, MPI_Comm_impl* c, CollSlot
     return rc;
 }
 
+// ---- small Alltoallv without a job: every member pulls its own pieces ----
+// The members publish their buffers, counts and displacements and pass a barrier; then, when the size
+// estimate every member computes from the same 8 members' counts says the members receive little, each
+// member pulls its n pieces (senders q = 0..n-1 into its own buffer) with the pull executor's tile copies,
+// and a second barrier keeps the senders' buffers valid until every member has read them.  Otherwise the
+// call continues on the job path.
+struct SmallPullV {
+    JobParams j;
+    Job* jg;
+    long long p0;
+    int n;
+};
+__shared__ SmallPullV s_spv;
+
+__device__ void small_pullv_task(void* arg, int tid, int nt) {
+    SmallPullV* w = (SmallPullV*)arg;
+    for (int k = 0; k < w->n; k += nt) pull_tile(&w->j, w->jg, w->p0 + k, min(nt, w->n - k), tid, nt);
+}
+
+__device__ __noinline__ int alltoallv_collective(MPI_Comm_impl* c, CollSlot& my, long long sbytes, long long rbytes,
+                                                 long long est_piece) {
+    if (c_rt.variant_override >= 0 || c_rt.static_pull_bytes <= 0 || c->size < 2)
+        return pull_collective(JOB_ALLTOALLV, c, my, sbytes, rbytes, est_piece, 0);
+    Stage ss, rs;
+    const void* gsb = stage_in(ss, my.sbuf, sbytes, true);
+    void* grb = stage_in(rs, my.rbuf, rbytes, false);
+    if ((my.sbuf && sbytes > 0 && !gsb) || (my.rbuf && rbytes > 0 && !grb)) return GPUMPI_ERR_NO_MEM;
+    my.sbuf = gsb;
+    my.rbuf = grb;
+    const int cr = comm_rank_of(c, me());
+    const int n = c->size;
+    c->slots[cr] = my;
+    int rc = comm_barrier(c, []() {}, __LINE__);
+    const long long est = rc ? -1 : shared_piece_estimate(c);
+    if (!rc && est >= 0 && est * n <= c_rt.static_pull_bytes) {
+        Job* jg = &c_rt.ranks[me()].p2p_job;  // idle during a collective: collects the truncation flag
+        jg->err = 0;
+        SmallPullV* w = &s_spv;
+        JobParams& j = w->j;
+        memset(&j, 0, sizeof(j));
+        j.kind = JOB_ALLTOALLV;
+        j.variant = GPUMPI_VARIANT_DIRECT;  // receiver-major pieces: member cr's are [cr * n, cr * n + n)
+        j.comm = c;
+        j.vec = 1;
+        j.tile = nthreads();
+        j.count = (long long)n * n;
+        j.dt = my.stype;
+        w->jg = jg;
+        w->p0 = (long long)cr * n;
+        w->n = n;
+        Task t;
+        t.kind = TASK_USER;
+        t.p0 = (const void*)&small_pullv_task;
+        t.p1 = w;
+        dispatch(t);
+        rc = comm_barrier(c, []() {}, __LINE__);
+        if (!rc && ld_relaxed(&jg->err)) rc = GPUMPI_ERR_TRUNCATE;
+    } else if (!rc) {
+        CollArgs a;
+        a.kind = JOB_ALLTOALLV;
+        a.count = 0;
+        a.dt = my.stype;
+        a.op = 0;
+        a.root = 0;
+        a.esize = 0;
+        a.ufn = nullptr;
+        a.est_piece = est_piece;
+        a.variant = -1;
+        a.learned = c_rt.selector_mode == 2 && c_rt.mlp_params;
+        rc = coll_run(c, my, a, __LINE__);
+    }
+    stage_out(ss, false);
+    stage_out(rs, true);
+    return rc;
+}
+
 __device__ long long sample_counts(const int* counts, int n) {
     if (!counts || n <= 0) return 0;
     long long s = 0;
@@ -1305,7 +1381,7 @@ __device__ int MPI_Alltoallv(const void* sendbuf, const int sendcounts[], const 
     my.stype = sendtype;
     my.rtype = recvtype;
     long long est = sample_counts(sendcounts, n) * st->size;
-    int rc = pull_collective(JOB_ALLTOALLV, c, my, sspan, rspan, est, 0);
+    int rc = alltoallv_collective(c, my, sspan, rspan, est);
     stage_out(s1, false);
     stage_out(s2, false);
     stage_out(s3, false);

@@ -400,6 +400,8 @@ struct Runtime {
     long long static_fold_bytes;      // reductions of at most this many bytes per member (and at most one
                                       // chunk per member) split their chunks statically, without a job
     long long static_bcast_bytes;     // broadcasts of at most this many bytes copy from the root without a job
+    long long static_pull_bytes;      // an Alltoallv whose members receive about this many bytes or fewer
+                                      // pulls its pieces without a job
     int variant_override;             // -1: selector decides
     int selector_mode;                // 0 plain (DIRECT), 1 tuned table, 2 learned MLP, 3 heuristic
     int dyn_smem;                     // dynamic shared memory bytes of this launch (STAGED stages)

@@ -190,6 +190,10 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
 /* GPUMPI_TUNE_STATIC_BCAST: a Bcast of more than 64 bytes and at most this many runs without a job, every
  * member copying its piece from the root between two barriers (0 = always the job path; default 64 KiB). */
 #define GPUMPI_TUNE_STATIC_BCAST 14
+/* GPUMPI_TUNE_STATIC_PULL: an Alltoallv whose members receive about this many bytes or fewer (the estimate
+ * every member computes from 8 members' counts) pulls its pieces without a job: every member pulls its own
+ * pieces from the senders between two barriers (0 = always the job path; default 64 KiB). */
+#define GPUMPI_TUNE_STATIC_PULL 15
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Launcher of a converted program (the reference's gpu_main): argv holds the program's arguments, then
  * optionally `---gpumpi` and the run's options (gpumpi_parse_args); creates the world, runs `program` on
