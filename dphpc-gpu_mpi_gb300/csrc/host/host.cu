@@ -307,7 +307,7 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     r.engine_min_bytes = cfg.engine_min_bytes;
     r.static_fold_bytes = 4096;
     r.static_bcast_bytes = 64 << 10;
-    r.static_pull_bytes = 64 << 10;
+    r.static_pull_bytes = 128 << 10;
     r.variant_override = -1;
     r.selector_mode = 0;
     r.trace_cap = cfg.trace_capacity;
