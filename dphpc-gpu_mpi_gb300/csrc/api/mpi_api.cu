@@ -315,6 +315,7 @@ __device__ int pick_vec(long long count, int T, int es, long long target, int al
 
 __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, unsigned e_next) {
     Job* j = &c->job;
+    j->own_pulls = 0;
     unsigned mis = ld_relaxed(&c->misalign[e_next & 1]);
     c->misalign[(e_next + 1) & 1] = 0;
     j->kind = a.kind;
@@ -410,6 +411,14 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         j->variant = variant;
         j->sel_bytes = a_est * n;
         bytes = a_est * P;
+        // a small Alltoallv takes no job: every member pulls its own pieces (coll_run, own_pulls)
+        if (a.kind == JOB_ALLTOALLV && a.variant < 0 && c_rt.static_pull_bytes > 0 &&
+            a_est * n <= c_rt.static_pull_bytes) {
+            j->own_pulls = 1;
+            j->variant = GPUMPI_VARIANT_DIRECT;
+            job_open(j, 0);
+            return;
+        }
         may_post = may_post && bytes >= c_rt.engine_min_bytes;
         long long target = n + (may_post ? c_rt.nengines : 0);
         if (a_est >= 65536) {
@@ -431,6 +440,50 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
     if (may_post && nchunks > n) board_post(j, e);
 }
 
+// ---- small Alltoallv without a job: every member pulls its own pieces ----
+// When the set-up (the last member to arrive at the collective's barrier) finds the size estimate every
+// member would compute from the same 8 members' counts small, it opens no chunks: each member pulls its n
+// pieces (senders q = 0..n-1 into its own buffer) with the pull executor's tile copies, and a second
+// barrier keeps the senders' buffers valid until every member has read them.
+struct OwnPulls {
+    JobParams j;
+    Job* jg;
+    long long p0;
+    int n;
+};
+__shared__ OwnPulls s_own_pulls;
+
+__device__ void own_pulls_task(void* arg, int tid, int nt) {
+    OwnPulls* w = (OwnPulls*)arg;
+    for (int k = 0; k < w->n; k += nt) pull_tile(&w->j, w->jg, w->p0 + k, min(nt, w->n - k), tid, nt);
+}
+
+__device__ __noinline__ int own_pulls(MPI_Comm_impl* c, int cr, int line) {
+    const int n = c->size;
+    Job* jg = &c_rt.ranks[me()].p2p_job;  // idle during a collective: collects the truncation flag
+    jg->err = 0;
+    OwnPulls* w = &s_own_pulls;
+    JobParams& j = w->j;
+    memset(&j, 0, sizeof(j));
+    j.kind = JOB_ALLTOALLV;
+    j.variant = GPUMPI_VARIANT_DIRECT;  // receiver-major pieces: member cr's are [cr * n, cr * n + n)
+    j.comm = c;
+    j.vec = 1;
+    j.tile = nthreads();
+    j.count = (long long)n * n;
+    w->jg = jg;
+    w->p0 = (long long)cr * n;
+    w->n = n;
+    Task t;
+    t.kind = TASK_USER;
+    t.p0 = (const void*)&own_pulls_task;
+    t.p1 = w;
+    dispatch(t);
+    int rc = comm_barrier(c, []() {}, line);
+    if (!rc && ld_relaxed(&jg->err)) rc = GPUMPI_ERR_TRUNCATE;
+    return rc;
+}
+
 __device__ __noinline__ int coll_run(MPI_Comm_impl* c, const CollSlot& mine, const CollArgs& a, int line) {
     const int cr = comm_rank_of(c, me());
     c->slots[cr] = mine;
@@ -443,6 +496,7 @@ __device__ __noinline__ int coll_run(MPI_Comm_impl* c, const CollSlot& mine, con
     int rc = comm_barrier(c, [&]() { coll_setup(c, a, e_next); }, line);
     if (rc) return rc;
     if (a.kind == JOB_BARRIER) return 0;
+    if (a.kind == JOB_ALLTOALLV && ld_relaxed(&c->job.own_pulls)) return own_pulls(c, cr, line);
     rc = job_run_and_wait(&c->job, line);
     if (rc) return rc;
     if (c_rt.trace_enabled && cr == 0) trace_record(c, a.kind, c->job.variant, a.dt, a.op, c->job.sel_bytes,
@@ -858,82 +912,6 @@ __device__ __noinline__ int pull_collective(int kind, MPI_Comm_impl* c, CollSlot
     a.variant = c_rt.variant_override;
     a.learned = a.variant < 0 && kind == JOB_ALLTOALLV && c_rt.selector_mode == 2 && c_rt.mlp_params;
     int rc = coll_run(c, my, a, __LINE__);
-    stage_out(ss, false);
-    stage_out(rs, true);
-    return rc;
-}
-
-// ---- small Alltoallv without a job: every member pulls its own pieces ----
-// The members publish their buffers, counts and displacements and pass a barrier; then, when the size
-// estimate every member computes from the same 8 members' counts says the members receive little, each
-// member pulls its n pieces (senders q = 0..n-1 into its own buffer) with the pull executor's tile copies,
-// and a second barrier keeps the senders' buffers valid until every member has read them.  Otherwise the
-// call continues on the job path.
-struct SmallPullV {
-    JobParams j;
-    Job* jg;
-    long long p0;
-    int n;
-};
-__shared__ SmallPullV s_spv;
-
-__device__ void small_pullv_task(void* arg, int tid, int nt) {
-    SmallPullV* w = (SmallPullV*)arg;
-    for (int k = 0; k < w->n; k += nt) pull_tile(&w->j, w->jg, w->p0 + k, min(nt, w->n - k), tid, nt);
-}
-
-__device__ __noinline__ int alltoallv_collective(MPI_Comm_impl* c, CollSlot& my, long long sbytes, long long rbytes,
-                                                 long long est_piece) {
-    if (c_rt.variant_override >= 0 || c_rt.static_pull_bytes <= 0 || c->size < 2)
-        return pull_collective(JOB_ALLTOALLV, c, my, sbytes, rbytes, est_piece, 0);
-    Stage ss, rs;
-    const void* gsb = stage_in(ss, my.sbuf, sbytes, true);
-    void* grb = stage_in(rs, my.rbuf, rbytes, false);
-    if ((my.sbuf && sbytes > 0 && !gsb) || (my.rbuf && rbytes > 0 && !grb)) return GPUMPI_ERR_NO_MEM;
-    my.sbuf = gsb;
-    my.rbuf = grb;
-    const int cr = comm_rank_of(c, me());
-    const int n = c->size;
-    c->slots[cr] = my;
-    int rc = comm_barrier(c, []() {}, __LINE__);
-    const long long est = rc ? -1 : shared_piece_estimate(c);
-    if (!rc && est >= 0 && est * n <= c_rt.static_pull_bytes) {
-        Job* jg = &c_rt.ranks[me()].p2p_job;  // idle during a collective: collects the truncation flag
-        jg->err = 0;
-        SmallPullV* w = &s_spv;
-        JobParams& j = w->j;
-        memset(&j, 0, sizeof(j));
-        j.kind = JOB_ALLTOALLV;
-        j.variant = GPUMPI_VARIANT_DIRECT;  // receiver-major pieces: member cr's are [cr * n, cr * n + n)
-        j.comm = c;
-        j.vec = 1;
-        j.tile = nthreads();
-        j.count = (long long)n * n;
-        j.dt = my.stype;
-        w->jg = jg;
-        w->p0 = (long long)cr * n;
-        w->n = n;
-        Task t;
-        t.kind = TASK_USER;
-        t.p0 = (const void*)&small_pullv_task;
-        t.p1 = w;
-        dispatch(t);
-        rc = comm_barrier(c, []() {}, __LINE__);
-        if (!rc && ld_relaxed(&jg->err)) rc = GPUMPI_ERR_TRUNCATE;
-    } else if (!rc) {
-        CollArgs a;
-        a.kind = JOB_ALLTOALLV;
-        a.count = 0;
-        a.dt = my.stype;
-        a.op = 0;
-        a.root = 0;
-        a.esize = 0;
-        a.ufn = nullptr;
-        a.est_piece = est_piece;
-        a.variant = -1;
-        a.learned = c_rt.selector_mode == 2 && c_rt.mlp_params;
-        rc = coll_run(c, my, a, __LINE__);
-    }
     stage_out(ss, false);
     stage_out(rs, true);
     return rc;
@@ -1381,7 +1359,7 @@ __device__ int MPI_Alltoallv(const void* sendbuf, const int sendcounts[], const 
     my.stype = sendtype;
     my.rtype = recvtype;
     long long est = sample_counts(sendcounts, n) * st->size;
-    int rc = alltoallv_collective(c, my, sspan, rspan, est);
+    int rc = pull_collective(JOB_ALLTOALLV, c, my, sspan, rspan, est, 0);
     stage_out(s1, false);
     stage_out(s2, false);
     stage_out(s3, false);

@@ -173,6 +173,7 @@ struct alignas(128) Job {
     void* dst;
     MPI_User_function* ufn;
     unsigned long long t_setup;  // globaltimer at set-up (traces)
+    unsigned own_pulls;          // set-up chose the job-free route: every member pulls its own pieces
     long long sel_bytes;         // bytes per rank the variant choice was made for (traces)
 };
 
