@@ -400,6 +400,16 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             const long long est = shared_piece_estimate(c);
             if (est >= 0) a_est = est;
         }
+        // a small Alltoallv takes no job (no variant choice either): every member pulls its own pieces
+        // (coll_run, own_pulls)
+        if (a.kind == JOB_ALLTOALLV && a.variant < 0 && c_rt.static_pull_bytes > 0 &&
+            a_est * n <= c_rt.static_pull_bytes) {
+            j->own_pulls = 1;
+            j->variant = GPUMPI_VARIANT_DIRECT;
+            j->sel_bytes = a_est * n;
+            job_open(j, 0);
+            return;
+        }
         int variant = a.kind != JOB_ALLTOALLV
                           ? (matrix && a.variant >= 0 && a.variant < GPUMPI_NUM_VARIANTS ? a.variant
                                                                                           : GPUMPI_VARIANT_DIRECT)
@@ -411,14 +421,6 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
         j->variant = variant;
         j->sel_bytes = a_est * n;
         bytes = a_est * P;
-        // a small Alltoallv takes no job: every member pulls its own pieces (coll_run, own_pulls)
-        if (a.kind == JOB_ALLTOALLV && a.variant < 0 && c_rt.static_pull_bytes > 0 &&
-            a_est * n <= c_rt.static_pull_bytes) {
-            j->own_pulls = 1;
-            j->variant = GPUMPI_VARIANT_DIRECT;
-            job_open(j, 0);
-            return;
-        }
         may_post = may_post && bytes >= c_rt.engine_min_bytes;
         long long target = n + (may_post ? c_rt.nengines : 0);
         if (a_est >= 65536) {
