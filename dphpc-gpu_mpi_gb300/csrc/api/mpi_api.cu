@@ -400,9 +400,10 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             const long long est = shared_piece_estimate(c);
             if (est >= 0) a_est = est;
         }
-        // a small Alltoallv takes no job (no variant choice either): every member pulls its own pieces
-        // (coll_run, own_pulls)
-        if (a.kind == JOB_ALLTOALLV && a.variant < 0 && c_rt.static_pull_bytes > 0 &&
+        // a small Alltoallv among at most 512 members takes no job (no variant choice either): every member
+        // pulls its own pieces (coll_run, own_pulls); with more members one member's n piece resolutions
+        // take longer than the job's shared chunks
+        if (a.kind == JOB_ALLTOALLV && a.variant < 0 && c_rt.static_pull_bytes > 0 && n <= 512 &&
             a_est * n <= c_rt.static_pull_bytes) {
             j->own_pulls = 1;
             j->variant = GPUMPI_VARIANT_DIRECT;

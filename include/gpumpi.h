@@ -190,9 +190,9 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
 /* GPUMPI_TUNE_STATIC_BCAST: a Bcast of more than 64 bytes and at most this many runs without a job, every
  * member copying its piece from the root between two barriers (0 = always the job path; default 64 KiB). */
 #define GPUMPI_TUNE_STATIC_BCAST 14
-/* GPUMPI_TUNE_STATIC_PULL: an Alltoallv whose members receive about this many bytes or fewer (the estimate
- * every member computes from 8 members' counts) pulls its pieces without a job: every member pulls its own
- * pieces from the senders between two barriers (0 = always the job path; default 128 KiB). */
+/* GPUMPI_TUNE_STATIC_PULL: an Alltoallv among at most 512 members whose members receive about this many bytes
+ * or fewer (the estimate of the variant choice, from 8 members' counts) runs without a job: every member
+ * pulls its own pieces from the senders between two barriers (0 = always the job path; default 128 KiB). */
 #define GPUMPI_TUNE_STATIC_PULL 15
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Launcher of a converted program (the reference's gpu_main): argv holds the program's arguments, then
