@@ -493,8 +493,6 @@ __device__ __noinline__ int coll_run(MPI_Comm_impl* c, const CollSlot& mine, con
     const unsigned e_next = c->job.epoch + 1;
     unsigned mis = (unsigned)((size_t)mine.sbuf | (size_t)mine.rbuf) & 15u;
     if (mis) atomicOr(&c->misalign[e_next & 1], mis);
-    RankState* R = &c_rt.ranks[me()];
-    R->coll_calls++;
     unsigned long long t0 = c_rt.trace_enabled ? now_ns() : 0;
     int rc = comm_barrier(c, [&]() { coll_setup(c, a, e_next); }, line);
     if (rc) return rc;
@@ -535,7 +533,6 @@ __device__ __forceinline__ bool static_fold_ok(long long count, int es, int n) {
 __device__ __noinline__ int coll_run_static(MPI_Comm_impl* c, const CollSlot& mine, const CollArgs& a, int line) {
     const int cr = comm_rank_of(c, me());
     c->slots[cr] = mine;
-    c_rt.ranks[me()].coll_calls++;
     int rc = comm_barrier(c, []() {}, line);
     if (rc) return rc;
     StaticFold* w = &s_sfold;

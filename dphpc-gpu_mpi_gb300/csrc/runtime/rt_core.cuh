@@ -333,7 +333,6 @@ struct alignas(128) RankState {
     int uq_free_top;
     int req_hwm;
     int uq_hwm;
-    unsigned long long coll_calls;
     void* attrs;                    // keyvals and cached attributes (device heap, made on first use)
     Job p2p_job;
 };
