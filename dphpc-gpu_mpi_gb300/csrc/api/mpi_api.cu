@@ -430,8 +430,8 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
             j->tile = 1;
             nchunks = (int)(P * parts);
         } else {
-            // one piece per thread of the block prepares the chunk; about two chunks per worker block
-            long long tile = P / (2 * (target > 0 ? target : 1));
+            // one piece per thread of the block prepares the chunk; about pull_chunks chunks per worker block
+            long long tile = P / ((long long)c_rt.pull_chunks * (target > 0 ? target : 1));
             if (tile < 1) tile = 1;
             if (tile > T) tile = T;
             j->vec = 1;

@@ -308,6 +308,7 @@ int gpumpi_world_create(const gpumpi_config* cfg_in, gpumpi_world** out) {
     r.static_fold_bytes = 4096;
     r.static_bcast_bytes = 64 << 10;
     r.static_pull_bytes = 128 << 10;
+    r.pull_chunks = 2;
     r.variant_override = -1;
     r.selector_mode = 0;
     r.trace_cap = cfg.trace_capacity;
@@ -455,6 +456,10 @@ int gpumpi_set_tuning(gpumpi_world* w, int key, long long value) {
     case GPUMPI_TUNE_STATIC_FOLD: w->h_rt.static_fold_bytes = value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_STATIC_BCAST: w->h_rt.static_bcast_bytes = value; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_STATIC_PULL: w->h_rt.static_pull_bytes = value; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_PULL_CHUNKS:
+        if (value < 1 || value > 64) return GPUMPI_ERR_ARG;
+        w->h_rt.pull_chunks = (int)value;
+        return GPUMPI_SUCCESS;
     // the learned policy's cached choices include the margin rule: a new margin starts a new epoch
     case GPUMPI_TUNE_MLP_MARGIN:
         w->h_rt.mlp_margin = (float)value * 1e-3f;
@@ -483,6 +488,7 @@ int gpumpi_get_tuning(gpumpi_world* w, int key, long long* value) {
     case GPUMPI_TUNE_STATIC_FOLD: *value = w->h_rt.static_fold_bytes; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_STATIC_BCAST: *value = w->h_rt.static_bcast_bytes; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_STATIC_PULL: *value = w->h_rt.static_pull_bytes; return GPUMPI_SUCCESS;
+    case GPUMPI_TUNE_PULL_CHUNKS: *value = w->h_rt.pull_chunks; return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_MLP_MARGIN: *value = (long long)(w->h_rt.mlp_margin * 1e3f + 0.5f); return GPUMPI_SUCCESS;
     case GPUMPI_TUNE_MLP_MARGIN_PULL: *value = (long long)(w->h_rt.mlp_margin_pull * 1e3f + 0.5f); return GPUMPI_SUCCESS;
     default: return GPUMPI_ERR_ARG;

@@ -72,8 +72,6 @@ __device__ __forceinline__ long long job_claim(Job* j) {
     return idx;
 }
 
-__device__ __forceinline__ void job_finish(Job* j) { atom_add_acqrel64(&j->done, 1ULL); }
-
 // Posts job j (epoch e) on the board so copy-engine blocks help with it.
 __device__ __forceinline__ void board_post(Job* j, unsigned e) {
     Board* b = c_rt.board;
@@ -135,7 +133,7 @@ __device__ int comm_barrier(MPI_Comm_impl* c, F&& setup, int line) {
 // Parameters of the job epoch being executed, read once per chunk with L2-only loads (the Job
 // struct is rewritten by every epoch, so no executing block may keep it in L1).
 struct JobParams {
-    int kind, dt, op, root, esize, vec, tile, aligned16, variant;
+    int kind, dt, op, root, esize, vec, tile, aligned16, variant, nchunks;
     unsigned epoch;
     long long count, chunk;
     const MPI_Comm_impl* comm;
@@ -148,6 +146,7 @@ __device__ __forceinline__ void load_params(const Job* j, JobParams& P) {
     P.kind = __ldcg(&j->kind);
     P.variant = __ldcg(&j->variant);
     P.epoch = __ldcg(&j->epoch);
+    P.nchunks = __ldcg(&j->nchunks);
     P.dt = __ldcg(&j->dt);
     P.op = __ldcg(&j->op);
     P.root = __ldcg(&j->root);
@@ -579,42 +578,32 @@ __device__ __noinline__ void copy_chunk(const JobParams* j, long long idx, int t
 // with most of the SM's L1 given to shared memory, cost L2 traffic on every access).  Thread 0 starts a
 // chunk only after every helper finished the previous task, so no reader of the old values remains.
 __shared__ JobParams s_jp;
-
 __shared__ long long s_next_chunk;
-__shared__ int s_next_same_epoch;
-
-// Claims one chunk like job_claim and also returns the epoch it belongs to.
-__device__ __forceinline__ long long job_claim_epoch(Job* j, unsigned* epoch) {
-    const unsigned long long t = atom_add_acqrel64(&j->next, 1ULL);
-    const unsigned e = (unsigned)(t >> 32);
-    const unsigned idx = (unsigned)t;
-    const unsigned long long lim = ld_acquire64(&j->limit);
-    if ((unsigned)(lim >> 32) != e || idx >= (unsigned)lim) return -1;
-    *epoch = e;
-    return idx;
-}
 
 // Runs chunk idx of job jg, then keeps claiming and running chunks until none is left; thread 0 marks
 // each chunk finished once every thread of the block is done with it (the barrier orders the block's
 // writes before thread 0's release).  One task per job and block keeps the call chain (and its saved
-// registers) out of the per-chunk path.  A job is reused: once its last chunk is finished its owner may
-// open the next epoch with new parameters, so a claim can return a chunk of a newer epoch than the
-// parameters in s_jp.  Such a chunk is not run here: the loop returns it in s_next_chunk and exec_chunk
-// reloads the parameters (stable while the chunk is unfinished) before running it.
+// registers) out of the per-chunk path.
+// Thread 0 claims the next chunk before it marks this one finished: while this chunk is unfinished the
+// epoch cannot end (its owner reopens the job only after every chunk is finished), so the claim returns a
+// chunk of the epoch whose parameters are in s_jp, or an index past its end.  The claim is relaxed (the
+// block acquired the epoch's parameters and data with its first claim, so no acquire, which would also
+// drop the SM's L1 contents, is needed) and the finish is a release add nobody waits for: the two round
+// trips overlap.
 template <class F>
 __device__ __forceinline__ void chunk_loop(Job* jg, long long idx, int tid, int nt, F&& body) {
     for (;;) {
         body(idx);
         bar_sync(BAR_TASK, nt);
         if (tid == 0) {
-            job_finish(jg);
-            unsigned e = 0;
-            s_next_chunk = job_claim_epoch(jg, &e);
-            s_next_same_epoch = s_next_chunk >= 0 && e == s_jp.epoch;
+            const unsigned long long t = atom_add_relaxed64(&jg->next, 1ULL);
+            red_add_release64(&jg->done, 1ULL);
+            const unsigned i = (unsigned)t;
+            s_next_chunk = ((unsigned)(t >> 32) == s_jp.epoch && i < (unsigned)s_jp.nchunks) ? (long long)i : -1;
         }
         bar_sync(BAR_TASK, nt);
         idx = s_next_chunk;
-        if (idx < 0 || !s_next_same_epoch) return;
+        if (idx < 0) return;
     }
 }
 
@@ -629,20 +618,15 @@ __device__ __noinline__ void copy_run(const JobParams* j, Job* jg, long long idx
 }
 
 __device__ __noinline__ void exec_chunk(Job* jg, long long idx, int tid, int nt) {
-    for (;;) {
-        // parameters of the epoch that chunk idx belongs to (the claim that returned it synchronised with
-        // the release that opened the epoch, and the epoch cannot end before this chunk is finished)
-        if (tid == 0) load_params(jg, s_jp);
-        bar_sync(BAR_TASK, nt);
-        const JobParams* j = &s_jp;
-        switch (j->kind) {
-        case JOB_COPY: copy_run(j, jg, idx, tid, nt); break;
-        case JOB_ALLREDUCE: case JOB_REDUCE: fold_run(j, jg, idx, tid, nt); break;
-        default: pull_run(j, jg, idx, tid, nt); break;
-        }
-        idx = s_next_chunk;  // -1, or a claimed chunk of a newer epoch
-        bar_sync(BAR_TASK, nt);  // every thread has read it before thread 0 reloads the parameters
-        if (idx < 0) return;
+    // parameters of the epoch that chunk idx belongs to (the claim that returned it synchronised with
+    // the release that opened the epoch, and the epoch cannot end before this chunk is finished)
+    if (tid == 0) load_params(jg, s_jp);
+    bar_sync(BAR_TASK, nt);
+    const JobParams* j = &s_jp;
+    switch (j->kind) {
+    case JOB_COPY: copy_run(j, jg, idx, tid, nt); break;
+    case JOB_ALLREDUCE: case JOB_REDUCE: fold_run(j, jg, idx, tid, nt); break;
+    default: pull_run(j, jg, idx, tid, nt); break;
     }
 }
 

@@ -61,6 +61,16 @@ __device__ __forceinline__ unsigned long long atom_add_acqrel64(unsigned long lo
     asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
     return old;
 }
+__device__ __forceinline__ unsigned long long atom_add_relaxed64(unsigned long long* p, unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.relaxed.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+// an add whose result nobody waits for (release: the caller's and, through a barrier, its block's earlier
+// writes are visible to whoever acquires the new value)
+__device__ __forceinline__ void red_add_release64(unsigned long long* p, unsigned long long v) {
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ unsigned long long atom_exch_release64(unsigned long long* p, unsigned long long v) {
     unsigned long long old;
     asm volatile("atom.release.gpu.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
@@ -402,6 +412,7 @@ struct Runtime {
     long long static_bcast_bytes;     // broadcasts of at most this many bytes copy from the root without a job
     long long static_pull_bytes;      // an Alltoallv whose members receive about this many bytes or fewer
                                       // pulls its pieces without a job
+    int pull_chunks;                  // pull jobs of small pieces: chunks per worker block (>= 1)
     int variant_override;             // -1: selector decides
     int selector_mode;                // 0 plain (DIRECT), 1 tuned table, 2 learned MLP, 3 heuristic
     int dyn_smem;                     // dynamic shared memory bytes of this launch (STAGED stages)

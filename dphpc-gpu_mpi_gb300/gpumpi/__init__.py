@@ -34,7 +34,7 @@ ERR_OTHER, ERR_RANK, ERR_TRUNCATE, ERR_TIMEOUT = 1, 7, 12, 15
 MPI_CART = 1
 (TUNE_VEC, TUNE_STAGE_GROUP, TUNE_ENGINES, TUNE_COPY_CHUNK, TUNE_ENGINE_MIN_BYTES, TUNE_MLP_MARGIN, TUNE_DYN_SMEM,
  TUNE_HOST_DIRECT, TUNE_MLP_MARGIN_PULL, TUNE_HOST_SLICE, TUNE_HOST_STREAMS) = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11
-TUNE_STATIC_FOLD, TUNE_STATIC_BCAST, TUNE_STATIC_PULL = 13, 14, 15
+TUNE_STATIC_FOLD, TUNE_STATIC_BCAST, TUNE_STATIC_PULL, TUNE_PULL_CHUNKS = 13, 14, 15, 16
 
 TESTS = {
     "single_int": 1, "transfer_array": 2, "send_recv": 3, "repeat_send_recv": 4, "network_flood": 5,

@@ -194,6 +194,9 @@ int gpumpi_set_policy(gpumpi_world* w, int variant, int mode);
  * or fewer (the estimate of the variant choice, from 8 members' counts) runs without a job: every member
  * pulls its own pieces from the senders between two barriers (0 = always the job path; default 128 KiB). */
 #define GPUMPI_TUNE_STATIC_PULL 15
+/* GPUMPI_TUNE_PULL_CHUNKS: a pull job (Alltoall(v), Allgather(v), Gather(v), Scatter(v), Bcast) whose pieces
+ * are under 64 KiB is cut into about this many chunks per worker block (1..64; default 2). */
+#define GPUMPI_TUNE_PULL_CHUNKS 16
 int gpumpi_set_tuning(gpumpi_world* w, int key, long long value);
 /* Launcher of a converted program (the reference's gpu_main): argv holds the program's arguments, then
  * optionally `---gpumpi` and the run's options (gpumpi_parse_args); creates the world, runs `program` on
