@@ -213,17 +213,30 @@ __device__ __forceinline__ int learned_choice(MPI_Comm_impl* c, int kind, long l
 __device__ __noinline__ long long shared_piece_estimate(const MPI_Comm_impl* c) {
     const int n = c->size;
     const CollSlot* sl = c->slots;
-    long long sum = 0;
+    // two rounds of independent loads, the 8 members' slots and then their counts and type sizes (this
+    // runs on the critical path of the collective, in the set-up of the last member to arrive)
+    const int* cnt[8];
+    const TypeDesc* d[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
         const int m = (int)(((long long)(2 * q + 1) * n) / 16);
-        const int* cnt = (const int*)__ldcg((const unsigned long long*)&sl[m].scounts);
-        const TypeDesc* d = (const TypeDesc*)__ldcg((const unsigned long long*)&sl[m].sdesc);
-        if (!cnt || !d) return -1;
+        cnt[q] = (const int*)__ldcg((const unsigned long long*)&sl[m].scounts);
+        d[q] = (const TypeDesc*)__ldcg((const unsigned long long*)&sl[m].sdesc);
+    }
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < 8; q++) ok = ok && cnt[q] != nullptr && d[q] != nullptr;
+    if (!ok) return -1;
+    long long ssz[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) ssz[q] = __ldcg(&d[q]->size);
+    long long sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
         long long part = 0;
 #pragma unroll
-        for (int i = 0; i < 8; i++) part += __ldcg(cnt + ((long long)(2 * i + 1) * n) / 16);
-        sum += part * d->size;
+        for (int i = 0; i < 8; i++) part += __ldcg(cnt[q] + ((long long)(2 * i + 1) * n) / 16);
+        sum += part * ssz[q];
     }
     return sum / 64;
 }
@@ -320,6 +333,8 @@ __device__ __noinline__ void coll_setup(MPI_Comm_impl* c, const CollArgs& a, uns
     c->misalign[(e_next + 1) & 1] = 0;
     j->kind = a.kind;
     j->comm = c;
+    j->slots = c->slots;
+    j->csize = c->size;
     j->dt = a.dt;
     j->op = a.op;
     j->root = a.root;
@@ -471,6 +486,8 @@ __device__ __noinline__ int own_pulls(MPI_Comm_impl* c, int cr, int line) {
     j.kind = JOB_ALLTOALLV;
     j.variant = GPUMPI_VARIANT_DIRECT;  // receiver-major pieces: member cr's are [cr * n, cr * n + n)
     j.comm = c;
+    j.slots = c->slots;
+    j.csize = n;
     j.vec = 1;
     j.tile = nthreads();
     j.count = (long long)n * n;
@@ -550,6 +567,8 @@ __device__ __noinline__ int coll_run_static(MPI_Comm_impl* c, const CollSlot& mi
     j.count = a.count;
     j.chunk = nthreads();
     j.comm = c;
+    j.slots = c->slots;
+    j.csize = c->size;
     j.src = nullptr;
     j.dst = nullptr;
     j.ufn = a.ufn;
@@ -1358,7 +1377,8 @@ __device__ int MPI_Alltoallv(const void* sendbuf, const int sendcounts[], const 
     my.rdesc = rt;
     my.stype = sendtype;
     my.rtype = recvtype;
-    long long est = sample_counts(sendcounts, n) * st->size;
+    // the set-up estimates from 8 members' counts with 16 or more members (shared_piece_estimate)
+    long long est = n < 16 ? sample_counts(sendcounts, n) * st->size : 0;
     int rc = pull_collective(JOB_ALLTOALLV, c, my, sspan, rspan, est, 0);
     stage_out(s1, false);
     stage_out(s2, false);

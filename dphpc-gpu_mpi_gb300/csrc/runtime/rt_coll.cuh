@@ -86,7 +86,13 @@ __device__ __forceinline__ void board_post(Job* j, unsigned e) {
 // Thread 0: executes chunks of j until none is left (one block task claims them in a loop and finishes
 // each), then waits for all chunks to finish.
 __device__ __noinline__ int job_run_and_wait(Job* j, int line) {
-    const long long idx = job_claim(j);
+    // the caller opened the job itself or acquired its opening through the communicator barrier, and the
+    // epoch cannot end before the caller is done with it: a relaxed claim and a relaxed read of the limit,
+    // issued together, cost one round trip
+    const unsigned long long tk = atom_add_relaxed64(&j->next, 1ULL);
+    const unsigned long long lim = ld_relaxed64(&j->limit);
+    const long long idx =
+        ((unsigned)(tk >> 32) == (unsigned)(lim >> 32) && (unsigned)tk < (unsigned)lim) ? (long long)(unsigned)tk : -1;
     if (idx >= 0) {
         Task t;
         t.kind = TASK_CHUNK;
@@ -94,7 +100,7 @@ __device__ __noinline__ int job_run_and_wait(Job* j, int line) {
         t.n0 = idx;
         dispatch(t);
     }
-    const unsigned long long target = ld_acquire64(&j->limit);  // (epoch << 32) | nchunks
+    const unsigned long long target = lim;  // (epoch << 32) | nchunks
     if (ld_acquire64(&j->done) == target) return 0;
     Deadline d = make_deadline();
     while (ld_relaxed64(&j->done) != target) {
@@ -137,6 +143,8 @@ struct JobParams {
     unsigned epoch;
     long long count, chunk;
     const MPI_Comm_impl* comm;
+    const CollSlot* slots;
+    int csize;
     const void* src;
     void* dst;
     MPI_User_function* ufn;
@@ -157,6 +165,8 @@ __device__ __forceinline__ void load_params(const Job* j, JobParams& P) {
     P.count = __ldcg(&j->count);
     P.chunk = __ldcg(&j->chunk);
     P.comm = (const MPI_Comm_impl*)__ldcg((const unsigned long long*)&j->comm);
+    P.slots = (const CollSlot*)__ldcg((const unsigned long long*)&j->slots);
+    P.csize = __ldcg(&j->csize);
     P.src = (const void*)__ldcg((const unsigned long long*)&j->src);
     P.dst = (void*)__ldcg((const unsigned long long*)&j->dst);
     P.ufn = (MPI_User_function*)__ldcg((const unsigned long long*)&j->ufn);
@@ -235,9 +245,8 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
     constexpr int BYTES = V * (int)sizeof(T);
     // ranks folded per step: ~128 bytes of loads in flight per thread (at most 16 loads)
     constexpr int U = 128 / BYTES > 16 ? 16 : 128 / BYTES < 1 ? 1 : 128 / BYTES;
-    const MPI_Comm_impl* c = j->comm;
-    const CollSlot* slots = c->slots;
-    const int n = c->size;
+    const CollSlot* slots = j->slots;
+    const int n = j->csize;
     const long long count = j->count;
     const long long e = e0 + (long long)tid * V;
     const int nv = e < count ? (int)min((long long)V, count - e) : 0;
@@ -297,9 +306,8 @@ namespace gpumpi {
 
 // Any legal (op, type) and user-defined ops, one element per thread, same canonical order.
 __device__ __noinline__ void fold_generic(const JobParams* j, long long e0, int tid, int nt) {
-    const MPI_Comm_impl* c = j->comm;
-    const CollSlot* slots = c->slots;
-    const int n = c->size;
+    const CollSlot* slots = j->slots;
+    const int n = j->csize;
     const int es = j->esize;
     const long long e = e0 + tid;
     const bool act = e < j->count;
@@ -471,9 +479,8 @@ struct Piece {
 __device__ __forceinline__ int ldcg_int(const int* p) { return __ldcg(p); }
 
 __device__ __forceinline__ void piece_of(const JobParams* j, long long p, Piece& pc) {
-    const MPI_Comm_impl* c = j->comm;
-    const CollSlot* S = c->slots;
-    const int n = c->size;
+    const CollSlot* S = j->slots;
+    const int n = j->csize;
     int r, s;
     switch (j->kind) {
     case JOB_ALLTOALLV: case JOB_ALLGATHERV:
@@ -500,6 +507,7 @@ __device__ __forceinline__ void piece_of(const JobParams* j, long long p, Piece&
     const TypeDesc* rd = (const TypeDesc*)__ldcg((const unsigned long long*)&rs->rdesc);
     long long sext = __ldcg(&sd->extent), rext = __ldcg(&rd->extent);
     long long ssz = __ldcg(&sd->size), rsz = __ldcg(&rd->size);
+    const bool sflat = desc_contiguous(sd), rflat = desc_contiguous(rd);
     long long scount, rcount, soff, roff;
     switch (j->kind) {
     case JOB_ALLTOALLV: {
@@ -551,8 +559,8 @@ __device__ __forceinline__ void piece_of(const JobParams* j, long long p, Piece&
         pc.bytes = 0;
     pc.src = sbuf + soff;
     pc.dst = rbuf + roff;
-    pc.sdesc = desc_contiguous(sd) ? nullptr : sd;
-    pc.rdesc = desc_contiguous(rd) ? nullptr : rd;
+    pc.sdesc = sflat ? nullptr : sd;
+    pc.rdesc = rflat ? nullptr : rd;
 }
 
 __device__ __forceinline__ void piece_copy(const Piece& pc, long long b0, long long b1, int lane, int nl) {

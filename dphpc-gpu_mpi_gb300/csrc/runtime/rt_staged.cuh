@@ -62,9 +62,8 @@ __device__ __noinline__ void drain_stages(unsigned long long* full, unsigned gi,
 template <class T, int OP, int V>
 __device__ __noinline__ void fold_staged(const JobParams* j, long long idx, int tid, int nt) {
     constexpr int S = 2;
-    const MPI_Comm_impl* c = j->comm;
-    const CollSlot* slots = c->slots;
-    const int n = c->size;
+    const CollSlot* slots = j->slots;
+    const int n = j->csize;
     const long long E = j->chunk;
     const long long e0 = idx * E;
     const long long ne = min(E, j->count - e0);

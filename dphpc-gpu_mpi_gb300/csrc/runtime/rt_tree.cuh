@@ -51,9 +51,8 @@ __device__ __forceinline__ void tree_fold_range(const CollSlot* slots, int g0, i
 
 template <class T, int OP, int V>
 __device__ __noinline__ void fold_tree(const JobParams* j, long long idx, int tid, int nt) {
-    const MPI_Comm_impl* c = j->comm;
-    const CollSlot* slots = c->slots;
-    const int n = c->size;
+    const CollSlot* slots = j->slots;
+    const int n = j->csize;
     const int R = j->tile;
     const long long E = j->chunk;
     const long long count = j->count;
