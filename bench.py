@@ -210,9 +210,10 @@ def pct(v, q):
     return v[k]
 
 
-def bench_alltoallv(gpumpi, torch, w_kw):
-    """Bucket-sort shape: 2^25 int32 keys over 256 ranks, keys ~ mean of four U(0,1), bucketed by range."""
-    import numpy as np
+def bucket_shape(torch):
+    """Bucket-sort shape: 2^25 int32 keys over 256 ranks, keys ~ mean of four U(0,1), bucketed by range
+    (middle buckets hold about 2.7x the mean, edge buckets almost nothing); returns the send buffer, its
+    row stride in bytes, counts and displacements of both sides, the receive buffer and its row stride."""
     n, kpr = 256, (1 << 25) // 256
     g = torch.Generator(device="cuda").manual_seed(1234)
     keys = (torch.rand((n, kpr, 4), generator=g, device="cuda", dtype=torch.float64).sum(-1) * (1 << 19)).floor()
@@ -226,16 +227,40 @@ def bench_alltoallv(gpumpi, torch, w_kw):
     rd = torch.cumsum(rc, 1, dtype=torch.int32) - rc
     R = int(rc.sum(1).max().item())
     recv = torch.zeros((n, R), dtype=torch.int32, device="cuda")
+    return n, send, kpr * 4, sc, sd, rc, rd, recv, R * 4
+
+
+def bench_alltoallv(gpumpi, torch, w_kw):
+    """Alltoallv of the bucket-sort shape (bucket_shape)."""
+    import numpy as np
+    n, send, sst, sc, sd, rc, rd, recv, rst = bucket_shape(torch)
     total_bytes = int(sc.sum().item()) * 4
     with gpumpi.World(n, **w_kw) as w:
-        w.alltoallv(send, kpr * 4, sc, sd, recv, R * 4, rc, rd, gpumpi.INT, iters=3)
+        w.alltoallv(send, sst, sc, sd, recv, rst, rc, rd, gpumpi.INT, iters=3)
         iters = 20
         ns = np.zeros(iters, dtype=np.uint64)
-        w.alltoallv(send, kpr * 4, sc, sd, recv, R * 4, rc, rd, gpumpi.INT, iters=iters, iter_ns=ns)
+        w.alltoallv(send, sst, sc, sd, recv, rst, rc, rd, gpumpi.INT, iters=iters, iter_ns=ns)
         ms = w.last_kernel_ms() / iters
     return {"ranks": n, "keys": 1 << 25, "bytes_moved_per_call": total_bytes,
             "gbs": 2.0 * total_bytes / (ms * 1e-3) / 1e9, "ms_per_call": ms,
             "p50_us": float(pct(list(ns), 0.5)) / 1e3, "p99_us": float(pct(list(ns), 0.99)) / 1e3}
+
+
+def bucket_alltoallv_case(args, gpumpi, torch, local):
+    """Alltoallv of the bucket-sort shape (bucket_shape; 128 MiB read + 128 MiB written per call): the
+    profiled case of small uneven pieces."""
+    n, send, sst, sc, sd, rc, rd, recv, rst = bucket_shape(torch)
+    total = int(sc.sum().item()) * 4
+    with gpumpi.World(n, device=local, timeout_s=120.0) as w:
+        if args.variant >= 0:
+            w.set_policy(args.variant, 0)
+        w.alltoallv(send, sst, sc, sd, recv, rst, rc, rd, gpumpi.INT, iters=max(1, args.warmup))
+        w.alltoallv(send, sst, sc, sd, recv, rst, rc, rd, gpumpi.INT, iters=max(1, args.steps))
+        ms = w.last_kernel_ms() / max(1, args.steps)
+        info = w.info()
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "alltoallv_bucket", "variant": args.variant, "ranks": n, "bytes_moved": total,
+                      "ms_per_step": ms, "gbs": 2.0 * total / (ms * 1e-3) / 1e9, "world": info}), flush=True)
 
 
 def bench_alltoallv_1024(gpumpi, torch, w_kw, uniform: bool):
@@ -666,10 +691,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--case", default="full",
-                    choices=["full", "small", "alltoallv_small", "p2p_sweep", "coll_sweep"],
+                    choices=["full", "small", "alltoallv_small", "alltoallv_bucket", "p2p_sweep", "coll_sweep"],
                     help="small: Allreduce 1024 ranks x 256 KiB; alltoallv_small: Alltoallv 1024 ranks x "
-                         "256 KiB; device timing only (the ncu capture cases); p2p_sweep / coll_sweep: the "
-                         "point-to-point and collectives sweeps")
+                         "256 KiB; alltoallv_bucket: Alltoallv of the bucket-sort shape; device timing only "
+                         "(the ncu capture cases); p2p_sweep / coll_sweep: the point-to-point and collectives "
+                         "sweeps")
     ap.add_argument("--variant", type=int, default=-1, help="variant override for the small cases")
     ap.add_argument("--max-bytes", type=int, default=1 << 24, help="largest bytes per rank of the collectives sweep")
     args = ap.parse_args()
@@ -689,6 +715,9 @@ def main():
         return
     if args.case == "alltoallv_small":
         small_alltoallv_case(args, gpumpi, torch, local)
+        return
+    if args.case == "alltoallv_bucket":
+        bucket_alltoallv_case(args, gpumpi, torch, local)
         return
     if args.case == "p2p_sweep":
         p2p_sweep(args, gpumpi, torch, local)

@@ -28,6 +28,13 @@ def test_header_and_python_mirror_agree():
     assert declared_functions() == sorted(gpumpi.EXPORTS)
 
 
+def test_tuning_keys_match_the_header():
+    import gpumpi
+    text = (ROOT / "include" / "gpumpi.h").read_text()
+    keys = dict(re.findall(r"^#define GPUMPI_(TUNE_\w+) (\d+)", text, re.M))
+    assert keys and all(getattr(gpumpi, k) == int(v) for k, v in keys.items())
+
+
 def test_library_exports_every_declared_symbol(built):
     L = ctypes.CDLL(str(built))
     for name in declared_functions():

@@ -252,6 +252,25 @@ def test_alltoallv_uneven_and_zero_counts(gpulib, oracle, n, maxc, zero_frac):
     assert np.array_equal(got, ref)
 
 
+def test_alltoallv_chunks_per_worker(gpulib, oracle):
+    """Pull jobs cut into 1..7 chunks per worker block (and a knob out of range refused): the pieces reach
+    the same places whatever the chunking, including chunks that end inside a run of touching pieces."""
+    n = 160
+    rng = np.random.default_rng(31)
+    sc, sd, rc, rd, S, R = uneven_exchange(rng, n, 900, 0.2, min_c=0)
+    x = oracle.fill_i32(n + 3, n * S).reshape(n, S)
+    ref = oracle.alltoallv(x, sc, sd, R, rc, rd)
+    with gpulib.World(n, timeout_s=20.0) as w:
+        with pytest.raises(gpulib.GpumpiError):
+            w.set_tuning(gpulib.TUNE_PULL_CHUNKS, 0)
+        for ch in (1, 3, 7):
+            w.set_tuning(gpulib.TUNE_PULL_CHUNKS, ch)
+            assert w.get_tuning(gpulib.TUNE_PULL_CHUNKS) == ch
+            s, r = dev(x), dev(np.zeros((n, R), np.int32))
+            w.alltoallv(s, S * 4, dev(sc), dev(sd), r, R * 4, dev(rc), dev(rd), 2, iters=2)
+            assert np.array_equal(host(r), ref), ch
+
+
 def uneven_exchange(rng, n, maxc, zero_frac, min_c=1):
     sc = rng.integers(min_c, maxc + 1, (n, n)).astype(np.int32)
     sc[rng.random((n, n)) < zero_frac] = 0
