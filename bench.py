@@ -366,6 +366,22 @@ def bench_halo(gpumpi, torch, w_kw):
     return out
 
 
+def halo_case(args, gpumpi, torch, local):
+    """3D fp64 halo exchange, 512^3 grid over 8x8x8 ranks, vector/hvector faces: --warmup exchanges in one
+    launch, then --steps exchanges in a second (the profiled launch)."""
+    import numpy as np
+    from gpumpi import apps
+    P, L = 8, 64
+    with gpumpi.World(P ** 3, device=local, timeout_s=120.0) as w:
+        rc, blocks = apps.halo(w, P, L, iters=max(1, args.warmup), mode=0)
+        ns = np.zeros(max(1, args.steps), dtype=np.uint64)
+        rc2, _ = apps.halo(w, P, L, iters=max(1, args.steps), mode=0, blocks=blocks, iter_ns=ns)
+        info = w.info()
+    us = float(np.median(ns)) / 1e3
+    print(json.dumps({"case": "halo", "rc": rc or rc2, "ranks": P ** 3, "us_per_exchange_p50": us,
+                      "gbs": 2.0 * apps.halo_face_bytes(P, L) / (us * 1e-6) / 1e9, "world": info}), flush=True)
+
+
 def bench_batch(gpumpi, torch, w_kw):
     """64 communicators of uneven sizes (8..512 ranks, log-uniform, seeded) on 512 world ranks, each an
     fp32 SUM Allreduce of 4 B .. 64 KiB per rank, in one persistent launch: as a plain launch and as a
@@ -691,9 +707,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--case", default="full",
-                    choices=["full", "small", "alltoallv_small", "alltoallv_bucket", "p2p_sweep", "coll_sweep"],
+                    choices=["full", "small", "alltoallv_small", "alltoallv_bucket", "halo", "p2p_sweep",
+                             "coll_sweep"],
                     help="small: Allreduce 1024 ranks x 256 KiB; alltoallv_small: Alltoallv 1024 ranks x "
-                         "256 KiB; alltoallv_bucket: Alltoallv of the bucket-sort shape; device timing only "
+                         "256 KiB; alltoallv_bucket: Alltoallv of the bucket-sort shape; halo: 3D halo "
+                         "exchange 512^3 / 512 ranks; device timing only "
                          "(the ncu capture cases); p2p_sweep / coll_sweep: the point-to-point and collectives "
                          "sweeps")
     ap.add_argument("--variant", type=int, default=-1, help="variant override for the small cases")
@@ -718,6 +736,9 @@ def main():
         return
     if args.case == "alltoallv_bucket":
         bucket_alltoallv_case(args, gpumpi, torch, local)
+        return
+    if args.case == "halo":
+        halo_case(args, gpumpi, torch, local)
         return
     if args.case == "p2p_sweep":
         p2p_sweep(args, gpumpi, torch, local)
