@@ -112,20 +112,39 @@ __device__ void sort_gen_task(void* arg, int tid, int nt) {
     }
 }
 
-// Calls f(i, key) for this thread's keys i = tid, tid + nt, ... < count, loading KB keys before handling
-// any: the handler's atomics and stores may alias the keys as far as the compiler knows, so one key at a
-// time would cost a full memory round trip per key.
-template <int KB, class F>
+// Calls f(key) for every key of keys[0, count), in no particular order.  The 16-byte-aligned body is read
+// as uint4 vectors, NV of them per thread before any key is handled (the handler's atomics and stores may
+// alias the keys as far as the compiler knows, so one load at a time would cost a full memory round trip
+// each): one block alone reads a rank's keys, so the bytes it keeps in flight set the speed.
+template <int NV, class F>
 __device__ __forceinline__ void for_keys(const int* keys, long long count, int tid, int nt, F&& f) {
+    if (count <= 0) return;
+    const long long head = min(count, (long long)(((16 - ((unsigned long long)keys & 15)) & 15) >> 2));
+    if (tid < head) f(__ldcg(keys + tid));
+    const uint4* v = (const uint4*)(keys + head);
+    const long long nv = (count - head) >> 2;
     long long i = tid;
-    for (; i + (long long)(KB - 1) * nt < count; i += (long long)KB * nt) {
-        int k[KB];
+    for (; i + (long long)(NV - 1) * nt < nv; i += (long long)NV * nt) {
+        uint4 k[NV];
 #pragma unroll
-        for (int j = 0; j < KB; j++) k[j] = __ldcg(keys + i + (long long)j * nt);
+        for (int j = 0; j < NV; j++) k[j] = __ldcg(v + i + (long long)j * nt);
 #pragma unroll
-        for (int j = 0; j < KB; j++) f(i + (long long)j * nt, k[j]);
+        for (int j = 0; j < NV; j++) {
+            f((int)k[j].x);
+            f((int)k[j].y);
+            f((int)k[j].z);
+            f((int)k[j].w);
+        }
     }
-    for (; i < count; i += nt) f(i, __ldcg(keys + i));
+    for (; i < nv; i += nt) {
+        const uint4 k = __ldcg(v + i);
+        f((int)k.x);
+        f((int)k.y);
+        f((int)k.z);
+        f((int)k.w);
+    }
+    const long long t = head + nv * 4 + tid;
+    if (t < count) f(__ldcg(keys + t));
 }
 
 // bucket counts, send displacements and the packed send buffer (keys grouped by destination rank)
@@ -138,8 +157,7 @@ __device__ void sort_pack_task(void* arg, int tid, int nt) {
     if (!in_smem) bins = w->sc;
     for (int d = tid; d < n; d += nt) bins[d] = 0;
     gpumpi_block_sync(nt);
-    for_keys<8>(w->keys, w->kpr, tid, nt,
-                 [&](long long, int k) { atomicAdd(&bins[((long long)k * n) >> KEY_BITS], 1); });
+    for_keys<8>(w->keys, w->kpr, tid, nt, [&](int k) { atomicAdd(&bins[((long long)k * n) >> KEY_BITS], 1); });
     gpumpi_block_sync(nt);
     int* sd = w->sc + n;
     for (int d = tid; d < n; d += nt) {
@@ -154,23 +172,50 @@ __device__ void sort_pack_task(void* arg, int tid, int nt) {
     for (int d = tid; d < n; d += nt) cur[d] = sd[d];
     gpumpi_block_sync(nt);
     int* send = w->send;
-    // eight keys at a time: their loads, then their cursor atomics, then their stores (a store between two
-    // atomics would keep the second from issuing before the first returned)
+    // each key takes a slot of its bucket with a cursor atomic and is stored there; the keys come in uint4
+    // vectors, sixteen keys per thread at a time: their loads, then their cursor atomics, then their stores
+    // (a store between two atomics would keep the second from issuing before the first returned)
     const int* keys = w->keys;
     const long long kpr = w->kpr;
-    long long i = tid;
-    for (; i + 7LL * nt < kpr; i += 8LL * nt) {
-        int k[8], pos[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) k[j] = __ldcg(keys + i + (long long)j * nt);
-#pragma unroll
-        for (int j = 0; j < 8; j++) pos[j] = atomicAdd(&cur[((long long)k[j] * n) >> KEY_BITS], 1);
-#pragma unroll
-        for (int j = 0; j < 8; j++) send[pos[j]] = k[j];
+    auto slot = [&](int k) { return atomicAdd(&cur[((long long)k * n) >> KEY_BITS], 1); };
+    const long long head = min(kpr, (long long)(((16 - ((unsigned long long)keys & 15)) & 15) >> 2));
+    if (tid < head) {
+        const int k = __ldcg(keys + tid);
+        send[slot(k)] = k;
     }
-    for (; i < kpr; i += nt) {
-        const int k = __ldcg(keys + i);
-        send[atomicAdd(&cur[((long long)k * n) >> KEY_BITS], 1)] = k;
+    const uint4* v = (const uint4*)(keys + head);
+    const long long nv = (kpr - head) >> 2;
+    long long i = tid;
+    for (; i + 3LL * nt < nv; i += 4LL * nt) {
+        uint4 a[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) a[u] = __ldcg(v + i + (long long)u * nt);
+        int k[16], pos[16];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            k[4 * u] = (int)a[u].x;
+            k[4 * u + 1] = (int)a[u].y;
+            k[4 * u + 2] = (int)a[u].z;
+            k[4 * u + 3] = (int)a[u].w;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; j++) pos[j] = slot(k[j]);
+#pragma unroll
+        for (int j = 0; j < 16; j++) send[pos[j]] = k[j];
+    }
+    for (; i < nv; i += nt) {
+        const uint4 a = __ldcg(v + i);
+        const int k[4] = {(int)a.x, (int)a.y, (int)a.z, (int)a.w};
+        int pos[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) pos[j] = slot(k[j]);
+#pragma unroll
+        for (int j = 0; j < 4; j++) send[pos[j]] = k[j];
+    }
+    const long long t = head + nv * 4 + tid;
+    if (t < kpr) {
+        const int k = __ldcg(keys + t);
+        send[slot(k)] = k;
     }
 }
 
@@ -195,25 +240,41 @@ __device__ void sort_local_task(void* arg, int tid, int nt) {
     gpumpi_block_sync(nt);
     const int lo = w->lo, range = w->range;
     bool bad = false;
-    for_keys<8>(w->recv, w->nrecv, tid, nt, [&](long long, int key) {
+    for_keys<4>(w->recv, w->nrecv, tid, nt, [&](int key) {
         const int k = key - lo;
         if (k >= 0 && k < range) atomicAdd(&hist[k], 1);
         else bad = true;
     });
     if (bad) w->err = 1;
     gpumpi_block_sync(nt);
-    // positions: exclusive prefix of the histogram by segments, then each thread writes its values' runs
-    const int seg = (w->range + nt - 1) / nt;
-    const int a = min(w->range, tid * seg), b = min(w->range, a + seg);
-    int s = 0;
-    for (int k = a; k < b; k++) s += hist[k];
-    s_scan[tid] = s;
-    scan_thread_sums(tid, nt);
-    int pos = s_scan[tid];
-    for (int k = a; k < b; k++) {
-        const int c = hist[k];
-        for (int q = 0; q < c; q++) w->out[pos + q] = w->lo + k;
-        pos += c;
+    // start of every value's run in the output; then a warp takes 32 consecutive values at a time, whose
+    // runs fill one contiguous range of the output, and its lanes store 32 consecutive positions per step
+    // (coalesced), each finding its value by a binary search over the 32 starts held in the warp's lanes.
+    // Four steps are interleaved so that their shuffles overlap; a range without keys costs nothing.
+    const int total = block_exclusive_scan(hist, range, tid, nt);
+    gpumpi_block_sync(nt);
+    const int lane = tid & 31, wi = tid >> 5, nw = nt >> 5;
+    int* out = w->out;
+    for (int k0 = wi * 32; k0 < range; k0 += nw * 32) {
+        const int st = k0 + lane < range ? hist[k0 + lane] : total;  // values past the range start at the end
+        const int s0 = __shfl_sync(0xffffffffu, st, 0);
+        const int s1 = k0 + 32 < range ? hist[k0 + 32] : total;
+        for (int base = s0; base < s1; base += 128) {
+            int q[4], v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                q[u] = base + 32 * u + lane;
+                v[u] = 0;
+            }
+#pragma unroll
+            for (int b = 16; b; b >>= 1)
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (__shfl_sync(0xffffffffu, st, v[u] + b) <= q[u]) v[u] += b;
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (q[u] < s1) out[q[u]] = lo + k0 + v[u];
+        }
     }
 }
 

@@ -13,7 +13,8 @@ def oracle_keys(oracle, seed, n, kpr):
     return np.stack([oracle.bucket_keys(seed, r, kpr) for r in range(n)])
 
 
-@pytest.mark.parametrize("n,total,iters", [(16, 1 << 16, 2), (37, 37 * 1000, 1), (256, 1 << 25, 2)])
+# 1001 keys per rank: rows of keys and of received keys start at every 4-byte offset modulo 16
+@pytest.mark.parametrize("n,total,iters", [(16, 1 << 16, 2), (37, 37 * 1000, 1), (12, 12 * 1001, 2), (256, 1 << 25, 2)])
 def test_bucket_sort_matches_oracle(gpulib, oracle, n, total, iters):
     from gpumpi import apps
     seed = 20251203
