@@ -238,13 +238,36 @@ __device__ __forceinline__ void st_elems(T* p, const T (&v)[V], int nv, bool vec
         if (k < nv) __stcg(p + k, v[k]);
 }
 
+// Member pointers of ranks [r0, r0 + m) of the fold order (sbuf, or rbuf when `out`) copied into dst[0, m)
+// of shared memory by asynchronous copies (no registers held while they are in flight); async_ptrs_wait
+// returns once this thread's copies have landed.  The slots were published before the collective's
+// barrier, whose acquire dropped any older copy of them from this SM's L1, and stay unchanged until the
+// job's last chunk is finished.
+__device__ __forceinline__ void async_ptrs(unsigned long long* dst, const CollSlot* slots, int r0, int m, bool out,
+                                           int rot, int n, int tid, int nt) {
+    for (int i = tid; i < m; i += nt) {
+        const int r = rot ? (r0 + i + rot) % n : r0 + i;
+        const void* src = out ? (const void*)&slots[r].rbuf : (const void*)&slots[r].sbuf;
+        unsigned long long g;
+        asm("cvta.to.global.u64 %0, %1;" : "=l"(g) : "l"(src));
+        const unsigned d = (unsigned)__cvta_generic_to_shared(dst + i);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(g) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void async_ptrs_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // Canonical-order fold of elements [e0, e0 + nt*V): thread tid owns V consecutive elements.
 // order: acc = x_0; acc = op(x_s, acc) for s = 1..n-1 (in comm-rank order).
+// The members' pointers come through the two halves of the block's pointer tile: while the ranks of one
+// half are folded (or written), the next half's pointers are already being copied into the other half, so
+// each group of PTILE / 2 ranks costs one block barrier and no exposed pointer round trip.
 template <class T, int OP, int V>
 __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid, int nt) {
     constexpr int BYTES = V * (int)sizeof(T);
     // ranks folded per step: ~128 bytes of loads in flight per thread (at most 16 loads)
     constexpr int U = 128 / BYTES > 16 ? 16 : 128 / BYTES < 1 ? 1 : 128 / BYTES;
+    constexpr int H = PTILE / 2;
     const CollSlot* slots = j->slots;
     const int n = j->csize;
     const long long count = j->count;
@@ -256,19 +279,26 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
     T acc[V];
 #pragma unroll
     for (int k = 0; k < V; k++) acc[k] = T();
-    for (int r0 = 0; r0 < n; r0 += PTILE) {
-        const int m = min(PTILE, n - r0);
-        load_ptile(slots, r0, m, 0, tid, nt, rot, n);
+    bar_sync(BAR_TASK, nt);  // the previous chunk's readers are done with the tile
+    async_ptrs(s_chunk.f.ptile, slots, 0, min(H, n), false, rot, n, tid, nt);
+    async_ptrs_wait();
+    bar_sync(BAR_TASK, nt);
+    int half = 0;
+    for (int r0 = 0; r0 < n; r0 += H) {
+        const int m = min(H, n - r0);
+        const bool more = r0 + H < n;
+        if (more) async_ptrs(s_chunk.f.ptile + (half ^ 1) * H, slots, r0 + H, min(H, n - r0 - H), false, rot, n, tid, nt);
+        const unsigned long long* pt = s_chunk.f.ptile + half * H;
         if (nv > 0) {
             int i = 0;
             if (r0 == 0) {
-                ld_elems<T, V>((const T*)s_chunk.f.ptile[0] + e, acc, nv, vec16);
+                ld_elems<T, V>((const T*)pt[0] + e, acc, nv, vec16);
                 i = 1;
             }
             for (; i + U <= m; i += U) {
                 T v[U][V];
 #pragma unroll
-                for (int u = 0; u < U; u++) ld_elems<T, V>((const T*)s_chunk.f.ptile[i + u] + e, v[u], nv, vec16);
+                for (int u = 0; u < U; u++) ld_elems<T, V>((const T*)pt[i + u] + e, v[u], nv, vec16);
 #pragma unroll
                 for (int u = 0; u < U; u++)
 #pragma unroll
@@ -276,11 +306,14 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
             }
             for (; i < m; i++) {
                 T v[V];
-                ld_elems<T, V>((const T*)s_chunk.f.ptile[i] + e, v, nv, vec16);
+                ld_elems<T, V>((const T*)pt[i] + e, v, nv, vec16);
 #pragma unroll
                 for (int k = 0; k < V; k++) acc[k] = op_apply<OP, T>(v[k], acc[k]);
             }
         }
+        if (more) async_ptrs_wait();
+        bar_sync(BAR_TASK, nt);  // the next half is filled; nobody reads this half any more
+        half ^= 1;
     }
     if (j->kind == JOB_REDUCE) {
         if (nv > 0) {
@@ -289,11 +322,20 @@ __device__ __noinline__ void fold_fast(const JobParams* j, long long e0, int tid
         }
         return;
     }
-    for (int r0 = 0; r0 < n; r0 += PTILE) {
-        const int m = min(PTILE, n - r0);
-        load_ptile(slots, r0, m, 1, tid, nt);
+    // every member's result: the same two halves, receive pointers in rank order
+    async_ptrs(s_chunk.f.ptile + half * H, slots, 0, min(H, n), true, 0, n, tid, nt);
+    async_ptrs_wait();
+    bar_sync(BAR_TASK, nt);
+    for (int r0 = 0; r0 < n; r0 += H) {
+        const int m = min(H, n - r0);
+        const bool more = r0 + H < n;
+        if (more) async_ptrs(s_chunk.f.ptile + (half ^ 1) * H, slots, r0 + H, min(H, n - r0 - H), true, 0, n, tid, nt);
+        const unsigned long long* pt = s_chunk.f.ptile + half * H;
         if (nv > 0)
-            for (int i = 0; i < m; i++) st_elems<T, V>((T*)s_chunk.f.ptile[i] + e, acc, nv, vec16);
+            for (int i = 0; i < m; i++) st_elems<T, V>((T*)pt[i] + e, acc, nv, vec16);
+        if (more) async_ptrs_wait();
+        bar_sync(BAR_TASK, nt);
+        half ^= 1;
     }
 }
 
