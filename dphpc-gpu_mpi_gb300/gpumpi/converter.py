@@ -132,6 +132,29 @@ def tokenize(src: str) -> list[Tok]:
     return out
 
 
+def c_string_length(lit: str) -> int:
+    """Characters of a narrow C string literal's contents (escape sequences count as one)."""
+    body = lit[lit.index('"') + 1:-1]
+    n, i = 0, 0
+    while i < len(body):
+        if body[i] == "\\" and i + 1 < len(body):
+            i += 1
+            if body[i] == "x":
+                i += 1
+                while i < len(body) and body[i] in "0123456789abcdefABCDEF":
+                    i += 1
+            elif body[i] in "01234567":
+                j = i
+                while i < len(body) and i < j + 3 and body[i] in "01234567":
+                    i += 1
+            else:
+                i += 1
+        else:
+            i += 1
+        n += 1
+    return n
+
+
 def is_sig(t: Tok) -> bool:
     return t.kind not in ("ws", "nl", "comment", "dir")
 
@@ -161,7 +184,7 @@ class Declaration:
 
 class Converter:
     def __init__(self, src: str, max_ranks: int, extra_types=(), is_main_file=True, globals_in=None,
-                 include_map=None, structs_in=None, functions_in=None):
+                 include_map=None, structs_in=None, functions_in=None, array_sizes_in=None):
         self.toks = tokenize(src)
         self.sig = [i for i, t in enumerate(self.toks) if is_sig(t)]
         self.max_ranks = max_ranks
@@ -176,6 +199,8 @@ class Converter:
         self.saw_main = False
         self.structs: dict[str, dict] = dict(structs_in or {})  # struct key -> member -> (type, stars, brackets)
         self.functions: dict[str, tuple] = dict(functions_in or {})  # name -> (return type, parameters or None)
+        # name -> first extent of a file-scope array defined with one (an `extern T x[];` elsewhere needs it)
+        self.array_sizes: dict[str, str] = dict(array_sizes_in or {})
         self._ret = None                       # return type of the function being converted
 
     # ---- token helpers (k = sig index) ----
@@ -334,6 +359,9 @@ class Converter:
                             (d.type_text, dd.stars, 0), self._param_infos(dd.name + 1, self.match[dd.name + 1]))
                     else:
                         self.globals[self.t(dd.name)] = (d.type_text, dd.stars, dd.brackets)
+                        ext = self._first_extent(dd) if dd.brackets else None
+                        if ext is not None:
+                            self.array_sizes[self.t(dd.name)] = ext
             elif body is not None:
                 d = self.parse_declaration(k, body[0])
                 fn = next((dd for dd in d.decls if dd.name is not None and dd.is_function), None)
@@ -548,20 +576,80 @@ class Converter:
         self._function_definition(k, open_, close)
         return close + 1
 
+    def _object_const(self, d: Declaration, dd: Declarator) -> bool:
+        """Whether the declared object itself is const (not only what it points to)."""
+        if dd.stars == 0:
+            return "const" in d.type_text.split()
+        last_star = max(k for k in range(dd.start, dd.name) if self.t(k) == "*")
+        return any(self.t(k) == "const" for k in range(last_star + 1, dd.name))
+
     def _global_declaration(self, a: int, b: int):
         d = self.parse_declaration(a, b)
         if "typedef" in d.storage or not d.decls:
             return
         if any(dd.name is not None for dd in d.decls):
             self.add_prefix(a, "__device__ ")
+        # a const object at file scope has external linkage in C but internal linkage in C++: its
+        # definition keeps it visible to the other files' extern declarations
+        objs = [dd for dd in d.decls if dd.name is not None and not dd.is_function]
+        if (objs and not ({"static", "extern"} & d.storage) and all(dd.init is not None for dd in objs)
+                and any(self._object_const(d, dd) for dd in objs)):
+            self.add_prefix(a, "extern ")
         for dd in d.decls:
             if dd.name is None or dd.is_function:
                 continue
             self._make_per_rank(d, dd)
 
+    def _first_extent(self, dd: Declarator):
+        """The first dimension of array declarator dd as text: written in the brackets, else the element
+        count of its initializer (a braced list, designators included, or a string literal); None when
+        neither says."""
+        lb = dd.name + 1
+        if self.t(lb) != "[":
+            return None
+        if self.match[lb] != lb + 1:
+            return self.raw_text(lb + 1, self.match[lb] - 1).strip()
+        if dd.init is None:
+            return None
+        if self.kind(dd.init) == "str":
+            n, k = 0, dd.init
+            while k < dd.end and self.kind(k) == "str":
+                n += c_string_length(self.t(k))
+                k += 1
+            return str(n + 1)
+        if self.t(dd.init) != "{":
+            return None
+        close = self.match[dd.init]
+        pos = size = 0
+        k = dd.init + 1
+        while k < close:
+            if self.t(k) == "[":  # designator [index] = value
+                idx = self.raw_text(k + 1, self.match[k] - 1).strip()
+                if not re.fullmatch(r"[0-9]+[uUlL]*", idx):
+                    return None
+                pos = int(re.match(r"[0-9]+", idx).group())
+            e = k
+            while e < close and self.t(e) != ",":
+                if self.t(e) in ("(", "[", "{"):
+                    e = self.match[e]
+                e += 1
+            if e > k:
+                size = max(size, pos + 1)
+                pos += 1
+            k = e + 1
+        return str(size)
+
     def _make_per_rank(self, d: Declaration, dd: Declarator):
         name = self.t(dd.name)
         self.add_suffix(dd.name, f"[{self.max_ranks}]")
+        if self.t(dd.name + 1) == "[" and self.match[dd.name + 1] == dd.name + 2:
+            # an array of unknown first extent cannot be an element type: give it the extent its
+            # initializer, or (extern) its definition in another converted file, implies
+            ext = self._first_extent(dd) or self.array_sizes.get(name)
+            if ext is None:
+                raise ConversionError(f"array '{name}' has no size here and its definition is not among the "
+                                      "converted files")
+            self.add_suffix(dd.name + 1, ext)
         if dd.init is not None:
             last = dd.end - 1
             text = self.raw_text(dd.init, last).strip()
@@ -909,6 +997,13 @@ def convert_files(sources, out_dir, max_ranks: int | None = None, include_dirs=(
     out_dir.mkdir(parents=True, exist_ok=True)
     srcs = [Path(s).resolve() for s in sources]
     project = Path(project or os.environ.get(PROJECT_ENV) or srcs[0].parent).resolve()
+    # first extents of the file-scope arrays defined in any of the sources (for extern declarations of
+    # unknown extent in the others)
+    sizes: dict[str, str] = {}
+    for src in srcs:
+        c = Converter(src.read_text(), max_ranks, extra_types)
+        c._collect_typedefs_and_globals()
+        sizes.update(c.array_sizes)
     converted = []
     for src in srcs:
         headers = _project_headers(src, project, [Path(d).resolve() for d in include_dirs], {})
@@ -923,7 +1018,8 @@ def convert_files(sources, out_dir, max_ranks: int | None = None, include_dirs=(
             globs.update(c.globals)
             structs.update(c.structs)
             funcs.update(c.functions)
-        known = dict(include_map=imap, globals_in=globs, structs_in=structs, functions_in=funcs)
+        known = dict(include_map=imap, globals_in=globs, structs_in=structs, functions_in=funcs,
+                     array_sizes_in=sizes)
         for h in headers:
             text = Converter(h.read_text(), max_ranks, types, **known).run()
             (out_dir / (h.name + ".cuh")).write_text(text)

@@ -88,6 +88,66 @@ void f(int n) { double *x = malloc(n * sizeof(double)); node *t; t = calloc(1, s
     assert "__gpu_global(grid) = (int **)malloc(8); __gpu_global(grid)[0] = (int *)malloc(4);" in out
 
 
+def test_unsized_arrays_get_the_extent_their_initializer_implies():
+    src = """static const char *names[] = {"a", "b", "c",};
+int tab[] = { [5] = 1, 2, [1] = 3 };
+char msg[] = "hi\\n" "there";
+int g(void) { static int loc[] = {1, 2, 3}; return loc[2] + tab[6] + msg[0] + names[2][0]; }
+"""
+    out = squash(conv(src, 2))
+    assert '__device__ static const char *names[2][3] = {{"a", "b", "c",}, {"a", "b", "c",}};' in out
+    assert "__device__ int tab[2][7] =" in out
+    assert "__device__ char msg[2][9] =" in out
+    assert "static int loc[2][3] = {{1, 2, 3}, {1, 2, 3}};" in out
+
+
+def test_extern_array_of_unknown_extent_takes_its_definitions(tmp_path):
+    (tmp_path / "def.c").write_text("double table[] = {1.0, 2.0, 3.0};\nint rows = 3;\n")
+    (tmp_path / "use.c").write_text("extern double table[];\nextern int rows;\n"
+                                    "double last(void) { return table[rows - 1]; }\n")
+    out = cv.convert_files([tmp_path / "use.c", tmp_path / "def.c"], tmp_path / "conv", max_ranks=4)
+    assert "__device__ extern double table[4][3];" in squash(out[0].read_text())
+    assert "__device__ double table[4][3] =" in squash(out[1].read_text())
+    with pytest.raises(cv.ConversionError):
+        cv.convert_source("extern double other[];\ndouble f(void) { return other[0]; }\n", max_ranks=2)
+
+
+def test_const_definitions_keep_external_linkage():
+    out = squash(conv("const int N = 4;\nstatic const int M = 2;\nconst char *name = \"x\";\n"
+                      "char * const fixed = 0;\nextern const int K;\nint f(void) { return N + M + K; }\n", 2))
+    assert "__device__ extern const int N[2] = {4, 4};" in out
+    assert "__device__ static const int M[2] = {2, 2};" in out
+    assert '__device__ const char *name[2] = {"x", "x"};' in out       # a pointer to const: already external
+    assert "__device__ extern char * const fixed[2] = {0, 0};" in out
+    assert "__device__ extern const int K[2];" in out
+
+
+@pytest.mark.skipif(shutil.which("nvcc") is None and not Path("/usr/local/cuda/bin/nvcc").exists(),
+                    reason="no nvcc")
+def test_tables_shared_across_files_device_link(tmp_path):
+    # const and unsized file-scope arrays defined in one file and used through extern declarations in
+    # another: both converted, compiled for sm_103a and device-linked (every symbol resolves)
+    import build as gbuild
+    (tmp_path / "tabdef.c").write_text('const int primes[] = {2, 3, 5, 7, 11, 13};\n'
+                                       'const char *words[] = {"alpha", "beta", "gamma"};\n'
+                                       'char banner[] = "tables";\nconst double scale = 0.5;\n')
+    (tmp_path / "tabuse.c").write_text('extern const int primes[];\nextern const char *words[];\n'
+                                       'extern char banner[];\nextern const double scale;\n'
+                                       'double score(int r) { return (primes[r % 6] + words[r % 3][0] + '
+                                       'banner[0]) * scale; }\n')
+    out = cv.convert_files([tmp_path / "tabuse.c", tmp_path / "tabdef.c"], tmp_path / "conv", max_ranks=8)
+    objs = []
+    for f in out:
+        o = f.with_suffix(".o")
+        r = subprocess.run([gbuild.nvcc(), *gbuild.common_flags(), "-c", str(f), "-o", str(o)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-4000:]
+        objs.append(str(o))
+    r = subprocess.run([gbuild.nvcc(), *gbuild.ARCH, "-dlink", *objs, "-o", str(tmp_path / "dlink.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+
+
 def test_void_pointer_members_get_casts():
     # the reference's converter casts every implicit conversion from void*; here: values of void* struct
     # members reaching typed pointers through assignment, initialisation, return and call arguments
