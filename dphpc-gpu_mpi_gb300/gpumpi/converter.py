@@ -14,7 +14,10 @@ stream, with a scope-aware pass over function bodies instead of an AST:
   with one element per rank: `__device__ T name[MAX_RANKS]` with its C initializer repeated for every
   rank (converter.cpp:118-144), and every reference to it becomes `__gpu_global(name)`, the calling
   rank's element (converter.cpp:145-164) -- in function bodies, honouring local declarations and
-  parameters that shadow it, and in `#define` bodies;
+  parameters that shadow it, and in `#define` bodies; in rank r's copy of an initializer a variable it
+  names (an address constant such as `&base`) becomes rank r's element `base[r]`; an array of unknown
+  extent gets the extent its initializer, or for `extern`, its definition in another converted file,
+  implies; a `const` object defined at file scope is defined `extern` (external in C, internal in C++);
 * results of malloc/calloc/realloc stored into typed pointers get an explicit cast, the implicit
   `void*` conversion being invalid in CUDA C++ (the reference casts every implicit bit cast,
   converter.cpp:112-116);
@@ -25,9 +28,8 @@ stream, with a scope-aware pass over function bodies instead of an AST:
   project are converted too and included as `name.h.cuh` (the reference's gpumpicc.py renames the same
   way).
 
-Limits (as for the reference's tool, plus those of working on tokens): a global initialised from another
-global's value, or a char array sized by its string initializer, does not compile after conversion;
-macros are rewritten where they are defined, so a macro whose body names a global is rewritten for every
+Limits (as for the reference's tool, plus those of working on tokens): an `extern` array of unknown
+extent whose definition is not converted with it is refused; macros are rewritten where they are defined, so a macro whose body names a global is rewritten for every
 use; block-scope function prototypes are left alone; the program is expected to be C (C++ classes are
 not converted).  Output files: `x.c` -> `x.cu`, a project header `y.h` -> `y.h.cuh`.
 """
@@ -639,6 +641,21 @@ class Converter:
             k = e + 1
         return str(size)
 
+    def _rank_text(self, a: int, b: int, r: int) -> str:
+        """Raw text of tokens [a, b] for rank r's copy of an initializer: a file-scope variable named in it
+        (an address constant such as `&base` or an array decaying to its first element) becomes rank r's
+        element of that variable, `name[r]`."""
+        out, prev = [], None
+        for i in range(self.sig[a], self.sig[b] + 1):
+            tok = self.toks[i]
+            txt = tok.text
+            if tok.kind == "id" and txt in self.globals and prev not in (".", "->"):
+                txt = f"{txt}[{r}]"
+            if is_sig(tok):
+                prev = tok.text
+            out.append(txt)
+        return "".join(out).strip()
+
     def _make_per_rank(self, d: Declaration, dd: Declarator):
         name = self.t(dd.name)
         self.add_suffix(dd.name, f"[{self.max_ranks}]")
@@ -652,10 +669,10 @@ class Converter:
             self.add_suffix(dd.name + 1, ext)
         if dd.init is not None:
             last = dd.end - 1
-            text = self.raw_text(dd.init, last).strip()
             if self.t(dd.init) == "{" and self.match[dd.init] != last:
                 raise ConversionError(f"initializer of '{name}' is not a single braced list")
-            self.replace(dd.init, "{" + ", ".join([text] * self.max_ranks) + "}")
+            self.replace(dd.init, "{" + ", ".join(self._rank_text(dd.init, last, r)
+                                                   for r in range(self.max_ranks)) + "}")
             for q in range(dd.init + 1, last + 1):
                 self.replace(q, "")
             # drop the layout between the removed tokens (their text is inside the replacement)

@@ -112,6 +112,15 @@ def test_extern_array_of_unknown_extent_takes_its_definitions(tmp_path):
         cv.convert_source("extern double other[];\ndouble f(void) { return other[0]; }\n", max_ranks=2)
 
 
+def test_initializers_naming_globals_use_each_ranks_copy():
+    src = ("int base = 3;\nint arr[4];\nint *pb = &base, *pa = arr + 1;\n"
+           "struct S { int *p; int n; } s = { &base, sizeof(arr) };\nint f(void) { static int *q = &base; return *q; }\n")
+    out = squash(conv(src, 2))
+    assert "__device__ int *pb[2] = {&base[0], &base[1]}, *pa[2] = {arr[0] + 1, arr[1] + 1};" in out
+    assert "s[2] = {{ &base[0], sizeof(arr[0]) }, { &base[1], sizeof(arr[1]) }};" in out
+    assert "static int *q[2] = {&base[0], &base[1]};" in out
+
+
 def test_const_definitions_keep_external_linkage():
     out = squash(conv("const int N = 4;\nstatic const int M = 2;\nconst char *name = \"x\";\n"
                       "char * const fixed = 0;\nextern const int K;\nint f(void) { return N + M + K; }\n", 2))
