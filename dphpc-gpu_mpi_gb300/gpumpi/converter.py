@@ -610,7 +610,7 @@ class Converter:
         if self.t(lb) != "[":
             return None
         if self.match[lb] != lb + 1:
-            return self.raw_text(lb + 1, self.match[lb] - 1).strip()
+            return self._rank_text(lb + 1, self.match[lb] - 1, 0)
         if dd.init is None:
             return None
         if self.kind(dd.init) == "str":
@@ -667,6 +667,13 @@ class Converter:
                 raise ConversionError(f"array '{name}' has no size here and its definition is not among the "
                                       "converted files")
             self.add_suffix(dd.name + 1, ext)
+        # a global named in the dimensions (`sizeof(src) / sizeof(src[0])`) means one rank's copy of it
+        k = dd.name + 1
+        while self.t(k) == "[":
+            for q in range(k + 1, self.match[k]):
+                if self.kind(q) == "id" and self.t(q) in self.globals and self.t(q - 1) not in (".", "->"):
+                    self.add_suffix(q, "[0]")
+            k = self.match[k] + 1
         if dd.init is not None:
             last = dd.end - 1
             if self.t(dd.init) == "{" and self.match[dd.init] != last:

@@ -121,6 +121,11 @@ def test_initializers_naming_globals_use_each_ranks_copy():
     assert "static int *q[2] = {&base[0], &base[1]};" in out
 
 
+def test_globals_in_array_dimensions_mean_one_ranks_copy():
+    out = squash(conv("double src[] = {1, 2, 3};\ndouble copy[sizeof(src) / sizeof(src[0])];\n", 2))
+    assert "__device__ double copy[2][sizeof(src[0]) / sizeof(src[0][0])];" in out
+
+
 def test_const_definitions_keep_external_linkage():
     out = squash(conv("const int N = 4;\nstatic const int M = 2;\nconst char *name = \"x\";\n"
                       "char * const fixed = 0;\nextern const int K;\nint f(void) { return N + M + K; }\n", 2))
